@@ -1,0 +1,853 @@
+// CPU oracle for the coupled LBM-MPM timestep of lizhuoh9/taichi-mpm-lbm.
+//
+// TEST INFRASTRUCTURE ONLY. This file is a literal restatement of the
+// reference's Taichi kernels in plain C++ (templated on float / double) so
+// that the CUDA implementation can be checked against it. It is never linked
+// into, loaded by, or called from the product library; only tests/, the smoke
+// check and bench.py's CPU-baseline leg use it.
+//
+// Arithmetic follows the reference source order term by term (sequential sums
+// in index order, no fused multiply-add: build with -ffp-contract=off), so the
+// float instantiation reproduces what the reference computes in FP32 up to the
+// reference runtime's own freedom (Taichi fast-math, atomic ordering).
+//
+// Layouts are the reference's numpy layouts (C order):
+//   f, F      [nx, ny, nz, 19]      rho [nx, ny, nz]     v, force [nx, ny, nz, 3]
+//   solid     [nx, ny, nz] int32    particles x, v, f_p [P, 3]; C, F [P, 3, 3]
+//   grid_v    [nx, ny, nz, 3]       grid_m [nx, ny, nz]
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr int Q = 19;
+
+// D3Q19 velocity ordering, fsi/lbm3d.py:221-239.
+const int E[Q][3] = {{0, 0, 0},  {1, 0, 0},   {-1, 0, 0}, {0, 1, 0},  {0, -1, 0},
+                     {0, 0, 1},  {0, 0, -1},  {1, 1, 0},  {-1, -1, 0}, {1, -1, 0},
+                     {-1, 1, 0}, {1, 0, 1},   {-1, 0, -1}, {1, 0, -1}, {-1, 0, 1},
+                     {0, 1, 1},  {0, -1, -1}, {0, 1, -1}, {0, -1, 1}};
+// Opposite directions, fsi/lbm3d.py:171-174.
+const int LR[Q] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+
+inline int nthreads_or_default(int n) { return n > 0 ? n : 1; }
+
+template <class T>
+struct Lattice {
+  int nx, ny, nz;
+  const T* M;     // [19][19] MRT matrix (fsi/lbm3d.py:30-54)
+  const T* invM;  // [19][19] numpy inverse of M in float32, widened (lbm3d.py:170)
+  const T* S;     // [19] relaxation rates (lbm3d.py:141-168)
+  const T* w;     // [19] lattice weights (lbm3d.py:244-248)
+  long cell(int i, int j, int k) const { return ((long)i * ny + j) * nz + k; }
+  long ncell() const { return (long)nx * ny * nz; }
+};
+
+template <class T>
+inline T dot3(const T a[3], const T b[3]) {
+  // Taichi Vector.dot: elementwise product then sequential sum.
+  T s = a[0] * b[0];
+  s = s + a[1] * b[1];
+  s = s + a[2] * b[2];
+  return s;
+}
+
+// feq, fsi/lbm3d.py:250-254.
+template <class T>
+inline T feq(const Lattice<T>& L, int q, T rho, const T u[3]) {
+  T e[3] = {(T)E[q][0], (T)E[q][1], (T)E[q][2]};
+  T eu = dot3(e, u);
+  T uv = dot3(u, u);
+  T inner = (T)1.0 + (T)3.0 * eu;
+  inner = inner + ((T)4.5 * eu) * eu;
+  inner = inner - (T)1.5 * uv;
+  return (L.w[q] * rho) * inner;
+}
+
+// meq_vec, fsi/lbm3d.py:285-312.
+template <class T>
+inline T meq_vec(int m, T rho, const T u[3]) {
+  T out = 0;
+  if (m == 0) out = rho;
+  if (m == 1) out = dot3(u, u);
+  if (m == 3) out = u[0];
+  if (m == 5) out = u[1];
+  if (m == 7) out = u[2];
+  if (m == 9) out = (((T)2.0 * u[0]) * u[0] - u[1] * u[1]) - u[2] * u[2];
+  if (m == 11) out = u[1] * u[1] - u[2] * u[2];
+  if (m == 13) out = u[0] * u[1];
+  if (m == 14) out = u[1] * u[2];
+  if (m == 15) out = u[0] * u[2];
+  return out;
+}
+
+// guo_force, fsi/lbm3d.py:276-283.
+template <class T>
+inline T guo_force(const Lattice<T>& L, int m, const T u[3], const T G[3]) {
+  T out = 0;
+  for (int q = 0; q < Q; ++q) {
+    T e[3] = {(T)E[q][0], (T)E[q][1], (T)E[q][2]};
+    T emu[3] = {e[0] - u[0], e[1] - u[1], e[2] - u[2]};
+    T a = dot3(emu, G);
+    T b = dot3(e, u) * dot3(e, G);
+    out = out + (L.w[q] * (a + b)) * L.M[m * Q + q];
+  }
+  return out;
+}
+
+// collide, fsi/lbm3d.py:314-333 (fluid cells only; writes f from F).
+template <class T>
+void collide(const Lattice<T>& L, T* f, const T* F, const T* rho, const T* v, const T* force,
+             const int32_t* solid, int nthreads) {
+  const long n = L.ncell();
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads))
+  for (long c = 0; c < n; ++c) {
+    if (solid[c] != 0) continue;
+    const T* Fc = F + c * Q;
+    T u[3] = {v[3 * c], v[3 * c + 1], v[3 * c + 2]};
+    T G[3] = {force[3 * c], force[3 * c + 1], force[3 * c + 2]};
+    T mom[Q];
+    for (int m = 0; m < Q; ++m) {
+      T mv = 0;
+      for (int q = 0; q < Q; ++q) mv = mv + L.M[m * Q + q] * Fc[q];
+      T meq = meq_vec(m, rho[c], u);
+      mv = mv - L.S[m] * (mv - meq);
+      mv = mv + ((T)1.0 - (T)0.5 * L.S[m]) * guo_force(L, m, u, G);
+      mom[m] = mv;
+    }
+    for (int q = 0; q < Q; ++q) {
+      T acc = 0;
+      for (int m = 0; m < Q; ++m) acc = acc + L.invM[q * Q + m] * mom[m];
+      f[c * Q + q] = acc;
+    }
+  }
+}
+
+// stream + periodic_index, fsi/lbm3d.py:335-361.
+template <class T>
+void stream(const Lattice<T>& L, const T* f, T* F, const int32_t* solid, int nthreads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads))
+  for (int i = 0; i < L.nx; ++i)
+    for (int j = 0; j < L.ny; ++j)
+      for (int k = 0; k < L.nz; ++k) {
+        long c = L.cell(i, j, k);
+        if (solid[c] != 0) continue;
+        for (int q = 0; q < Q; ++q) {
+          int ti = i + E[q][0], tj = j + E[q][1], tk = k + E[q][2];
+          if (ti < 0) ti = L.nx - 1;
+          if (ti > L.nx - 1) ti = 0;
+          if (tj < 0) tj = L.ny - 1;
+          if (tj > L.ny - 1) tj = 0;
+          if (tk < 0) tk = L.nz - 1;
+          if (tk > L.nz - 1) tk = 0;
+          long t = L.cell(ti, tj, tk);
+          if (solid[t] == 0)
+            F[t * Q + q] = f[c * Q + q];
+          else
+            F[c * Q + LR[q]] = f[c * Q + q];
+        }
+      }
+}
+
+// apply_boundary, fsi/lbm3d.py:363-407. mode 1 = pressure, 2 = velocity.
+template <class T>
+void apply_boundary_face(const Lattice<T>& L, T* F, const T* v, const int32_t* solid, int xi,
+                         int xin, int mode, T bc_rho, const T bc_vel[3], T rho0) {
+  if (mode == 0) return;
+  for (int j = 0; j < L.ny; ++j)
+    for (int k = 0; k < L.nz; ++k) {
+      long c = L.cell(xi, j, k);
+      if (solid[c] != 0) continue;
+      if (mode == 1) {
+        long ci = L.cell(xin, j, k);
+        const T* uu = solid[ci] > 0 ? v + 3 * ci : v + 3 * c;
+        T u[3] = {uu[0], uu[1], uu[2]};
+        for (int q = 0; q < Q; ++q) F[c * Q + q] = feq(L, q, bc_rho, u);
+      } else {
+        for (int q = 0; q < Q; ++q) {
+          int o = LR[q];
+          T val = feq(L, o, rho0, bc_vel) - F[c * Q + o];
+          val = val + feq(L, q, rho0, bc_vel);
+          F[c * Q + q] = val;
+        }
+      }
+    }
+}
+
+// update_macro, fsi/lbm3d.py:409-425.
+template <class T>
+void update_macro(const Lattice<T>& L, T* f, const T* F, T* rho, T* v, const T* force,
+                  const int32_t* solid, T rho0, int nthreads) {
+  const long n = L.ncell();
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads))
+  for (long c = 0; c < n; ++c) {
+    if (solid[c] == 0) {
+      T r = 0;
+      T u[3] = {0, 0, 0};
+      for (int q = 0; q < Q; ++q) {
+        T fq = F[c * Q + q];
+        f[c * Q + q] = fq;
+        r = r + fq;
+        for (int a = 0; a < 3; ++a) u[a] = u[a] + (T)E[q][a] * fq;
+      }
+      for (int a = 0; a < 3; ++a) u[a] = u[a] / r;
+      for (int a = 0; a < 3; ++a) u[a] = u[a] + (force[3 * c + a] * (T)0.5) / r;
+      rho[c] = r;
+      for (int a = 0; a < 3; ++a) v[3 * c + a] = u[a];
+    } else {
+      rho[c] = rho0;
+      v[3 * c] = v[3 * c + 1] = v[3 * c + 2] = 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- MPM -----
+
+template <class T>
+struct Particles {
+  int n;
+  T* x;        // [P,3]
+  T* v;        // [P,3]
+  T* C;        // [P,9]
+  T* Fd;       // [P,9]
+  const T* mass;
+  const T* vol;
+  const int32_t* active;
+  T* fp;       // [P,3] particle_force
+};
+
+template <class T>
+struct Grid {
+  int nx, ny, nz;
+  T* gv;  // [N,3]
+  T* gm;  // [N]
+  long cell(int i, int j, int k) const { return ((long)i * ny + j) * nz + k; }
+  bool inside(int i, int j, int k) const {
+    return 0 <= i && i < nx && 0 <= j && j < ny && 0 <= k && k < nz;
+  }
+};
+
+// _weights, fsi/mpm3d.py:227-232 (also coupling.py:314-319).
+template <class T>
+inline void bspline(T fx, T w[3]) {
+  T a = (T)1.5 - fx;
+  T b = fx - (T)1.0;
+  T c = fx - (T)0.5;
+  w[0] = (T)0.5 * (a * a);
+  w[1] = (T)0.75 - b * b;
+  w[2] = (T)0.5 * (c * c);
+}
+
+// base = trunc(x * inv_dx - 0.5), fx = x * inv_dx - base (mpm3d.py:239-241).
+template <class T>
+inline void base_fx(const T x[3], T inv_dx, int base[3], T fx[3]) {
+  for (int a = 0; a < 3; ++a) {
+    T g = x[a] * inv_dx;
+    base[a] = (int)(g - (T)0.5);
+    fx[a] = x[a] * inv_dx - (T)base[a];
+  }
+}
+
+template <class T>
+inline void matmul3(const T A[9], const T B[9], T out[9]) {
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      T s = A[3 * a] * B[b];
+      s = s + A[3 * a + 1] * B[3 + b];
+      s = s + A[3 * a + 2] * B[6 + b];
+      out[3 * a + b] = s;
+    }
+}
+
+template <class T>
+inline T det3(const T a[9]) {
+  // Cofactor expansion along the first column.
+  T t0 = a[4] * a[8] - a[7] * a[5];
+  T t1 = a[1] * a[8] - a[7] * a[2];
+  T t2 = a[1] * a[5] - a[4] * a[2];
+  T d = a[0] * t0 - a[3] * t1;
+  d = d + a[6] * t2;
+  return d;
+}
+
+// Rotation R of the polar decomposition F = R S, computed in double precision
+// by the one-sided Jacobi SVD (Hestenes 1958) of F: orthogonalise the columns
+// of A = F V by plane rotations, then R = U V^T with U = A / |A| column-wise.
+// The reference takes R = U V^T from ti.svd (mpm3d.py:245-246); for det F > 0
+// this rotation is unique, so any accurate method agrees with it to rounding.
+// For det F <= 0 the sign of the column with the smallest norm is flipped to
+// return a proper rotation, which is the convention of 3x3 SVDs that keep
+// det U = det V = +1.
+inline void polar_rotation_f64(const double F[9], double R[9]) {
+  double A[9], V[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  for (int i = 0; i < 9; ++i) A[i] = F[i];
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        double alpha = 0, beta = 0, gamma = 0;
+        for (int r = 0; r < 3; ++r) {
+          alpha += A[3 * r + p] * A[3 * r + p];
+          beta += A[3 * r + q] * A[3 * r + q];
+          gamma += A[3 * r + p] * A[3 * r + q];
+        }
+        if (gamma == 0.0) continue;
+        off = std::fmax(off, std::fabs(gamma) / std::sqrt(alpha * beta));
+        double zeta = (beta - alpha) / (2.0 * gamma);
+        double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+        double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
+        for (int r = 0; r < 3; ++r) {
+          double ap = A[3 * r + p], aq = A[3 * r + q];
+          A[3 * r + p] = c * ap - s * aq;
+          A[3 * r + q] = s * ap + c * aq;
+          double vp = V[3 * r + p], vq = V[3 * r + q];
+          V[3 * r + p] = c * vp - s * vq;
+          V[3 * r + q] = s * vp + c * vq;
+        }
+      }
+    if (off < 1e-15) break;
+  }
+  double nrm[3];
+  for (int c = 0; c < 3; ++c)
+    nrm[c] = std::sqrt(A[c] * A[c] + A[3 + c] * A[3 + c] + A[6 + c] * A[6 + c]);
+  double U[9];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) U[3 * r + c] = nrm[c] > 0 ? A[3 * r + c] / nrm[c] : (r == c ? 1.0 : 0.0);
+  double detF = F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+                F[6] * (F[1] * F[5] - F[4] * F[2]);
+  double detU = U[0] * (U[4] * U[8] - U[7] * U[5]) - U[3] * (U[1] * U[8] - U[7] * U[2]) +
+                U[6] * (U[1] * U[5] - U[4] * U[2]);
+  double detV = V[0] * (V[4] * V[8] - V[7] * V[5]) - V[3] * (V[1] * V[8] - V[7] * V[2]) +
+                V[6] * (V[1] * V[5] - V[4] * V[2]);
+  if (detU * detV < 0) {
+    // Improper U V^T: flip the singular vector pair with the smallest singular value.
+    int cmin = 0;
+    for (int c = 1; c < 3; ++c)
+      if (nrm[c] < nrm[cmin]) cmin = c;
+    for (int r = 0; r < 3; ++r) U[3 * r + cmin] = -U[3 * r + cmin];
+  }
+  (void)detF;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      double s = 0;
+      for (int c = 0; c < 3; ++c) s += U[3 * a + c] * V[3 * b + c];
+      R[3 * a + b] = s;
+    }
+}
+
+template <class T>
+struct MpmParams {
+  T dt, dx, inv_dx, mu, lam, gravity[3], damping;
+  int bw, apic;
+};
+
+template <class T>
+inline void p2g_particle(int p, const Particles<T>& P, Grid<T>& G, const MpmParams<T>& mp,
+                         bool atomic) {
+  if (P.active[p] == 0) return;
+  T x[3] = {P.x[3 * p], P.x[3 * p + 1], P.x[3 * p + 2]};
+  int base[3];
+  T fx[3];
+  base_fx(x, mp.inv_dx, base, fx);
+  T w[3][3];
+  for (int a = 0; a < 3; ++a) {
+    T ww[3];
+    bspline(fx[a], ww);
+    for (int i = 0; i < 3; ++i) w[i][a] = ww[i];
+  }
+  const T dt = mp.dt;
+  T* Cp = P.C + 9 * p;
+  T* Fp = P.Fd + 9 * p;
+  // F <- (I + dt C) F, mpm3d.py:243.
+  T A[9];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) A[3 * a + b] = (T)(a == b ? 1 : 0) + dt * Cp[3 * a + b];
+  T Fn[9];
+  matmul3(A, Fp, Fn);
+  for (int i = 0; i < 9; ++i) Fp[i] = Fn[i];
+  T J = det3(Fn);
+  double Fd64[9], R64[9];
+  for (int i = 0; i < 9; ++i) Fd64[i] = (double)Fn[i];
+  polar_rotation_f64(Fd64, R64);
+  T R[9];
+  for (int i = 0; i < 9; ++i) R[i] = (T)R64[i];
+  // stress = 2 mu (F - R) F^T + lam J (J - 1) I, mpm3d.py:247-251.
+  T twomu = (T)2.0 * mp.mu;
+  T Pm[9];
+  for (int i = 0; i < 9; ++i) Pm[i] = twomu * (Fn[i] - R[i]);
+  T Ft[9];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) Ft[3 * a + b] = Fn[3 * b + a];
+  T stress[9];
+  matmul3(Pm, Ft, stress);
+  T lj = (mp.lam * J) * (J - (T)1.0);
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) stress[3 * a + b] = stress[3 * a + b] + lj * (T)(a == b ? 1 : 0);
+  T coef = (((-dt) * P.vol[p]) * (T)4.0) * mp.inv_dx;
+  coef = coef * mp.inv_dx;
+  T affine[9];
+  const T m = P.mass[p];
+  for (int i = 0; i < 9; ++i) affine[i] = coef * stress[i] + m * Cp[i];
+  T mv[3], dtf[3];
+  for (int a = 0; a < 3; ++a) {
+    mv[a] = m * P.v[3 * p + a];
+    dtf[a] = dt * P.fp[3 * p + a];
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k) {
+        int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+        if (!G.inside(ni, nj, nk)) continue;
+        T dpos[3] = {((T)i - fx[0]) * mp.dx, ((T)j - fx[1]) * mp.dx, ((T)k - fx[2]) * mp.dx};
+        T weight = (w[i][0] * w[j][1]) * w[k][2];
+        long c = G.cell(ni, nj, nk);
+        for (int a = 0; a < 3; ++a) {
+          T ad = affine[3 * a] * dpos[0];
+          ad = ad + affine[3 * a + 1] * dpos[1];
+          ad = ad + affine[3 * a + 2] * dpos[2];
+          T mom = (mv[a] + ad) + dtf[a];
+          T add = weight * mom;
+          if (atomic) {
+#pragma omp atomic
+            G.gv[3 * c + a] += add;
+          } else {
+            G.gv[3 * c + a] = G.gv[3 * c + a] + add;
+          }
+        }
+        T addm = weight * m;
+        if (atomic) {
+#pragma omp atomic
+          G.gm[c] += addm;
+        } else {
+          G.gm[c] = G.gm[c] + addm;
+        }
+      }
+}
+
+// grid_op, fsi/mpm3d.py:268-288.
+template <class T>
+void grid_op(Grid<T>& G, const MpmParams<T>& mp, int nthreads) {
+  const T dtg[3] = {mp.dt * mp.gravity[0], mp.dt * mp.gravity[1], mp.dt * mp.gravity[2]};
+  const T nd = -mp.damping;
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads))
+  for (int i = 0; i < G.nx; ++i)
+    for (int j = 0; j < G.ny; ++j)
+      for (int k = 0; k < G.nz; ++k) {
+        long c = G.cell(i, j, k);
+        T m = G.gm[c];
+        if (!(m > (T)0)) continue;
+        T* gv = G.gv + 3 * c;
+        for (int a = 0; a < 3; ++a) gv[a] = gv[a] / m;
+        for (int a = 0; a < 3; ++a) gv[a] = gv[a] + dtg[a];
+        const int node[3] = {i, j, k};
+        const int n[3] = {G.nx, G.ny, G.nz};
+        for (int a = 0; a < 3; ++a) {
+          if (node[a] < mp.bw && gv[a] < (T)0) gv[a] = nd * gv[a];
+          if (node[a] >= n[a] - mp.bw && gv[a] > (T)0) gv[a] = nd * gv[a];
+        }
+      }
+}
+
+// g2p + _clamp_particle_position, fsi/mpm3d.py:290-328.
+template <class T>
+inline void g2p_particle(int p, Particles<T>& P, const Grid<T>& G, const MpmParams<T>& mp,
+                         const T lower, const T upper[3]) {
+  if (P.active[p] == 0) return;
+  T x[3] = {P.x[3 * p], P.x[3 * p + 1], P.x[3 * p + 2]};
+  int base[3];
+  T fx[3];
+  base_fx(x, mp.inv_dx, base, fx);
+  T w[3][3];
+  for (int a = 0; a < 3; ++a) {
+    T ww[3];
+    bspline(fx[a], ww);
+    for (int i = 0; i < 3; ++i) w[i][a] = ww[i];
+  }
+  T nv[3] = {0, 0, 0};
+  T nc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const T four_inv_dx = (T)4.0 * mp.inv_dx;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k) {
+        int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+        if (!G.inside(ni, nj, nk)) continue;
+        T dpos[3] = {(T)i - fx[0], (T)j - fx[1], (T)k - fx[2]};
+        T weight = (w[i][0] * w[j][1]) * w[k][2];
+        const T* gv = G.gv + 3 * G.cell(ni, nj, nk);
+        for (int a = 0; a < 3; ++a) nv[a] = nv[a] + weight * gv[a];
+        T s = four_inv_dx * weight;
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) nc[3 * a + b] = nc[3 * a + b] + s * (gv[a] * dpos[b]);
+      }
+  for (int a = 0; a < 3; ++a) P.v[3 * p + a] = nv[a];
+  for (int i = 0; i < 9; ++i) P.C[9 * p + i] = mp.apic ? nc[i] : (T)0;
+  for (int a = 0; a < 3; ++a) {
+    T xa = P.x[3 * p + a] + mp.dt * nv[a];
+    xa = std::fmin(std::fmax(xa, lower), upper[a]);
+    P.x[3 * p + a] = xa;
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ C interface --
+// All functions take the reference numpy layouts. `nthreads` <= 0 means 1.
+
+#define FSI_ORACLE_EXPORT extern "C" __attribute__((visibility("default")))
+
+template <class T>
+static void lbm_step_impl(int nx, int ny, int nz, T* f, T* F, T* rho, T* v, const T* force,
+                          const int32_t* solid, const T* M, const T* invM, const T* S, const T* w,
+                          int bc_left, int bc_right, T bc_rho_l, T bc_rho_r, const T* bc_vel_l,
+                          const T* bc_vel_r, T rho0, int nthreads) {
+  Lattice<T> L{nx, ny, nz, M, invM, S, w};
+  collide(L, f, F, rho, v, force, solid, nthreads);
+  stream(L, f, F, solid, nthreads);
+  apply_boundary_face(L, F, v, solid, 0, 1, bc_left, bc_rho_l, bc_vel_l, rho0);
+  apply_boundary_face(L, F, v, solid, nx - 1, nx - 2, bc_right, bc_rho_r, bc_vel_r, rho0);
+  update_macro(L, f, F, rho, v, force, solid, rho0, nthreads);
+}
+
+// fsi/lbm3d.py:427-433: collide -> stream -> apply_boundary -> update_macro.
+FSI_ORACLE_EXPORT void oracle_lbm_step_f32(int nx, int ny, int nz, float* f, float* F, float* rho,
+                                           float* v, const float* force, const int32_t* solid,
+                                           const float* M, const float* invM, const float* S,
+                                           const float* w, int bc_left, int bc_right,
+                                           float bc_rho_l, float bc_rho_r, const float* bc_vel_l,
+                                           const float* bc_vel_r, float rho0, int nthreads) {
+  lbm_step_impl<float>(nx, ny, nz, f, F, rho, v, force, solid, M, invM, S, w, bc_left, bc_right,
+                       bc_rho_l, bc_rho_r, bc_vel_l, bc_vel_r, rho0, nthreads);
+}
+
+FSI_ORACLE_EXPORT void oracle_lbm_step_f64(int nx, int ny, int nz, double* f, double* F,
+                                           double* rho, double* v, const double* force,
+                                           const int32_t* solid, const double* M,
+                                           const double* invM, const double* S, const double* w,
+                                           int bc_left, int bc_right, double bc_rho_l,
+                                           double bc_rho_r, const double* bc_vel_l,
+                                           const double* bc_vel_r, double rho0, int nthreads) {
+  lbm_step_impl<double>(nx, ny, nz, f, F, rho, v, force, solid, M, invM, S, w, bc_left, bc_right,
+                        bc_rho_l, bc_rho_r, bc_vel_l, bc_vel_r, rho0, nthreads);
+}
+
+// init_fields, fsi/lbm3d.py:256-267.
+template <class T>
+static void lbm_init_impl(int nx, int ny, int nz, T* f, T* F, T* rho, T* v, const int32_t* solid,
+                          const T* w, T rho0, const T* u0) {
+  Lattice<T> L{nx, ny, nz, nullptr, nullptr, nullptr, w};
+  for (long c = 0; c < L.ncell(); ++c) {
+    rho[c] = rho0;
+    T u[3] = {u0[0], u0[1], u0[2]};
+    if (solid[c] != 0) u[0] = u[1] = u[2] = 0;
+    for (int a = 0; a < 3; ++a) v[3 * c + a] = u[a];
+    for (int q = 0; q < Q; ++q) {
+      T val = feq(L, q, rho[c], u);
+      f[c * Q + q] = val;
+      F[c * Q + q] = val;
+    }
+  }
+}
+
+FSI_ORACLE_EXPORT void oracle_lbm_init_f32(int nx, int ny, int nz, float* f, float* F, float* rho,
+                                           float* v, const int32_t* solid, const float* w,
+                                           float rho0, const float* u0) {
+  lbm_init_impl<float>(nx, ny, nz, f, F, rho, v, solid, w, rho0, u0);
+}
+
+FSI_ORACLE_EXPORT void oracle_lbm_init_f64(int nx, int ny, int nz, double* f, double* F,
+                                           double* rho, double* v, const int32_t* solid,
+                                           const double* w, double rho0, const double* u0) {
+  lbm_init_impl<double>(nx, ny, nz, f, F, rho, v, solid, w, rho0, u0);
+}
+
+// MPMSolver3D.substep, fsi/mpm3d.py:189-203: clear_grid -> p2g -> grid_op -> g2p.
+// `deterministic` != 0 runs P2G serially in particle order; otherwise P2G runs
+// on `nthreads` threads with atomic adds, like a parallel Taichi CPU loop.
+template <class T>
+static void mpm_substep_impl(int nx, int ny, int nz, int n, T* x, T* v, T* C, T* Fd, const T* mass,
+                             const T* vol, const int32_t* active, T* fp, T* gv, T* gm, T dt, T dx,
+                             T inv_dx, T mu, T lam, const T* gravity, int bw, T damping, int apic,
+                             T lower, const T* upper, int nthreads, int deterministic) {
+  Particles<T> P{n, x, v, C, Fd, mass, vol, active, fp};
+  Grid<T> G{nx, ny, nz, gv, gm};
+  MpmParams<T> mp{dt, dx, inv_dx, mu, lam, {gravity[0], gravity[1], gravity[2]}, damping, bw, apic};
+  const long N = (long)nx * ny * nz;
+  std::memset(gv, 0, sizeof(T) * 3 * N);
+  std::memset(gm, 0, sizeof(T) * N);
+  if (deterministic) {
+    for (int p = 0; p < n; ++p) p2g_particle(p, P, G, mp, false);
+  } else {
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads))
+    for (int p = 0; p < n; ++p) p2g_particle(p, P, G, mp, true);
+  }
+  grid_op(G, mp, deterministic ? 1 : nthreads);
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads))
+  for (int p = 0; p < n; ++p) g2p_particle(p, P, G, mp, lower, upper);
+}
+
+FSI_ORACLE_EXPORT void oracle_mpm_substep_f32(int nx, int ny, int nz, int n, float* x, float* v,
+                                              float* C, float* Fd, const float* mass,
+                                              const float* vol, const int32_t* active, float* fp,
+                                              float* gv, float* gm, float dt, float dx,
+                                              float inv_dx, float mu, float lam,
+                                              const float* gravity, int bw, float damping, int apic,
+                                              float lower, const float* upper, int nthreads,
+                                              int deterministic) {
+  mpm_substep_impl<float>(nx, ny, nz, n, x, v, C, Fd, mass, vol, active, fp, gv, gm, dt, dx, inv_dx,
+                          mu, lam, gravity, bw, damping, apic, lower, upper, nthreads,
+                          deterministic);
+}
+
+FSI_ORACLE_EXPORT void oracle_mpm_substep_f64(int nx, int ny, int nz, int n, double* x, double* v,
+                                              double* C, double* Fd, const double* mass,
+                                              const double* vol, const int32_t* active, double* fp,
+                                              double* gv, double* gm, double dt, double dx,
+                                              double inv_dx, double mu, double lam,
+                                              const double* gravity, int bw, double damping,
+                                              int apic, double lower, const double* upper,
+                                              int nthreads, int deterministic) {
+  mpm_substep_impl<double>(nx, ny, nz, n, x, v, C, Fd, mass, vol, active, fp, gv, gm, dt, dx,
+                           inv_dx, mu, lam, gravity, bw, damping, apic, lower, upper, nthreads,
+                           deterministic);
+}
+
+// Polar rotation of 3x3 matrices (row-major), for checking the device routine.
+FSI_ORACLE_EXPORT void oracle_polar_rotation_f64(int n, const double* F, double* R) {
+  for (int i = 0; i < n; ++i) polar_rotation_f64(F + 9 * i, R + 9 * i);
+}
+
+// _compute_coupling_forces_kernel, fsi/coupling.py:332-406 (serial particle order).
+// counters[0..2] += unsupported, partial, clipped.
+template <class T>
+static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv, const T* mass,
+                          const T* vol, const int32_t* active, T* fp, const T* lbm_v,
+                          const int32_t* solid, T* cforce, T* phi, T* valid_out, int32_t* mask_out,
+                          int32_t* counters, T inv_dx, T gamma_eff, T dt_ratio, T cell_volume,
+                          int build_fraction, T min_valid_weight, int use_rel, T rel_limit,
+                          int use_force_limit, T force_limit) {
+  Grid<T> G{nx, ny, nz, nullptr, nullptr};
+  const T support_tolerance = (T)1.0e-5;
+  for (int p = 0; p < n; ++p) {
+    if (active[p] == 0) continue;
+    T xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+    int base[3];
+    T fx[3];
+    base_fx(xp, inv_dx, base, fx);
+    T w[3][3];
+    for (int a = 0; a < 3; ++a) {
+      T ww[3];
+      bspline(fx[a], ww);
+      for (int i = 0; i < 3; ++i) w[i][a] = ww[i];
+    }
+    T valid = 0;
+    T uf[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+          if (!G.inside(ni, nj, nk)) continue;
+          long c = G.cell(ni, nj, nk);
+          if (solid[c] != 0) continue;
+          T weight = (w[i][0] * w[j][1]) * w[k][2];
+          valid = valid + weight;
+          for (int a = 0; a < 3; ++a) uf[a] = uf[a] + weight * lbm_v[3 * c + a];
+        }
+    valid_out[p] = valid;
+    if (valid > min_valid_weight) {
+      if (valid < (T)1.0 - support_tolerance) counters[1] += 1;
+      T dv[3];
+      for (int a = 0; a < 3; ++a) {
+        uf[a] = uf[a] / valid;
+        dv[a] = uf[a] - pv[3 * p + a];
+      }
+      int clipped = 0;
+      if (use_rel) {
+        T nrm = std::sqrt(dot3(dv, dv));
+        if (nrm > rel_limit && nrm > (T)0) {
+          for (int a = 0; a < 3; ++a) dv[a] = (dv[a] / nrm) * rel_limit;
+          clipped = 1;
+        }
+      }
+      T pf[3];
+      for (int a = 0; a < 3; ++a) pf[a] = (gamma_eff * mass[p]) * dv[a];
+      if (use_force_limit) {
+        T nrm = std::sqrt(dot3(pf, pf));
+        if (nrm > force_limit && nrm > (T)0) {
+          for (int a = 0; a < 3; ++a) pf[a] = (pf[a] / nrm) * force_limit;
+          clipped = 1;
+        }
+      }
+      for (int a = 0; a < 3; ++a) fp[3 * p + a] = pf[a];
+      mask_out[p] = 1;
+      if (clipped) counters[2] += 1;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int k = 0; k < 3; ++k) {
+            int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+            if (!G.inside(ni, nj, nk)) continue;
+            long c = G.cell(ni, nj, nk);
+            if (solid[c] != 0) continue;
+            T weight = (w[i][0] * w[j][1]) * w[k][2];
+            T nw = weight / valid;
+            for (int a = 0; a < 3; ++a) {
+              T add = (((-nw) * pf[a]) * dt_ratio) / cell_volume;
+              cforce[3 * c + a] = cforce[3 * c + a] + add;
+            }
+            if (build_fraction) phi[c] = phi[c] + (nw * vol[p]) / cell_volume;
+          }
+    } else {
+      fp[3 * p] = fp[3 * p + 1] = fp[3 * p + 2] = 0;
+      mask_out[p] = 0;
+      counters[0] += 1;
+    }
+  }
+}
+
+FSI_ORACLE_EXPORT void oracle_coupling_f32(int nx, int ny, int nz, int n, const float* x,
+                                           const float* pv, const float* mass, const float* vol,
+                                           const int32_t* active, float* fp, const float* lbm_v,
+                                           const int32_t* solid, float* cforce, float* phi,
+                                           float* valid_out, int32_t* mask_out, int32_t* counters,
+                                           float inv_dx, float gamma_eff, float dt_ratio,
+                                           float cell_volume, int build_fraction,
+                                           float min_valid_weight, int use_rel, float rel_limit,
+                                           int use_force_limit, float force_limit) {
+  coupling_impl<float>(nx, ny, nz, n, x, pv, mass, vol, active, fp, lbm_v, solid, cforce, phi,
+                       valid_out, mask_out, counters, inv_dx, gamma_eff, dt_ratio, cell_volume,
+                       build_fraction, min_valid_weight, use_rel, rel_limit, use_force_limit,
+                       force_limit);
+}
+
+FSI_ORACLE_EXPORT void oracle_coupling_f64(int nx, int ny, int nz, int n, const double* x,
+                                           const double* pv, const double* mass, const double* vol,
+                                           const int32_t* active, double* fp, const double* lbm_v,
+                                           const int32_t* solid, double* cforce, double* phi,
+                                           double* valid_out, int32_t* mask_out, int32_t* counters,
+                                           double inv_dx, double gamma_eff, double dt_ratio,
+                                           double cell_volume, int build_fraction,
+                                           double min_valid_weight, int use_rel, double rel_limit,
+                                           int use_force_limit, double force_limit) {
+  coupling_impl<double>(nx, ny, nz, n, x, pv, mass, vol, active, fp, lbm_v, solid, cforce, phi,
+                        valid_out, mask_out, counters, inv_dx, gamma_eff, dt_ratio, cell_volume,
+                        build_fraction, min_valid_weight, use_rel, rel_limit, use_force_limit,
+                        force_limit);
+}
+
+// _compute_immersed_boundary_force_kernel, fsi/coupling.py:421-452 (serial cell order).
+// counters[0..1] = active, clipped; total[3] = summed force.
+template <class T>
+static void ib_impl(long ncell, const T* phi, const T* rho, const T* v, const int32_t* solid,
+                    T* ib, int32_t* counters, T* total, int enabled, T drag, T threshold,
+                    int use_max, T max_force) {
+  counters[0] = counters[1] = 0;
+  total[0] = total[1] = total[2] = 0;
+  for (long c = 0; c < ncell; ++c) {
+    T f[3] = {0, 0, 0};
+    if (enabled != 0 && drag > (T)0 && solid[c] == 0) {
+      T ph = phi[c];
+      if (ph > (T)0 && ph >= threshold) {
+        T s = ((-drag) * ph) * rho[c];
+        for (int a = 0; a < 3; ++a) f[a] = s * v[3 * c + a];
+        T nrm = std::sqrt(dot3(f, f));
+        if (use_max != 0 && nrm > max_force && nrm > (T)0) {
+          for (int a = 0; a < 3; ++a) f[a] = (f[a] / nrm) * max_force;
+          counters[1] += 1;
+        }
+        counters[0] += 1;
+        for (int a = 0; a < 3; ++a) total[a] = total[a] + f[a];
+      }
+    }
+    for (int a = 0; a < 3; ++a) ib[3 * c + a] = f[a];
+  }
+}
+
+FSI_ORACLE_EXPORT void oracle_ib_f32(long ncell, const float* phi, const float* rho,
+                                     const float* v, const int32_t* solid, float* ib,
+                                     int32_t* counters, float* total, int enabled, float drag,
+                                     float threshold, int use_max, float max_force) {
+  ib_impl<float>(ncell, phi, rho, v, solid, ib, counters, total, enabled, drag, threshold, use_max,
+                 max_force);
+}
+
+FSI_ORACLE_EXPORT void oracle_ib_f64(long ncell, const double* phi, const double* rho,
+                                     const double* v, const int32_t* solid, double* ib,
+                                     int32_t* counters, double* total, int enabled, double drag,
+                                     double threshold, int use_max, double max_force) {
+  ib_impl<double>(ncell, phi, rho, v, solid, ib, counters, total, enabled, drag, threshold,
+                  use_max, max_force);
+}
+
+// _compute_contact_diagnostics_kernel, fsi/coupling.py:463-496.
+// counters[0..1] = candidates, damped.
+template <class T>
+static void contact_impl(int nx, int ny, int nz, int n, const T* x, T* pv, const int32_t* active,
+                         const T* phi, const int32_t* solid, int32_t* mask, int32_t* counters,
+                         T inv_dx, int enabled, T threshold, T damping) {
+  Grid<T> G{nx, ny, nz, nullptr, nullptr};
+  counters[0] = counters[1] = 0;
+  for (int p = 0; p < n; ++p) {
+    mask[p] = 0;
+    if (enabled == 0 || active[p] == 0) continue;
+    T xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+    int base[3];
+    T fx[3];
+    base_fx(xp, inv_dx, base, fx);
+    T w[3][3];
+    for (int a = 0; a < 3; ++a) {
+      T ww[3];
+      bspline(fx[a], ww);
+      for (int i = 0; i < 3; ++i) w[i][a] = ww[i];
+    }
+    T dyn = 0, stat = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+          if (!G.inside(ni, nj, nk)) continue;
+          long c = G.cell(ni, nj, nk);
+          T weight = (w[i][0] * w[j][1]) * w[k][2];
+          dyn = dyn + weight * phi[c];
+          if (solid[c] != 0) stat = stat + weight;
+        }
+    if (dyn >= threshold || stat >= threshold) {
+      mask[p] = 1;
+      counters[0] += 1;
+      if (damping > (T)0) {
+        T s = (T)1.0 - damping;
+        for (int a = 0; a < 3; ++a) pv[3 * p + a] = pv[3 * p + a] * s;
+        counters[1] += 1;
+      }
+    }
+  }
+}
+
+FSI_ORACLE_EXPORT void oracle_contact_f32(int nx, int ny, int nz, int n, const float* x, float* pv,
+                                          const int32_t* active, const float* phi,
+                                          const int32_t* solid, int32_t* mask, int32_t* counters,
+                                          float inv_dx, int enabled, float threshold,
+                                          float damping) {
+  contact_impl<float>(nx, ny, nz, n, x, pv, active, phi, solid, mask, counters, inv_dx, enabled,
+                      threshold, damping);
+}
+
+FSI_ORACLE_EXPORT void oracle_contact_f64(int nx, int ny, int nz, int n, const double* x,
+                                          double* pv, const int32_t* active, const double* phi,
+                                          const int32_t* solid, int32_t* mask, int32_t* counters,
+                                          double inv_dx, int enabled, double threshold,
+                                          double damping) {
+  contact_impl<double>(nx, ny, nz, n, x, pv, active, phi, solid, mask, counters, inv_dx, enabled,
+                       threshold, damping);
+}
+
+FSI_ORACLE_EXPORT int oracle_max_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
