@@ -1,0 +1,265 @@
+/*
+ * fsi_gb300.h -- C ABI of the GB300 (sm_103a) coupled LBM-MPM timestep.
+ *
+ * Each entry point replaces one or more Taichi kernels of the reference
+ * lizhuoh9/taichi-mpm-lbm (cited as file:line). Conventions:
+ *   - all array arguments are device pointers owned by the caller (the Python
+ *     package allocates them as torch CUDA tensors); the library never
+ *     allocates or frees device memory;
+ *   - descriptor structs and small `const float*` parameter vectors marked
+ *     "host" are read on the host during the call;
+ *   - work is enqueued on `stream` (a cudaStream_t passed as void*, NULL = the
+ *     legacy default stream) and runs asynchronously;
+ *   - the return value is an FSI_* status; on failure fsi_last_error()
+ *     returns a message. No C++ exception crosses this boundary.
+ *
+ * Data layouts (N = nx*ny*nz cells, linear cell c = (i*ny + j)*nz + k, i.e.
+ * the C order of the reference's numpy arrays):
+ *   pops    float[19][N]  populations, structure of arrays, AA-pattern storage
+ *   macro   float[N][4]   (ux, uy, uz, rho) per cell
+ *   force   float[3][N]   body force density, structure of arrays
+ *   flags   uint32[N]     bit 0 solid; bit q (1..18) neighbour x+e_q solid;
+ *                         bit 20/21 x=0 / x=nx-1 face cell
+ *   solid   int32[N]      0/1 solid mask as the reference stores it
+ */
+#ifndef FSI_GB300_H
+#define FSI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSI_OK 0
+#define FSI_ERR_INVALID_ARG 1
+#define FSI_ERR_CUDA 2
+#define FSI_ERR_GUARD 3
+#define FSI_ERR_TIMEOUT 4
+#define FSI_ERR_UNSUPPORTED 5
+
+#define FSI_ABI_VERSION 1
+
+/* Library ABI version (FSI_ABI_VERSION). No reference counterpart. */
+int fsi_abi_version(void);
+
+/* Copies the last error message of the calling thread into buf (NUL-terminated);
+ * returns the message length. No reference counterpart (Taichi raises Python
+ * exceptions directly). */
+size_t fsi_last_error(char* buf, size_t len);
+
+/* ------------------------------------------------------------------ LBM -- */
+
+/* Lattice description. Replaces the scalar fields of LBMSolver3D
+ * (fsi/lbm3d.py:110-191): relaxation rates, rho0 and the x-face conditions. */
+typedef struct fsi_lbm_desc {
+  int32_t nx, ny, nz;
+  int32_t bc_mode_left;   /* x = 0 face: 0 periodic, 1 pressure, 2 velocity (lbm3d.py:16-27) */
+  int32_t bc_mode_right;  /* x = nx-1 face, same codes */
+  float s[19];            /* MRT relaxation rates S_k (lbm3d.py:141-168) */
+  float rho0;
+  float bc_rho_left, bc_rho_right;
+  float bc_vel_left[3], bc_vel_right[3];
+} fsi_lbm_desc;
+
+/* Builds the per-cell flag word from the normalised 0/1 mask.
+ * Replaces the neighbour tests of LBMSolver3D.stream (fsi/lbm3d.py:335-361),
+ * evaluated once at initialisation instead of every step. */
+int fsi_lbm_build_flags(const fsi_lbm_desc* desc, const int32_t* solid, uint32_t* flags,
+                        void* stream);
+
+/* Equilibrium initialisation: rho = rho0, u = u0 (0 on solid cells),
+ * populations = feq(rho0, u). u0 is host float[3].
+ * Replaces LBMSolver3D.init_fields (fsi/lbm3d.py:256-267). */
+int fsi_lbm_init_fields(const fsi_lbm_desc* desc, const uint32_t* flags, const float* u0,
+                        float* pops, float* macro, void* stream);
+
+/* One lattice step: collide (MRT + Guo forcing) and stream (half-way
+ * bounce-back, periodic wrap) in one in-place AA-pattern pass, followed by the
+ * x-face conditions. `steps_done` is the number of steps already taken (its
+ * parity selects the AA access pattern).
+ *   force_prev == NULL: rho and u of the current state are read from `macro`
+ *                       (valid after fsi_lbm_init_fields / fsi_lbm_update_macro);
+ *   force_prev != NULL: they are recomputed in-register from the populations and
+ *                       force_prev, the force the previous step used, exactly as
+ *                       update_macro would have stored them.
+ * `macro` is left stale except on x-face cells; call fsi_lbm_update_macro to
+ * materialise rho and u of the new state.
+ * Replaces LBMSolver3D.collide/stream/apply_boundary (fsi/lbm3d.py:314-407,
+ * called from step() at lbm3d.py:427-433). */
+int fsi_lbm_step(const fsi_lbm_desc* desc, float* pops, float* macro, const float* force,
+                 const float* force_prev, const uint32_t* flags, int64_t steps_done,
+                 void* stream);
+
+/* rho = sum f, u = sum e f / rho + force / (2 rho) on fluid cells; rho0 and 0
+ * on solid cells. `force` is the force of the last step.
+ * Replaces LBMSolver3D.update_macro (fsi/lbm3d.py:409-425). */
+int fsi_lbm_update_macro(const fsi_lbm_desc* desc, const float* pops, const float* force,
+                         const uint32_t* flags, int64_t steps_done, float* macro,
+                         void* stream);
+
+/* Writes the post-stream distribution in the reference layout float[N][19].
+ * Replaces LBMSolver3D.distribution_numpy (fsi/lbm3d.py:444-445). */
+int fsi_lbm_distribution(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
+                         int64_t steps_done, float* out, void* stream);
+
+/* Force-field operations on float[3][N] (value is host float[3]):
+ *   FSI_FORCE_CLEAR     out = 0                         (lbm3d.py:499-502)
+ *   FSI_FORCE_SET       out = fluid ? value : 0          (lbm3d.py:504-519)
+ *   FSI_FORCE_ADD       out = fluid ? in + value : 0     (lbm3d.py:521-528)
+ *   FSI_FORCE_ZERO_SOLID out = fluid ? in : 0            (lbm3d.py:530-534)
+ * `in` may equal `out`. */
+#define FSI_FORCE_CLEAR 0
+#define FSI_FORCE_SET 1
+#define FSI_FORCE_ADD 2
+#define FSI_FORCE_ZERO_SOLID 3
+int fsi_lbm_force_op(const fsi_lbm_desc* desc, const uint32_t* flags, int op, const float* in,
+                     const float* value, float* out, void* stream);
+
+/* Lattice diagnostics into device double[8]:
+ *   [0] sum of rho over fluid cells            (total_mass, lbm3d.py:450-453)
+ *   [1] max |u| over all cells                 (max_velocity_norm, lbm3d.py:455-457)
+ *   [2..4] sum of force over fluid cells       (total_force, lbm3d.py:480-483)
+ * `out` must be zero-initialised except that it is overwritten here. */
+int fsi_lbm_reduce(const fsi_lbm_desc* desc, const float* macro, const float* force,
+                   const uint32_t* flags, double* out, void* stream);
+
+/* ------------------------------------------------------------------ MPM -- */
+
+/* Solid (MLS-MPM) description. Replaces the scalar fields of MPMSolver3D
+ * (fsi/mpm3d.py:17-67). mu and lam are the Lame parameters of mpm3d.py:33-38;
+ * clamp_lower / clamp_upper the position limits of mpm3d.py:320-328. */
+typedef struct fsi_mpm_desc {
+  int32_t nx, ny, nz;
+  int32_t num_particles; /* particles live in slots [0, num_particles) */
+  float dt, dx, inv_dx;
+  float mu, lam;
+  float gravity[3];
+  float boundary_damping;
+  int32_t boundary_width;
+  int32_t apic;
+  float clamp_lower;
+  float clamp_upper[3];
+} fsi_mpm_desc;
+
+/* Particle arrays, structure of arrays with component stride `capacity`:
+ * x, v, force float[3][capacity]; C, F float[9][capacity] (row-major 3x3
+ * components); mass, volume float[capacity]; active int32[capacity].
+ * Replaces the particle fields of mpm3d.py:44-55. */
+typedef struct fsi_particles {
+  float* x;
+  float* v;
+  float* C;
+  float* F;
+  float* mass;
+  float* volume;
+  int32_t* active;
+  float* force;
+  int64_t capacity;
+} fsi_particles;
+
+/* One MPM substep: P2G (deformation update, fixed-corotated stress, 27-node
+ * scatter), grid update and G2P (APIC gather, advection, clamp).
+ * `grid` is float[N][4] (momentum xyz, mass), 16-byte aligned, all zero on
+ * entry and left all zero on return; `dirty` is uint8[ceil(nx/4)*ceil(ny/4)*
+ * ceil(nz/4)], zero on entry and on return. dt is desc->dt.
+ * Replaces MPMSolver3D.clear_grid/p2g/grid_op/g2p (fsi/mpm3d.py:189-318). */
+int fsi_mpm_substep(const fsi_mpm_desc* desc, const fsi_particles* particles, float* grid,
+                    uint8_t* dirty, void* stream);
+
+/* Rotation R of the polar decomposition of n row-major 3x3 matrices (float[n][9]).
+ * Replaces the ti.svd call of MPMSolver3D.p2g (fsi/mpm3d.py:245-246). */
+int fsi_mpm_polar(const float* F, float* R, int64_t n, void* stream);
+
+/* Particle-to-cell indices base = trunc(x * inv_dx - 0.5) as int32[n][3].
+ * Exposes the index computation of mpm3d.py:239 and coupling.py:343-344. */
+int fsi_mpm_base_cells(const fsi_mpm_desc* desc, const fsi_particles* particles, int32_t* out,
+                       void* stream);
+
+/* Particle diagnostics into device double[8]: [0] sum m, [1..3] sum m x,
+ * [4] max |v|, [5..7] sum particle force. Replaces the host reductions of
+ * center_of_mass / max_velocity_norm (mpm3d.py:353-368) and
+ * total_particle_coupling_force (coupling.py:226-227). `reserved` must be NULL. */
+int fsi_mpm_reduce(const fsi_mpm_desc* desc, const fsi_particles* particles, double* out,
+                   void* reserved, void* stream);
+
+/* ------------------------------------------------------------- coupling -- */
+
+/* Coupling parameters (CouplingConfig, fsi/config.py:141-196, as the fields of
+ * LBMMpmCoupler, fsi/coupling.py:58-133). gamma_eff is the ramped gamma of
+ * coupling.py:321-330 for the current coupled step. */
+typedef struct fsi_coupling_desc {
+  float gamma_eff;
+  float dt_ratio;
+  float cell_volume;
+  float inv_dx;
+  float min_valid_weight;
+  float rel_limit;
+  float force_limit;
+  int32_t build_fraction;
+  int32_t use_rel_limit;
+  int32_t use_force_limit;
+  int32_t ib_enabled;
+  float ib_drag;
+  float ib_threshold;
+  int32_t ib_use_max;
+  float ib_max_force;
+  int32_t contact_enabled;
+  float contact_threshold;
+  float contact_damping;
+} fsi_coupling_desc;
+
+/* Device-side counters of one coupled step (coupling.py:79-92). */
+typedef struct fsi_coupling_counters {
+  int32_t unsupported, partial, clipped;
+  int32_t contact_candidates, contact_damped;
+  int32_t ib_active, ib_clipped;
+  int32_t reserved;
+  float ib_total[4];
+} fsi_coupling_counters;
+
+/* Penalty coupling of every particle against the current fluid velocity
+ * (`macro`, float[N][4]): writes particle force, valid weight and coupling
+ * mask (0 for inactive particles), increments the unsupported / partial /
+ * clipped counters, and adds the fluid reaction (xyz) and, if
+ * desc->build_fraction, the solid volume fraction (w) into `accum` float[N][4].
+ * Replaces _compute_coupling_forces_kernel (fsi/coupling.py:332-406). */
+int fsi_coupling_forces(const fsi_coupling_desc* desc, const fsi_mpm_desc* mpm,
+                        const fsi_particles* particles, const float* macro,
+                        const uint32_t* flags, float* accum, float* valid_weight,
+                        int32_t* coupling_mask, void* counters, void* stream);
+
+/* Rebuilds the LBM force field float[3][N] for the next lattice step:
+ *   FSI_ASSEMBLE_CLAMP_FRACTION  accum.w = min(accum.w, 1)   (coupling.py:408-411)
+ *   (always)                     force = fluid ? base : 0     (lbm3d.py:504-510)
+ *   FSI_ASSEMBLE_COUPLING        force += accum.xyz on fluid  (coupling.py:413-419)
+ *   FSI_ASSEMBLE_IB              Brinkman drag into ib_force float[3][N], counters
+ *                                and totals, force += ib      (coupling.py:421-461)
+ * base_force is host float[3]; force may be NULL to update accum/ib_force only.
+ * IB counters/totals must be zeroed by the caller. */
+#define FSI_ASSEMBLE_CLAMP_FRACTION 1
+#define FSI_ASSEMBLE_COUPLING 2
+#define FSI_ASSEMBLE_IB 4
+int fsi_coupling_assemble(const fsi_coupling_desc* desc, const fsi_lbm_desc* lbm,
+                          const uint32_t* flags, const float* base_force, int mode, float* accum,
+                          const float* macro, float* force, float* ib_force, void* counters,
+                          void* stream);
+
+/* Contact detection and damping after an MPM substep; resets and fills the
+ * contact counters and the contact mask.
+ * Replaces _compute_contact_diagnostics_kernel (fsi/coupling.py:463-496). */
+int fsi_contact(const fsi_coupling_desc* desc, const fsi_mpm_desc* mpm,
+                const fsi_particles* particles, const float* accum, const uint32_t* flags,
+                int32_t* contact_mask, void* counters, void* stream);
+
+/* Sum of the fluid reaction force density over fluid cells into device
+ * double[4] ([0..2]). Replaces total_fluid_coupling_force (coupling.py:229-232). */
+int fsi_coupling_reduce(const fsi_lbm_desc* lbm, const float* accum, const uint32_t* flags,
+                        double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FSI_GB300_H */

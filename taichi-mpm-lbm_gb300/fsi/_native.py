@@ -1,0 +1,187 @@
+"""ctypes binding of the sm_103a library ``_lib/libfsi_gb300.so`` (C ABI: include/fsi_gb300.h).
+
+The library is built in-tree by ``build_native.py``. There is no CPU fallback:
+every solver call goes through this module, and a missing library or CUDA
+device raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import torch
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfsi_gb300.so"
+_lib = None
+
+FSI_OK = 0
+FSI_ERR_INVALID_ARG = 1
+FSI_ERR_CUDA = 2
+FSI_ERR_GUARD = 3
+FSI_ERR_TIMEOUT = 4
+FSI_ERR_UNSUPPORTED = 5
+ABI_VERSION = 1
+
+FORCE_CLEAR, FORCE_SET, FORCE_ADD, FORCE_ZERO_SOLID = 0, 1, 2, 3
+ASSEMBLE_CLAMP_FRACTION, ASSEMBLE_COUPLING, ASSEMBLE_IB = 1, 2, 4
+
+c_float3 = ctypes.c_float * 3
+
+
+class LbmDesc(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("bc_mode_left", ctypes.c_int32), ("bc_mode_right", ctypes.c_int32),
+        ("s", ctypes.c_float * 19),
+        ("rho0", ctypes.c_float),
+        ("bc_rho_left", ctypes.c_float), ("bc_rho_right", ctypes.c_float),
+        ("bc_vel_left", c_float3), ("bc_vel_right", c_float3),
+    ]
+
+
+class MpmDesc(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("num_particles", ctypes.c_int32),
+        ("dt", ctypes.c_float), ("dx", ctypes.c_float), ("inv_dx", ctypes.c_float),
+        ("mu", ctypes.c_float), ("lam", ctypes.c_float),
+        ("gravity", c_float3),
+        ("boundary_damping", ctypes.c_float),
+        ("boundary_width", ctypes.c_int32),
+        ("apic", ctypes.c_int32),
+        ("clamp_lower", ctypes.c_float),
+        ("clamp_upper", c_float3),
+    ]
+
+
+class Particles(ctypes.Structure):
+    _fields_ = [
+        ("x", ctypes.c_void_p), ("v", ctypes.c_void_p), ("C", ctypes.c_void_p),
+        ("F", ctypes.c_void_p), ("mass", ctypes.c_void_p), ("volume", ctypes.c_void_p),
+        ("active", ctypes.c_void_p), ("force", ctypes.c_void_p),
+        ("capacity", ctypes.c_int64),
+    ]
+
+
+class CouplingDesc(ctypes.Structure):
+    _fields_ = [
+        ("gamma_eff", ctypes.c_float),
+        ("dt_ratio", ctypes.c_float),
+        ("cell_volume", ctypes.c_float),
+        ("inv_dx", ctypes.c_float),
+        ("min_valid_weight", ctypes.c_float),
+        ("rel_limit", ctypes.c_float),
+        ("force_limit", ctypes.c_float),
+        ("build_fraction", ctypes.c_int32),
+        ("use_rel_limit", ctypes.c_int32),
+        ("use_force_limit", ctypes.c_int32),
+        ("ib_enabled", ctypes.c_int32),
+        ("ib_drag", ctypes.c_float),
+        ("ib_threshold", ctypes.c_float),
+        ("ib_use_max", ctypes.c_int32),
+        ("ib_max_force", ctypes.c_float),
+        ("contact_enabled", ctypes.c_int32),
+        ("contact_threshold", ctypes.c_float),
+        ("contact_damping", ctypes.c_float),
+    ]
+
+
+_VP = ctypes.c_void_p
+_SIGNATURES = {
+    "fsi_abi_version": ([], ctypes.c_int),
+    "fsi_last_error": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_size_t),
+    "fsi_lbm_build_flags": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP], ctypes.c_int),
+    "fsi_lbm_init_fields": ([ctypes.POINTER(LbmDesc), _VP, ctypes.POINTER(ctypes.c_float), _VP, _VP, _VP], ctypes.c_int),
+    "fsi_lbm_step": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "fsi_lbm_update_macro": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "fsi_lbm_distribution": ([ctypes.POINTER(LbmDesc), _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "fsi_lbm_force_op": ([ctypes.POINTER(LbmDesc), _VP, ctypes.c_int, _VP, ctypes.POINTER(ctypes.c_float), _VP, _VP], ctypes.c_int),
+    "fsi_lbm_reduce": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_mpm_substep": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),
+    "fsi_mpm_polar": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "fsi_mpm_base_cells": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP], ctypes.c_int),
+    "fsi_mpm_reduce": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),
+    "fsi_coupling_forces": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_coupling_assemble": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(LbmDesc), _VP, ctypes.POINTER(ctypes.c_float), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_contact": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_coupling_reduce": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP], ctypes.c_int),
+}
+
+
+class NativeError(RuntimeError):
+    """A C ABI call returned a non-OK status."""
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("FSI_GB300_LIB", str(_LIB_PATH)))
+
+
+def load():
+    """Load and bind the native library; raises RuntimeError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        raise RuntimeError(
+            f"native library {path} is missing: build it with "
+            "`python taichi-mpm-lbm_gb300/build_native.py` (no CPU fallback exists)."
+        )
+    lib = ctypes.CDLL(str(path))
+    for name, (argtypes, restype) in _SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.argtypes = argtypes
+        fn.restype = restype
+    if lib.fsi_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{path}: ABI version {lib.fsi_abi_version()} != {ABI_VERSION}")
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+def last_error() -> str:
+    lib = load()
+    buf = ctypes.create_string_buffer(512)
+    lib.fsi_last_error(buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def call(name: str, *args) -> None:
+    """Invoke an entry point and translate its status into a Python exception."""
+    lib = load()
+    status = getattr(lib, name)(*args)
+    if status != FSI_OK:
+        msg = f"{name} failed ({status}): {last_error()}"
+        if status == FSI_ERR_INVALID_ARG:
+            raise ValueError(msg)
+        raise NativeError(msg)
+
+
+def device() -> torch.device:
+    """The CUDA device the solvers allocate on; raises if CUDA is unavailable."""
+    if not torch.cuda.is_available():
+        raise RuntimeError(
+            "fsi requires a CUDA device (sm_103a); this build has no CPU fallback."
+        )
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def ptr(t: torch.Tensor | None):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def vec3(values) -> ctypes.Array:
+    a = c_float3()
+    for i in range(3):
+        a[i] = float(values[i])
+    return a

@@ -1,0 +1,273 @@
+"""Explicit penalty LBM-MPM coupling on the GPU (drop-in for the reference's fsi/coupling.py).
+
+Per coupled step the coupler runs ``substeps`` x [penalty coupling kernel, MPM
+substep, optional contact kernel] against the fluid velocity of the last
+lattice step, then one assembly kernel that clamps the solid fraction and
+rebuilds the lattice force (base + coupling reaction + optional immersed
+boundary drag), then one lattice step. The fluid reaction force density and
+the solid volume fraction share one float4 accumulator per cell; counters
+live in a small device struct.
+
+Public methods, accessors, diagnostics keys and exceptions follow
+fsi/coupling.py:11-496.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .config import CouplingConfig
+from .lbm3d import LBMSolver3D
+from .mpm3d import MPMSolver3D
+
+_SUPPORT_TOLERANCE = 1.0e-5
+
+
+class LBMMpmCoupler:
+    """Explicit partitioned penalty coupling between the LBM and MPM solvers."""
+
+    def __init__(self, config: CouplingConfig, lbm: LBMSolver3D, mpm: MPMSolver3D):
+        self.config = config
+        self.config.validate()
+        self.lbm = lbm
+        self.mpm = mpm
+        self._validate_solver_contract()
+        self.enabled = bool(config.enabled)
+        self.build_solid_volume_fraction = bool(config.build_solid_volume_fraction)
+        self.immersed_boundary_enabled = bool(config.immersed_boundary_enabled)
+        self.contact_enabled = bool(config.contact_enabled)
+        self.substeps = int(config.mpm_substeps_per_lbm_step)
+        self.nx, self.ny, self.nz = int(lbm.nx), int(lbm.ny), int(lbm.nz)
+        self.inv_dx = 1.0 / float(mpm.dx)
+        self.cell_volume = float(mpm.dx) ** 3
+
+        dev = nat.device()
+        n = self.nx * self.ny * self.nz
+        cap = mpm.max_particles
+        self._accum = torch.zeros((n, 4), dtype=torch.float32, device=dev)  # reaction xyz, phi
+        self._ib = torch.zeros((3, n), dtype=torch.float32, device=dev)
+        self._valid = torch.zeros(cap, dtype=torch.float32, device=dev)
+        self._mask = torch.zeros(cap, dtype=torch.int32, device=dev)
+        self._contact_mask = torch.zeros(cap, dtype=torch.int32, device=dev)
+        self._counters = torch.zeros(12, dtype=torch.int32, device=dev)  # fsi_coupling_counters
+        self._diag = torch.zeros(4, dtype=torch.float64, device=dev)
+        self._coupled_step = 0
+        self._desc = nat.CouplingDesc()
+        self._fill_desc()
+
+    def _validate_solver_contract(self) -> None:
+        if self.config.kernel != "quadratic":
+            raise ValueError(f"Unsupported coupling kernel: {self.config.kernel}.")
+        lbm_shape = (self.lbm.nx, self.lbm.ny, self.lbm.nz)
+        mpm_shape = (self.mpm.nx, self.mpm.ny, self.mpm.nz)
+        if lbm_shape != mpm_shape:
+            raise ValueError(
+                "LBM and MPM grids must match for Step 5 coupling. "
+                f"Got LBM={lbm_shape}, MPM={mpm_shape}."
+            )
+        if self.mpm.dx <= 0.0:
+            raise ValueError("MPM dx must be positive.")
+
+    def _fill_desc(self) -> None:
+        c, d = self.config, self._desc
+        f32 = lambda v: float(np.float32(v))  # noqa: E731
+        d.cell_volume = f32(self.cell_volume)
+        d.inv_dx = f32(self.inv_dx)
+        d.min_valid_weight = f32(c.min_valid_weight)
+        d.use_rel_limit = int(c.relative_velocity_limit is not None)
+        d.rel_limit = f32(c.relative_velocity_limit or 0.0)
+        d.use_force_limit = int(c.force_limit is not None)
+        d.force_limit = f32(c.force_limit or 0.0)
+        d.ib_enabled = int(self.immersed_boundary_enabled)
+        d.ib_drag = f32(c.immersed_boundary_drag)
+        d.ib_threshold = f32(c.immersed_boundary_fraction_threshold)
+        d.ib_use_max = int(c.immersed_boundary_max_force is not None)
+        d.ib_max_force = f32(c.immersed_boundary_max_force or 0.0)
+        d.contact_enabled = int(self.contact_enabled)
+        d.contact_threshold = f32(c.contact_fraction_threshold)
+        d.contact_damping = f32(c.contact_velocity_damping)
+
+    # ------------------------------------------------------------ stepping
+    def _gamma_for_kernel(self) -> float:
+        """_effective_gamma of coupling.py:321-330, evaluated in float32."""
+        g = np.float32(self.config.gamma)
+        ramp = int(self.config.gamma_ramp_steps)
+        if ramp > 0:
+            r = (np.float32(self._coupled_step) + np.float32(1.0)) / np.float32(ramp)
+            g = np.float32(g * min(np.float32(1.0), r))
+        return float(g)
+
+    def _coupling_kernel(self, dt_ratio: float, build_fraction: bool) -> None:
+        self._desc.gamma_eff = self._gamma_for_kernel()
+        self._desc.dt_ratio = float(np.float32(dt_ratio))
+        self._desc.build_fraction = int(build_fraction)
+        nat.call("fsi_coupling_forces", self._desc, self.mpm.desc, self.mpm.particles,
+                 nat.ptr(self.lbm.macro), nat.ptr(self.lbm.flags), nat.ptr(self._accum),
+                 nat.ptr(self._valid), nat.ptr(self._mask), nat.ptr(self._counters),
+                 nat.stream_ptr())
+
+    def _contact_kernel(self) -> None:
+        nat.call("fsi_contact", self._desc, self.mpm.desc, self.mpm.particles,
+                 nat.ptr(self._accum), nat.ptr(self.lbm.flags), nat.ptr(self._contact_mask),
+                 nat.ptr(self._counters), nat.stream_ptr())
+
+    def _assemble(self, mode: int, force: torch.Tensor | None) -> None:
+        base = np.asarray(self.lbm.config.force, dtype=np.float32)
+        base_p = base.ctypes.data_as(nat.ctypes.POINTER(nat.ctypes.c_float))
+        if mode & nat.ASSEMBLE_IB:
+            self._counters[5:7].zero_()
+            self._counters[8:12].zero_()
+        macro = self.lbm.macro if mode & nat.ASSEMBLE_IB else None
+        nat.call("fsi_coupling_assemble", self._desc, self.lbm._desc, nat.ptr(self.lbm.flags),
+                 base_p, mode, nat.ptr(self._accum), nat.ptr(macro), nat.ptr(force),
+                 nat.ptr(self._ib), nat.ptr(self._counters), nat.stream_ptr())
+
+    def step(self, lbm_dt: float) -> None:
+        """One explicit coupled lattice step with the configured MPM substeps (coupling.py:135-173)."""
+        lbm_dt_value = float(lbm_dt)
+        if lbm_dt_value <= 0.0:
+            raise ValueError("lbm_dt must be positive.")
+        self._validate_initialized()
+        self.clear_coupling_fields()
+        mpm_dt = lbm_dt_value / float(self.substeps)
+        dt_ratio = mpm_dt / lbm_dt_value
+        for substep in range(self.substeps):
+            if self.enabled:
+                self.clear_particle_diagnostics()
+                self._coupling_kernel(dt_ratio, substep == 0 and self.build_solid_volume_fraction)
+            else:
+                self.mpm.clear_particle_force()
+            self.mpm.substep(dt=mpm_dt)
+            if self.contact_enabled:
+                self._contact_kernel()
+        mode = 0
+        if self.enabled and self.build_solid_volume_fraction:
+            mode |= nat.ASSEMBLE_CLAMP_FRACTION
+        if self.enabled:
+            mode |= nat.ASSEMBLE_COUPLING
+        if self.immersed_boundary_enabled:
+            mode |= nat.ASSEMBLE_IB
+        self._assemble(mode, self.lbm._writable_force())
+        self.lbm.step()
+        if self.enabled:
+            self._coupled_step += 1
+
+    def compute_coupling_forces(self, dt_ratio: float = 1.0) -> None:
+        """Particle force and fluid reaction without stepping (coupling.py:175-196)."""
+        dt_ratio_value = float(dt_ratio)
+        if dt_ratio_value < 0.0:
+            raise ValueError("dt_ratio must be non-negative.")
+        self._validate_initialized()
+        self.clear_coupling_fields()
+        self.mpm.clear_particle_force()
+        if not self.enabled:
+            return
+        self._coupling_kernel(dt_ratio_value, self.build_solid_volume_fraction)
+        if self.build_solid_volume_fraction:
+            self._assemble(nat.ASSEMBLE_CLAMP_FRACTION, None)
+        if self.contact_enabled:
+            self._contact_kernel()
+        if self.immersed_boundary_enabled:
+            self._assemble(nat.ASSEMBLE_IB, None)
+
+    def clear_coupling_fields(self) -> None:
+        self._accum.zero_()
+        self._ib.zero_()
+        self._counters.zero_()
+        self.clear_particle_diagnostics()
+
+    def clear_particle_diagnostics(self) -> None:
+        self._counters[0:5].zero_()
+        self._valid.zero_()
+        self._mask.zero_()
+        self._contact_mask.zero_()
+
+    # ----------------------------------------------------------- accessors
+    def _cells(self, t: torch.Tensor) -> np.ndarray:
+        return t.reshape(self.nx, self.ny, self.nz, *t.shape[1:]).cpu().numpy()
+
+    def coupling_force_numpy(self) -> np.ndarray:
+        return self._cells(self._accum[:, :3])
+
+    def solid_volume_fraction_numpy(self) -> np.ndarray:
+        return self._cells(self._accum[:, 3])
+
+    def immersed_boundary_force_numpy(self) -> np.ndarray:
+        return self._cells(self._ib.t())
+
+    def _per_particle(self, t: torch.Tensor) -> np.ndarray:
+        return t[: self.mpm.particle_count()].cpu().numpy().copy()
+
+    def particle_valid_weights_numpy(self) -> np.ndarray:
+        return self._per_particle(self._valid)
+
+    def particle_coupling_mask_numpy(self) -> np.ndarray:
+        return self._per_particle(self._mask)
+
+    def particle_contact_mask_numpy(self) -> np.ndarray:
+        return self._per_particle(self._contact_mask)
+
+    def total_particle_coupling_force(self) -> np.ndarray:
+        return self.mpm.total_particle_force()
+
+    def total_fluid_coupling_force(self) -> np.ndarray:
+        nat.call("fsi_coupling_reduce", self.lbm._desc, nat.ptr(self._accum),
+                 nat.ptr(self.lbm.flags), nat.ptr(self._diag), nat.stream_ptr())
+        return self._diag[:3].cpu().numpy().astype(np.float32)
+
+    def _counter_values(self) -> tuple[np.ndarray, np.ndarray]:
+        raw = self._counters.cpu().numpy()
+        return raw[:8].copy(), raw[8:12].view(np.float32).copy()
+
+    def immersed_boundary_diagnostics(self) -> dict[str, int | float]:
+        counts, totals = self._counter_values()
+        t = totals[:3].astype(np.float64)
+        return {
+            "ib_active_cell_count": int(counts[5]),
+            "ib_clipped_cell_count": int(counts[6]),
+            "ib_total_force_x": float(t[0]),
+            "ib_total_force_y": float(t[1]),
+            "ib_total_force_z": float(t[2]),
+            "ib_total_force_norm": float(np.linalg.norm(t)),
+            "contact_candidate_count": int(counts[3]),
+            "contact_damped_particle_count": int(counts[4]),
+        }
+
+    def effective_gamma(self) -> float:
+        gamma = float(np.float32(self.config.gamma))
+        ramp = int(self.config.gamma_ramp_steps)
+        if ramp <= 0:
+            return gamma
+        return gamma * min(1.0, float(self._coupled_step + 1) / float(ramp))
+
+    @property
+    def coupled_step(self) -> int:
+        return self._coupled_step
+
+    def coupling_diagnostics(self) -> dict[str, int | float]:
+        n = self.mpm.particle_count()
+        if n == 0:
+            min_w = mean_w = 0.0
+        else:
+            vw = self._valid[:n]
+            min_w = float(vw.min().item())
+            mean_w = float(vw.double().mean().item())
+        counts, _ = self._counter_values()
+        return {
+            "unsupported_particle_count": int(counts[0]),
+            "partial_support_particle_count": int(counts[1]),
+            "clipped_particle_count": int(counts[2]),
+            "min_particle_valid_weight": min_w,
+            "mean_particle_valid_weight": mean_w,
+            "effective_gamma": self.effective_gamma(),
+            **self.immersed_boundary_diagnostics(),
+        }
+
+    def _validate_initialized(self) -> None:
+        if not getattr(self.lbm, "_initialized", False):
+            raise RuntimeError("LBMSolver3D.initialize must be called before coupling.")
+        if not getattr(self.mpm, "_initialized", False):
+            raise RuntimeError(
+                "MPMSolver3D particle initialization must be called before coupling."
+            )

@@ -1,0 +1,147 @@
+"""GPU MLS-MPM vs the CPU oracle and analytic checks.
+
+Bit-exact: particle-to-cell indices (trunc(x/dx - 0.5), negative positions
+included) and a full substep while no rotation is involved. Tolerance: the
+polar rotation (float32 Newton iteration vs a float64 SVD) and multi-particle
+runs, whose grid sums are accumulated in a different order on the GPU.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from fsi import _native as nat
+from fsi.config import MPMConfig
+from fsi.mpm3d import MPMSolver3D
+from helpers import rel_l2
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def mpm_cfg(**kw) -> MPMConfig:
+    p = dict(nx=16, ny=16, nz=16, max_particles=10_000, dt=1.0e-3, gravity=(0.0, 0.0, 0.0),
+             boundary_width=2)
+    p.update(kw)
+    return MPMConfig(**p)
+
+
+def svd_rotation(f: np.ndarray) -> np.ndarray:
+    u, _, vt = np.linalg.svd(f)
+    if np.linalg.det(u @ vt) < 0:
+        u[:, -1] = -u[:, -1]
+    return u @ vt
+
+
+def test_polar_rotation_against_svd():
+    rng = np.random.default_rng(11)
+    F = np.eye(3)[None] + rng.normal(0, 0.25, (4000, 3, 3))
+    F[:200] = np.eye(3) + rng.normal(0, 1e-4, (200, 3, 3))       # near identity
+    F[200:300] = F[200:300] * np.array([1.0, -1.0, 1.0])          # inverted
+    F = F.astype(np.float32)
+    Fd = torch.from_numpy(F.reshape(-1, 9)).cuda()
+    Rd = torch.empty_like(Fd)
+    nat.call("fsi_mpm_polar", nat.ptr(Fd), nat.ptr(Rd), F.shape[0], nat.stream_ptr())
+    R = Rd.cpu().numpy().reshape(-1, 3, 3).astype(np.float64)
+    ref = O.polar_rotation(F.astype(np.float64))
+    err = np.abs(R - ref).max(axis=(1, 2))
+    assert err.max() < 2e-5, err.max()
+    for f, r in zip(F[:50].astype(np.float64), R[:50]):
+        np.testing.assert_allclose(r, svd_rotation(f), atol=2e-5)
+    dets = np.linalg.det(R)
+    np.testing.assert_allclose(dets, 1.0, atol=1e-5)
+
+
+def test_particle_cell_indices_bit_exact():
+    rng = np.random.default_rng(2)
+    pos = rng.uniform(-2.0, 18.0, (5000, 3)).astype(np.float32)
+    pos[:10] = [[-0.75, 4, 4], [0.4999, 0.5, 0.5001], [-0.5, -0.49, 0], [15.5, 15.49, 0.0],
+                [3.0, 3.5, 4.5], [1e-8, -1e-8, 7.25], [2.5, 2.4999998, 2.5000002],
+                [-1.5, -1.0, -0.25], [8.0, 8.0, 8.0], [0.0, 0.0, 0.0]]
+    for dx in (1.0, 0.5, 0.3):
+        s = MPMSolver3D(mpm_cfg(dx=dx))
+        s.initialize_particles_from_numpy(pos)
+        inv = np.float32(1.0 / dx)
+        expect = ((pos * inv) - np.float32(0.5)).astype(np.int32)  # C cast truncates toward 0
+        np.testing.assert_array_equal(s.base_cells_numpy(), expect)
+
+
+def test_first_substep_bit_exact_single_particle():
+    """With F = I and C = 0 the first substep needs no rotation: results are bit-exact."""
+    cfg = mpm_cfg(gravity=(0.0, -1.0e-3, 0.0), dt=1e-2)
+    for pos, vel in (((4.3, 5.7, 6.1), (0.1, -0.2, 0.05)), ((0.7, 8.0, 14.9), (0.0, 0.0, -1.0))):
+        g, o = MPMSolver3D(cfg), O.MPMSolver3D(cfg)
+        for s in (g, o):
+            s.initialize_particles_from_numpy(np.array([pos], np.float32),
+                                              np.array([vel], np.float32), 1.3, 0.7)
+            s.substep()
+        np.testing.assert_array_equal(g.positions_numpy(), o.positions_numpy())
+        np.testing.assert_array_equal(g.velocities_numpy(), o.velocities_numpy())
+        np.testing.assert_array_equal(g.deformation_gradients_numpy(), o.deformation_gradients_numpy())
+        np.testing.assert_array_equal(g.affine_velocities_numpy(), o.C[:1])
+
+
+@pytest.mark.parametrize("gravity,dt,steps", [((0.0, -1.0e-3, 0.0), 1.0e-2, 10),
+                                               ((0.0, 0.0, 0.0), 1.0e-3, 10),
+                                               ((1e-3, -2e-3, 5e-4), 5.0e-2, 40)])
+def test_box_against_oracle(gravity, dt, steps):
+    cfg = mpm_cfg(gravity=gravity, dt=dt, youngs_modulus=1000.0)
+    g, o = MPMSolver3D(cfg), O.MPMSolver3D(cfg)
+    rng = np.random.default_rng(4)
+    for s in (g, o):
+        s.initialize_particles_box((6.0, 8.0, 6.0), (10.0, 12.0, 10.0), spacing=0.5)
+    vel = rng.normal(0, 1e-2, (g.particle_count(), 3)).astype(np.float32)
+    pos = g.positions_numpy()
+    for s in (g, o):
+        s.initialize_particles_from_numpy(pos, vel, particle_volume=0.125)
+    for _ in range(steps):
+        g.substep()
+        o.substep()
+    assert rel_l2(g.positions_numpy(), o.positions_numpy()) < 1e-6
+    assert rel_l2(g.velocities_numpy(), o.velocities_numpy()) < 1e-4
+    assert rel_l2(g.deformation_gradients_numpy(), o.deformation_gradients_numpy()) < 1e-5
+    np.testing.assert_allclose(g.center_of_mass(), o.center_of_mass(), rtol=1e-6)
+
+
+def test_reference_mpm_behaviour():
+    """The reference's tests/test_mpm3d.py assertions on the GPU solver."""
+    s = MPMSolver3D(mpm_cfg())
+    with pytest.raises(RuntimeError):
+        s.substep()
+    n = s.initialize_particles_box((6.0, 6.0, 6.0), (10.0, 10.0, 10.0), spacing=1.0)
+    assert n == 64 and s.particle_count() == n and np.all(s.active_numpy() == 1)
+    p = s.positions_numpy()
+    assert p.shape == (n, 3) and p.min() >= 6.0 and p.max() < 10.0
+    with pytest.raises(ValueError):
+        s.substep(0.0)
+    with pytest.raises(ValueError):
+        MPMSolver3D(mpm_cfg(max_particles=10)).initialize_particles_box((2.0,) * 3, (10.0,) * 3, 0.5)
+    com0 = s.center_of_mass()
+    for _ in range(5):
+        s.substep()
+    assert np.linalg.norm(s.center_of_mass() - com0) < 1e-3
+    gcfg = mpm_cfg(gravity=(0.0, -1.0e-3, 0.0), dt=1.0e-2)
+    g = MPMSolver3D(gcfg)
+    g.initialize_particles_box((6.0, 8.0, 6.0), (10.0, 12.0, 10.0), spacing=1.0)
+    c0 = g.center_of_mass()
+    for _ in range(10):
+        g.substep()
+    assert g.center_of_mass()[1] < c0[1]
+    d = MPMSolver3D(mpm_cfg(gravity=(0.0, -1.0e-3, 0.0)))
+    d.initialize_particles_box((2.0, 2.0, 2.0), (5.0, 5.0, 5.0), spacing=1.0)
+    for _ in range(20):
+        d.substep()
+    pos = d.positions_numpy()
+    assert np.isfinite(pos).all() and np.isfinite(d.deformation_gradients_numpy()).all()
+    assert (pos >= 0.0).all() and (pos <= 16 - 1e-4).all()
+
+
+def test_grid_is_left_clean_between_substeps():
+    cfg = mpm_cfg(gravity=(0.0, -1e-3, 0.0), dt=1e-2)
+    s = MPMSolver3D(cfg)
+    s.initialize_particles_box((3.0, 3.0, 3.0), (12.0, 6.0, 5.0), spacing=0.5)
+    for _ in range(3):
+        s.substep()
+        assert float(s._grid.abs().max()) == 0.0
+        assert int(s._dirty.max()) == 0

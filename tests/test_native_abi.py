@@ -1,0 +1,56 @@
+"""The C-ABI library builds, loads without a GPU and exports every declared entry point."""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from fsi import _native
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "fsi_gb300.h"
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|size_t)\s+(fsi_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "fsi_lbm_step" in names and "fsi_mpm_substep" in names
+    assert len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.load()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    assert set(declared_functions()) <= set(_native.exported_symbols())
+
+
+def test_abi_version_and_error_channel():
+    lib = _native.load()
+    assert lib.fsi_abi_version() == _native.ABI_VERSION
+    buf = ctypes.create_string_buffer(64)
+    lib.fsi_last_error(buf, 64)  # callable without a GPU
+
+
+def test_invalid_descriptor_is_rejected_without_touching_the_gpu():
+    d = _native.LbmDesc()
+    d.nx = d.ny = d.nz = 2  # too small
+    with pytest.raises(ValueError, match="too small"):
+        _native.call("fsi_lbm_step", d, None, None, None, None, None, 0, None)
+
+
+def test_struct_sizes_match_header_layout():
+    assert ctypes.sizeof(_native.LbmDesc) == 4 * (5 + 19 + 3 + 6)
+    assert ctypes.sizeof(_native.MpmDesc) == 4 * 19
+    assert ctypes.sizeof(_native.Particles) == 8 * 9
+    assert ctypes.sizeof(_native.CouplingDesc) == 4 * 18
