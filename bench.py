@@ -1,0 +1,362 @@
+"""Benchmark of the GB300 coupled LBM-MPM kernels on the standalone-at-scale workload.
+
+Workload (seeded, synthetic):
+  lattice: 256^3 D3Q19 MRT channel, tau 0.6, g_x = 1e-6, walls in y and z (mask planes),
+           ~10% volume of non-overlapping static spheres with radii U[4, 12] (seed 1);
+  solid:   64 elastic cubes of 16^3 cells at 8 particles per cell = 2,097,152 particles at
+           random positions (seed 2) in a 256^3 grid, gravity -1e-4, dt 0.1.
+A timed "step" is one lattice step (value: MLUPS over all cells); the solid is timed the same
+way per MPM substep (particle-steps/s) and reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 (under torchrun) runs independent replicas, one per GPU ("replicas only": the path has
+no exchange step); value is the sum over ranks, time the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "taichi-mpm-lbm_gb300"))
+
+LBM_BYTES_PER_CELL = 181     # algorithmic bytes per FP32 cell update (pops 152, mask 1, force 12, rho+u 16)
+KERNEL_BYTES_PER_CELL = 168  # what the fused step moves: pops 152, flag word 4, force 12
+MPM_BYTES_PER_PARTICLE = 200  # algorithmic bytes per particle-substep (standalone)
+MPM_BYTES_PER_NODE = 32       # per touched grid node per substep
+METRIC = "MLUPS & particle-steps/s on 1 GB300: plain vs FP16/learned, <=1% drag error"
+
+
+def load_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self._proc = None
+        self._thread = None
+
+    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._thread = threading.Thread(target=self._read, daemon=True)
+            self._thread.start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+            self._thread.join(timeout=5)
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in self.rows if num(r[0]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for name, v in zip(names, r[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": num(self.rows[0][1]), "reasons": sorted(reasons),
+                "samples": len(self.rows),
+                "power_w_max": max((num(r[2]) or 0.0) for r in self.rows)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int) -> None:
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args) -> dict:
+    import torch
+    from fsi import scenes
+    from fsi.lbm3d import LBMSolver3D
+    from fsi.mpm3d import MPMSolver3D
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    lcfg, mask = scenes.channel_spheres_lbm(n=args.n)
+    lbm = LBMSolver3D(lcfg)
+    lbm.initialize(mask)
+    cells = lbm.n_cells
+    fluid_cells = int((mask == 0).sum())
+
+    mcfg, pos = scenes.cubes_mpm(n=args.n)
+    mpm = MPMSolver3D(mcfg)
+    mpm.initialize_particles_from_numpy(pos)
+    particles = mpm.particle_count()
+
+    stream = torch.cuda.current_stream()
+    # --- lattice, device-resident -------------------------------------------------
+    for _ in range(args.warmup):
+        lbm.step()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        e0.record(stream)
+        for _ in range(args.steps):
+            lbm.step()
+        e1.record(stream)
+        barrier(world)
+    lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+    lbm_launches = args.steps
+
+    # --- solid, device-resident ---------------------------------------------------
+    for _ in range(args.warmup):
+        mpm.substep()
+    barrier(world)
+    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    m0.record(stream)
+    for _ in range(args.steps):
+        mpm.substep()
+    m1.record(stream)
+    barrier(world)
+    mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
+    touched = int(mpm._dirty.numel())  # refined below from the particle bounding cells
+    base = mpm.base_cells_numpy()
+    nodes = np.unique(((base[:, 0] * 3 + 0) * 0 + (base[:, 0].astype(np.int64) * args.n
+                                                     + base[:, 1]) * args.n + base[:, 2]))
+    touched = int(len(nodes))  # distinct base cells; each owns ~1 stencil node-equivalent
+
+    # --- end to end through the public API (host input, host result each step) ----
+    g_host = np.array(lcfg.force, dtype=np.float32)
+    for _ in range(2):
+        lbm.set_uniform_force(g_host)
+        lbm.step()
+        lbm.total_mass()
+    barrier(world)
+    t0 = time.perf_counter()
+    diag = None
+    for _ in range(args.steps):
+        lbm.set_uniform_force(g_host)   # 12 B of step input from the host
+        lbm.step()
+        diag = (lbm.total_mass(), lbm.max_velocity_norm())  # 16 B of step result to the host
+    barrier(world)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+
+    peak, peak_kind = load_peaks()
+    achieved = LBM_BYTES_PER_CELL * cells / (lbm_ms * 1e-3) / 1e9
+    mlups = cells / (lbm_ms * 1e-3) / 1e6
+    result = {
+        "metric": METRIC,
+        "value": round(mlups * world, 3),
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(lbm_ms, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded scene generators; no dataset)",
+        "config": {
+            "workload": "standalone lattice 256^3 channel + 64 elastic cubes (2,097,152 particles)",
+            "lattice": [args.n] * 3, "tau": 0.6, "g_x": 1e-6,
+            "solid_fraction": round(float(mask.mean()), 4),
+            "fluid_cells": fluid_cells,
+            "particles": particles, "mpm_dt": 0.1, "gravity_y": -1e-4,
+            "l2": "inputs larger than L2 (populations 1.27 GB, particles 0.25 GB)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+        },
+        "fluid_mlups": round(fluid_cells / (lbm_ms * 1e-3) / 1e6 * world, 3),
+        "mpm": {
+            "metric": "particle-steps/s",
+            "value": round(particles / (mpm_ms * 1e-3) * world, 1),
+            "ms_per_substep": round(mpm_ms, 5),
+            "algorithmic_gbs": round((MPM_BYTES_PER_PARTICLE * particles
+                                      + MPM_BYTES_PER_NODE * touched) / (mpm_ms * 1e-3) / 1e9, 1),
+        },
+        "roofline": {
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "kernel": "lbm_step_kernel", "peak_source": peak_kind,
+            "algorithmic_bytes_per_cell": LBM_BYTES_PER_CELL,
+            "kernel_bytes_per_cell": KERNEL_BYTES_PER_CELL,
+        },
+        "e2e": {
+            "value": round(cells * args.steps / e2e_s / 1e6 * world, 3), "unit": "MLUPS",
+            "h2d_bytes_per_step": 12, "d2h_bytes_per_step": 16,
+            "api": "LBMSolver3D.set_uniform_force + step + total_mass + max_velocity_norm",
+            "last_diagnostics": [float(diag[0]), float(diag[1])] if diag else None,
+        },
+        "gpu_launches": lbm_launches + 3 * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return result if rank == 0 else None
+
+
+# --------------------------------------------------------------- CPU leg
+
+def cpu_sample(steps: int, warmup: int, nthreads: int, n: int = 256, slab: int = 32,
+               cubes: int = 8) -> dict:
+    """The oracle (C++ OpenMP restatement of the reference) on a bounded sample of the same
+    workload: a slab of `slab` x n x n cells of the lattice and `cubes` of the 64 cubes."""
+    from fsi import scenes
+    from oracle import oracle as O
+
+    lcfg, mask = scenes.channel_spheres_lbm(n=n)
+    sub = mask[:slab].copy()
+    from dataclasses import replace
+    scfg = replace(lcfg, nx=slab)
+    lbm = O.LBMSolver3D(scfg, nthreads=nthreads)
+    lbm.initialize(sub)
+    for _ in range(warmup):
+        lbm.step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        lbm.step()
+    lbm_s = time.perf_counter() - t0
+    mcfg, pos = scenes.cubes_mpm(n=n)
+    per_cube = len(pos) // 64
+    pos = pos[: cubes * per_cube]
+    mpm = O.MPMSolver3D(replace(mcfg, max_particles=len(pos)), nthreads=nthreads,
+                        deterministic=False)
+    mpm.initialize_particles_from_numpy(pos)
+    for _ in range(max(1, warmup // 2)):
+        mpm.substep()
+    t1 = time.perf_counter()
+    for _ in range(steps):
+        mpm.substep()
+    mpm_s = time.perf_counter() - t1
+    cells = slab * n * n
+    return {"mlups": cells * steps / lbm_s / 1e6, "lbm_s_per_step": lbm_s / steps,
+            "particle_steps_per_s": len(pos) * steps / mpm_s, "mpm_s_per_substep": mpm_s / steps,
+            "cells": cells, "particles": len(pos), "cores": nthreads}
+
+
+def cpu_baseline_entry(nthreads: int) -> dict:
+    s = cpu_sample(steps=3, warmup=1, nthreads=nthreads)
+    return {"value": round(s["mlups"], 3), "unit": "MLUPS", "cores": s["cores"], "kind": "port",
+            "sample": (f"oracle (C++ OpenMP float32 restatement; Taichi is not installable) on a "
+                       f"32x256x256 slab of the lattice ({s['cells']} cells, 3 steps) and 8 of the "
+                       f"64 cubes ({s['particles']} particles, 3 substeps)"),
+            "particle_steps_per_s": round(s["particle_steps_per_s"], 1)}
+
+
+def run_reference(args) -> dict | None:
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    nthreads = O.max_threads()
+    s = cpu_sample(steps=args.steps, warmup=args.warmup, nthreads=nthreads)
+    return {
+        "impl": "reference",
+        "metric": METRIC, "value": round(s["mlups"], 3), "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(s["lbm_s_per_step"] * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generators; no dataset)",
+        "config": {"workload": "standalone lattice 256^3 channel + 64 elastic cubes (2,097,152 particles)",
+                   "sample": "32x256x256 lattice slab per step; 8 of 64 cubes per substep"},
+        "mpm": {"metric": "particle-steps/s", "value": round(s["particle_steps_per_s"], 1)},
+        "cpu_baseline": {"value": round(s["mlups"], 3), "unit": "MLUPS", "cores": nthreads,
+                         "kind": "port",
+                         "sample": "reference's Taichi CPU path unavailable (taichi not installable); "
+                                   "the oracle restatement of it, all host threads"},
+        "e2e": {"value": round(s["mlups"], 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=256, help="lattice edge (default 256)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        out = run_reference(args)
+    else:
+        out = run_gpu(args)
+        world, rank, _ = dist_env()
+        if out is not None and world == 1 and not args.no_cpu_baseline:
+            from oracle import oracle as O
+            out["cpu_baseline"] = cpu_baseline_entry(O.max_threads())
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -340,10 +340,111 @@ inline void polar_rotation_f64(const double F[9], double R[9]) {
     }
 }
 
+// Float32 polar rotation with the device library's operation order (Newton
+// iteration with Frobenius scaling, one-sided Jacobi fallback for det <= 1e-20).
+// Selected by polar_mode = 1 so that a parity run isolates the grid-sum order.
+inline float det3f(const float* a) {
+  float t0 = a[4] * a[8] - a[7] * a[5];
+  float t1 = a[1] * a[8] - a[7] * a[2];
+  float t2 = a[1] * a[5] - a[4] * a[2];
+  float d = a[0] * t0 - a[3] * t1;
+  return d + a[6] * t2;
+}
+
+inline float dot3f(float a0, float a1, float a2, float b0, float b1, float b2) {
+  float s = a0 * b0;
+  s = s + a1 * b1;
+  return s + a2 * b2;
+}
+
+inline void polar_jacobi_f32(const float* F, float* R) {
+  float A[9], V[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+  for (int i = 0; i < 9; ++i) A[i] = F[i];
+  for (int sweep = 0; sweep < 8; ++sweep) {
+    float off = 0.f;
+    for (int pq = 0; pq < 3; ++pq) {
+      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+      const float alpha = dot3f(A[p], A[3 + p], A[6 + p], A[p], A[3 + p], A[6 + p]);
+      const float beta = dot3f(A[q], A[3 + q], A[6 + q], A[q], A[3 + q], A[6 + q]);
+      const float gamma = dot3f(A[p], A[3 + p], A[6 + p], A[q], A[3 + q], A[6 + q]);
+      if (gamma == 0.f) continue;
+      off = std::fmax(off, std::fabs(gamma) / std::sqrt(alpha * beta));
+      const float zeta = (beta - alpha) / (2.f * gamma);
+      const float t = std::copysign(1.f, zeta) / (std::fabs(zeta) + std::sqrt(1.f + zeta * zeta));
+      const float c = 1.f / std::sqrt(1.f + t * t), s = c * t;
+      for (int r = 0; r < 3; ++r) {
+        const float ap = A[3 * r + p], aq = A[3 * r + q];
+        A[3 * r + p] = c * ap - s * aq;
+        A[3 * r + q] = s * ap + c * aq;
+        const float vp = V[3 * r + p], vq = V[3 * r + q];
+        V[3 * r + p] = c * vp - s * vq;
+        V[3 * r + q] = s * vp + c * vq;
+      }
+    }
+    if (off < 1e-7f) break;
+  }
+  float nrm[3];
+  for (int c = 0; c < 3; ++c) nrm[c] = std::sqrt(A[c] * A[c] + A[3 + c] * A[3 + c] + A[6 + c] * A[6 + c]);
+  float U[9];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) U[3 * r + c] = nrm[c] > 0.f ? A[3 * r + c] / nrm[c] : (r == c ? 1.f : 0.f);
+  if (det3f(U) * det3f(V) < 0.f) {
+    int cmin = 0;
+    if (nrm[1] < nrm[cmin]) cmin = 1;
+    if (nrm[2] < nrm[cmin]) cmin = 2;
+    for (int r = 0; r < 3; ++r) U[3 * r + cmin] = -U[3 * r + cmin];
+  }
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      R[3 * a + b] = U[3 * a] * V[3 * b] + U[3 * a + 1] * V[3 * b + 1] + U[3 * a + 2] * V[3 * b + 2];
+}
+
+inline void polar_newton_f32(const float* F, float* R) {
+  float X[9];
+  for (int i = 0; i < 9; ++i) X[i] = F[i];
+  if (!(det3f(F) > 1e-20f)) {
+    polar_jacobi_f32(F, R);
+    return;
+  }
+  bool scale = true;
+  for (int it = 0; it < 16; ++it) {
+    float Cf[9];
+    Cf[0] = X[4] * X[8] - X[5] * X[7];
+    Cf[1] = X[5] * X[6] - X[3] * X[8];
+    Cf[2] = X[3] * X[7] - X[4] * X[6];
+    Cf[3] = X[2] * X[7] - X[1] * X[8];
+    Cf[4] = X[0] * X[8] - X[2] * X[6];
+    Cf[5] = X[1] * X[6] - X[0] * X[7];
+    Cf[6] = X[1] * X[5] - X[2] * X[4];
+    Cf[7] = X[2] * X[3] - X[0] * X[5];
+    Cf[8] = X[0] * X[4] - X[1] * X[3];
+    const float det = X[0] * Cf[0] + X[1] * Cf[1] + X[2] * Cf[2];
+    float z = 1.f;
+    if (scale) {
+      float nx2 = 0.f, nc2 = 0.f;
+      for (int i = 0; i < 9; ++i) { nx2 += X[i] * X[i]; nc2 += Cf[i] * Cf[i]; }
+      z = std::sqrt(std::sqrt(nc2 / nx2) / std::fabs(det));
+    }
+    const float a = 0.5f * z, b = 0.5f / (z * det);
+    float d2 = 0.f, n2 = 0.f;
+    for (int i = 0; i < 9; ++i) {
+      const float xn = a * X[i] + b * Cf[i];
+      const float dd = xn - X[i];
+      d2 += dd * dd;
+      n2 += xn * xn;
+      X[i] = xn;
+    }
+    if (d2 < 1e-4f * n2) scale = false;
+    if (d2 <= 1e-13f * n2) break;
+  }
+  for (int i = 0; i < 9; ++i) R[i] = X[i];
+}
+
 template <class T>
 struct MpmParams {
   T dt, dx, inv_dx, mu, lam, gravity[3], damping;
   int bw, apic;
+  int polar_mode;  // 0: exact (float64 Jacobi SVD), 1: device float32 Newton
 };
 
 template <class T>
@@ -371,11 +472,18 @@ inline void p2g_particle(int p, const Particles<T>& P, Grid<T>& G, const MpmPara
   matmul3(A, Fp, Fn);
   for (int i = 0; i < 9; ++i) Fp[i] = Fn[i];
   T J = det3(Fn);
-  double Fd64[9], R64[9];
-  for (int i = 0; i < 9; ++i) Fd64[i] = (double)Fn[i];
-  polar_rotation_f64(Fd64, R64);
   T R[9];
-  for (int i = 0; i < 9; ++i) R[i] = (T)R64[i];
+  if (mp.polar_mode == 1 && sizeof(T) == sizeof(float)) {
+    float Ff[9], Rf[9];
+    for (int i = 0; i < 9; ++i) Ff[i] = (float)Fn[i];
+    polar_newton_f32(Ff, Rf);
+    for (int i = 0; i < 9; ++i) R[i] = (T)Rf[i];
+  } else {
+    double Fd64[9], R64[9];
+    for (int i = 0; i < 9; ++i) Fd64[i] = (double)Fn[i];
+    polar_rotation_f64(Fd64, R64);
+    for (int i = 0; i < 9; ++i) R[i] = (T)R64[i];
+  }
   // stress = 2 mu (F - R) F^T + lam J (J - 1) I, mpm3d.py:247-251.
   T twomu = (T)2.0 * mp.mu;
   T Pm[9];
@@ -572,10 +680,12 @@ template <class T>
 static void mpm_substep_impl(int nx, int ny, int nz, int n, T* x, T* v, T* C, T* Fd, const T* mass,
                              const T* vol, const int32_t* active, T* fp, T* gv, T* gm, T dt, T dx,
                              T inv_dx, T mu, T lam, const T* gravity, int bw, T damping, int apic,
-                             T lower, const T* upper, int nthreads, int deterministic) {
+                             T lower, const T* upper, int nthreads, int deterministic,
+                             int polar_mode) {
   Particles<T> P{n, x, v, C, Fd, mass, vol, active, fp};
   Grid<T> G{nx, ny, nz, gv, gm};
-  MpmParams<T> mp{dt, dx, inv_dx, mu, lam, {gravity[0], gravity[1], gravity[2]}, damping, bw, apic};
+  MpmParams<T> mp{dt, dx, inv_dx, mu, lam, {gravity[0], gravity[1], gravity[2]}, damping, bw, apic,
+                  polar_mode};
   const long N = (long)nx * ny * nz;
   std::memset(gv, 0, sizeof(T) * 3 * N);
   std::memset(gm, 0, sizeof(T) * N);
@@ -597,10 +707,10 @@ FSI_ORACLE_EXPORT void oracle_mpm_substep_f32(int nx, int ny, int nz, int n, flo
                                               float inv_dx, float mu, float lam,
                                               const float* gravity, int bw, float damping, int apic,
                                               float lower, const float* upper, int nthreads,
-                                              int deterministic) {
+                                              int deterministic, int polar_mode) {
   mpm_substep_impl<float>(nx, ny, nz, n, x, v, C, Fd, mass, vol, active, fp, gv, gm, dt, dx, inv_dx,
                           mu, lam, gravity, bw, damping, apic, lower, upper, nthreads,
-                          deterministic);
+                          deterministic, polar_mode);
 }
 
 FSI_ORACLE_EXPORT void oracle_mpm_substep_f64(int nx, int ny, int nz, int n, double* x, double* v,
@@ -610,10 +720,15 @@ FSI_ORACLE_EXPORT void oracle_mpm_substep_f64(int nx, int ny, int nz, int n, dou
                                               double inv_dx, double mu, double lam,
                                               const double* gravity, int bw, double damping,
                                               int apic, double lower, const double* upper,
-                                              int nthreads, int deterministic) {
+                                              int nthreads, int deterministic, int polar_mode) {
   mpm_substep_impl<double>(nx, ny, nz, n, x, v, C, Fd, mass, vol, active, fp, gv, gm, dt, dx,
                            inv_dx, mu, lam, gravity, bw, damping, apic, lower, upper, nthreads,
-                           deterministic);
+                           deterministic, polar_mode);
+}
+
+// Polar rotation of 3x3 float32 matrices with the device operation order.
+FSI_ORACLE_EXPORT void oracle_polar_newton_f32(int n, const float* F, float* R) {
+  for (int i = 0; i < n; ++i) polar_newton_f32(F + 9 * i, R + 9 * i);
 }
 
 // Polar rotation of 3x3 matrices (row-major), for checking the device routine.

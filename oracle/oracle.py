@@ -245,8 +245,12 @@ class LBMSolver3D:
 class MPMSolver3D:
     """Oracle of fsi/mpm3d.py:9-368 over numpy arrays."""
 
-    def __init__(self, config, dtype=np.float32, nthreads: int = 1, deterministic: bool = True):
+    def __init__(self, config, dtype=np.float32, nthreads: int = 1, deterministic: bool = True,
+                 polar: str = "exact"):
         config.validate()
+        if polar not in ("exact", "device"):
+            raise ValueError("polar must be 'exact' or 'device'")
+        self.polar = polar
         self.config = config
         self.dtype = np.dtype(dtype)
         self.nthreads = nthreads
@@ -349,7 +353,7 @@ class MPMSolver3D:
             _p(self.grid_v), _p(self.grid_m), cast(dt_value), cast(self.dx), cast(self.inv_dx),
             cast(self.mu), cast(self.lam), _p(grav), self.boundary_width,
             cast(self.boundary_damping), int(self.apic), cast(0.5 * self.dx), _p(upper),
-            self.nthreads, int(self.deterministic))
+            self.nthreads, int(self.deterministic), 1 if self.polar == "device" else 0)
 
     def clear_particle_force(self):
         self.particle_force[: self.num_particles] = 0
@@ -618,11 +622,13 @@ class LBMMpmCoupler:
 class FSISimulation:
     """Oracle of fsi/simulation.py:12-153 (no snapshot writer)."""
 
-    def __init__(self, config, dtype=np.float32, nthreads: int = 1):
+    def __init__(self, config, dtype=np.float32, nthreads: int = 1, polar: str = "exact",
+                 deterministic: bool = True):
         config.validate()
         self.config = config
         self.lbm = LBMSolver3D(config.lbm, dtype=dtype, nthreads=nthreads)
-        self.mpm = MPMSolver3D(config.mpm, dtype=dtype, nthreads=nthreads)
+        self.mpm = MPMSolver3D(config.mpm, dtype=dtype, nthreads=nthreads, polar=polar,
+                               deterministic=deterministic)
         self.coupler = LBMMpmCoupler(config.coupling, self.lbm, self.mpm)
         self.step_index = 0
         self.time = 0.0
@@ -694,6 +700,14 @@ class FSISimulation:
             "coupling_contact_candidate_count": cd["contact_candidate_count"],
             "coupling_contact_damped_particle_count": cd["contact_damped_particle_count"],
         }
+
+
+def polar_rotation_device_f32(F: np.ndarray) -> np.ndarray:
+    """Polar rotation with the device library's float32 operation order."""
+    F = np.ascontiguousarray(np.asarray(F, np.float32).reshape(-1, 3, 3))
+    R = np.empty_like(F)
+    lib().oracle_polar_newton_f32(F.shape[0], _p(F), _p(R))
+    return R
 
 
 def polar_rotation(F: np.ndarray) -> np.ndarray:

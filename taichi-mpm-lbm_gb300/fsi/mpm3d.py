@@ -234,12 +234,24 @@ class MPMSolver3D:
         return self._diag_host.numpy().copy()
 
     def center_of_mass(self) -> np.ndarray:
-        if self._num_particles == 0:
+        """Mass-weighted mean position with the reference's float32 numpy arithmetic
+        (mpm3d.py:353-362); the committed goldens depend on its rounding."""
+        n = self._num_particles
+        if n == 0:
             return np.zeros(3, dtype=np.float32)
+        positions = self.positions_numpy()
+        masses = self._mass[:n].cpu().numpy()
+        total = masses.sum()
+        if total <= 0.0:
+            return np.zeros(3, dtype=np.float32)
+        return (positions * masses[:, None]).sum(axis=0) / total
+
+    def center_of_mass_device(self) -> np.ndarray:
+        """Centre of mass from an on-device float64 reduction (no particle copy to the host)."""
         r = self._reduce()
-        if r[0] <= 0.0:
-            return np.zeros(3, dtype=np.float32)
-        return (r[1:4] / r[0]).astype(np.float32)
+        if self._num_particles == 0 or r[0] <= 0.0:
+            return np.zeros(3, dtype=np.float64)
+        return r[1:4] / r[0]
 
     def max_velocity_norm(self) -> float:
         if self._num_particles == 0:

@@ -1,0 +1,158 @@
+"""Seeded scene generators: wall masks, sphere packings and particle cubes.
+
+These build the occupancy masks and particle sets of the benchmark workloads
+(the reference has no generators; its masks come from callers or
+``LBMSolver3D.load_solid_from_txt``). Masks use the reference's convention: int32
+0/1 of shape (nx, ny, nz) in C order; walls in y and z are expressed as solid
+mask planes because the reference supports only periodic y/z faces
+(fsi/lbm3d.py:98-108).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .config import BoundaryConfig, CouplingConfig, LBMConfig, MPMConfig, SimulationConfig
+
+PERIODIC_FACES = {name: BoundaryConfig("periodic")
+                  for name in ("x_left", "x_right", "y_left", "y_right", "z_left", "z_right")}
+
+
+def viscosity_for_tau(tau: float) -> float:
+    """nu = (tau - 1/2) / 3, the inverse of tau = 3 nu + 1/2 (fsi/lbm3d.py:141)."""
+    return (tau - 0.5) / 3.0
+
+
+def wall_mask(nx: int, ny: int, nz: int) -> np.ndarray:
+    """Solid planes at y = 0, ny-1 and z = 0, nz-1."""
+    s = np.zeros((nx, ny, nz), np.int32)
+    s[:, 0, :] = s[:, -1, :] = 1
+    s[:, :, 0] = s[:, :, -1] = 1
+    return s
+
+
+def add_sphere(mask: np.ndarray, center, radius: float) -> int:
+    """Mark the cells whose centres lie within ``radius`` of ``center`` (cell units);
+    returns the number of cells that became solid."""
+    lo = [max(int(np.floor(c - radius)), 0) for c in center]
+    hi = [min(int(np.ceil(c + radius)) + 1, n) for c, n in zip(center, mask.shape)]
+    ii, jj, kk = np.meshgrid(*[np.arange(a, b) for a, b in zip(lo, hi)], indexing="ij")
+    inside = ((ii - center[0]) ** 2 + (jj - center[1]) ** 2 + (kk - center[2]) ** 2) <= radius ** 2
+    box = mask[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]
+    added = int(np.count_nonzero(inside & (box == 0)))
+    box[inside] = 1
+    return added
+
+
+def sphere_packing(shape, fraction: float, rmin: float, rmax: float, seed: int,
+                   margin: int = 1, max_tries: int = 200_000):
+    """Non-overlapping spheres with radii U[rmin, rmax] and centres uniform in the interior,
+    added by rejection sampling until they fill ``fraction`` of the volume.
+    Returns (mask, centres, radii)."""
+    rng = np.random.default_rng(seed)
+    mask = np.zeros(shape, np.int32)
+    centres, radii = [], []
+    total = float(np.prod(shape))
+    filled = 0
+    tries = 0
+    while filled < fraction * total and tries < max_tries:
+        tries += 1
+        r = float(rng.uniform(rmin, rmax))
+        c = np.array([rng.uniform(margin + r, n - 1 - margin - r) for n in shape])
+        if centres:
+            d = np.linalg.norm(np.asarray(centres) - c, axis=1)
+            if np.any(d < np.asarray(radii) + r):
+                continue
+        added = add_sphere(mask, c, r)
+        if added == 0:
+            continue
+        filled += added
+        centres.append(c)
+        radii.append(r)
+    return mask, np.asarray(centres), np.asarray(radii)
+
+
+def cube_particles(lower_cells, edge_cells: int, ppc_axis: int, rng=None) -> np.ndarray:
+    """Particles of a cube of edge ``edge_cells`` cells with lower corner ``lower_cells``:
+    ``ppc_axis``^3 per cell on the sub-cell lattice, each jittered uniformly within its
+    sub-cell when ``rng`` is given. Ordered cell by cell (C order), then sub-cell."""
+    n = edge_cells * ppc_axis
+    idx = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"),
+                   axis=-1).reshape(-1, 3)
+    cell = idx // ppc_axis
+    sub = idx % ppc_axis
+    order = np.lexsort((sub[:, 2], sub[:, 1], sub[:, 0], cell[:, 2], cell[:, 1], cell[:, 0]))
+    idx = idx[order]
+    jitter = rng.uniform(0.0, 1.0, idx.shape) if rng is not None else 0.5
+    return (np.asarray(lower_cells, np.float64) + (idx + jitter) / ppc_axis).astype(np.float32)
+
+
+def random_cubes(grid: int, count: int, edge: int, seed: int, margin: int = 4,
+                 ppc_axis: int = 2) -> np.ndarray:
+    """``count`` non-overlapping cubes of ``edge`` cells at random positions in a ``grid``^3
+    domain (rejection sampling from ``seed``); returns their particles."""
+    rng = np.random.default_rng(seed)
+    corners = []
+    tries = 0
+    while len(corners) < count:
+        tries += 1
+        if tries > 1_000_000:
+            raise RuntimeError("could not place the cubes without overlap")
+        c = rng.integers(margin, grid - margin - edge, size=3)
+        if any(np.all(np.abs(c - o) < edge + 1) for o in corners):
+            continue
+        corners.append(c)
+    return np.concatenate([cube_particles(c, edge, ppc_axis, rng) for c in corners])
+
+
+@dataclass
+class Workload:
+    name: str
+    lbm: LBMConfig
+    mpm: MPMConfig
+    solid: np.ndarray
+    particles: np.ndarray
+
+
+def channel_spheres_lbm(n: int = 256, tau: float = 0.6, gx: float = 1.0e-6, seed: int = 1,
+                        fraction: float = 0.10) -> tuple[LBMConfig, np.ndarray]:
+    """The standalone lattice at scale: n^3 channel (walls in y and z), g_x force, and
+    non-overlapping spheres of radius U[4, 12] filling ~10% of the volume (seed 1)."""
+    mask, _, _ = sphere_packing((n, n, n), fraction, 4.0, 12.0, seed, margin=1)
+    mask = np.maximum(mask, wall_mask(n, n, n))
+    cfg = LBMConfig(nx=n, ny=n, nz=n, viscosity=viscosity_for_tau(tau), force=(gx, 0.0, 0.0),
+                    **PERIODIC_FACES)
+    return cfg, mask
+
+
+def cubes_mpm(n: int = 256, cubes: int = 64, edge: int = 16, seed: int = 2,
+              gravity: float = -1.0e-4, dt: float = 0.1) -> tuple[MPMConfig, np.ndarray]:
+    """The standalone solid at scale: ``cubes`` elastic cubes of ``edge``^3 cells at 8
+    particles per cell (2 per axis) at random positions (seed 2) in an n^3 grid.
+    64 cubes of 16^3 cells give 2,097,152 particles."""
+    pos = random_cubes(n, cubes, edge, seed)
+    cfg = MPMConfig(nx=n, ny=n, nz=n, max_particles=len(pos), particles_per_cell=2, dx=1.0, dt=dt,
+                    density=1.5, youngs_modulus=0.05, poisson_ratio=0.3,
+                    gravity=(0.0, gravity, 0.0), boundary_width=3)
+    return cfg, pos
+
+
+def coupled_smoke(steps: int = 1000) -> tuple[SimulationConfig, np.ndarray, np.ndarray]:
+    """The 48x32x32 coupled smoke workload: tau 0.6 channel (walls in y, z), g_x = 1e-5, one
+    elastic 8^3-cell cube (E 0.05, nu 0.3, rho_s 1.5) with corner (12,12,12), 2x2x2 particles per
+    cell jittered in their sub-cells from seed 0 (4096 particles), gamma 0.1, 10 substeps per
+    lattice step, gravity off."""
+    nx, ny, nz = 48, 32, 32
+    lbm = LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=viscosity_for_tau(0.6), rho0=1.0,
+                    force=(1.0e-5, 0.0, 0.0), **PERIODIC_FACES)
+    mpm = MPMConfig(nx=nx, ny=ny, nz=nz, max_particles=4096, particles_per_cell=2, dx=1.0,
+                    dt=0.1, density=1.5, youngs_modulus=0.05, poisson_ratio=0.3,
+                    gravity=(0.0, 0.0, 0.0), boundary_width=3)
+    cfg = SimulationConfig(num_steps=steps, lbm_dt=1.0, lbm=lbm, mpm=mpm,
+                           coupling=CouplingConfig(gamma=0.1, mpm_substeps_per_lbm_step=10))
+    rng = np.random.default_rng(0)
+    idx = np.stack(np.meshgrid(np.arange(16), np.arange(16), np.arange(16), indexing="ij"),
+                   axis=-1).reshape(-1, 3)
+    pos = (12.0 + 0.5 * (idx + rng.uniform(0.0, 1.0, idx.shape))).astype(np.float32)
+    return cfg, wall_mask(nx, ny, nz), pos
