@@ -141,7 +141,15 @@ typedef struct fsi_mpm_desc {
   int32_t apic;
   float clamp_lower;
   float clamp_upper[3];
+  int32_t material; /* FSI_MATERIAL_*; the reference's model is fixed-corotated */
 } fsi_mpm_desc;
+
+/* Constitutive models. FIXED_COROTATED is the reference's
+ * 2 mu (F - R) F^T + lam J (J - 1) I (mpm3d.py:247-251); NEO_HOOKEAN is the
+ * compressible mu (F F^T - I) + lam ln(J) I, an extension with no reference
+ * counterpart (its oracle is the CPU restatement). */
+#define FSI_MATERIAL_FIXED_COROTATED 0
+#define FSI_MATERIAL_NEO_HOOKEAN 1
 
 /* Particle arrays, structure of arrays with component stride `capacity`:
  * x, v, force float[3][capacity]; C, F float[9][capacity] (row-major 3x3
@@ -157,6 +165,8 @@ typedef struct fsi_particles {
   int32_t* active;
   float* force;
   int64_t capacity;
+  float* mu;  /* per-particle Lame parameters float[capacity], or both NULL to use the */
+  float* lam; /* descriptor's scalars (the reference has one material per solver) */
 } fsi_particles;
 
 /* One MPM substep: P2G (deformation update, fixed-corotated stress, 27-node

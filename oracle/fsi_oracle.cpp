@@ -219,6 +219,8 @@ struct Particles {
   const T* vol;
   const int32_t* active;
   T* fp;       // [P,3] particle_force
+  const T* mu_p;   // per-particle Lame parameters or nullptr
+  const T* lam_p;
 };
 
 template <class T>
@@ -445,6 +447,7 @@ struct MpmParams {
   T dt, dx, inv_dx, mu, lam, gravity[3], damping;
   int bw, apic;
   int polar_mode;  // 0: exact (float64 Jacobi SVD), 1: device float32 Newton
+  int material;    // 0: fixed-corotated (reference), 1: Neo-Hookean extension
 };
 
 template <class T>
@@ -472,30 +475,41 @@ inline void p2g_particle(int p, const Particles<T>& P, Grid<T>& G, const MpmPara
   matmul3(A, Fp, Fn);
   for (int i = 0; i < 9; ++i) Fp[i] = Fn[i];
   T J = det3(Fn);
-  T R[9];
-  if (mp.polar_mode == 1 && sizeof(T) == sizeof(float)) {
-    float Ff[9], Rf[9];
-    for (int i = 0; i < 9; ++i) Ff[i] = (float)Fn[i];
-    polar_newton_f32(Ff, Rf);
-    for (int i = 0; i < 9; ++i) R[i] = (T)Rf[i];
-  } else {
-    double Fd64[9], R64[9];
-    for (int i = 0; i < 9; ++i) Fd64[i] = (double)Fn[i];
-    polar_rotation_f64(Fd64, R64);
-    for (int i = 0; i < 9; ++i) R[i] = (T)R64[i];
-  }
-  // stress = 2 mu (F - R) F^T + lam J (J - 1) I, mpm3d.py:247-251.
-  T twomu = (T)2.0 * mp.mu;
-  T Pm[9];
-  for (int i = 0; i < 9; ++i) Pm[i] = twomu * (Fn[i] - R[i]);
+  const T mu = P.mu_p ? P.mu_p[p] : mp.mu;
+  const T lam = P.lam_p ? P.lam_p[p] : mp.lam;
   T Ft[9];
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) Ft[3 * a + b] = Fn[3 * b + a];
   T stress[9];
-  matmul3(Pm, Ft, stress);
-  T lj = (mp.lam * J) * (J - (T)1.0);
-  for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 3; ++b) stress[3 * a + b] = stress[3 * a + b] + lj * (T)(a == b ? 1 : 0);
+  if (mp.material == 1) {
+    // Compressible Neo-Hookean Kirchhoff stress mu (F F^T - I) + lam ln(J) I (extension).
+    matmul3(Fn, Ft, stress);
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) stress[3 * a + b] = mu * (stress[3 * a + b] - (T)(a == b ? 1 : 0));
+    T ll = lam * std::log(J);
+    for (int a = 0; a < 3; ++a) stress[4 * a] = stress[4 * a] + ll;
+  } else {
+    T R[9];
+    if (mp.polar_mode == 1 && sizeof(T) == sizeof(float)) {
+      float Ff[9], Rf[9];
+      for (int i = 0; i < 9; ++i) Ff[i] = (float)Fn[i];
+      polar_newton_f32(Ff, Rf);
+      for (int i = 0; i < 9; ++i) R[i] = (T)Rf[i];
+    } else {
+      double Fd64[9], R64[9];
+      for (int i = 0; i < 9; ++i) Fd64[i] = (double)Fn[i];
+      polar_rotation_f64(Fd64, R64);
+      for (int i = 0; i < 9; ++i) R[i] = (T)R64[i];
+    }
+    // stress = 2 mu (F - R) F^T + lam J (J - 1) I, mpm3d.py:247-251.
+    T twomu = (T)2.0 * mu;
+    T Pm[9];
+    for (int i = 0; i < 9; ++i) Pm[i] = twomu * (Fn[i] - R[i]);
+    matmul3(Pm, Ft, stress);
+    T lj = (lam * J) * (J - (T)1.0);
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) stress[3 * a + b] = stress[3 * a + b] + lj * (T)(a == b ? 1 : 0);
+  }
   T coef = (((-dt) * P.vol[p]) * (T)4.0) * mp.inv_dx;
   coef = coef * mp.inv_dx;
   T affine[9];
@@ -681,11 +695,11 @@ static void mpm_substep_impl(int nx, int ny, int nz, int n, T* x, T* v, T* C, T*
                              const T* vol, const int32_t* active, T* fp, T* gv, T* gm, T dt, T dx,
                              T inv_dx, T mu, T lam, const T* gravity, int bw, T damping, int apic,
                              T lower, const T* upper, int nthreads, int deterministic,
-                             int polar_mode) {
-  Particles<T> P{n, x, v, C, Fd, mass, vol, active, fp};
+                             int polar_mode, const T* mu_p, const T* lam_p, int material) {
+  Particles<T> P{n, x, v, C, Fd, mass, vol, active, fp, mu_p, lam_p};
   Grid<T> G{nx, ny, nz, gv, gm};
   MpmParams<T> mp{dt, dx, inv_dx, mu, lam, {gravity[0], gravity[1], gravity[2]}, damping, bw, apic,
-                  polar_mode};
+                  polar_mode, material};
   const long N = (long)nx * ny * nz;
   std::memset(gv, 0, sizeof(T) * 3 * N);
   std::memset(gm, 0, sizeof(T) * N);
@@ -707,10 +721,11 @@ FSI_ORACLE_EXPORT void oracle_mpm_substep_f32(int nx, int ny, int nz, int n, flo
                                               float inv_dx, float mu, float lam,
                                               const float* gravity, int bw, float damping, int apic,
                                               float lower, const float* upper, int nthreads,
-                                              int deterministic, int polar_mode) {
+                                              int deterministic, int polar_mode,
+                                              const float* mu_p, const float* lam_p, int material) {
   mpm_substep_impl<float>(nx, ny, nz, n, x, v, C, Fd, mass, vol, active, fp, gv, gm, dt, dx, inv_dx,
                           mu, lam, gravity, bw, damping, apic, lower, upper, nthreads,
-                          deterministic, polar_mode);
+                          deterministic, polar_mode, mu_p, lam_p, material);
 }
 
 FSI_ORACLE_EXPORT void oracle_mpm_substep_f64(int nx, int ny, int nz, int n, double* x, double* v,
@@ -720,10 +735,11 @@ FSI_ORACLE_EXPORT void oracle_mpm_substep_f64(int nx, int ny, int nz, int n, dou
                                               double inv_dx, double mu, double lam,
                                               const double* gravity, int bw, double damping,
                                               int apic, double lower, const double* upper,
-                                              int nthreads, int deterministic, int polar_mode) {
+                                              int nthreads, int deterministic, int polar_mode,
+                                              const double* mu_p, const double* lam_p, int material) {
   mpm_substep_impl<double>(nx, ny, nz, n, x, v, C, Fd, mass, vol, active, fp, gv, gm, dt, dx,
                            inv_dx, mu, lam, gravity, bw, damping, apic, lower, upper, nthreads,
-                           deterministic, polar_mode);
+                           deterministic, polar_mode, mu_p, lam_p, material);
 }
 
 // Polar rotation of 3x3 float32 matrices with the device operation order.

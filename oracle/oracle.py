@@ -279,6 +279,7 @@ class MPMSolver3D:
         self.particle_force = np.zeros((P, 3), dt)
         self.grid_v = np.zeros((self.nx, self.ny, self.nz, 3), dt)
         self.grid_m = np.zeros((self.nx, self.ny, self.nz), dt)
+        self.mu_p = self.lam_p = None
         self._initialized = False
 
     def initialize_particles_box(self, lower, upper, spacing=None, initial_velocity=(0.0, 0.0, 0.0)):
@@ -303,7 +304,8 @@ class MPMSolver3D:
         return self.initialize_particles_from_numpy(pos, velocities=vel, particle_volume=float(np.prod(sp)))
 
     def initialize_particles_from_numpy(self, positions, velocities=None, particle_mass=None,
-                                        particle_volume=None):
+                                        particle_volume=None, youngs_modulus=None,
+                                        poisson_ratio=None):
         pos = np.asarray(positions, dtype=np.float32)
         if pos.ndim != 2 or pos.shape[1] != 3:
             raise ValueError("positions must have shape (n, 3).")
@@ -331,6 +333,18 @@ class MPMSolver3D:
         self.mass[:n] = dt.type(np.float32(mass))
         self.volume[:n] = dt.type(np.float32(vol))
         self.active[:n] = 1
+        self.mu_p = self.lam_p = None
+        if youngs_modulus is not None or poisson_ratio is not None:
+            E = np.broadcast_to(np.asarray(self.config.youngs_modulus if youngs_modulus is None
+                                           else youngs_modulus, np.float64), (n,))
+            nu = np.broadcast_to(np.asarray(self.config.poisson_ratio if poisson_ratio is None
+                                            else poisson_ratio, np.float64), (n,))
+            mu = E / (2.0 * (1.0 + nu))
+            lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+            self.mu_p = np.zeros(self.max_particles, self.dtype)
+            self.lam_p = np.zeros(self.max_particles, self.dtype)
+            self.mu_p[:n] = mu.astype(np.float32).astype(self.dtype)
+            self.lam_p[:n] = lam.astype(np.float32).astype(self.dtype)
         self.num_particles = n
         self._initialized = True
         return n
@@ -353,7 +367,10 @@ class MPMSolver3D:
             _p(self.grid_v), _p(self.grid_m), cast(dt_value), cast(self.dx), cast(self.inv_dx),
             cast(self.mu), cast(self.lam), _p(grav), self.boundary_width,
             cast(self.boundary_damping), int(self.apic), cast(0.5 * self.dx), _p(upper),
-            self.nthreads, int(self.deterministic), 1 if self.polar == "device" else 0)
+            self.nthreads, int(self.deterministic), 1 if self.polar == "device" else 0,
+            _p(self.mu_p) if self.mu_p is not None else None,
+            _p(self.lam_p) if self.lam_p is not None else None,
+            1 if getattr(self.config, "constitutive_model", "fixed_corotated") == "neo_hookean" else 0)
 
     def clear_particle_force(self):
         self.particle_force[: self.num_particles] = 0

@@ -37,6 +37,7 @@ struct Mpm {
   float lower, upper[3];
   long long cap;
   int nbx, nby, nbz;  // 4^3 block grid
+  int material;       // FSI_MATERIAL_*
 };
 
 struct PView {
@@ -48,6 +49,8 @@ struct PView {
   const float* __restrict__ vol;
   const int32_t* __restrict__ active;
   float* __restrict__ fp;
+  const float* __restrict__ mu;   // per-particle Lame parameters, or NULL
+  const float* __restrict__ lam;
 };
 
 __device__ __forceinline__ void base_fx(const Mpm& m, const float x[3], int base[3], float fx[3]) {
@@ -269,20 +272,32 @@ __global__ void __launch_bounds__(kBlock) p2g_kernel(Mpm m, PView P, float4* __r
 #pragma unroll
     for (int i = 0; i < 9; ++i) P.F[i * cap + p] = Fn[i];
     const float J = det3(Fn);
-    float R[9];
-    polar_rotation(Fn, R);
-    // stress = 2 mu (F - R) F^T + lam J (J - 1) I (mpm3d.py:247-251)
-    const float twomu = __fmul_rn(2.f, m.mu);
-    float Pm[9], Ft[9], S[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) Pm[i] = __fmul_rn(twomu, __fsub_rn(Fn[i], R[i]));
+    const float mu = P.mu ? P.mu[p] : m.mu;
+    const float lam = P.lam ? P.lam[p] : m.lam;
+    float Ft[9], S[9];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int b = 0; b < 3; ++b) Ft[3 * a + b] = Fn[3 * b + a];
-    matmul3(Pm, Ft, S);
-    const float lj = __fmul_rn(__fmul_rn(m.lam, J), __fsub_rn(J, 1.f));
-    S[0] = __fadd_rn(S[0], lj); S[4] = __fadd_rn(S[4], lj); S[8] = __fadd_rn(S[8], lj);
+    if (m.material == FSI_MATERIAL_NEO_HOOKEAN) {
+      // Kirchhoff stress of compressible Neo-Hookean: mu (F F^T - I) + lam ln(J) I.
+      matmul3(Fn, Ft, S);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) S[i] = __fmul_rn(mu, __fsub_rn(S[i], (i % 4 == 0) ? 1.f : 0.f));
+      const float ll = __fmul_rn(lam, logf(J));
+      S[0] = __fadd_rn(S[0], ll); S[4] = __fadd_rn(S[4], ll); S[8] = __fadd_rn(S[8], ll);
+    } else {
+      // Fixed-corotated: 2 mu (F - R) F^T + lam J (J - 1) I (mpm3d.py:247-251)
+      float R[9];
+      polar_rotation(Fn, R);
+      const float twomu = __fmul_rn(2.f, mu);
+      float Pm[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) Pm[i] = __fmul_rn(twomu, __fsub_rn(Fn[i], R[i]));
+      matmul3(Pm, Ft, S);
+      const float lj = __fmul_rn(__fmul_rn(lam, J), __fsub_rn(J, 1.f));
+      S[0] = __fadd_rn(S[0], lj); S[4] = __fadd_rn(S[4], lj); S[8] = __fadd_rn(S[8], lj);
+    }
     float coef = __fmul_rn(__fmul_rn(__fmul_rn(-m.dt, P.vol[p]), 4.f), m.inv_dx);
     coef = __fmul_rn(coef, m.inv_dx);
     mass = P.mass[p];
@@ -551,8 +566,12 @@ int make_mpm(const fsi_mpm_desc* d, const fsi_particles* p, Mpm& m, PView& v) {
   m.lower = d->clamp_lower;
   m.cap = p->capacity;
   m.nbx = (d->nx + 3) / 4; m.nby = (d->ny + 3) / 4; m.nbz = (d->nz + 3) / 4;
+  FSI_REQUIRE(d->material == FSI_MATERIAL_FIXED_COROTATED || d->material == FSI_MATERIAL_NEO_HOOKEAN,
+              "unknown material %d", d->material);
+  FSI_REQUIRE((p->mu == nullptr) == (p->lam == nullptr), "per-particle mu and lam go together");
+  m.material = d->material;
   v.x = p->x; v.v = p->v; v.C = p->C; v.F = p->F; v.mass = p->mass; v.vol = p->volume;
-  v.active = p->active; v.fp = p->force;
+  v.active = p->active; v.fp = p->force; v.mu = p->mu; v.lam = p->lam;
   return FSI_OK;
 }
 

@@ -52,6 +52,7 @@ class MpmDesc(ctypes.Structure):
         ("apic", ctypes.c_int32),
         ("clamp_lower", ctypes.c_float),
         ("clamp_upper", c_float3),
+        ("material", ctypes.c_int32),
     ]
 
 
@@ -61,6 +62,7 @@ class Particles(ctypes.Structure):
         ("F", ctypes.c_void_p), ("mass", ctypes.c_void_p), ("volume", ctypes.c_void_p),
         ("active", ctypes.c_void_p), ("force", ctypes.c_void_p),
         ("capacity", ctypes.c_int64),
+        ("mu", ctypes.c_void_p), ("lam", ctypes.c_void_p),
     ]
 
 

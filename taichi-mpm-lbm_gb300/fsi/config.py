@@ -112,6 +112,10 @@ class MPMConfig:
     boundary_width: int = 3
     boundary_damping: float = 0.0
 
+    # Extension (no reference counterpart): the elastic model. The reference's solver is
+    # fixed-corotated (mpm3d.py:247-251); "neo_hookean" selects mu (F F^T - I) + lam ln(J) I.
+    constitutive_model: Literal["fixed_corotated", "neo_hookean"] = "fixed_corotated"
+
     def validate(self) -> None:
         _check_grid("MPM", self.nx, self.ny, self.nz)
         if self.max_particles <= 0:
@@ -135,6 +139,11 @@ class MPMConfig:
             raise ValueError("boundary_width must be at least 1.")
         if not (0.0 <= self.boundary_damping <= 1.0):
             raise ValueError("boundary_damping must be in [0, 1].")
+        if self.constitutive_model not in _CONSTITUTIVE_MODELS:
+            raise ValueError(f"Unsupported constitutive model: {self.constitutive_model}.")
+
+
+_CONSTITUTIVE_MODELS = frozenset({"fixed_corotated", "neo_hookean"})
 
 
 @dataclass(frozen=True)

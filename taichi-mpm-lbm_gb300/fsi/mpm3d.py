@@ -81,7 +81,38 @@ class MPMSolver3D:
         d.clamp_lower = float(np.float32(0.5 * self.dx))
         for i, n in enumerate((self.nx, self.ny, self.nz)):
             d.clamp_upper[i] = float(np.float32((n - 1.5) * self.dx))
+        d.material = 1 if self.config.constitutive_model == "neo_hookean" else 0
         return d
+
+    @staticmethod
+    def lame_parameters(youngs_modulus, poisson_ratio):
+        """(mu, lam) of mpm3d.py:33-38 for scalars or arrays."""
+        E = np.asarray(youngs_modulus, dtype=np.float64)
+        nu = np.asarray(poisson_ratio, dtype=np.float64)
+        mu = E / (2.0 * (1.0 + nu))
+        lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+        return mu, lam
+
+    def _set_particle_materials(self, count: int, youngs_modulus, poisson_ratio) -> None:
+        if youngs_modulus is None and poisson_ratio is None:
+            self._mu_p = self._lam_p = None
+            self._parts.mu = self._parts.lam = None
+            return
+        E = np.broadcast_to(np.asarray(self.config.youngs_modulus if youngs_modulus is None
+                                       else youngs_modulus, np.float64), (count,))
+        nu = np.broadcast_to(np.asarray(self.config.poisson_ratio if poisson_ratio is None
+                                        else poisson_ratio, np.float64), (count,))
+        if np.any(E <= 0.0):
+            raise ValueError("Young's modulus must be positive.")
+        if np.any((nu <= -1.0) | (nu >= 0.5)):
+            raise ValueError("Poisson ratio must be in (-1, 0.5).")
+        mu, lam = self.lame_parameters(E, nu)
+        self._mu_p = torch.zeros(self.max_particles, dtype=torch.float32, device=self._device)
+        self._lam_p = torch.zeros(self.max_particles, dtype=torch.float32, device=self._device)
+        self._mu_p[:count] = torch.from_numpy(mu.astype(np.float32))
+        self._lam_p[:count] = torch.from_numpy(lam.astype(np.float32))
+        self._parts.mu = self._mu_p.data_ptr()
+        self._parts.lam = self._lam_p.data_ptr()
 
     def _make_particles(self) -> nat.Particles:
         p = nat.Particles()
@@ -115,8 +146,14 @@ class MPMSolver3D:
                                                     particle_volume=float(np.prod(sp)))
 
     def initialize_particles_from_numpy(self, positions, velocities=None, particle_mass=None,
-                                        particle_volume=None) -> int:
-        """Load particles; F = I, C = 0, active = 1 (mpm3d.py:98-165)."""
+                                        particle_volume=None, youngs_modulus=None,
+                                        poisson_ratio=None) -> int:
+        """Load particles; F = I, C = 0, active = 1 (mpm3d.py:98-165).
+
+        ``youngs_modulus`` / ``poisson_ratio`` (scalar or one value per particle) are an
+        extension: per-particle materials, e.g. bodies of different stiffness in one solver.
+        When both are None the configuration's single material applies, as in the reference.
+        """
         pos = np.asarray(positions, dtype=np.float32)
         if pos.ndim != 2 or pos.shape[1] != 3:
             raise ValueError("positions must have shape (n, 3).")
@@ -150,6 +187,7 @@ class MPMSolver3D:
         self._mass[:count] = float(np.float32(mass))
         self._volume[:count] = float(np.float32(volume))
         self._active[:count] = 1
+        self._set_particle_materials(count, youngs_modulus, poisson_ratio)
         self._num_particles = count
         self._desc.num_particles = count
         self._initialized = True

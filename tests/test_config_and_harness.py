@@ -44,6 +44,7 @@ def test_defaults_validate_and_mpm_dt():
     CouplingConfig(contact_velocity_damping=1.1), CouplingConfig(contact_fraction_threshold=-0.1),
     CouplingConfig(contact_fraction_threshold=1.1), OutputConfig(output_interval=0),
     OutputConfig(output_format="bad"), BoundaryConfig(velocity=(0.0, 1.0)),
+    MPMConfig(constitutive_model="plastic"),
     SimulationConfig(lbm=LBMConfig(nx=64, ny=32, nz=16), mpm=MPMConfig(nx=32, ny=32, nz=16)),
 ])
 def test_invalid_configs_raise_value_error(bad):

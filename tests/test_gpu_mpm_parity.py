@@ -146,3 +146,30 @@ def test_grid_is_left_clean_between_substeps():
         s.substep()
         assert float(s._grid.abs().max()) == 0.0
         assert int(s._dirty.max()) == 0
+
+
+@pytest.mark.parametrize("model", ["fixed_corotated", "neo_hookean"])
+def test_material_models_and_per_particle_moduli(model):
+    """Extensions with no reference counterpart, checked against the oracle restatement:
+    the Neo-Hookean model and per-particle Young's moduli (two bodies of different stiffness)."""
+    cfg = mpm_cfg(gravity=(0.0, -1.0e-3, 0.0), dt=1.0e-2, youngs_modulus=500.0,
+                  constitutive_model=model)
+    g, o = MPMSolver3D(cfg), O.MPMSolver3D(cfg)
+    rng = np.random.default_rng(8)
+    a = np.stack(np.meshgrid(*[np.arange(4.0, 6.0, 0.5)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    b = a + np.array([5.0, 1.0, 3.0])
+    pos = np.concatenate([a, b]).astype(np.float32)
+    vel = rng.normal(0, 1e-2, pos.shape).astype(np.float32)
+    E = np.concatenate([np.full(len(a), 200.0), np.full(len(b), 800.0)])
+    for s in (g, o):
+        s.initialize_particles_from_numpy(pos, vel, particle_volume=0.125, youngs_modulus=E)
+    for _ in range(20):
+        g.substep()
+        o.substep()
+    assert rel_l2(g.positions_numpy(), o.positions_numpy()) < 1e-6
+    assert rel_l2(g.velocities_numpy(), o.velocities_numpy()) < 1e-3
+    assert rel_l2(g.deformation_gradients_numpy(), o.deformation_gradients_numpy()) < 1e-5
+    # the stiffer body deforms less
+    Fg = g.deformation_gradients_numpy()
+    dev = np.linalg.norm(Fg - np.eye(3), axis=(1, 2))
+    assert dev[len(a):].mean() < dev[: len(a)].mean()
