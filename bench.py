@@ -62,7 +62,7 @@ class ClockSampler:
         try:
             self._proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._thread = threading.Thread(target=self._read, daemon=True)
             self._thread.start()
@@ -164,31 +164,38 @@ def run_gpu(args) -> dict:
         lbm.step()
     barrier(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
+    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    with clocks:
+        time.sleep(0.3)  # let the sampler start before the timed region
         e0.record(stream)
         for _ in range(args.steps):
             lbm.step()
         e1.record(stream)
         barrier(world)
+        # --- solid, device-resident -----------------------------------------------
+        for _ in range(args.warmup):
+            mpm.substep()
+        barrier(world)
+        m0.record(stream)
+        for _ in range(args.steps):
+            mpm.substep()
+        m1.record(stream)
+        barrier(world)
     lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
     lbm_launches = args.steps
-
-    # --- solid, device-resident ---------------------------------------------------
-    for _ in range(args.warmup):
-        mpm.substep()
-    barrier(world)
-    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    m0.record(stream)
-    for _ in range(args.steps):
-        mpm.substep()
-    m1.record(stream)
-    barrier(world)
     mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
-    touched = int(mpm._dirty.numel())  # refined below from the particle bounding cells
-    base = mpm.base_cells_numpy()
-    nodes = np.unique(((base[:, 0] * 3 + 0) * 0 + (base[:, 0].astype(np.int64) * args.n
-                                                     + base[:, 1]) * args.n + base[:, 2]))
-    touched = int(len(nodes))  # distinct base cells; each owns ~1 stencil node-equivalent
+    base = mpm.base_cells_numpy().astype(np.int64)
+    # grid nodes touched per substep: the union of the particles' 27-node stencils
+    cells = np.unique((base[:, 0] * args.n + base[:, 1]) * args.n + base[:, 2])
+    touched = int(len(cells)) + 0
+    ci, cj, ck = cells // (args.n * args.n), (cells // args.n) % args.n, cells % args.n
+    stencil = set()
+    for di in range(3):
+        for dj in range(3):
+            for dk in range(3):
+                stencil.update(((ci + di) * args.n + cj + dj) * args.n + ck + dk)
+    touched = len(stencil)
 
     # --- end to end through the public API (host input, host result each step) ----
     g_host = np.array(lcfg.force, dtype=np.float32)
@@ -338,7 +345,7 @@ def run_reference(args) -> dict | None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (default 256)")

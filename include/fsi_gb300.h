@@ -125,6 +125,14 @@ int fsi_lbm_force_op(const fsi_lbm_desc* desc, const uint32_t* flags, int op, co
 int fsi_lbm_reduce(const fsi_lbm_desc* desc, const float* macro, const float* force,
                    const uint32_t* flags, double* out, void* stream);
 
+/* fsi_lbm_update_macro fused with the two per-step runner diagnostics: writes `macro` and
+ * device double out[0] = sum of rho over fluid cells, out[1] = max |u| over all cells
+ * (LBMSolver3D.total_mass / max_velocity_norm, lbm3d.py:450-457, as called by
+ * FSISimulation.diagnostics, simulation.py:117-147), in one pass over the populations. */
+int fsi_lbm_macro_diagnostics(const fsi_lbm_desc* desc, const float* pops, const float* force,
+                              const uint32_t* flags, int64_t steps_done, float* macro,
+                              double* out, void* stream);
+
 /* ------------------------------------------------------------------ MPM -- */
 
 /* Solid (MLS-MPM) description. Replaces the scalar fields of MPMSolver3D

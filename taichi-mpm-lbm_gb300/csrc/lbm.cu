@@ -170,22 +170,72 @@ struct StepArgs {
   int write_faces;
 };
 
+// Launch shape of the cell kernels: x = z (contiguous, coalesced), y = y rows, z = x planes,
+// so a thread knows (i, j, k) without integer division.
+struct CellLaunch {
+  dim3 grid, block;
+};
+
+CellLaunch cell_launch(const LbmGeom& g) {
+  int bz = ((g.nz + 31) / 32) * 32;
+  if (bz > kBlock) bz = kBlock;
+  int by = kBlock / bz;
+  if (by > g.ny) by = g.ny;
+  return CellLaunch{dim3((g.nz + bz - 1) / bz, (g.ny + by - 1) / by, g.nx), dim3(bz, by, 1)};
+}
+
+// Signed 32-bit offsets from a cell to its +-1 neighbours on each axis, periodic wrap included
+// (lbm3d.py:335-350). A neighbour index is then one three-operand add.
+struct Deltas {
+  uint32_t c;
+  int xp, xm, yp, ym, zp, zm;
+  __device__ __forceinline__ Deltas(const LbmGeom& g, int i, int j, int k) {
+    const int nyz = g.ny * g.nz;
+    c = (uint32_t)((i * g.ny + j) * g.nz + k);
+    xp = i == g.nx - 1 ? -(g.nx - 1) * nyz : nyz;
+    xm = i == 0 ? (g.nx - 1) * nyz : -nyz;
+    yp = j == g.ny - 1 ? -(g.ny - 1) * g.nz : g.nz;
+    ym = j == 0 ? (g.ny - 1) * g.nz : -g.nz;
+    zp = k == g.nz - 1 ? -(g.nz - 1) : 1;
+    zm = k == 0 ? g.nz - 1 : -1;
+  }
+  // Index of x + s * e_q.
+  __device__ __forceinline__ uint32_t nb(int q, int s) const {
+    const int dx = s * ex(q), dy = s * ey(q), dz = s * ez(q);
+    const int ox = dx > 0 ? xp : (dx < 0 ? xm : 0);
+    const int oy = dy > 0 ? yp : (dy < 0 ? ym : 0);
+    const int oz = dz > 0 ? zp : (dz < 0 ? zm : 0);
+    return c + (uint32_t)(ox + oy + oz);
+  }
+};
+
 template <bool kOdd, bool kRecompute>
 __global__ void __launch_bounds__(kBlock) lbm_step_kernel(StepArgs a) {
-  const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-  if (c >= a.g.n) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  if (k >= a.g.nz || j >= a.g.ny) return;
+  const Deltas d(a.g, i, j, k);
+  const uint32_t c = d.c;
   const uint32_t fl = a.flags[c];
   if (fl & kFlagSolid) return;
-  const long long n = a.g.n;
-  const Nbr nb(c, a.g);
+  const uint32_t n = (uint32_t)a.g.n;
+  float* __restrict__ pops = a.pops;
 
   float F[19];
   if (!kOdd) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) F[q] = a.pops[(long long)q * n + c];
+    for (int q = 0; q < 19; ++q) F[q] = pops[q * n + c];
   } else {
+    F[0] = pops[c];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) F[q] = gather_post_stream(a.pops, n, c, nb, fl, q, 1);
+    for (int q = 1; q < 19; ++q) {
+      // F_q(x) = f*_q(x - e_q) in slot opp(q) there, or f*_opp(q)(x) in slot q here when
+      // x - e_q is solid (half-way bounce-back).
+      const bool bounce = (fl >> opp(q)) & 1u;
+      const uint32_t idx = bounce ? q * n + c : opp(q) * n + d.nb(q, -1);
+      F[q] = pops[idx];
+    }
   }
 
   const float gx = a.force[c], gy = a.force[n + c], gz = a.force[2 * n + c];
@@ -204,14 +254,14 @@ __global__ void __launch_bounds__(kBlock) lbm_step_kernel(StepArgs a) {
 
   if (!kOdd) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) a.pops[(long long)opp(q) * n + c] = out[q];
+    for (int q = 0; q < 19; ++q) pops[opp(q) * n + c] = out[q];
   } else {
+    pops[c] = out[0];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) {
-      if (q == 0 || (fl & (1u << q)))
-        a.pops[(long long)opp(q) * n + c] = out[q];
-      else
-        a.pops[(long long)q * n + nb.at(q, +1)] = out[q];
+    for (int q = 1; q < 19; ++q) {
+      const bool bounce = (fl >> q) & 1u;
+      const uint32_t idx = bounce ? opp(q) * n + c : q * n + d.nb(q, +1);
+      pops[idx] = out[q];
     }
   }
 }
@@ -284,22 +334,89 @@ struct MacroArgs {
   float rho0;
 };
 
-__global__ void __launch_bounds__(kBlock) lbm_macro_kernel(MacroArgs a) {
-  const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-  if (c >= a.g.n) return;
-  const uint32_t fl = a.flags[c];
-  if (fl & kFlagSolid) {
-    a.macro[c] = make_float4(0.f, 0.f, 0.f, a.rho0);
-    return;
-  }
-  const long long n = a.g.n;
-  const Nbr nb(c, a.g);
-  float F[19];
+// Post-stream F_q(x) of a fluid cell in a state of the given parity (32-bit addressing).
+__device__ __forceinline__ float gather32(const float* __restrict__ pops, uint32_t n,
+                                          const Deltas& d, uint32_t fl, int q, int parity) {
+  if (parity == 0 || q == 0 || ((fl >> opp(q)) & 1u)) return pops[q * n + d.c];
+  return pops[opp(q) * n + d.nb(q, -1)];
+}
+
+// numpy float32 norm of a 3-vector: sqrt((x*x + y*y) + z*z).
+__device__ __forceinline__ float norm3_ref(float x, float y, float z) {
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+  atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+// Adds this block's sums of `s` (float32 within a warp, float64 across warps) into
+// sums[0..NS) and, when max_out is not NULL, raises *max_out to the block maximum of `mx`.
+// Every thread of the block must call it; each instantiation owns its shared scratch.
+template <int NS>
+__device__ void block_accumulate(double* __restrict__ sums, const float (&s)[NS],
+                                 double* __restrict__ max_out, float mx) {
+  float v[NS];
 #pragma unroll
-  for (int q = 0; q < 19; ++q) F[q] = gather_post_stream(a.pops, n, c, nb, fl, q, a.parity);
-  float rho, ux, uy, uz;
-  macro_of(F, a.force[c], a.force[n + c], a.force[2 * n + c], rho, ux, uy, uz);
-  a.macro[c] = make_float4(ux, uy, uz, rho);
+  for (int i = 0; i < NS; ++i) v[i] = s[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  }
+  __shared__ double sh[NS][kBlock / 32];
+  __shared__ float shm[kBlock / 32];
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  const int nwarps = (blockDim.x * blockDim.y + 31) / 32;
+  if ((t & 31) == 0) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) sh[i][t >> 5] = (double)v[i];
+    shm[t >> 5] = mx;
+  }
+  __syncthreads();
+  if (t == 0) {
+    float m = 0.f;
+    for (int w = 0; w < nwarps; ++w) m = fmaxf(m, shm[w]);
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      double acc = 0.0;
+      for (int w = 0; w < nwarps; ++w) acc += sh[i][w];
+      atomicAdd(sums + i, acc);
+    }
+    if (max_out) atomic_max_nonneg(max_out, (double)m);
+  }
+}
+
+// update_macro (lbm3d.py:409-425) on the current state; with `diag` non-NULL it also adds
+// sum(rho) over fluid cells to diag[0] and raises diag[1] to max |u| (lbm3d.py:450-457).
+__global__ void __launch_bounds__(kBlock) lbm_macro_kernel(MacroArgs a, double* __restrict__ diag) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  float mass = 0.f, vmax = 0.f;
+  if (k < a.g.nz && j < a.g.ny) {
+    const Deltas d(a.g, i, j, k);
+    const uint32_t c = d.c;
+    const uint32_t fl = a.flags[c];
+    if (fl & kFlagSolid) {
+      a.macro[c] = make_float4(0.f, 0.f, 0.f, a.rho0);
+    } else {
+      const uint32_t n = (uint32_t)a.g.n;
+      float F[19];
+#pragma unroll
+      for (int q = 0; q < 19; ++q) F[q] = gather32(a.pops, n, d, fl, q, a.parity);
+      float rho, ux, uy, uz;
+      macro_of(F, a.force[c], a.force[n + c], a.force[2 * n + c], rho, ux, uy, uz);
+      a.macro[c] = make_float4(ux, uy, uz, rho);
+      mass = rho;
+      vmax = norm3_ref(ux, uy, uz);
+    }
+  }
+  if (diag) {
+    const float s[1] = {mass};
+    block_accumulate<1>(diag, s, diag + 1, vmax);
+  }
 }
 
 __global__ void __launch_bounds__(kBlock) lbm_distribution_kernel(LbmGeom g,
@@ -365,70 +482,39 @@ __global__ void __launch_bounds__(kBlock) lbm_force_kernel(LbmGeom g,
   }
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ float warp_max(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
-  return v;
-}
-
-__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
-  atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
-}
-
+// Lattice diagnostics of the current macro and force fields (lbm3d.py:450-483):
+// out[0] += sum rho over fluid, out[1] = max |u| over all cells, out[2..4] += sum force over fluid.
 __global__ void __launch_bounds__(kBlock) lbm_reduce_kernel(LbmGeom g,
                                                             const float4* __restrict__ macro,
                                                             const float* __restrict__ force,
                                                             const uint32_t* __restrict__ flags,
                                                             double* __restrict__ out) {
-  double mass = 0, fx = 0, fy = 0, fz = 0;
-  float vmax = 0.f;
-  for (long long c = (long long)blockIdx.x * kBlock + threadIdx.x; c < g.n;
-       c += (long long)gridDim.x * kBlock) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  float mass = 0.f, vmax = 0.f, f[3] = {0.f, 0.f, 0.f};
+  if (k < g.nz && j < g.ny) {
+    const uint32_t c = (uint32_t)((i * g.ny + j) * g.nz + k);
+    const uint32_t n = (uint32_t)g.n;
     const float4 m = macro[c];
-    // numpy float32 norm of a length-3 vector: sqrt((x*x + y*y) + z*z).
-    const float nrm = __fsqrt_rn(
-        __fadd_rn(__fadd_rn(__fmul_rn(m.x, m.x), __fmul_rn(m.y, m.y)), __fmul_rn(m.z, m.z)));
-    vmax = fmaxf(vmax, nrm);
+    vmax = norm3_ref(m.x, m.y, m.z);
     if (!(flags[c] & kFlagSolid)) {
-      mass += (double)m.w;
-      if (force) {
-        fx += (double)force[c];
-        fy += (double)force[g.n + c];
-        fz += (double)force[2 * g.n + c];
-      }
+      mass = m.w;
+      if (force) { f[0] = force[c]; f[1] = force[n + c]; f[2] = force[2 * n + c]; }
     }
   }
-  __shared__ double sh[4][kBlock / 32];
-  __shared__ float shm[kBlock / 32];
-  mass = warp_sum(mass); fx = warp_sum(fx); fy = warp_sum(fy); fz = warp_sum(fz);
-  vmax = warp_max(vmax);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) { sh[0][wid] = mass; sh[1][wid] = fx; sh[2][wid] = fy; sh[3][wid] = fz; shm[wid] = vmax; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s[4] = {0, 0, 0, 0};
-    float mx = 0.f;
-    for (int w = 0; w < kBlock / 32; ++w) {
-      for (int i = 0; i < 4; ++i) s[i] += sh[i][w];
-      mx = fmaxf(mx, shm[w]);
-    }
-    atomicAdd(out + 0, s[0]);
-    atomic_max_nonneg(out + 1, (double)mx);
-    atomicAdd(out + 2, s[1]);
-    atomicAdd(out + 3, s[2]);
-    atomicAdd(out + 4, s[3]);
-  }
+  const float s1[1] = {mass};
+  block_accumulate<1>(out, s1, out + 1, vmax);
+  block_accumulate<3>(out + 2, f, nullptr, 0.f);
 }
 
 int check_desc(const fsi_lbm_desc* d) {
   FSI_REQUIRE(d != nullptr, "lbm descriptor is NULL");
   FSI_REQUIRE(d->nx > 4 && d->ny > 4 && d->nz > 4, "lattice %dx%dx%d too small", d->nx, d->ny, d->nz);
-  FSI_REQUIRE((long long)d->nx * d->ny * d->nz < (1ll << 40), "lattice too large");
+  FSI_REQUIRE(19ll * d->nx * d->ny * d->nz < (1ll << 32),
+              "lattice of %lld cells too large for 32-bit population indexing",
+              (long long)d->nx * d->ny * d->nz);
+  FSI_REQUIRE(d->nx <= 65535, "nx must be at most 65535");
   FSI_REQUIRE(d->s[0] == 0.f && d->s[3] == 0.f && d->s[5] == 0.f && d->s[7] == 0.f,
               "conserved moments (0, 3, 5, 7) must have zero relaxation rate");
   for (int side = 0; side < 2; ++side) {
@@ -478,14 +564,14 @@ extern "C" int fsi_lbm_step(const fsi_lbm_desc* d, float* pops, float* macro, co
   for (int k = 0; k < 19; ++k) a.s[k] = d->s[k];
   a.write_faces = (d->bc_mode_left != 0 || d->bc_mode_right != 0) ? 1 : 0;
   cudaStream_t s = as_stream(stream);
-  const unsigned grid = grid_for(a.g.n, kBlock);
+  const CellLaunch L = cell_launch(a.g);
   const bool odd = (steps_done & 1) != 0;
   if (force_prev) {
-    if (odd) lbm_step_kernel<true, true><<<grid, kBlock, 0, s>>>(a);
-    else lbm_step_kernel<false, true><<<grid, kBlock, 0, s>>>(a);
+    if (odd) lbm_step_kernel<true, true><<<L.grid, L.block, 0, s>>>(a);
+    else lbm_step_kernel<false, true><<<L.grid, L.block, 0, s>>>(a);
   } else {
-    if (odd) lbm_step_kernel<true, false><<<grid, kBlock, 0, s>>>(a);
-    else lbm_step_kernel<false, false><<<grid, kBlock, 0, s>>>(a);
+    if (odd) lbm_step_kernel<true, false><<<L.grid, L.block, 0, s>>>(a);
+    else lbm_step_kernel<false, false><<<L.grid, L.block, 0, s>>>(a);
   }
   if (int e = check_launch("lbm_step_kernel")) return e;
   if (a.write_faces) {
@@ -518,7 +604,8 @@ extern "C" int fsi_lbm_update_macro(const fsi_lbm_desc* d, const float* pops, co
   FSI_REQUIRE(pops && force && flags && macro, "NULL array");
   MacroArgs a{geom_of(d), pops, force, flags, reinterpret_cast<float4*>(macro),
               (int)(steps_done & 1), d->rho0};
-  lbm_macro_kernel<<<grid_for(a.g.n, kBlock), kBlock, 0, as_stream(stream)>>>(a);
+  const CellLaunch L = cell_launch(a.g);
+  lbm_macro_kernel<<<L.grid, L.block, 0, as_stream(stream)>>>(a, nullptr);
   return check_launch("lbm_macro_kernel");
 }
 
@@ -554,9 +641,23 @@ extern "C" int fsi_lbm_reduce(const fsi_lbm_desc* d, const float* macro, const f
   LbmGeom g = geom_of(d);
   cudaStream_t s = as_stream(stream);
   if (cudaMemsetAsync(out, 0, 8 * sizeof(double), s) != cudaSuccess) return check_launch("memset");
-  int blocks = (int)grid_for(g.n, kBlock);
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  lbm_reduce_kernel<<<blocks, kBlock, 0, s>>>(g, reinterpret_cast<const float4*>(macro), force,
-                                              flags, out);
+  const CellLaunch L = cell_launch(g);
+  lbm_reduce_kernel<<<L.grid, L.block, 0, s>>>(g, reinterpret_cast<const float4*>(macro), force,
+                                               flags, out);
   return check_launch("lbm_reduce_kernel");
+}
+
+extern "C" int fsi_lbm_macro_diagnostics(const fsi_lbm_desc* d, const float* pops,
+                                         const float* force, const uint32_t* flags,
+                                         int64_t steps_done, float* macro, double* out,
+                                         void* stream) {
+  if (int e = check_desc(d)) return e;
+  FSI_REQUIRE(pops && force && flags && macro && out, "NULL array");
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(out, 0, 2 * sizeof(double), s) != cudaSuccess) return check_launch("memset");
+  MacroArgs a{geom_of(d), pops, force, flags, reinterpret_cast<float4*>(macro),
+              (int)(steps_done & 1), d->rho0};
+  const CellLaunch L = cell_launch(a.g);
+  lbm_macro_kernel<<<L.grid, L.block, 0, s>>>(a, out);
+  return check_launch("lbm_macro_kernel (diagnostics)");
 }

@@ -633,3 +633,4 @@ extern "C" int fsi_mpm_reduce(const fsi_mpm_desc* d, const fsi_particles* parts,
   particle_reduce_kernel<<<blocks, kBlock, 0, s>>>(m, P, out);
   return check_launch("particle_reduce_kernel");
 }
+

@@ -86,6 +86,7 @@ class LBMSolver3D:
         self._macro_fresh = True
         self._fcur = 0
         self._fprev = -1
+        self._mass_speed_cache = None
         self._build_flags()
         self._initialized = False
 
@@ -141,6 +142,7 @@ class LBMSolver3D:
         self._steps_done = 0
         self._macro_fresh = True
         self._fprev = -1
+        self._mass_speed_cache = None
         self.reset_force()
         self._initialized = True
 
@@ -221,19 +223,42 @@ class LBMSolver3D:
         """The current force field as a float32[3, N] device tensor (read-only view)."""
         return self._force_buf[self._fcur]
 
+    def _fetch_diag(self, count: int) -> np.ndarray:
+        self._diag_host[:count].copy_(self._diag[:count], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return self._diag_host[:count].numpy().copy()
+
     def _reduce(self) -> np.ndarray:
         self._ensure_macro()
         self._call("fsi_lbm_reduce", nat.ptr(self._macro), nat.ptr(self._force_buf[self._fcur]),
                    nat.ptr(self._flags), nat.ptr(self._diag), nat.stream_ptr())
-        self._diag_host.copy_(self._diag, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        return self._diag_host.numpy().copy()
+        return self._fetch_diag(5)
+
+    def _mass_and_speed(self) -> tuple[float, float]:
+        """(total mass, max |u|) of the current state, computed once per state: when rho and u
+        are stale the refresh and both reductions run as one fused pass."""
+        key = (self._steps_done, self._initialized)
+        if self._mass_speed_cache is not None and self._mass_speed_cache[0] == key:
+            return self._mass_speed_cache[1]
+        if self._macro_fresh:
+            r = self._reduce()
+            val = (float(r[0]), float(r[1]))
+        else:
+            self._call("fsi_lbm_macro_diagnostics", nat.ptr(self._pops),
+                       nat.ptr(self._force_buf[self._fprev]), nat.ptr(self._flags),
+                       self._steps_done, nat.ptr(self._macro), nat.ptr(self._diag),
+                       nat.stream_ptr())
+            self._macro_fresh = True
+            r = self._fetch_diag(2)
+            val = (float(r[0]), float(r[1]))
+        self._mass_speed_cache = (key, val)
+        return val
 
     def total_mass(self) -> float:
-        return float(self._reduce()[0])
+        return self._mass_and_speed()[0]
 
     def max_velocity_norm(self) -> float:
-        return float(self._reduce()[1])
+        return self._mass_and_speed()[1]
 
     def total_force(self) -> np.ndarray:
         return self._reduce()[2:5].astype(np.float32)
