@@ -187,15 +187,11 @@ def run_gpu(args) -> dict:
     mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
     base = mpm.base_cells_numpy().astype(np.int64)
     # grid nodes touched per substep: the union of the particles' 27-node stencils
-    cells = np.unique((base[:, 0] * args.n + base[:, 1]) * args.n + base[:, 2])
-    touched = int(len(cells)) + 0
-    ci, cj, ck = cells // (args.n * args.n), (cells // args.n) % args.n, cells % args.n
-    stencil = set()
-    for di in range(3):
-        for dj in range(3):
-            for dk in range(3):
-                stencil.update(((ci + di) * args.n + cj + dj) * args.n + ck + dk)
-    touched = len(stencil)
+    occupied = np.unique((base[:, 0] * args.n + base[:, 1]) * args.n + base[:, 2])
+    oi, oj, ok = occupied // (args.n * args.n), (occupied // args.n) % args.n, occupied % args.n
+    stencil = np.unique(np.concatenate([((oi + di) * args.n + oj + dj) * args.n + ok + dk
+                                        for di in range(3) for dj in range(3) for dk in range(3)]))
+    touched = int(len(stencil))
 
     # --- end to end through the public API (host input, host result each step) ----
     g_host = np.array(lcfg.force, dtype=np.float32)
