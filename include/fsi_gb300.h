@@ -186,6 +186,22 @@ typedef struct fsi_particles {
 int fsi_mpm_substep(const fsi_mpm_desc* desc, const fsi_particles* particles, float* grid,
                     uint8_t* dirty, void* stream);
 
+/* fsi_mpm_substep for callers that cannot allocate device memory (no counterpart in the
+ * reference, which allocates its grid as Taichi fields). Hosts such as real-time loops that
+ * may not take the device synchronisation of cudaMalloc, plugins inside an application that
+ * owns the device memory pool, or plain FFI callers without a device allocator pass only the
+ * particles; the grid and dirty-block map live in one static device array of this library
+ * (FSI_NOALLOC_MAX_NODES float4 nodes + FSI_NOALLOC_MAX_BLOCKS bytes, about 4 MB held on every
+ * GPU that loads the library until exit). Grids above either limit are rejected with
+ * FSI_ERR_INVALID_ARG. The first call on a device looks up the array's device address with
+ * cudaGetSymbolAddress (that device current) and caches it; make that first call before any
+ * stream capture. All calls share the array: each call clears the part it uses, and calls
+ * whose work overlaps on the GPU (other streams, other threads) race on it. Nothing is
+ * allocated or freed. */
+#define FSI_NOALLOC_MAX_NODES (64 * 64 * 64)
+#define FSI_NOALLOC_MAX_BLOCKS 32768
+int fsi_mpm_substep_noalloc(const fsi_mpm_desc* desc, const fsi_particles* particles, void* stream);
+
 /* Rotation R of the polar decomposition of n row-major 3x3 matrices (float[n][9]).
  * Replaces the ti.svd call of MPMSolver3D.p2g (fsi/mpm3d.py:245-246). */
 int fsi_mpm_polar(const float* F, float* R, int64_t n, void* stream);

@@ -634,3 +634,88 @@ extern "C" int fsi_mpm_reduce(const fsi_mpm_desc* d, const fsi_particles* parts,
   return check_launch("particle_reduce_kernel");
 }
 
+// ----------------------------------------------------------------------------
+// Substep for callers that cannot allocate device memory.
+//
+// Some hosts of this library may not call cudaMalloc: a real-time loop in which
+// the implicit device synchronisation of an allocation is not allowed, a plugin
+// inside an application that owns the device memory pool, or a plain FFI caller
+// with no device allocator of its own. For them the grid and the dirty-block map
+// of fsi_mpm_substep live in one library-owned array of static device memory,
+// sized for grids of at most FSI_NOALLOC_MAX_NODES nodes. Every GPU that loads
+// the library holds this array (about 4 MB) until the process exits.
+// ----------------------------------------------------------------------------
+#include <mutex>
+
+namespace fsi {
+namespace {
+
+constexpr long long kNoAllocGridBytes = (long long)FSI_NOALLOC_MAX_NODES * 16;
+constexpr long long kNoAllocBytes = kNoAllocGridBytes + FSI_NOALLOC_MAX_BLOCKS;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the static array on the current device. Host code cannot
+// use the symbol itself (it names a host-side stand-in), so the address is
+// looked up once per device, with that device current, and cached.
+int noalloc_scratch(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("cudaGetDevice: %s", cudaGetErrorString(e));
+    return FSI_ERR_CUDA;
+  }
+  FSI_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_error("cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+      return FSI_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return FSI_OK;
+}
+
+}  // namespace
+}  // namespace fsi
+
+extern "C" int fsi_mpm_substep_noalloc(const fsi_mpm_desc* d, const fsi_particles* parts,
+                                       void* stream) {
+  Mpm m;
+  PView P;
+  if (int e = make_mpm(d, parts, m, P)) return e;
+  const long long nodes = (long long)m.nx * m.ny * m.nz;
+  const long long nblocks = (long long)m.nbx * m.nby * m.nbz;
+  FSI_REQUIRE(nodes <= FSI_NOALLOC_MAX_NODES,
+              "grid %dx%dx%d has %lld nodes; fsi_mpm_substep_noalloc supports at most %d "
+              "(use fsi_mpm_substep with a caller-allocated grid)",
+              m.nx, m.ny, m.nz, nodes, FSI_NOALLOC_MAX_NODES);
+  FSI_REQUIRE(nblocks <= FSI_NOALLOC_MAX_BLOCKS,
+              "grid %dx%dx%d has %lld 4^3 node blocks; fsi_mpm_substep_noalloc supports at most %d",
+              m.nx, m.ny, m.nz, nblocks, FSI_NOALLOC_MAX_BLOCKS);
+  if (m.n == 0) return FSI_OK;
+  void* base = nullptr;
+  if (int e = noalloc_scratch(&base)) return e;
+  float4* g4 = reinterpret_cast<float4*>(base);
+  uint8_t* dirty = reinterpret_cast<uint8_t*>(base) + kNoAllocGridBytes;
+  cudaStream_t s = as_stream(stream);
+  // The array keeps whatever the previous call left; the part this call uses must start at 0.
+  if (cudaMemsetAsync(g4, 0, (size_t)nodes * sizeof(float4), s) != cudaSuccess ||
+      cudaMemsetAsync(dirty, 0, (size_t)nblocks, s) != cudaSuccess)
+    return check_launch("no-alloc scratch clear");
+  const unsigned pg = grid_for(m.n, kBlock);
+  p2g_kernel<<<pg, kBlock, 0, s>>>(m, P, g4, dirty);
+  if (int e = check_launch("p2g_kernel (no-alloc)")) return e;
+  g2p_kernel<<<pg, kBlock, 0, s>>>(m, P, g4);
+  if (int e = check_launch("g2p_kernel (no-alloc)")) return e;
+  clear_kernel<<<grid_for(nblocks * 32, kBlock), kBlock, 0, s>>>(m, g4, dirty);
+  return check_launch("clear_kernel (no-alloc)");
+}

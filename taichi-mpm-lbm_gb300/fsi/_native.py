@@ -102,6 +102,7 @@ _SIGNATURES = {
     "fsi_lbm_reduce": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_lbm_macro_diagnostics": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64, _VP, _VP, _VP], ctypes.c_int),
     "fsi_mpm_substep": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),
+    "fsi_mpm_substep_noalloc": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP], ctypes.c_int),
     "fsi_mpm_polar": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "fsi_mpm_base_cells": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP], ctypes.c_int),
     "fsi_mpm_reduce": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),
