@@ -264,6 +264,21 @@ class LBMMpmCoupler:
             **self.immersed_boundary_diagnostics(),
         }
 
+    # ------------------------------------------------------- checkpointing
+    def state_dict(self) -> dict:
+        """Coupler state: accumulated fields, per-particle diagnostics, counters, step count."""
+        return {"kind": "LBMMpmCoupler", "accum": self._accum.clone(), "ib": self._ib.clone(),
+                "valid": self._valid.clone(), "mask": self._mask.clone(),
+                "contact_mask": self._contact_mask.clone(), "counters": self._counters.clone(),
+                "coupled_step": self._coupled_step}
+
+    def load_state_dict(self, state: dict) -> None:
+        if state.get("kind") != "LBMMpmCoupler":
+            raise ValueError("not a coupler checkpoint")
+        for name in ("accum", "ib", "valid", "mask", "contact_mask", "counters"):
+            getattr(self, "_" + name).copy_(state[name])
+        self._coupled_step = int(state["coupled_step"])
+
     def _validate_initialized(self) -> None:
         if not getattr(self.lbm, "_initialized", False):
             raise RuntimeError("LBMSolver3D.initialize must be called before coupling.")

@@ -320,6 +320,36 @@ class LBMSolver3D:
             raise ValueError(f"force_np shape must be {expected}, got {arr.shape}.")
         return np.ascontiguousarray(arr)
 
+    # ------------------------------------------------------- checkpointing
+    def state_dict(self) -> dict:
+        """Complete lattice state (device tensors are cloned; no reference counterpart)."""
+        return {
+            "kind": "LBMSolver3D", "shape": (self.nx, self.ny, self.nz),
+            "pops": self._pops.clone(), "macro": self._macro.clone(),
+            "force": [f.clone() for f in self._force_buf], "solid": self._solid_host.copy(),
+            "steps_done": self._steps_done, "macro_fresh": self._macro_fresh,
+            "fcur": self._fcur, "fprev": self._fprev, "initialized": self._initialized,
+        }
+
+    def load_state_dict(self, state: dict) -> None:
+        if state.get("kind") != "LBMSolver3D" or tuple(state["shape"]) != (self.nx, self.ny, self.nz):
+            raise ValueError("checkpoint does not match this lattice")
+        if state["pops"].dtype != self._pops.dtype:
+            raise ValueError(f"checkpoint populations are {state['pops'].dtype}, this lattice "
+                             f"stores {self._pops.dtype}")
+        self._solid_host = np.ascontiguousarray(state["solid"], dtype=np.int32)
+        self._solid_dev.copy_(torch.from_numpy(self._solid_host.reshape(-1)))
+        self._build_flags()
+        self._pops.copy_(state["pops"])
+        self._macro.copy_(state["macro"])
+        for dst, src in zip(self._force_buf, state["force"]):
+            dst.copy_(src)
+        self._steps_done = int(state["steps_done"])
+        self._macro_fresh = bool(state["macro_fresh"])
+        self._fcur, self._fprev = int(state["fcur"]), int(state["fprev"])
+        self._initialized = bool(state["initialized"])
+        self._mass_speed_cache = None
+
     # ------------------------------------------------- coupler entry points
     def _writable_force(self) -> torch.Tensor:
         """Buffer that the coupler may overwrite with the next step's force."""

@@ -58,6 +58,7 @@ class MPMSolver3D:
         self._diag = torch.zeros(8, dtype=torch.float64, device=dev)
         self._diag_host = torch.zeros(8, dtype=torch.float64).pin_memory()
         self._num_particles = 0
+        self._mu_p = self._lam_p = None
         self._desc = self._make_desc()
         self._parts = self._make_particles()
         self._initialized = False
@@ -298,6 +299,33 @@ class MPMSolver3D:
 
     def total_particle_force(self) -> np.ndarray:
         return self._reduce()[5:8].astype(np.float32)
+
+    # ------------------------------------------------------- checkpointing
+    _STATE = ("_x", "_v", "_C", "_F", "_mass", "_volume", "_active", "_force")
+
+    def state_dict(self) -> dict:
+        """Complete particle state (device tensors cloned; no reference counterpart)."""
+        state = {name: getattr(self, name).clone() for name in self._STATE}
+        state.update(kind="MPMSolver3D", capacity=self.max_particles,
+                     num_particles=self._num_particles, initialized=self._initialized,
+                     mu=None if self._mu_p is None else self._mu_p.clone(),
+                     lam=None if self._lam_p is None else self._lam_p.clone())
+        return state
+
+    def load_state_dict(self, state: dict) -> None:
+        if state.get("kind") != "MPMSolver3D" or int(state["capacity"]) != self.max_particles:
+            raise ValueError("checkpoint does not match this particle capacity")
+        for name in self._STATE:
+            getattr(self, name).copy_(state[name])
+        if state.get("mu") is None:
+            self._mu_p = self._lam_p = None
+            self._parts.mu = self._parts.lam = None
+        else:
+            self._mu_p, self._lam_p = state["mu"].clone(), state["lam"].clone()
+            self._parts.mu, self._parts.lam = self._mu_p.data_ptr(), self._lam_p.data_ptr()
+        self._num_particles = int(state["num_particles"])
+        self._desc.num_particles = self._num_particles
+        self._initialized = bool(state["initialized"])
 
     # ---------------------------------------------------- device tensors
     @property

@@ -104,6 +104,45 @@ class FSISimulation:
             "coupling_contact_damped_particle_count": cd["contact_damped_particle_count"],
         }
 
+    # ------------------------------------------------------- checkpointing
+    def state_dict(self) -> dict:
+        """Full coupled state for restart (the reference writes snapshots but cannot resume)."""
+        return {"kind": "FSISimulation", "step_index": self.step_index, "time": self.time,
+                "lbm_initialized": self._lbm_initialized, "mpm_initialized": self._mpm_initialized,
+                "lbm": self.lbm.state_dict(), "mpm": self.mpm.state_dict(),
+                "coupler": self.coupler.state_dict()}
+
+    def load_state_dict(self, state: dict) -> None:
+        if state.get("kind") != "FSISimulation":
+            raise ValueError("not a simulation checkpoint")
+        self.lbm.load_state_dict(state["lbm"])
+        self.mpm.load_state_dict(state["mpm"])
+        self.coupler.load_state_dict(state["coupler"])
+        self.step_index = int(state["step_index"])
+        self.time = float(state["time"])
+        self._lbm_initialized = bool(state["lbm_initialized"])
+        self._mpm_initialized = bool(state["mpm_initialized"])
+
+    def save_checkpoint(self, path) -> None:
+        """Write the full state with torch.save (device tensors are stored as CPU tensors)."""
+        import torch
+
+        def to_cpu(v):
+            if isinstance(v, torch.Tensor):
+                return v.detach().cpu()
+            if isinstance(v, dict):
+                return {k: to_cpu(x) for k, x in v.items()}
+            if isinstance(v, list):
+                return [to_cpu(x) for x in v]
+            return v
+
+        torch.save(to_cpu(self.state_dict()), path)
+
+    def load_checkpoint(self, path) -> None:
+        import torch
+
+        self.load_state_dict(torch.load(path, map_location="cpu", weights_only=False))
+
     def _validate_initialized(self) -> None:
         if not self._lbm_initialized or not getattr(self.lbm, "_initialized", False):
             raise RuntimeError("FSISimulation.initialize_lbm must be called before stepping.")
