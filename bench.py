@@ -135,6 +135,49 @@ def barrier(world: int) -> None:
 
 # ------------------------------------------------------------------ GPU arm
 
+FORM_BYTES = {  # (algorithmic, moved by the fused step) bytes per cell update
+    ("f32", "fast"): (LBM_BYTES_PER_CELL, KERNEL_BYTES_PER_CELL),
+    ("f16", "fast"): (LBM_BYTES_PER_CELL - 76, KERNEL_BYTES_PER_CELL - 76),
+    ("bf16", "fast"): (LBM_BYTES_PER_CELL - 76, KERNEL_BYTES_PER_CELL - 76),
+}
+
+
+def time_lbm_forms(lcfg, mask, args, world, stream) -> dict:
+    """MLUPS of the lattice step in the other storage / arithmetic forms on the same scene."""
+    import dataclasses
+
+    import torch
+    from fsi.lbm3d import LBMSolver3D
+
+    peak, _ = load_peaks()
+    out = {}
+    for (storage, arithmetic), (alg, moved) in FORM_BYTES.items():
+        cfg = dataclasses.replace(lcfg, population_storage=storage, collision_arithmetic=arithmetic)
+        lbm = LBMSolver3D(cfg)
+        lbm.initialize(mask)
+        for _ in range(args.warmup):
+            lbm.step()
+        barrier(world)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            lbm.step()
+        b.record(stream)
+        barrier(world)
+        ms = max_over_ranks(a.elapsed_time(b), world) / args.steps
+        cells = lbm.n_cells
+        achieved = alg * cells / (ms * 1e-3) / 1e9
+        out[f"{storage}/{arithmetic}"] = {
+            "value": round(cells / (ms * 1e-3) / 1e6 * world, 3), "unit": "MLUPS",
+            "ms_per_step": round(ms, 5), "algorithmic_bytes_per_cell": alg,
+            "kernel_bytes_per_cell": moved, "achieved_gbs": round(achieved, 1),
+            "frac": round(achieved / peak, 4),
+        }
+        del lbm
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args) -> dict:
     import torch
     from fsi import scenes
@@ -182,6 +225,8 @@ def run_gpu(args) -> dict:
             mpm.substep()
         m1.record(stream)
         barrier(world)
+        # --- the lattice in the other storage / arithmetic forms ----------------
+        forms = time_lbm_forms(lcfg, mask, args, world, stream) if not args.no_forms else {}
     lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
     lbm_launches = args.steps
     mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
@@ -255,7 +300,10 @@ def run_gpu(args) -> dict:
             "api": "LBMSolver3D.set_uniform_force + step + total_mass + max_velocity_norm",
             "last_diagnostics": [float(diag[0]), float(diag[1])] if diag else None,
         },
-        "gpu_launches": lbm_launches + 3 * args.steps,
+        "lbm_forms": forms,
+        # lattice steps + 3 MPM launches per substep + 3 launches per end-to-end step
+        # (force op, step, fused macro + diagnostics) + one step per form per step
+        "gpu_launches": lbm_launches + 3 * args.steps + 3 * args.steps + len(forms) * args.steps,
         "clocks": clocks.summary(),
     }
     if world > 1:
@@ -346,6 +394,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip timing the FP32-fast / FP16 / BF16 lattice forms")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -39,7 +39,7 @@ extern "C" {
 #define FSI_ERR_TIMEOUT 4
 #define FSI_ERR_UNSUPPORTED 5
 
-#define FSI_ABI_VERSION 1
+#define FSI_ABI_VERSION 2
 
 /* Library ABI version (FSI_ABI_VERSION). No reference counterpart. */
 int fsi_abi_version(void);
@@ -61,7 +61,23 @@ typedef struct fsi_lbm_desc {
   float rho0;
   float bc_rho_left, bc_rho_right;
   float bc_vel_left[3], bc_vel_right[3];
+  int32_t storage;     /* FSI_STORAGE_*: element type of the population array */
+  int32_t arithmetic;  /* FSI_ARITH_*: operation order of the collision */
 } fsi_lbm_desc;
+
+/* Population storage. F32 holds f_q; F16 holds (f_q - w_q rho0) * 4096 as IEEE half;
+ * BF16 holds f_q - w_q rho0 as bfloat16. The population array has 19 * N elements of
+ * that type in every form; all arithmetic is float32. No reference counterpart: the
+ * reference stores float32 (lbm3d.py:117-122). */
+#define FSI_STORAGE_F32 0
+#define FSI_STORAGE_F16 1
+#define FSI_STORAGE_BF16 2
+/* Collision arithmetic. EXACT reproduces the reference's float32 operations in its
+ * order (bit-identical populations); FAST evaluates the same operator with fused
+ * multiply-adds and parity-split moments (about 2.5x fewer operations, results within
+ * float32 rounding). F16/BF16 storage requires FAST. */
+#define FSI_ARITH_EXACT 0
+#define FSI_ARITH_FAST 1
 
 /* Builds the per-cell flag word from the normalised 0/1 mask.
  * Replaces the neighbour tests of LBMSolver3D.stream (fsi/lbm3d.py:335-361),
@@ -73,7 +89,7 @@ int fsi_lbm_build_flags(const fsi_lbm_desc* desc, const int32_t* solid, uint32_t
  * populations = feq(rho0, u). u0 is host float[3].
  * Replaces LBMSolver3D.init_fields (fsi/lbm3d.py:256-267). */
 int fsi_lbm_init_fields(const fsi_lbm_desc* desc, const uint32_t* flags, const float* u0,
-                        float* pops, float* macro, void* stream);
+                        void* pops, float* macro, void* stream);
 
 /* One lattice step: collide (MRT + Guo forcing) and stream (half-way
  * bounce-back, periodic wrap) in one in-place AA-pattern pass, followed by the
@@ -88,20 +104,20 @@ int fsi_lbm_init_fields(const fsi_lbm_desc* desc, const uint32_t* flags, const f
  * materialise rho and u of the new state.
  * Replaces LBMSolver3D.collide/stream/apply_boundary (fsi/lbm3d.py:314-407,
  * called from step() at lbm3d.py:427-433). */
-int fsi_lbm_step(const fsi_lbm_desc* desc, float* pops, float* macro, const float* force,
+int fsi_lbm_step(const fsi_lbm_desc* desc, void* pops, float* macro, const float* force,
                  const float* force_prev, const uint32_t* flags, int64_t steps_done,
                  void* stream);
 
 /* rho = sum f, u = sum e f / rho + force / (2 rho) on fluid cells; rho0 and 0
  * on solid cells. `force` is the force of the last step.
  * Replaces LBMSolver3D.update_macro (fsi/lbm3d.py:409-425). */
-int fsi_lbm_update_macro(const fsi_lbm_desc* desc, const float* pops, const float* force,
+int fsi_lbm_update_macro(const fsi_lbm_desc* desc, const void* pops, const float* force,
                          const uint32_t* flags, int64_t steps_done, float* macro,
                          void* stream);
 
 /* Writes the post-stream distribution in the reference layout float[N][19].
  * Replaces LBMSolver3D.distribution_numpy (fsi/lbm3d.py:444-445). */
-int fsi_lbm_distribution(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
+int fsi_lbm_distribution(const fsi_lbm_desc* desc, const void* pops, const uint32_t* flags,
                          int64_t steps_done, float* out, void* stream);
 
 /* Force-field operations on float[3][N] (value is host float[3]):
@@ -129,7 +145,7 @@ int fsi_lbm_reduce(const fsi_lbm_desc* desc, const float* macro, const float* fo
  * device double out[0] = sum of rho over fluid cells, out[1] = max |u| over all cells
  * (LBMSolver3D.total_mass / max_velocity_norm, lbm3d.py:450-457, as called by
  * FSISimulation.diagnostics, simulation.py:117-147), in one pass over the populations. */
-int fsi_lbm_macro_diagnostics(const fsi_lbm_desc* desc, const float* pops, const float* force,
+int fsi_lbm_macro_diagnostics(const fsi_lbm_desc* desc, const void* pops, const float* force,
                               const uint32_t* flags, int64_t steps_done, float* macro,
                               double* out, void* stream);
 

@@ -137,6 +137,10 @@ class LBMSolver3D:
         self.bc_x_left_mode = boundary_mode(config.x_left)
         self.bc_x_right_mode = boundary_mode(config.x_right)
         M, invM, S, w = lattice_tables(config.viscosity)
+        # LBMConfig.mrt_rates (an extension with no reference counterpart) replaces single
+        # entries of S; every other rate is the reference's rule above.
+        for k, rate in (getattr(config, "mrt_rates", None) or {}).items():
+            S[int(k)] = np.float32(rate)
         dt = self.dtype
         self.M, self.invM, self.S, self.w = (np.ascontiguousarray(a.astype(dt)) for a in (M, invM, S, w))
         shape = (self.nx, self.ny, self.nz)

@@ -168,8 +168,108 @@ def gen() -> str:
         w("  { float a; " + " ".join(chain("a", terms)) + f" f[{q}] = a; }}")
     w("}")
     w("")
+    out.extend(gen_fast().splitlines())
     w("}  // namespace fsi")
     return "\n".join(out) + "\n"
+
+
+# ------------------------------------------------- reduced-operation collision --
+
+def _fmt(c: float) -> str:
+    return float(np.float32(c)).hex() + "f"
+
+
+def _lin(terms: list[tuple[float, str]]) -> str:
+    """Sum of coefficient * symbol with fused multiply-adds (coefficients +-1 become adds)."""
+    terms = [(c, s) for c, s in terms if c != 0.0]
+    if not terms:
+        return "0.0f"
+    c0, s0 = terms[0]
+    expr = s0 if c0 == 1.0 else (f"-{s0}" if c0 == -1.0 else f"({_fmt(c0)} * {s0})")
+    for c, s in terms[1:]:
+        if c == 1.0:
+            expr = f"({expr} + {s})"
+        elif c == -1.0:
+            expr = f"({expr} - {s})"
+        else:
+            expr = f"fmaf({_fmt(c)}, {s}, {expr})"
+    return expr
+
+
+def gen_fast() -> str:
+    """The same MRT + Guo operator with far fewer operations (not bit-identical):
+    M is block-diagonal in parity (even rows are symmetric under q <-> opp(q), odd rows
+    antisymmetric), so moments come from the 9 pair sums P and differences D; the forcing
+    moments M t have closed forms in u and G; inv(M) splits the same way."""
+    Md = M.astype(np.float64)
+    inv = np.linalg.inv(Md)
+    inv[np.abs(inv) < NOISE] = 0.0
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    E = np.array(E_LIST, float)
+    pairs = [(2 * p + 1, 2 * p + 2) for p in range(9)]
+    even = [k for k in range(Q) if all(Md[k, q] == Md[k, OPP[q]] for q in range(Q))]
+    odd = [k for k in range(Q) if k not in even]
+    A = np.einsum("kq,q,qa->ka", Md, w, E)
+    B = Md @ w
+    C = np.einsum("kq,q,qa,qb->kab", Md, w, E, E)
+    lines = []
+    w_ = lines.append
+    w_("")
+    w_("// Reduced-operation MRT + Guo collision (same operator, not the reference's rounding):")
+    w_("// parity-split moments from pair sums/differences, closed-form forcing moments")
+    w_("// g_k = A_k.G - B_k (u.G) + u^T C_k G, parity-split inverse. Used by the FP16/BF16")
+    w_("// storage forms and the FP32 fast form.")
+    w_("__device__ __forceinline__ void mrt_collide_fast(const float (&F)[19], float rho, float ux,")
+    w_("    float uy, float uz, float gx, float gy, float gz, const float* __restrict__ S,")
+    w_("    float (&out)[19]) {")
+    for p, (a, b) in enumerate(pairs):
+        w_(f"  const float P{p} = F[{a}] + F[{b}], D{p} = F[{a}] - F[{b}];")
+    for k in even:
+        terms = [(Md[k, 0], "F[0]")] + [(Md[k, a], f"P{p}") for p, (a, b) in enumerate(pairs)]
+        w_(f"  float m{k} = {_lin(terms)};")
+    for k in odd:
+        terms = [(Md[k, a], f"D{p}") for p, (a, b) in enumerate(pairs)]
+        w_(f"  float m{k} = {_lin(terms)};")
+    w_("  const float uG = fmaf(ux, gx, fmaf(uy, gy, uz * gz));")
+    w_("  const float pxx = ux * gx, pyy = uy * gy, pzz = uz * gz;")
+    w_("  const float sxy = fmaf(ux, gy, uy * gx), syz = fmaf(uy, gz, uz * gy), sxz = fmaf(ux, gz, uz * gx);")
+    sym = {(0, 0): "pxx", (1, 1): "pyy", (2, 2): "pzz", (0, 1): "sxy", (1, 2): "syz", (0, 2): "sxz"}
+    gnames = {}
+    for k in range(Q):
+        terms = [(A[k, 0], "gx"), (A[k, 1], "gy"), (A[k, 2], "gz"), (-B[k], "uG")]
+        for (a, b), s in sym.items():
+            coef = C[k, a, b] if a == b else C[k, a, b]  # C symmetric: C_ab u_a G_b + C_ba u_b G_a
+            terms.append((coef, s))
+        terms = [(float(c), s) for c, s in terms if abs(c) > 1e-14]
+        if terms:
+            w_(f"  const float g{k} = {_lin(terms)};")
+            gnames[k] = f"g{k}"
+    w_("  const float uu = fmaf(ux, ux, fmaf(uy, uy, uz * uz));")
+    meq = {0: "rho", 1: "uu", 3: "ux", 5: "uy", 7: "uz",
+           9: "fmaf(2.0f * ux, ux, -fmaf(uy, uy, uz * uz))", 11: "fmaf(uy, uy, -(uz * uz))",
+           13: "ux * uy", 14: "uy * uz", 15: "ux * uz"}
+    for k in range(Q):
+        g = gnames.get(k)
+        if k in (0, 3, 5, 7):
+            if g:
+                w_(f"  m{k} = m{k} + {g};")
+            continue
+        d = f"(m{k} - ({meq[k]}))" if k in meq else f"m{k}"
+        rel = f"fmaf(-S[{k}], {d}, m{k})"
+        if g:
+            w_(f"  m{k} = fmaf(fmaf(-0.5f, S[{k}], 1.0f), {g}, {rel});")
+        else:
+            w_(f"  m{k} = {rel};")
+    w_(f"  out[0] = {_lin([(inv[0, k], f'm{k}') for k in even])};")
+    for p, (a, b) in enumerate(pairs):
+        ev = _lin([(inv[a, k], f"m{k}") for k in even])
+        od = _lin([(inv[a, k], f"m{k}") for k in odd])
+        w_(f"  {{ const float e = {ev}, o = {od}; out[{a}] = e + o; out[{b}] = e - o; }}")
+    w_("}")
+    return "\n".join(lines)
+
+
+E_LIST = E
 
 
 # ---------------------------------------------------------------- checks --

@@ -9,11 +9,19 @@
 //               x + e_q is solid: half-way bounce-back).
 // Every slot is read and written by exactly one cell per step, so the update is
 // race-free in place. After an odd number of steps the populations sit in the
-// "AA-odd" arrangement that gather_post_stream() undoes.
+// "AA-odd" arrangement that gather32() undoes.
 //
-// The collision reproduces the reference's float32 arithmetic operation for
-// operation (the kernel is compiled with -fmad=false and uses *_rn intrinsics):
-// the MRT transforms are generated register formulas (lbm_formulas.cuh).
+// Two arithmetic forms:
+//   exact (default, FP32 storage): the reference's float32 operations in the
+//     reference's order (this file is compiled with -fmad=false and uses *_rn
+//     intrinsics; the MRT transforms are generated formulas, lbm_formulas.cuh);
+//   fast: the same collision operator with about 2.5x fewer operations
+//     (parity-split moments, closed-form forcing moments, fused multiply-adds).
+// Three storage forms: FP32 populations; FP16 or BF16 deviations from the rest
+// equilibrium, f_q - w_q rho0 (FP16 scaled by 2^12 into its normal range). All
+// arithmetic is FP32 in every form.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -35,46 +43,99 @@ __host__ LbmGeom geom_of(const fsi_lbm_desc* d) {
   return LbmGeom{d->nx, d->ny, d->nz, (long long)d->nx * d->ny * d->nz};
 }
 
-// Wrapped neighbour coordinates of a cell for offsets -1, 0, +1 on each axis.
-struct Nbr {
-  int i[3], j[3], k[3];
-  int ny, nz;
-  __device__ Nbr(long long c, const LbmGeom& g) : ny(g.ny), nz(g.nz) {
-    int kk = (int)(c % g.nz);
-    long long r = c / g.nz;
-    int jj = (int)(r % g.ny);
-    int ii = (int)(r / g.ny);
-    i[1] = ii; j[1] = jj; k[1] = kk;
-    i[0] = ii == 0 ? g.nx - 1 : ii - 1; i[2] = ii == g.nx - 1 ? 0 : ii + 1;
-    j[0] = jj == 0 ? g.ny - 1 : jj - 1; j[2] = jj == g.ny - 1 ? 0 : jj + 1;
-    k[0] = kk == 0 ? g.nz - 1 : kk - 1; k[2] = kk == g.nz - 1 ? 0 : kk + 1;
+// Launch shape of the cell kernels: x = z (contiguous, coalesced), y = y rows, z = x planes,
+// so a thread knows (i, j, k) without integer division.
+struct CellLaunch {
+  dim3 grid, block;
+};
+
+CellLaunch cell_launch(const LbmGeom& g) {
+  int bz = ((g.nz + 31) / 32) * 32;
+  if (bz > kBlock) bz = kBlock;
+  int by = kBlock / bz;
+  if (by > g.ny) by = g.ny;
+  return CellLaunch{dim3((g.nz + bz - 1) / bz, (g.ny + by - 1) / by, g.nx), dim3(bz, by, 1)};
+}
+
+// Signed 32-bit offsets from a cell to its +-1 neighbours on each axis, periodic wrap included
+// (lbm3d.py:335-350). A neighbour index is then one three-operand add.
+struct Deltas {
+  uint32_t c;
+  int xp, xm, yp, ym, zp, zm;
+  __device__ __forceinline__ Deltas(const LbmGeom& g, int i, int j, int k) {
+    const int nyz = g.ny * g.nz;
+    c = (uint32_t)((i * g.ny + j) * g.nz + k);
+    xp = i == g.nx - 1 ? -(g.nx - 1) * nyz : nyz;
+    xm = i == 0 ? (g.nx - 1) * nyz : -nyz;
+    yp = j == g.ny - 1 ? -(g.ny - 1) * g.nz : g.nz;
+    ym = j == 0 ? (g.ny - 1) * g.nz : -g.nz;
+    zp = k == g.nz - 1 ? -(g.nz - 1) : 1;
+    zm = k == 0 ? g.nz - 1 : -1;
   }
-  // Linear index of x + s*e_q (s = +1 or -1), periodic in all axes (lbm3d.py:335-350).
-  __device__ __forceinline__ long long at(int q, int s) const {
-    int I = i[1 + s * ex(q)], J = j[1 + s * ey(q)], K = k[1 + s * ez(q)];
-    return ((long long)I * ny + J) * nz + K;
+  // Index of x + s * e_q.
+  __device__ __forceinline__ uint32_t nb(int q, int s) const {
+    const int dx = s * ex(q), dy = s * ey(q), dz = s * ez(q);
+    const int ox = dx > 0 ? xp : (dx < 0 ? xm : 0);
+    const int oy = dy > 0 ? yp : (dy < 0 ? ym : 0);
+    const int oz = dz > 0 ? zp : (dz < 0 ? zm : 0);
+    return c + (uint32_t)(ox + oy + oz);
   }
 };
 
-// Post-stream population F_q(x) of the current state (parity = steps done mod 2).
-__device__ __forceinline__ float gather_post_stream(const float* __restrict__ pops, long long n,
-                                                    long long c, const Nbr& nb, uint32_t fl,
-                                                    int q, int parity) {
-  if (parity == 0 || q == 0) return pops[(long long)q * n + c];
-  const int o = opp(q);
-  if (fl & (1u << o)) return pops[(long long)q * n + c];
-  return pops[(long long)o * n + nb.at(q, -1)];
+// ------------------------------------------------------------- storage forms
+// ld(p, i, s) returns population i as float given its rest-equilibrium shift s = w_q rho0;
+// st(p, i, v, s) stores population value v.
+template <int kStore>
+struct Store;
+
+template <>
+struct Store<FSI_STORAGE_F32> {
+  using T = float;
+  static __device__ __forceinline__ float ld(const T* p, uint32_t i, float) { return p[i]; }
+  static __device__ __forceinline__ void st(T* p, uint32_t i, float v, float) { p[i] = v; }
+};
+
+constexpr float kF16Scale = 4096.0f;  // deviations of order 1e-8..1e-1 map into FP16's normal range
+
+template <>
+struct Store<FSI_STORAGE_F16> {
+  using T = __half;
+  static __device__ __forceinline__ float ld(const T* p, uint32_t i, float s) {
+    return fmaf(__half2float(p[i]), 1.0f / kF16Scale, s);
+  }
+  static __device__ __forceinline__ void st(T* p, uint32_t i, float v, float s) {
+    p[i] = __float2half_rn((v - s) * kF16Scale);
+  }
+};
+
+template <>
+struct Store<FSI_STORAGE_BF16> {
+  using T = __nv_bfloat16;
+  static __device__ __forceinline__ float ld(const T* p, uint32_t i, float s) {
+    return __bfloat162float(p[i]) + s;
+  }
+  static __device__ __forceinline__ void st(T* p, uint32_t i, float v, float s) {
+    p[i] = __float2bfloat16_rn(v - s);
+  }
+};
+
+// Post-stream F_q(x) of a fluid cell in a state of the given parity.
+template <int kStore>
+__device__ __forceinline__ float gather32(const typename Store<kStore>::T* __restrict__ pops,
+                                          uint32_t n, const Deltas& d, uint32_t fl, int q,
+                                          int parity, float shift) {
+  if (parity == 0 || q == 0 || ((fl >> opp(q)) & 1u)) return Store<kStore>::ld(pops, q * n + d.c, shift);
+  return Store<kStore>::ld(pops, opp(q) * n + d.nb(q, -1), shift);
 }
 
-__device__ __forceinline__ float* post_stream_slot(float* pops, long long n, long long c,
-                                                   const Nbr& nb, uint32_t fl, int q,
-                                                   int parity) {
-  if (parity == 0 || q == 0) return pops + (long long)q * n + c;
-  const int o = opp(q);
-  if (fl & (1u << o)) return pops + (long long)q * n + c;
-  return pops + (long long)o * n + nb.at(q, -1);
+// Storage index of F_q(x) in a state of the given parity (the slot a gather reads).
+__device__ __forceinline__ uint32_t slot32(uint32_t n, const Deltas& d, uint32_t fl, int q,
+                                           int parity) {
+  if (parity == 0 || q == 0 || ((fl >> opp(q)) & 1u)) return q * n + d.c;
+  return opp(q) * n + d.nb(q, -1);
 }
 
+// ---------------------------------------------------------------- macro fields
 // rho and u as update_macro computes them (lbm3d.py:409-425): sequential sums
 // in q order, then u = u / rho, u = u + (force * 0.5) / rho.
 __device__ __forceinline__ void macro_of(const float (&F)[19], float gx, float gy, float gz,
@@ -98,6 +159,32 @@ __device__ __forceinline__ void macro_of(const float (&F)[19], float gx, float g
   rho = r; ux = x; uy = y; uz = z;
 }
 
+// The same quantities with fused operations and one reciprocal (fast forms).
+__device__ __forceinline__ void macro_fast(const float (&F)[19], float gx, float gy, float gz,
+                                           float& rho, float& ux, float& uy, float& uz) {
+  const float P0 = F[1] + F[2], P1 = F[3] + F[4], P2 = F[5] + F[6], P3 = F[7] + F[8];
+  const float P4 = F[9] + F[10], P5 = F[11] + F[12], P6 = F[13] + F[14], P7 = F[15] + F[16];
+  const float P8 = F[17] + F[18];
+  const float r = (((F[0] + P0) + (P1 + P2)) + ((P3 + P4) + (P5 + P6))) + (P7 + P8);
+  const float D3 = F[7] - F[8], D4 = F[9] - F[10], D5 = F[11] - F[12], D6 = F[13] - F[14];
+  const float D7 = F[15] - F[16], D8 = F[17] - F[18];
+  const float jx = ((F[1] - F[2]) + (D3 + D4)) + (D5 + D6);
+  const float jy = ((F[3] - F[4]) + (D3 - D4)) + (D7 + D8);
+  const float jz = ((F[5] - F[6]) + (D5 - D6)) + (D7 - D8);
+  const float inv = __frcp_rn(r);
+  rho = r;
+  ux = fmaf(gx, 0.5f, jx) * inv;
+  uy = fmaf(gy, 0.5f, jy) * inv;
+  uz = fmaf(gz, 0.5f, jz) * inv;
+}
+
+template <bool kFast>
+__device__ __forceinline__ void macro_any(const float (&F)[19], float gx, float gy, float gz,
+                                          float& rho, float& ux, float& uy, float& uz) {
+  if (kFast) macro_fast(F, gx, gy, gz, rho, ux, uy, uz);
+  else macro_of(F, gx, gy, gz, rho, ux, uy, uz);
+}
+
 // Sum of the non-zero terms e_c * v_c in x, y, z order (Taichi Vector.dot with
 // exact zero products dropped).
 __device__ __forceinline__ float edot(int q, float vx, float vy, float vz) {
@@ -109,7 +196,7 @@ __device__ __forceinline__ float edot(int q, float vx, float vy, float vz) {
   return s;
 }
 
-// MRT collision with Guo forcing of one fluid cell (lbm3d.py:276-333).
+// MRT collision with Guo forcing of one fluid cell in the reference's order (lbm3d.py:276-333).
 __device__ __forceinline__ void collide_cell(const float (&F)[19], float rho, float ux, float uy,
                                              float uz, float gx, float gy, float gz,
                                              const float* __restrict__ S, float (&out)[19]) {
@@ -161,56 +248,19 @@ __device__ __forceinline__ void collide_cell(const float (&F)[19], float rho, fl
 
 struct StepArgs {
   LbmGeom g;
-  float* __restrict__ pops;
+  void* __restrict__ pops;
   float4* __restrict__ macro;
   const float* __restrict__ force;
   const float* __restrict__ force_prev;
   const uint32_t* __restrict__ flags;
   float s[19];
+  float shift[19];  // w_q rho0, the storage offset of the deviation forms
   int write_faces;
 };
 
-// Launch shape of the cell kernels: x = z (contiguous, coalesced), y = y rows, z = x planes,
-// so a thread knows (i, j, k) without integer division.
-struct CellLaunch {
-  dim3 grid, block;
-};
-
-CellLaunch cell_launch(const LbmGeom& g) {
-  int bz = ((g.nz + 31) / 32) * 32;
-  if (bz > kBlock) bz = kBlock;
-  int by = kBlock / bz;
-  if (by > g.ny) by = g.ny;
-  return CellLaunch{dim3((g.nz + bz - 1) / bz, (g.ny + by - 1) / by, g.nx), dim3(bz, by, 1)};
-}
-
-// Signed 32-bit offsets from a cell to its +-1 neighbours on each axis, periodic wrap included
-// (lbm3d.py:335-350). A neighbour index is then one three-operand add.
-struct Deltas {
-  uint32_t c;
-  int xp, xm, yp, ym, zp, zm;
-  __device__ __forceinline__ Deltas(const LbmGeom& g, int i, int j, int k) {
-    const int nyz = g.ny * g.nz;
-    c = (uint32_t)((i * g.ny + j) * g.nz + k);
-    xp = i == g.nx - 1 ? -(g.nx - 1) * nyz : nyz;
-    xm = i == 0 ? (g.nx - 1) * nyz : -nyz;
-    yp = j == g.ny - 1 ? -(g.ny - 1) * g.nz : g.nz;
-    ym = j == 0 ? (g.ny - 1) * g.nz : -g.nz;
-    zp = k == g.nz - 1 ? -(g.nz - 1) : 1;
-    zm = k == 0 ? g.nz - 1 : -1;
-  }
-  // Index of x + s * e_q.
-  __device__ __forceinline__ uint32_t nb(int q, int s) const {
-    const int dx = s * ex(q), dy = s * ey(q), dz = s * ez(q);
-    const int ox = dx > 0 ? xp : (dx < 0 ? xm : 0);
-    const int oy = dy > 0 ? yp : (dy < 0 ? ym : 0);
-    const int oz = dz > 0 ? zp : (dz < 0 ? zm : 0);
-    return c + (uint32_t)(ox + oy + oz);
-  }
-};
-
-template <bool kOdd, bool kRecompute>
+template <int kStore, bool kFast, bool kOdd, bool kRecompute>
 __global__ void __launch_bounds__(kBlock) lbm_step_kernel(StepArgs a) {
+  using St = Store<kStore>;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int i = blockIdx.z;
@@ -220,28 +270,29 @@ __global__ void __launch_bounds__(kBlock) lbm_step_kernel(StepArgs a) {
   const uint32_t fl = a.flags[c];
   if (fl & kFlagSolid) return;
   const uint32_t n = (uint32_t)a.g.n;
-  float* __restrict__ pops = a.pops;
+  typename St::T* __restrict__ pops = reinterpret_cast<typename St::T*>(a.pops);
 
   float F[19];
   if (!kOdd) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) F[q] = pops[q * n + c];
+    for (int q = 0; q < 19; ++q) F[q] = St::ld(pops, q * n + c, a.shift[q]);
   } else {
-    F[0] = pops[c];
+    F[0] = St::ld(pops, c, a.shift[0]);
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
       // F_q(x) = f*_q(x - e_q) in slot opp(q) there, or f*_opp(q)(x) in slot q here when
       // x - e_q is solid (half-way bounce-back).
       const bool bounce = (fl >> opp(q)) & 1u;
       const uint32_t idx = bounce ? q * n + c : opp(q) * n + d.nb(q, -1);
-      F[q] = pops[idx];
+      F[q] = St::ld(pops, idx, a.shift[q]);
     }
   }
 
   const float gx = a.force[c], gy = a.force[n + c], gz = a.force[2 * n + c];
   float rho, ux, uy, uz;
   if (kRecompute) {
-    macro_of(F, a.force_prev[c], a.force_prev[n + c], a.force_prev[2 * n + c], rho, ux, uy, uz);
+    macro_any<kFast>(F, a.force_prev[c], a.force_prev[n + c], a.force_prev[2 * n + c], rho, ux,
+                     uy, uz);
     if (a.write_faces && (fl & (kFlagFaceLeft | kFlagFaceRight)))
       a.macro[c] = make_float4(ux, uy, uz, rho);
   } else {
@@ -250,18 +301,20 @@ __global__ void __launch_bounds__(kBlock) lbm_step_kernel(StepArgs a) {
   }
 
   float out[19];
-  collide_cell(F, rho, ux, uy, uz, gx, gy, gz, a.s, out);
+  if (kFast) mrt_collide_fast(F, rho, ux, uy, uz, gx, gy, gz, a.s, out);
+  else collide_cell(F, rho, ux, uy, uz, gx, gy, gz, a.s, out);
 
   if (!kOdd) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) pops[opp(q) * n + c] = out[q];
+    for (int q = 0; q < 19; ++q) St::st(pops, opp(q) * n + c, out[q], a.shift[opp(q)]);
   } else {
-    pops[c] = out[0];
+    St::st(pops, c, out[0], a.shift[0]);
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
       const bool bounce = (fl >> q) & 1u;
-      const uint32_t idx = bounce ? opp(q) * n + c : q * n + d.nb(q, +1);
-      pops[idx] = out[q];
+      // The slot receiving f*_q holds direction q (neighbour) or opp(q) (bounce-back).
+      if (bounce) St::st(pops, opp(q) * n + c, out[q], a.shift[opp(q)]);
+      else St::st(pops, q * n + d.nb(q, +1), out[q], a.shift[q]);
     }
   }
 }
@@ -269,7 +322,7 @@ __global__ void __launch_bounds__(kBlock) lbm_step_kernel(StepArgs a) {
 // x-face conditions applied to the post-stream state (lbm3d.py:363-407).
 struct FaceArgs {
   LbmGeom g;
-  float* __restrict__ pops;
+  void* __restrict__ pops;
   const float4* __restrict__ macro;  // u of the state before this step, on face cells
   const uint32_t* __restrict__ flags;
   int parity;  // of the state after the step
@@ -277,26 +330,31 @@ struct FaceArgs {
   float bc_rho[2];
   float bc_vel[2][3];
   float rho0;
+  float shift[19];
 };
 
+template <int kStore>
 __global__ void __launch_bounds__(kBlock) lbm_face_kernel(FaceArgs a) {
-  const long long per_face = (long long)a.g.ny * a.g.nz;
-  const long long t = (long long)blockIdx.x * kBlock + threadIdx.x;
+  using St = Store<kStore>;
+  const int per_face = a.g.ny * a.g.nz;
+  const int t = blockIdx.x * kBlock + threadIdx.x;
   if (t >= 2 * per_face) return;
-  const int side = (int)(t / per_face);
+  const int side = t / per_face;
   const int mode = a.mode[side];
   if (mode == 0) return;
-  const long long c = (side == 0 ? 0 : (long long)(a.g.nx - 1) * per_face) + (t % per_face);
+  const int r = t - side * per_face;
+  const Deltas d(a.g, side == 0 ? 0 : a.g.nx - 1, r / a.g.nz, r % a.g.nz);
+  const uint32_t c = d.c;
   const uint32_t fl = a.flags[c];
   if (fl & kFlagSolid) return;
-  const long long n = a.g.n;
-  const Nbr nb(c, a.g);
+  const uint32_t n = (uint32_t)a.g.n;
+  typename St::T* __restrict__ pops = reinterpret_cast<typename St::T*>(a.pops);
   float F[19];
-  float* slot[19];
+  uint32_t slot[19];
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
-    slot[q] = post_stream_slot(a.pops, n, c, nb, fl, q, a.parity);
-    F[q] = *slot[q];
+    slot[q] = slot32(n, d, fl, q, a.parity);
+    F[q] = St::ld(pops, slot[q], a.shift[q]);
   }
   if (mode == 1) {
     // Pressure: equilibrium at bc_rho with the velocity of this cell, or of the
@@ -321,25 +379,19 @@ __global__ void __launch_bounds__(kBlock) lbm_face_kernel(FaceArgs a) {
     }
   }
 #pragma unroll
-  for (int q = 0; q < 19; ++q) *slot[q] = F[q];
+  for (int q = 0; q < 19; ++q) St::st(pops, slot[q], F[q], a.shift[q]);
 }
 
 struct MacroArgs {
   LbmGeom g;
-  const float* __restrict__ pops;
+  const void* __restrict__ pops;
   const float* __restrict__ force;
   const uint32_t* __restrict__ flags;
   float4* __restrict__ macro;
   int parity;
   float rho0;
+  float shift[19];
 };
-
-// Post-stream F_q(x) of a fluid cell in a state of the given parity (32-bit addressing).
-__device__ __forceinline__ float gather32(const float* __restrict__ pops, uint32_t n,
-                                          const Deltas& d, uint32_t fl, int q, int parity) {
-  if (parity == 0 || q == 0 || ((fl >> opp(q)) & 1u)) return pops[q * n + d.c];
-  return pops[opp(q) * n + d.nb(q, -1)];
-}
 
 // numpy float32 norm of a 3-vector: sqrt((x*x + y*y) + z*z).
 __device__ __forceinline__ float norm3_ref(float x, float y, float z) {
@@ -390,6 +442,7 @@ __device__ void block_accumulate(double* __restrict__ sums, const float (&s)[NS]
 
 // update_macro (lbm3d.py:409-425) on the current state; with `diag` non-NULL it also adds
 // sum(rho) over fluid cells to diag[0] and raises diag[1] to max |u| (lbm3d.py:450-457).
+template <int kStore, bool kFast>
 __global__ void __launch_bounds__(kBlock) lbm_macro_kernel(MacroArgs a, double* __restrict__ diag) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -403,11 +456,12 @@ __global__ void __launch_bounds__(kBlock) lbm_macro_kernel(MacroArgs a, double* 
       a.macro[c] = make_float4(0.f, 0.f, 0.f, a.rho0);
     } else {
       const uint32_t n = (uint32_t)a.g.n;
+      const auto* pops = reinterpret_cast<const typename Store<kStore>::T*>(a.pops);
       float F[19];
 #pragma unroll
-      for (int q = 0; q < 19; ++q) F[q] = gather32(a.pops, n, d, fl, q, a.parity);
+      for (int q = 0; q < 19; ++q) F[q] = gather32<kStore>(pops, n, d, fl, q, a.parity, a.shift[q]);
       float rho, ux, uy, uz;
-      macro_of(F, a.force[c], a.force[n + c], a.force[2 * n + c], rho, ux, uy, uz);
+      macro_any<kFast>(F, a.force[c], a.force[n + c], a.force[2 * n + c], rho, ux, uy, uz);
       a.macro[c] = make_float4(ux, uy, uz, rho);
       mass = rho;
       vmax = norm3_ref(ux, uy, uz);
@@ -419,47 +473,58 @@ __global__ void __launch_bounds__(kBlock) lbm_macro_kernel(MacroArgs a, double* 
   }
 }
 
-__global__ void __launch_bounds__(kBlock) lbm_distribution_kernel(LbmGeom g,
-                                                                  const float* __restrict__ pops,
+template <int kStore>
+__global__ void __launch_bounds__(kBlock) lbm_distribution_kernel(LbmGeom g, const void* pops_v,
                                                                   const uint32_t* __restrict__ flags,
-                                                                  int parity,
+                                                                  int parity, float rho0,
                                                                   float* __restrict__ out) {
-  const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-  if (c >= g.n) return;
-  const uint32_t fl = flags[c];
-  const Nbr nb(c, g);
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  if (k >= g.nz || j >= g.ny) return;
+  const Deltas d(g, i, j, k);
+  const uint32_t fl = flags[d.c];
   const int p = (fl & kFlagSolid) ? 0 : parity;
+  const auto* pops = reinterpret_cast<const typename Store<kStore>::T*>(pops_v);
 #pragma unroll
-  for (int q = 0; q < 19; ++q) out[c * 19 + q] = gather_post_stream(pops, g.n, c, nb, fl, q, p);
+  for (int q = 0; q < 19; ++q)
+    out[(size_t)d.c * 19 + q] =
+        gather32<kStore>(pops, (uint32_t)g.n, d, fl, q, p, __fmul_rn(weight_of(q), rho0));
 }
 
 __global__ void __launch_bounds__(kBlock) lbm_flags_kernel(LbmGeom g,
                                                            const int32_t* __restrict__ solid,
                                                            uint32_t* __restrict__ flags) {
-  const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-  if (c >= g.n) return;
-  const Nbr nb(c, g);
-  uint32_t f = solid[c] != 0 ? kFlagSolid : 0u;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  if (k >= g.nz || j >= g.ny) return;
+  const Deltas d(g, i, j, k);
+  uint32_t f = solid[d.c] != 0 ? kFlagSolid : 0u;
 #pragma unroll
   for (int q = 1; q < 19; ++q)
-    if (solid[nb.at(q, +1)] != 0) f |= 1u << q;
-  if (nb.i[1] == 0) f |= kFlagFaceLeft;
-  if (nb.i[1] == g.nx - 1) f |= kFlagFaceRight;
-  flags[c] = f;
+    if (solid[d.nb(q, +1)] != 0) f |= 1u << q;
+  if (i == 0) f |= kFlagFaceLeft;
+  if (i == g.nx - 1) f |= kFlagFaceRight;
+  flags[d.c] = f;
 }
 
+template <int kStore>
 __global__ void __launch_bounds__(kBlock) lbm_init_kernel(LbmGeom g,
                                                           const uint32_t* __restrict__ flags,
                                                           float rho0, float u0x, float u0y,
-                                                          float u0z, float* __restrict__ pops,
+                                                          float u0z, void* pops_v,
                                                           float4* __restrict__ macro) {
   const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (c >= g.n) return;
   const bool solid = flags[c] & kFlagSolid;
   const float ux = solid ? 0.f : u0x, uy = solid ? 0.f : u0y, uz = solid ? 0.f : u0z;
   macro[c] = make_float4(ux, uy, uz, rho0);
+  auto* pops = reinterpret_cast<typename Store<kStore>::T*>(pops_v);
 #pragma unroll
-  for (int q = 0; q < 19; ++q) pops[(long long)q * g.n + c] = feq_ref(q, rho0, ux, uy, uz);
+  for (int q = 0; q < 19; ++q)
+    Store<kStore>::st(pops, (uint32_t)(q * g.n + c), feq_ref(q, rho0, ux, uy, uz),
+                      __fmul_rn(weight_of(q), rho0));
 }
 
 __global__ void __launch_bounds__(kBlock) lbm_force_kernel(LbmGeom g,
@@ -521,7 +586,91 @@ int check_desc(const fsi_lbm_desc* d) {
     int m = side == 0 ? d->bc_mode_left : d->bc_mode_right;
     FSI_REQUIRE(m >= 0 && m <= 2, "unknown x boundary mode %d", m);
   }
+  FSI_REQUIRE(d->storage >= FSI_STORAGE_F32 && d->storage <= FSI_STORAGE_BF16,
+              "unknown population storage %d", d->storage);
+  FSI_REQUIRE(d->arithmetic == FSI_ARITH_EXACT || d->arithmetic == FSI_ARITH_FAST,
+              "unknown arithmetic form %d", d->arithmetic);
+  FSI_REQUIRE(d->storage == FSI_STORAGE_F32 || d->arithmetic == FSI_ARITH_FAST,
+              "FP16/BF16 population storage uses the fast arithmetic form");
   return FSI_OK;
+}
+
+void fill_shift(const fsi_lbm_desc* d, float (&shift)[19]) {
+  for (int q = 0; q < 19; ++q) shift[q] = d->storage == FSI_STORAGE_F32 ? 0.f : weight_of(q) * d->rho0;
+}
+
+// Launches kernel K<storage, fast, ...> for the descriptor's forms.
+template <template <int, bool> class Launcher, class... Args>
+void dispatch_forms(const fsi_lbm_desc* d, Args&&... args) {
+  const bool fast = d->arithmetic == FSI_ARITH_FAST;
+  switch (d->storage) {
+    case FSI_STORAGE_F16: Launcher<FSI_STORAGE_F16, true>::run(args...); break;
+    case FSI_STORAGE_BF16: Launcher<FSI_STORAGE_BF16, true>::run(args...); break;
+    default:
+      if (fast) Launcher<FSI_STORAGE_F32, true>::run(args...);
+      else Launcher<FSI_STORAGE_F32, false>::run(args...);
+  }
+}
+
+template <int S, bool F>
+struct StepLauncher {
+  static void run(const StepArgs& a, bool odd, bool recompute, const CellLaunch& L, cudaStream_t s) {
+    if (recompute) {
+      if (odd) lbm_step_kernel<S, F, true, true><<<L.grid, L.block, 0, s>>>(a);
+      else lbm_step_kernel<S, F, false, true><<<L.grid, L.block, 0, s>>>(a);
+    } else {
+      if (odd) lbm_step_kernel<S, F, true, false><<<L.grid, L.block, 0, s>>>(a);
+      else lbm_step_kernel<S, F, false, false><<<L.grid, L.block, 0, s>>>(a);
+    }
+  }
+};
+
+template <int S, bool F>
+struct MacroLauncher {
+  static void run(const MacroArgs& a, double* diag, cudaStream_t s) {
+    const CellLaunch L = cell_launch(a.g);
+    lbm_macro_kernel<S, F><<<L.grid, L.block, 0, s>>>(a, diag);
+  }
+};
+
+template <int S, bool F>
+struct FaceLauncher {
+  static void run(const FaceArgs& f, cudaStream_t s) {
+    const long long faces = 2ll * f.g.ny * f.g.nz;
+    lbm_face_kernel<S><<<grid_for(faces, kBlock), kBlock, 0, s>>>(f);
+  }
+};
+
+template <int S, bool F>
+struct DistLauncher {
+  static void run(const LbmGeom& g, const void* pops, const uint32_t* flags, int parity,
+                  float rho0, float* out, cudaStream_t s) {
+    const CellLaunch L = cell_launch(g);
+    lbm_distribution_kernel<S><<<L.grid, L.block, 0, s>>>(g, pops, flags, parity, rho0, out);
+  }
+};
+
+template <int S, bool F>
+struct InitLauncher {
+  static void run(const LbmGeom& g, const uint32_t* flags, float rho0, const float* u0, void* pops,
+                  float4* macro, cudaStream_t s) {
+    lbm_init_kernel<S><<<grid_for(g.n, kBlock), kBlock, 0, s>>>(g, flags, rho0, u0[0], u0[1],
+                                                                 u0[2], pops, macro);
+  }
+};
+
+MacroArgs macro_args(const fsi_lbm_desc* d, const void* pops, const float* force,
+                     const uint32_t* flags, int64_t steps_done, float* macro) {
+  MacroArgs a;
+  a.g = geom_of(d);
+  a.pops = pops;
+  a.force = force;
+  a.flags = flags;
+  a.macro = reinterpret_cast<float4*>(macro);
+  a.parity = (int)(steps_done & 1);
+  a.rho0 = d->rho0;
+  fill_shift(d, a.shift);
+  return a;
 }
 
 }  // namespace
@@ -534,21 +683,21 @@ extern "C" int fsi_lbm_build_flags(const fsi_lbm_desc* d, const int32_t* solid, 
   if (int e = check_desc(d)) return e;
   FSI_REQUIRE(solid && flags, "NULL array");
   LbmGeom g = geom_of(d);
-  lbm_flags_kernel<<<grid_for(g.n, kBlock), kBlock, 0, as_stream(stream)>>>(g, solid, flags);
+  const CellLaunch L = cell_launch(g);
+  lbm_flags_kernel<<<L.grid, L.block, 0, as_stream(stream)>>>(g, solid, flags);
   return check_launch("lbm_flags_kernel");
 }
 
 extern "C" int fsi_lbm_init_fields(const fsi_lbm_desc* d, const uint32_t* flags, const float* u0,
-                                   float* pops, float* macro, void* stream) {
+                                   void* pops, float* macro, void* stream) {
   if (int e = check_desc(d)) return e;
   FSI_REQUIRE(flags && u0 && pops && macro, "NULL array");
-  LbmGeom g = geom_of(d);
-  lbm_init_kernel<<<grid_for(g.n, kBlock), kBlock, 0, as_stream(stream)>>>(
-      g, flags, d->rho0, u0[0], u0[1], u0[2], pops, reinterpret_cast<float4*>(macro));
+  dispatch_forms<InitLauncher>(d, geom_of(d), flags, d->rho0, u0, pops,
+                               reinterpret_cast<float4*>(macro), as_stream(stream));
   return check_launch("lbm_init_kernel");
 }
 
-extern "C" int fsi_lbm_step(const fsi_lbm_desc* d, float* pops, float* macro, const float* force,
+extern "C" int fsi_lbm_step(const fsi_lbm_desc* d, void* pops, float* macro, const float* force,
                             const float* force_prev, const uint32_t* flags, int64_t steps_done,
                             void* stream) {
   if (int e = check_desc(d)) return e;
@@ -562,17 +711,11 @@ extern "C" int fsi_lbm_step(const fsi_lbm_desc* d, float* pops, float* macro, co
   a.force_prev = force_prev;
   a.flags = flags;
   for (int k = 0; k < 19; ++k) a.s[k] = d->s[k];
+  fill_shift(d, a.shift);
   a.write_faces = (d->bc_mode_left != 0 || d->bc_mode_right != 0) ? 1 : 0;
   cudaStream_t s = as_stream(stream);
-  const CellLaunch L = cell_launch(a.g);
   const bool odd = (steps_done & 1) != 0;
-  if (force_prev) {
-    if (odd) lbm_step_kernel<true, true><<<L.grid, L.block, 0, s>>>(a);
-    else lbm_step_kernel<false, true><<<L.grid, L.block, 0, s>>>(a);
-  } else {
-    if (odd) lbm_step_kernel<true, false><<<L.grid, L.block, 0, s>>>(a);
-    else lbm_step_kernel<false, false><<<L.grid, L.block, 0, s>>>(a);
-  }
+  dispatch_forms<StepLauncher>(d, a, odd, force_prev != nullptr, cell_launch(a.g), s);
   if (int e = check_launch("lbm_step_kernel")) return e;
   if (a.write_faces) {
     FaceArgs f;
@@ -590,33 +733,30 @@ extern "C" int fsi_lbm_step(const fsi_lbm_desc* d, float* pops, float* macro, co
       f.bc_vel[1][i] = d->bc_vel_right[i];
     }
     f.rho0 = d->rho0;
-    const long long faces = 2ll * d->ny * d->nz;
-    lbm_face_kernel<<<grid_for(faces, kBlock), kBlock, 0, s>>>(f);
+    fill_shift(d, f.shift);
+    dispatch_forms<FaceLauncher>(d, f, s);
     if (int e = check_launch("lbm_face_kernel")) return e;
   }
   return FSI_OK;
 }
 
-extern "C" int fsi_lbm_update_macro(const fsi_lbm_desc* d, const float* pops, const float* force,
+extern "C" int fsi_lbm_update_macro(const fsi_lbm_desc* d, const void* pops, const float* force,
                                     const uint32_t* flags, int64_t steps_done, float* macro,
                                     void* stream) {
   if (int e = check_desc(d)) return e;
   FSI_REQUIRE(pops && force && flags && macro, "NULL array");
-  MacroArgs a{geom_of(d), pops, force, flags, reinterpret_cast<float4*>(macro),
-              (int)(steps_done & 1), d->rho0};
-  const CellLaunch L = cell_launch(a.g);
-  lbm_macro_kernel<<<L.grid, L.block, 0, as_stream(stream)>>>(a, nullptr);
+  MacroArgs a = macro_args(d, pops, force, flags, steps_done, macro);
+  dispatch_forms<MacroLauncher>(d, a, (double*)nullptr, as_stream(stream));
   return check_launch("lbm_macro_kernel");
 }
 
-extern "C" int fsi_lbm_distribution(const fsi_lbm_desc* d, const float* pops,
+extern "C" int fsi_lbm_distribution(const fsi_lbm_desc* d, const void* pops,
                                     const uint32_t* flags, int64_t steps_done, float* out,
                                     void* stream) {
   if (int e = check_desc(d)) return e;
   FSI_REQUIRE(pops && flags && out, "NULL array");
-  LbmGeom g = geom_of(d);
-  lbm_distribution_kernel<<<grid_for(g.n, kBlock), kBlock, 0, as_stream(stream)>>>(
-      g, pops, flags, (int)(steps_done & 1), out);
+  dispatch_forms<DistLauncher>(d, geom_of(d), pops, flags, (int)(steps_done & 1), d->rho0, out,
+                               as_stream(stream));
   return check_launch("lbm_distribution_kernel");
 }
 
@@ -647,7 +787,7 @@ extern "C" int fsi_lbm_reduce(const fsi_lbm_desc* d, const float* macro, const f
   return check_launch("lbm_reduce_kernel");
 }
 
-extern "C" int fsi_lbm_macro_diagnostics(const fsi_lbm_desc* d, const float* pops,
+extern "C" int fsi_lbm_macro_diagnostics(const fsi_lbm_desc* d, const void* pops,
                                          const float* force, const uint32_t* flags,
                                          int64_t steps_done, float* macro, double* out,
                                          void* stream) {
@@ -655,9 +795,7 @@ extern "C" int fsi_lbm_macro_diagnostics(const fsi_lbm_desc* d, const float* pop
   FSI_REQUIRE(pops && force && flags && macro && out, "NULL array");
   cudaStream_t s = as_stream(stream);
   if (cudaMemsetAsync(out, 0, 2 * sizeof(double), s) != cudaSuccess) return check_launch("memset");
-  MacroArgs a{geom_of(d), pops, force, flags, reinterpret_cast<float4*>(macro),
-              (int)(steps_done & 1), d->rho0};
-  const CellLaunch L = cell_launch(a.g);
-  lbm_macro_kernel<<<L.grid, L.block, 0, s>>>(a, out);
+  MacroArgs a = macro_args(d, pops, force, flags, steps_done, macro);
+  dispatch_forms<MacroLauncher>(d, a, out, s);
   return check_launch("lbm_macro_kernel (diagnostics)");
 }

@@ -85,4 +85,84 @@ __device__ __forceinline__ void mrt_inverse(const float (&m)[19], float (&f)[19]
   { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p14_0); a = __fsub_rn(a, p17_0); a = __fsub_rn(a, p18_0); f[18] = a; }
 }
 
+
+// Reduced-operation MRT + Guo collision (same operator, not the reference's rounding):
+// parity-split moments from pair sums/differences, closed-form forcing moments
+// g_k = A_k.G - B_k (u.G) + u^T C_k G, parity-split inverse. Used by the FP16/BF16
+// storage forms and the FP32 fast form.
+__device__ __forceinline__ void mrt_collide_fast(const float (&F)[19], float rho, float ux,
+    float uy, float uz, float gx, float gy, float gz, const float* __restrict__ S,
+    float (&out)[19]) {
+  const float P0 = F[1] + F[2], D0 = F[1] - F[2];
+  const float P1 = F[3] + F[4], D1 = F[3] - F[4];
+  const float P2 = F[5] + F[6], D2 = F[5] - F[6];
+  const float P3 = F[7] + F[8], D3 = F[7] - F[8];
+  const float P4 = F[9] + F[10], D4 = F[9] - F[10];
+  const float P5 = F[11] + F[12], D5 = F[11] - F[12];
+  const float P6 = F[13] + F[14], D6 = F[13] - F[14];
+  const float P7 = F[15] + F[16], D7 = F[15] - F[16];
+  const float P8 = F[17] + F[18], D8 = F[17] - F[18];
+  float m0 = (((((((((F[0] + P0) + P1) + P2) + P3) + P4) + P5) + P6) + P7) + P8);
+  float m1 = ((((((-F[0] + P3) + P4) + P5) + P6) + P7) + P8);
+  float m2 = ((((((fmaf(-0x1.0000000000000p+1f, P2, fmaf(-0x1.0000000000000p+1f, P1, fmaf(-0x1.0000000000000p+1f, P0, F[0]))) + P3) + P4) + P5) + P6) + P7) + P8);
+  float m9 = fmaf(-0x1.0000000000000p+1f, P8, fmaf(-0x1.0000000000000p+1f, P7, (((((((0x1.0000000000000p+1f * P0) - P1) - P2) + P3) + P4) + P5) + P6)));
+  float m10 = fmaf(-0x1.0000000000000p+1f, P8, fmaf(-0x1.0000000000000p+1f, P7, (((((((-0x1.0000000000000p+1f * P0) + P1) + P2) + P3) + P4) + P5) + P6)));
+  float m11 = (((((P1 - P2) + P3) + P4) - P5) - P6);
+  float m12 = (((((-P1 + P2) + P3) + P4) - P5) - P6);
+  float m13 = (P3 - P4);
+  float m14 = (P7 - P8);
+  float m15 = (P5 - P6);
+  float m3 = ((((D0 + D3) + D4) + D5) + D6);
+  float m4 = (((((-0x1.0000000000000p+1f * D0) + D3) + D4) + D5) + D6);
+  float m5 = ((((D1 + D3) - D4) + D7) + D8);
+  float m6 = (((((-0x1.0000000000000p+1f * D1) + D3) - D4) + D7) + D8);
+  float m7 = ((((D2 + D5) - D6) + D7) - D8);
+  float m8 = (((((-0x1.0000000000000p+1f * D2) + D5) - D6) + D7) - D8);
+  float m16 = (((D3 + D4) - D5) - D6);
+  float m17 = (((-D3 + D4) + D7) + D8);
+  float m18 = (((D5 - D6) - D7) + D8);
+  const float uG = fmaf(ux, gx, fmaf(uy, gy, uz * gz));
+  const float pxx = ux * gx, pyy = uy * gy, pzz = uz * gz;
+  const float sxy = fmaf(ux, gy, uy * gx), syz = fmaf(uy, gz, uz * gy), sxz = fmaf(ux, gz, uz * gx);
+  const float g0 = fmaf(0x1.5555560000000p-2f, pzz, fmaf(0x1.5555560000000p-2f, pyy, fmaf(0x1.5555560000000p-2f, pxx, -uG)));
+  const float g1 = fmaf(0x1.c71c720000000p-3f, pzz, fmaf(0x1.c71c720000000p-3f, pyy, (0x1.c71c720000000p-3f * pxx)));
+  const float g3 = (0x1.5555560000000p-2f * gx);
+  const float g5 = (0x1.5555560000000p-2f * gy);
+  const float g7 = (0x1.5555560000000p-2f * gz);
+  const float g9 = fmaf(-0x1.c71c720000000p-3f, pzz, fmaf(-0x1.c71c720000000p-3f, pyy, (0x1.c71c720000000p-2f * pxx)));
+  const float g11 = fmaf(-0x1.c71c720000000p-3f, pzz, (0x1.c71c720000000p-3f * pyy));
+  const float g13 = (0x1.c71c720000000p-4f * sxy);
+  const float g14 = (0x1.c71c720000000p-4f * syz);
+  const float g15 = (0x1.c71c720000000p-4f * sxz);
+  const float uu = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+  m0 = m0 + g0;
+  m1 = fmaf(fmaf(-0.5f, S[1], 1.0f), g1, fmaf(-S[1], (m1 - (uu)), m1));
+  m2 = fmaf(-S[2], m2, m2);
+  m3 = m3 + g3;
+  m4 = fmaf(-S[4], m4, m4);
+  m5 = m5 + g5;
+  m6 = fmaf(-S[6], m6, m6);
+  m7 = m7 + g7;
+  m8 = fmaf(-S[8], m8, m8);
+  m9 = fmaf(fmaf(-0.5f, S[9], 1.0f), g9, fmaf(-S[9], (m9 - (fmaf(2.0f * ux, ux, -fmaf(uy, uy, uz * uz)))), m9));
+  m10 = fmaf(-S[10], m10, m10);
+  m11 = fmaf(fmaf(-0.5f, S[11], 1.0f), g11, fmaf(-S[11], (m11 - (fmaf(uy, uy, -(uz * uz)))), m11));
+  m12 = fmaf(-S[12], m12, m12);
+  m13 = fmaf(fmaf(-0.5f, S[13], 1.0f), g13, fmaf(-S[13], (m13 - (ux * uy)), m13));
+  m14 = fmaf(fmaf(-0.5f, S[14], 1.0f), g14, fmaf(-S[14], (m14 - (uy * uz)), m14));
+  m15 = fmaf(fmaf(-0.5f, S[15], 1.0f), g15, fmaf(-S[15], (m15 - (ux * uz)), m15));
+  m16 = fmaf(-S[16], m16, m16);
+  m17 = fmaf(-S[17], m17, m17);
+  m18 = fmaf(-S[18], m18, m18);
+  out[0] = fmaf(0x1.5555560000000p-3f, m2, fmaf(-0x1.0000000000000p-1f, m1, (0x1.5555560000000p-2f * m0)));
+  { const float e = fmaf(-0x1.5555560000000p-4f, m10, fmaf(0x1.5555560000000p-4f, m9, fmaf(-0x1.c71c720000000p-5f, m2, (0x1.c71c720000000p-5f * m0)))), o = fmaf(-0x1.5555560000000p-3f, m4, (0x1.5555560000000p-3f * m3)); out[1] = e + o; out[2] = e - o; }
+  { const float e = fmaf(-0x1.0000000000000p-3f, m12, fmaf(0x1.0000000000000p-3f, m11, fmaf(0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(-0x1.c71c720000000p-5f, m2, (0x1.c71c720000000p-5f * m0)))))), o = fmaf(-0x1.5555560000000p-3f, m6, (0x1.5555560000000p-3f * m5)); out[3] = e + o; out[4] = e - o; }
+  { const float e = fmaf(0x1.0000000000000p-3f, m12, fmaf(-0x1.0000000000000p-3f, m11, fmaf(0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(-0x1.c71c720000000p-5f, m2, (0x1.c71c720000000p-5f * m0)))))), o = fmaf(-0x1.5555560000000p-3f, m8, (0x1.5555560000000p-3f * m7)); out[5] = e + o; out[6] = e - o; }
+  { const float e = fmaf(0x1.0000000000000p-2f, m13, fmaf(0x1.0000000000000p-4f, m12, fmaf(0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(-0x1.0000000000000p-3f, m17, fmaf(0x1.0000000000000p-3f, m16, fmaf(0x1.5555560000000p-5f, m6, fmaf(0x1.5555560000000p-4f, m5, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[7] = e + o; out[8] = e - o; }
+  { const float e = fmaf(-0x1.0000000000000p-2f, m13, fmaf(0x1.0000000000000p-4f, m12, fmaf(0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(0x1.0000000000000p-3f, m17, fmaf(0x1.0000000000000p-3f, m16, fmaf(-0x1.5555560000000p-5f, m6, fmaf(-0x1.5555560000000p-4f, m5, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[9] = e + o; out[10] = e - o; }
+  { const float e = fmaf(0x1.0000000000000p-2f, m15, fmaf(-0x1.0000000000000p-4f, m12, fmaf(-0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(0x1.0000000000000p-3f, m18, fmaf(-0x1.0000000000000p-3f, m16, fmaf(0x1.5555560000000p-5f, m8, fmaf(0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[11] = e + o; out[12] = e - o; }
+  { const float e = fmaf(-0x1.0000000000000p-2f, m15, fmaf(-0x1.0000000000000p-4f, m12, fmaf(-0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(-0x1.0000000000000p-3f, m18, fmaf(-0x1.0000000000000p-3f, m16, fmaf(-0x1.5555560000000p-5f, m8, fmaf(-0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[13] = e + o; out[14] = e - o; }
+  { const float e = fmaf(0x1.0000000000000p-2f, m14, fmaf(-0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))), o = fmaf(-0x1.0000000000000p-3f, m18, fmaf(0x1.0000000000000p-3f, m17, fmaf(0x1.5555560000000p-5f, m8, fmaf(0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m6, (0x1.5555560000000p-4f * m5)))))); out[15] = e + o; out[16] = e - o; }
+  { const float e = fmaf(-0x1.0000000000000p-2f, m14, fmaf(-0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))), o = fmaf(0x1.0000000000000p-3f, m18, fmaf(0x1.0000000000000p-3f, m17, fmaf(-0x1.5555560000000p-5f, m8, fmaf(-0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m6, (0x1.5555560000000p-4f * m5)))))); out[17] = e + o; out[18] = e - o; }
+}
 }  // namespace fsi

@@ -21,8 +21,10 @@ FSI_ERR_CUDA = 2
 FSI_ERR_GUARD = 3
 FSI_ERR_TIMEOUT = 4
 FSI_ERR_UNSUPPORTED = 5
-ABI_VERSION = 1
+ABI_VERSION = 2
 
+STORAGE_F32, STORAGE_F16, STORAGE_BF16 = 0, 1, 2
+ARITH_EXACT, ARITH_FAST = 0, 1
 FORCE_CLEAR, FORCE_SET, FORCE_ADD, FORCE_ZERO_SOLID = 0, 1, 2, 3
 ASSEMBLE_CLAMP_FRACTION, ASSEMBLE_COUPLING, ASSEMBLE_IB = 1, 2, 4
 
@@ -37,6 +39,7 @@ class LbmDesc(ctypes.Structure):
         ("rho0", ctypes.c_float),
         ("bc_rho_left", ctypes.c_float), ("bc_rho_right", ctypes.c_float),
         ("bc_vel_left", c_float3), ("bc_vel_right", c_float3),
+        ("storage", ctypes.c_int32), ("arithmetic", ctypes.c_int32),
     ]
 
 

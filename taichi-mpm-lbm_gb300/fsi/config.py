@@ -21,6 +21,7 @@ _BOUNDARY_TYPES = frozenset({"periodic", "pressure", "velocity", "wall"})
 _COUPLING_KERNELS = frozenset({"quadratic"})
 _OUTPUT_FORMATS = frozenset({"npz", "vtk", "both"})
 _MATERIALS = frozenset({"elastic"})
+_FREE_MRT_MOMENTS = frozenset({1, 2, 4, 6, 8, 10, 12, 16, 17, 18})
 
 
 def _check_vec3(values, message: str) -> None:
@@ -74,7 +75,38 @@ class LBMConfig:
 
     use_sparse: bool = False
 
+    # Extensions (no reference counterpart; the reference stores and computes float32 in
+    # its own operation order, lbm3d.py:117-122, 276-333).
+    # population_storage: "f32" populations, or "f16" / "bf16" deviations from the rest
+    #   equilibrium f_q - w_q rho0 (half the memory traffic, float32 arithmetic).
+    # collision_arithmetic: "exact" (the reference's float32 operations, bit-identical),
+    #   "fast" (the same operator, fused and parity-split), or "auto" = "exact" for f32
+    #   storage and "fast" otherwise.
+    # mrt_rates: {moment index: rate} overriding the default relaxation rates S_k for the
+    #   non-conserved moments k in {1, 2, 4, 6, 8, 10, 12, 16, 17, 18}; the shear rates
+    #   (9, 11, 13, 14, 15) always follow from the viscosity.
+    population_storage: Literal["f32", "f16", "bf16"] = "f32"
+    collision_arithmetic: Literal["auto", "exact", "fast"] = "auto"
+    mrt_rates: dict | None = None
+
+    def resolved_arithmetic(self) -> str:
+        if self.collision_arithmetic != "auto":
+            return self.collision_arithmetic
+        return "exact" if self.population_storage == "f32" else "fast"
+
     def validate(self) -> None:
+        if self.population_storage not in ("f32", "f16", "bf16"):
+            raise ValueError(f"Unsupported population storage: {self.population_storage}.")
+        if self.collision_arithmetic not in ("auto", "exact", "fast"):
+            raise ValueError(f"Unsupported collision arithmetic: {self.collision_arithmetic}.")
+        if self.population_storage != "f32" and self.collision_arithmetic == "exact":
+            raise ValueError("f16/bf16 population storage uses the fast collision arithmetic.")
+        if self.mrt_rates is not None:
+            for k, rate in dict(self.mrt_rates).items():
+                if int(k) not in _FREE_MRT_MOMENTS:
+                    raise ValueError(f"MRT moment {k} has no free relaxation rate.")
+                if not (0.0 < float(rate) < 2.0):
+                    raise ValueError(f"MRT rate for moment {k} must be in (0, 2), got {rate}.")
         _check_grid("LBM", self.nx, self.ny, self.nz)
         if self.viscosity <= 0.0:
             raise ValueError(f"LBM viscosity must be positive, got {self.viscosity}.")

@@ -3,8 +3,9 @@
 Storage lives in torch CUDA tensors; every kernel is the library's sm_103a code
 reached through the C ABI (``fsi._native``):
 
-* populations ``float32[19, N]`` in one array updated in place by the fused
-  AA-pattern step (collide + stream + bounce-back in one pass);
+* populations ``[19, N]`` in one array updated in place by the fused
+  AA-pattern step (collide + stream + bounce-back in one pass): float32, or the
+  float16 / bfloat16 deviation forms selected by ``LBMConfig.population_storage``;
 * ``macro`` ``float32[N, 4]`` = (ux, uy, uz, rho), materialised on demand: the
   step kernel recomputes rho and u in registers, so the array is refreshed only
   when something reads it (accessors, diagnostics, the coupler);
@@ -41,14 +42,33 @@ def _boundary_mode(boundary: BoundaryConfig) -> int:
     return codes[kind]
 
 
-def relaxation_rates(viscosity: float) -> np.ndarray:
-    """MRT rates of lbm3d.py:141-168: s_v = 1/tau on the viscous moments, s_o on the others."""
+_STORAGE_DTYPE = {"f32": torch.float32, "f16": torch.float16, "bf16": torch.bfloat16}
+_STORAGE_CODE = {"f32": nat.STORAGE_F32, "f16": nat.STORAGE_F16, "bf16": nat.STORAGE_BF16}
+
+
+def relaxation_rates(viscosity: float, overrides: dict | None = None) -> np.ndarray:
+    """MRT rates of lbm3d.py:141-168: s_v = 1/tau on the viscous moments, s_o on the others.
+
+    ``overrides`` ({moment: rate}, LBMConfig.mrt_rates) replaces individual non-conserved,
+    non-shear rates (an extension; the reference fixes them)."""
     tau_f = 3.0 * viscosity + 0.5
     s_v = 1.0 / tau_f
     s_o = 8.0 * (2.0 - s_v) / (8.0 - s_v)
     v, o = s_v, s_o
-    return np.array([0.0, v, v, 0.0, o, 0.0, o, 0.0, o, v, v, v, v, v, v, v, o, o, o],
-                    dtype=np.float32)
+    s = np.array([0.0, v, v, 0.0, o, 0.0, o, 0.0, o, v, v, v, v, v, v, v, o, o, o],
+                 dtype=np.float32)
+    for k, rate in (overrides or {}).items():
+        s[int(k)] = np.float32(rate)
+    return s
+
+
+def dhumieres_rates(tau: float) -> dict[int, float]:
+    """Relaxation rates of d'Humieres et al. (2002) for LBMConfig.mrt_rates: s_e = 1.19 (k=1),
+    s_eps = 1.4 (k=2), s_q = 1.2 (k=4, 6, 8), s_pi = 1/tau (k=10, 12), s_m = 1.98 (k=16-18);
+    the shear rates stay 1/tau. The reference instead uses 1/tau and 8(2-s)/(8-s)."""
+    s_pi = 1.0 / tau
+    return {1: 1.19, 2: 1.4, 4: 1.2, 6: 1.2, 8: 1.2, 10: s_pi, 12: s_pi, 16: 1.98, 17: 1.98,
+            18: 1.98}
 
 
 class LBMSolver3D:
@@ -67,13 +87,14 @@ class LBMSolver3D:
         self.bc_x_left_mode = _boundary_mode(config.x_left)
         self.bc_x_right_mode = _boundary_mode(config.x_right)
 
-        self._s = relaxation_rates(config.viscosity)
+        self._s = relaxation_rates(config.viscosity, config.mrt_rates)
         self._desc = self._make_desc()
         self._device = nat.device()
         nat.load()
         n = self.n_cells
         dev = self._device
-        self._pops = torch.zeros((_Q, n), dtype=torch.float32, device=dev)
+        self._pops = torch.zeros((_Q, n), dtype=_STORAGE_DTYPE[config.population_storage],
+                                 device=dev)
         self._macro = torch.zeros((n, 4), dtype=torch.float32, device=dev)
         self._force_buf = [torch.zeros((3, n), dtype=torch.float32, device=dev) for _ in range(2)]
         self._flags = torch.zeros(n, dtype=torch.int32, device=dev)
@@ -118,6 +139,8 @@ class LBMSolver3D:
         for i in range(3):
             d.bc_vel_left[i] = float(np.float32(c.x_left.velocity[i]))
             d.bc_vel_right[i] = float(np.float32(c.x_right.velocity[i]))
+        d.storage = _STORAGE_CODE[c.population_storage]
+        d.arithmetic = nat.ARITH_FAST if c.resolved_arithmetic() == "fast" else nat.ARITH_EXACT
         return d
 
     def _call(self, name: str, *args) -> None:

@@ -45,6 +45,9 @@ def test_defaults_validate_and_mpm_dt():
     CouplingConfig(contact_fraction_threshold=1.1), OutputConfig(output_interval=0),
     OutputConfig(output_format="bad"), BoundaryConfig(velocity=(0.0, 1.0)),
     MPMConfig(constitutive_model="plastic"),
+    LBMConfig(population_storage="f8"), LBMConfig(collision_arithmetic="approx"),
+    LBMConfig(population_storage="f16", collision_arithmetic="exact"),
+    LBMConfig(mrt_rates={9: 1.5}), LBMConfig(mrt_rates={4: 2.5}),
     SimulationConfig(lbm=LBMConfig(nx=64, ny=32, nz=16), mpm=MPMConfig(nx=32, ny=32, nz=16)),
 ])
 def test_invalid_configs_raise_value_error(bad):
@@ -128,3 +131,20 @@ def test_package_exports():
                  "load_validation_summary", "validation_summary_table", "ReferenceDataset",
                  "ReferenceReport", "load_reference_dataset", "run_reference_validation_suite"):
         assert name in fsi.__all__
+
+
+def test_storage_forms_resolve_their_arithmetic():
+    assert LBMConfig().resolved_arithmetic() == "exact"
+    assert LBMConfig(population_storage="bf16").resolved_arithmetic() == "fast"
+    assert LBMConfig(collision_arithmetic="fast").resolved_arithmetic() == "fast"
+
+
+def test_mrt_rate_overrides_touch_only_the_named_moments():
+    import numpy as np
+    from fsi.lbm3d import dhumieres_rates, relaxation_rates
+    base = relaxation_rates(1 / 30)
+    rates = relaxation_rates(1 / 30, dhumieres_rates(0.6))
+    changed = {k for k in range(19) if rates[k] != base[k]}
+    assert changed == {1, 2, 4, 6, 8, 16, 17, 18}  # s_pi = 1/tau equals the default at k=10, 12
+    assert rates[4] == np.float32(1.2) and rates[16] == np.float32(1.98)
+    LBMConfig(mrt_rates=dhumieres_rates(0.6)).validate()

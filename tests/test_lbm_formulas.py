@@ -35,3 +35,81 @@ def test_tables_match_the_oracle():
     assert float(w[0]).hex() == "0x1.5555560000000p-2"
     assert float(w[1]).hex() == "0x1.c71c720000000p-5"
     assert float(w[7]).hex() == "0x1.c71c720000000p-6"
+
+
+def _split_top(text: str) -> list[str]:
+    """Split at commas outside parentheses/brackets."""
+    parts, depth, cur = [], 0, ""
+    for ch in text:
+        if ch in "([":
+            depth += 1
+        elif ch in ")]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            parts.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    parts.append(cur)
+    return [p.strip() for p in parts]
+
+
+def _fast_as_python(src: str) -> str:
+    """Body of the generated mrt_collide_fast as Python statements."""
+    import re
+    body = src.split("mrt_collide_fast(", 1)[1].split("{", 1)[1]
+    body = body[: body.index("\n}\n")]
+    body = re.sub(r"(-?0x[0-9a-f.]+p[+-]\d+)f", lambda m: repr(float.fromhex(m.group(1))), body)
+    body = re.sub(r"\b(\d+\.\d+)f\b", r"\1", body)
+    stmts = []
+    for line in body.strip().splitlines():
+        line = line.strip()
+        if line.startswith("{"):
+            line = line.strip("{} ")
+        for stmt in filter(None, (s.strip() for s in line.split(";"))):
+            stmt = stmt.replace("const float ", "").replace("float ", "")
+            stmts.extend(_split_top(stmt))
+    return "\n".join(stmts).replace("fmaf(", "fma(")
+
+
+def _collide_f64(gen, F, u, G, S):
+    """MRT + Guo collision of the reference written from its definition, in float64."""
+    E = np.array(gen.E, float)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    M = gen.M.astype(np.float64)
+    eu, eG = u @ E.T, G @ E.T
+    t = w * (eG - (u * G).sum(1)[:, None] + eu * eG)
+    m, g = F @ M.T, t @ M.T
+    ux, uy, uz = u.T
+    meq = np.zeros_like(m)
+    meq[:, 1] = ux * ux + uy * uy + uz * uz
+    meq[:, 9] = 2 * ux * ux - uy * uy - uz * uz
+    meq[:, 11] = uy * uy - uz * uz
+    meq[:, 13], meq[:, 14], meq[:, 15] = ux * uy, uy * uz, ux * uz
+    post = m - S * (m - meq) + (1 - 0.5 * S) * g
+    for k in (0, 3, 5, 7):
+        post[:, k] = m[:, k] + g[:, k]
+    return post @ np.linalg.inv(M).T
+
+
+def test_fast_collision_is_the_same_operator():
+    gen = load_gen()
+    code = _fast_as_python(gen.gen())
+    rng = np.random.default_rng(3)
+    n = 4000
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    F = w * rng.uniform(0.9, 1.1, (n, 1)) * (1 + rng.normal(0, 0.02, (n, 19)))
+    u = rng.normal(0, 0.05, (n, 3))
+    G = rng.normal(0, 1e-4, (n, 3))
+    S = np.array([0, 1.2, 1.3, 0, 1.1, 0, 1.1, 0, 1.1, 1.6, 1.6, 1.6, 1.6, 1.6, 1.6, 1.6, 1.4,
+                  1.4, 1.4])
+    out = [None] * 19
+    env = {"F": F.T, "rho": F.sum(1), "ux": u[:, 0], "uy": u[:, 1], "uz": u[:, 2],
+           "gx": G[:, 0], "gy": G[:, 1], "gz": G[:, 2], "S": S, "out": out,
+           "fma": lambda a, b, c: a * b + c}
+    exec(code, env)
+    want = _collide_f64(gen, F, u, G, S)
+    got = np.stack(out, axis=1)
+    # The generated coefficients are float32 roundings of 1/3, 1/18, ... (relative 3e-8); an
+    # algebra mistake in a moment or forcing term shows up at 1e-5 and above.
+    np.testing.assert_allclose(got, want, rtol=1e-7, atol=0)
