@@ -136,6 +136,7 @@ def barrier(world: int) -> None:
 # ------------------------------------------------------------------ GPU arm
 
 FORM_BYTES = {  # (algorithmic, moved by the fused step) bytes per cell update
+    ("f32", "exact"): (LBM_BYTES_PER_CELL, KERNEL_BYTES_PER_CELL),
     ("f32", "fast"): (LBM_BYTES_PER_CELL, KERNEL_BYTES_PER_CELL),
     ("f16", "fast"): (LBM_BYTES_PER_CELL - 76, KERNEL_BYTES_PER_CELL - 76),
     ("bf16", "fast"): (LBM_BYTES_PER_CELL - 76, KERNEL_BYTES_PER_CELL - 76),
@@ -152,6 +153,8 @@ def time_lbm_forms(lcfg, mask, args, world, stream) -> dict:
     peak, _ = load_peaks()
     out = {}
     for (storage, arithmetic), (alg, moved) in FORM_BYTES.items():
+        if f"{storage}/{arithmetic}" == args.lbm_form:
+            continue
         cfg = dataclasses.replace(lcfg, population_storage=storage, collision_arithmetic=arithmetic)
         lbm = LBMSolver3D(cfg)
         lbm.initialize(mask)
@@ -178,6 +181,69 @@ def time_lbm_forms(lcfg, mask, args, world, stream) -> dict:
     return out
 
 
+def time_coupled(args, world, stream) -> dict:
+    """Coupled LBM-MPM steps (LBMMpmCoupler.step) on the coupled smoke workload (48x32x32,
+    4096 particles) and the coupled workload at scale (384x192x192, 48 bodies), FP32 exact."""
+    import torch
+    from fsi import scenes
+    from fsi.simulation import FSISimulation
+
+    out = {}
+    cases = [("smoke_48x32x32", 100)]
+    if not args.no_coupled_scale:
+        cases.append(("bodies_384x192x192", 20))
+    for name, steps in cases:
+        if name.startswith("smoke"):
+            cfg, solid, pos = scenes.coupled_smoke(steps)
+            young = None
+        else:
+            cfg, solid, pos, young = scenes.coupled_bodies()
+        sim = FSISimulation(cfg)
+        sim.initialize_lbm(solid)
+        sim.initialize_mpm_from_numpy(pos, youngs_modulus=young,
+                                      poisson_ratio=None if young is None else 0.3)
+        for _ in range(3):
+            sim.coupler.step(cfg.lbm_dt)
+        barrier(world)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            sim.coupler.step(cfg.lbm_dt)
+        b.record(stream)
+        barrier(world)
+        eager_ms = max_over_ranks(a.elapsed_time(b), world) / steps
+        # the same steps replayed from a captured CUDA graph (capture outside the timed region)
+        sim.coupler.step_many(cfg.lbm_dt, 4)
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a.record(stream)
+        sim.coupler.step_many(cfg.lbm_dt, steps)
+        b.record(stream)
+        barrier(world)
+        torch.cuda.synchronize()
+        graph_wall_ms = (time.perf_counter() - t0) * 1e3 / steps
+        ms = max_over_ranks(a.elapsed_time(b), world) / steps
+        sub = cfg.coupling.mpm_substeps_per_lbm_step
+        cells = cfg.lbm.nx * cfg.lbm.ny * cfg.lbm.nz
+        out[name] = {
+            "coupled_steps_per_s": round(1e3 / ms * world, 2), "ms_per_step": round(ms, 4),
+            "eager_ms_per_step": round(eager_ms, 4),
+            "graph_wall_ms_per_step": round(graph_wall_ms, 4),
+            "mode": "step_many (CUDA graph of two coupled steps, capture included)",
+            "mlups": round(cells / (ms * 1e-3) / 1e6 * world, 2),
+            "particle_steps_per_s": round(len(pos) * sub / (ms * 1e-3) * world, 1),
+            "cells": cells, "particles": int(len(pos)), "substeps": sub, "timed_steps": steps,
+            # per substep: coupling forces + P2G + G2P + block clear; per step: force assembly,
+            # lattice step and, with x-face conditions, the face kernel
+            "gpu_launches": 2 * steps * (4 * sub + 2 + (1 if sim.lbm.bc_x_left_mode
+                                                        or sim.lbm.bc_x_right_mode else 0)),
+        }
+        del sim
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args) -> dict:
     import torch
     from fsi import scenes
@@ -190,8 +256,12 @@ def run_gpu(args) -> dict:
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
+    import dataclasses
     lcfg, mask = scenes.channel_spheres_lbm(n=args.n)
-    lbm = LBMSolver3D(lcfg)
+    storage, arithmetic = args.lbm_form.split("/")
+    head_cfg = dataclasses.replace(lcfg, population_storage=storage, collision_arithmetic=arithmetic)
+    alg_bytes, moved_bytes = FORM_BYTES[(storage, arithmetic)]
+    lbm = LBMSolver3D(head_cfg)
     lbm.initialize(mask)
     cells = lbm.n_cells
     fluid_cells = int((mask == 0).sum())
@@ -227,6 +297,8 @@ def run_gpu(args) -> dict:
         barrier(world)
         # --- the lattice in the other storage / arithmetic forms ----------------
         forms = time_lbm_forms(lcfg, mask, args, world, stream) if not args.no_forms else {}
+        # --- coupled steps -------------------------------------------------------
+        coupled = time_coupled(args, world, stream) if not args.no_coupled else {}
     lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
     lbm_launches = args.steps
     mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
@@ -255,7 +327,7 @@ def run_gpu(args) -> dict:
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
 
     peak, peak_kind = load_peaks()
-    achieved = LBM_BYTES_PER_CELL * cells / (lbm_ms * 1e-3) / 1e9
+    achieved = alg_bytes * cells / (lbm_ms * 1e-3) / 1e9
     mlups = cells / (lbm_ms * 1e-3) / 1e6
     result = {
         "metric": METRIC,
@@ -268,10 +340,11 @@ def run_gpu(args) -> dict:
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32" if storage == "f32" else f"{storage} storage, f32 arithmetic",
         "data": "synthetic (seeded scene generators; no dataset)",
         "config": {
             "workload": "standalone lattice 256^3 channel + 64 elastic cubes (2,097,152 particles)",
+            "lbm_form": args.lbm_form,
             "lattice": [args.n] * 3, "tau": 0.6, "g_x": 1e-6,
             "solid_fraction": round(float(mask.mean()), 4),
             "fluid_cells": fluid_cells,
@@ -291,8 +364,8 @@ def run_gpu(args) -> dict:
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": None,
             "kernel": "lbm_step_kernel", "peak_source": peak_kind,
-            "algorithmic_bytes_per_cell": LBM_BYTES_PER_CELL,
-            "kernel_bytes_per_cell": KERNEL_BYTES_PER_CELL,
+            "algorithmic_bytes_per_cell": alg_bytes,
+            "kernel_bytes_per_cell": moved_bytes,
         },
         "e2e": {
             "value": round(cells * args.steps / e2e_s / 1e6 * world, 3), "unit": "MLUPS",
@@ -301,9 +374,11 @@ def run_gpu(args) -> dict:
             "last_diagnostics": [float(diag[0]), float(diag[1])] if diag else None,
         },
         "lbm_forms": forms,
+        "coupled": coupled,
         # lattice steps + 3 MPM launches per substep + 3 launches per end-to-end step
-        # (force op, step, fused macro + diagnostics) + one step per form per step
-        "gpu_launches": lbm_launches + 3 * args.steps + 3 * args.steps + len(forms) * args.steps,
+        # (force op, step, fused macro + diagnostics) + one step per form per step + coupled
+        "gpu_launches": (lbm_launches + 3 * args.steps + 3 * args.steps + len(forms) * args.steps
+                         + sum(c["gpu_launches"] for c in coupled.values())),
         "clocks": clocks.summary(),
     }
     if world > 1:
@@ -394,6 +469,12 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lbm-form", default="f32/exact",
+                    choices=["f32/exact", "f32/fast", "f16/fast", "bf16/fast"],
+                    help="population storage / collision arithmetic of the headline lattice")
+    ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-step timings")
+    ap.add_argument("--no-coupled-scale", action="store_true",
+                    help="time only the small coupled workload")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip timing the FP32-fast / FP16 / BF16 lattice forms")
     args = ap.parse_args()

@@ -20,6 +20,11 @@ bit-identical to a literal evaluation of those sums in IEEE float32:
 Every claim above is checked numerically by ``self_check()`` (and by the test
 suite) against a literal sequential float32 evaluation with the full tables.
 
+The functions are templates over the value type V: ``float`` for one cell, or
+``float2`` for two cells at once through the packed FP32 instructions of sm_100+
+(``vadd``/``vsub``/``vmul``/``vfma`` of lbm_vec.cuh), whose per-lane results are
+those of the scalar round-to-nearest operations, so both are bit-identical.
+
 Run: python gen_lbm_formulas.py  (rewrites lbm_formulas.cuh next to this file)
 """
 from __future__ import annotations
@@ -109,12 +114,12 @@ def chain(var: str, terms: list[tuple[int, str]]) -> list[str]:
     """Sequential float sum of signed terms, in order, with explicit rounding per step."""
     lines = []
     if not terms:
-        lines.append(f"{var} = 0.0f;")
+        lines.append(f"{var} = splat<V>(0.0f);")
         return lines
     s0, e0 = terms[0]
-    lines.append(f"{var} = {e0 if s0 > 0 else '-' + e0};")
+    lines.append(f"{var} = {e0 if s0 > 0 else 'vneg(' + e0 + ')'};")
     for s, e in terms[1:]:
-        op = "__fadd_rn" if s > 0 else "__fsub_rn"
+        op = "vadd" if s > 0 else "vsub"
         lines.append(f"{var} = {op}({var}, {e});")
     return lines
 
@@ -127,15 +132,18 @@ def gen() -> str:
     w("// register formulas with the reference's float32 operation order.")
     w("#pragma once")
     w("")
+    w('#include "lbm_vec.cuh"')
+    w("")
     w("namespace fsi {")
     w("")
     # forward transform on an input array X (F or Guo terms t)
     w("// m[k] = sum_q M[k][q] * X[q], sequential in q (lbm3d.py:269-274).")
-    w("__device__ __forceinline__ void mrt_forward(const float (&X)[19], float (&m)[19]) {")
-    w("  float two[19];")
+    w("template <class V>")
+    w("__device__ __forceinline__ void mrt_forward(const V (&X)[19], V (&m)[19]) {")
+    w("  V two[19];")
     need_two = sorted({q for k in range(Q) for q in range(Q) if abs(M[k, q]) == 2})
     for q in need_two:
-        w(f"  two[{q}] = __fadd_rn(X[{q}], X[{q}]);")
+        w(f"  two[{q}] = vadd(X[{q}], X[{q}]);")
     for k in range(Q):
         terms = []
         for q in range(Q):
@@ -150,12 +158,13 @@ def gen() -> str:
     classes, entry = inverse_plan()
     w("// f[q] = sum_k inv(M)[q][k] * m[k], sequential in k (lbm3d.py:328-333).")
     w(f"// {len(classes)} rounded products; every other product is an exact power-of-two scaling.")
-    w("__device__ __forceinline__ void mrt_inverse(const float (&m)[19], float (&f)[19]) {")
+    w("template <class V>")
+    w("__device__ __forceinline__ void mrt_inverse(const V (&m)[19], V (&f)[19]) {")
     names = {}
     for (k, ci), b in classes:
         nm = f"p{k}_{ci}"
         names[(k, ci)] = nm
-        w(f"  const float {nm} = __fmul_rn({f32hex(b)}, m[{k}]);")
+        w(f"  const V {nm} = vmul(m[{k}], {f32hex(b)});")
     for q in range(Q):
         terms = []
         for k in range(Q):
@@ -163,9 +172,9 @@ def gen() -> str:
                 continue
             sign, cls, j = entry[(q, k)]
             base = names[cls]
-            expr = base if j == 0 else f"__fmul_rn({base}, {f32hex(2.0 ** j)})"
+            expr = base if j == 0 else f"vmul({base}, {f32hex(2.0 ** j)})"
             terms.append((sign, expr))
-        w("  { float a; " + " ".join(chain("a", terms)) + f" f[{q}] = a; }}")
+        w("  { V a; " + " ".join(chain("a", terms)) + f" f[{q}] = a; }}")
     w("}")
     w("")
     out.extend(gen_fast().splitlines())
@@ -183,16 +192,16 @@ def _lin(terms: list[tuple[float, str]]) -> str:
     """Sum of coefficient * symbol with fused multiply-adds (coefficients +-1 become adds)."""
     terms = [(c, s) for c, s in terms if c != 0.0]
     if not terms:
-        return "0.0f"
+        return "splat<V>(0.0f)"
     c0, s0 = terms[0]
-    expr = s0 if c0 == 1.0 else (f"-{s0}" if c0 == -1.0 else f"({_fmt(c0)} * {s0})")
+    expr = s0 if c0 == 1.0 else (f"vneg({s0})" if c0 == -1.0 else f"vmul({s0}, {_fmt(c0)})")
     for c, s in terms[1:]:
         if c == 1.0:
-            expr = f"({expr} + {s})"
+            expr = f"vadd({expr}, {s})"
         elif c == -1.0:
-            expr = f"({expr} - {s})"
+            expr = f"vsub({expr}, {s})"
         else:
-            expr = f"fmaf({_fmt(c)}, {s}, {expr})"
+            expr = f"vfma({_fmt(c)}, {s}, {expr})"
     return expr
 
 
@@ -219,20 +228,21 @@ def gen_fast() -> str:
     w_("// parity-split moments from pair sums/differences, closed-form forcing moments")
     w_("// g_k = A_k.G - B_k (u.G) + u^T C_k G, parity-split inverse. Used by the FP16/BF16")
     w_("// storage forms and the FP32 fast form.")
-    w_("__device__ __forceinline__ void mrt_collide_fast(const float (&F)[19], float rho, float ux,")
-    w_("    float uy, float uz, float gx, float gy, float gz, const float* __restrict__ S,")
-    w_("    float (&out)[19]) {")
+    w_("template <class V>")
+    w_("__device__ __forceinline__ void mrt_collide_fast(const V (&F)[19], V rho, V ux, V uy, V uz,")
+    w_("    V gx, V gy, V gz, const float* __restrict__ S, V (&out)[19]) {")
     for p, (a, b) in enumerate(pairs):
-        w_(f"  const float P{p} = F[{a}] + F[{b}], D{p} = F[{a}] - F[{b}];")
+        w_(f"  const V P{p} = vadd(F[{a}], F[{b}]), D{p} = vsub(F[{a}], F[{b}]);")
     for k in even:
         terms = [(Md[k, 0], "F[0]")] + [(Md[k, a], f"P{p}") for p, (a, b) in enumerate(pairs)]
-        w_(f"  float m{k} = {_lin(terms)};")
+        w_(f"  V m{k} = {_lin(terms)};")
     for k in odd:
         terms = [(Md[k, a], f"D{p}") for p, (a, b) in enumerate(pairs)]
-        w_(f"  float m{k} = {_lin(terms)};")
-    w_("  const float uG = fmaf(ux, gx, fmaf(uy, gy, uz * gz));")
-    w_("  const float pxx = ux * gx, pyy = uy * gy, pzz = uz * gz;")
-    w_("  const float sxy = fmaf(ux, gy, uy * gx), syz = fmaf(uy, gz, uz * gy), sxz = fmaf(ux, gz, uz * gx);")
+        w_(f"  V m{k} = {_lin(terms)};")
+    w_("  const V uG = vfma(ux, gx, vfma(uy, gy, vmul(uz, gz)));")
+    w_("  const V pxx = vmul(ux, gx), pyy = vmul(uy, gy), pzz = vmul(uz, gz);")
+    w_("  const V sxy = vfma(ux, gy, vmul(uy, gx)), syz = vfma(uy, gz, vmul(uz, gy)), "
+       "sxz = vfma(ux, gz, vmul(uz, gx));")
     sym = {(0, 0): "pxx", (1, 1): "pyy", (2, 2): "pzz", (0, 1): "sxy", (1, 2): "syz", (0, 2): "sxz"}
     gnames = {}
     for k in range(Q):
@@ -242,29 +252,30 @@ def gen_fast() -> str:
             terms.append((coef, s))
         terms = [(float(c), s) for c, s in terms if abs(c) > 1e-14]
         if terms:
-            w_(f"  const float g{k} = {_lin(terms)};")
+            w_(f"  const V g{k} = {_lin(terms)};")
             gnames[k] = f"g{k}"
-    w_("  const float uu = fmaf(ux, ux, fmaf(uy, uy, uz * uz));")
+    w_("  const V uu = vfma(ux, ux, vfma(uy, uy, vmul(uz, uz)));")
     meq = {0: "rho", 1: "uu", 3: "ux", 5: "uy", 7: "uz",
-           9: "fmaf(2.0f * ux, ux, -fmaf(uy, uy, uz * uz))", 11: "fmaf(uy, uy, -(uz * uz))",
-           13: "ux * uy", 14: "uy * uz", 15: "ux * uz"}
+           9: "vfma(vadd(ux, ux), ux, vneg(vfma(uy, uy, vmul(uz, uz))))",
+           11: "vfma(uy, uy, vneg(vmul(uz, uz)))",
+           13: "vmul(ux, uy)", 14: "vmul(uy, uz)", 15: "vmul(ux, uz)"}
     for k in range(Q):
         g = gnames.get(k)
         if k in (0, 3, 5, 7):
             if g:
-                w_(f"  m{k} = m{k} + {g};")
+                w_(f"  m{k} = vadd(m{k}, {g});")
             continue
-        d = f"(m{k} - ({meq[k]}))" if k in meq else f"m{k}"
-        rel = f"fmaf(-S[{k}], {d}, m{k})"
+        d = f"vsub(m{k}, {meq[k]})" if k in meq else f"m{k}"
+        rel = f"vfma(-S[{k}], {d}, m{k})"
         if g:
-            w_(f"  m{k} = fmaf(fmaf(-0.5f, S[{k}], 1.0f), {g}, {rel});")
+            w_(f"  m{k} = vfma(fmaf(-0.5f, S[{k}], 1.0f), {g}, {rel});")
         else:
             w_(f"  m{k} = {rel};")
     w_(f"  out[0] = {_lin([(inv[0, k], f'm{k}') for k in even])};")
     for p, (a, b) in enumerate(pairs):
         ev = _lin([(inv[a, k], f"m{k}") for k in even])
         od = _lin([(inv[a, k], f"m{k}") for k in odd])
-        w_(f"  {{ const float e = {ev}, o = {od}; out[{a}] = e + o; out[{b}] = e - o; }}")
+        w_(f"  {{ const V e = {ev}, o = {od}; out[{a}] = vadd(e, o); out[{b}] = vsub(e, o); }}")
     w_("}")
     return "\n".join(lines)
 

@@ -25,9 +25,11 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "fsi_common.cuh"
 #include "lbm_formulas.cuh"
+#include "lbm_vec.cuh"
 
 namespace fsi {
 namespace {
@@ -62,6 +64,7 @@ CellLaunch cell_launch(const LbmGeom& g) {
 struct Deltas {
   uint32_t c;
   int xp, xm, yp, ym, zp, zm;
+  __device__ __forceinline__ Deltas() {}
   __device__ __forceinline__ Deltas(const LbmGeom& g, int i, int j, int k) {
     const int nyz = g.ny * g.nz;
     c = (uint32_t)((i * g.ny + j) * g.nz + k);
@@ -93,6 +96,13 @@ struct Store<FSI_STORAGE_F32> {
   using T = float;
   static __device__ __forceinline__ float ld(const T* p, uint32_t i, float) { return p[i]; }
   static __device__ __forceinline__ void st(T* p, uint32_t i, float v, float) { p[i] = v; }
+  static __device__ __forceinline__ float2 ld2(const T* p, uint32_t i0, uint32_t i1, float) {
+    return make_float2(p[i0], p[i1]);
+  }
+  static __device__ __forceinline__ void st2(T* p, uint32_t i0, uint32_t i1, float2 v, float) {
+    p[i0] = v.x;
+    p[i1] = v.y;
+  }
 };
 
 constexpr float kF16Scale = 4096.0f;  // deviations of order 1e-8..1e-1 map into FP16's normal range
@@ -106,6 +116,16 @@ struct Store<FSI_STORAGE_F16> {
   static __device__ __forceinline__ void st(T* p, uint32_t i, float v, float s) {
     p[i] = __float2half_rn((v - s) * kF16Scale);
   }
+  // Two values at once: one packed conversion and one packed fma / sub+mul per pair.
+  static __device__ __forceinline__ float2 ld2(const T* p, uint32_t i0, uint32_t i1, float s) {
+    const float2 h = __half22float2(__halves2half2(p[i0], p[i1]));
+    return vfma(h, make_float2(1.0f / kF16Scale, 1.0f / kF16Scale), make_float2(s, s));
+  }
+  static __device__ __forceinline__ void st2(T* p, uint32_t i0, uint32_t i1, float2 v, float s) {
+    const __half2 h = __float22half2_rn(vmul(vsub(v, s), kF16Scale));
+    p[i0] = __low2half(h);
+    p[i1] = __high2half(h);
+  }
 };
 
 template <>
@@ -116,6 +136,14 @@ struct Store<FSI_STORAGE_BF16> {
   }
   static __device__ __forceinline__ void st(T* p, uint32_t i, float v, float s) {
     p[i] = __float2bfloat16_rn(v - s);
+  }
+  static __device__ __forceinline__ float2 ld2(const T* p, uint32_t i0, uint32_t i1, float s) {
+    return vadd(__bfloat1622float2(__halves2bfloat162(p[i0], p[i1])), s);
+  }
+  static __device__ __forceinline__ void st2(T* p, uint32_t i0, uint32_t i1, float2 v, float s) {
+    const __nv_bfloat162 h = __float22bfloat162_rn(vsub(v, s));
+    p[i0] = __low2bfloat16(h);
+    p[i1] = __high2bfloat16(h);
   }
 };
 
@@ -138,109 +166,113 @@ __device__ __forceinline__ uint32_t slot32(uint32_t n, const Deltas& d, uint32_t
 // ---------------------------------------------------------------- macro fields
 // rho and u as update_macro computes them (lbm3d.py:409-425): sequential sums
 // in q order, then u = u / rho, u = u + (force * 0.5) / rho.
-__device__ __forceinline__ void macro_of(const float (&F)[19], float gx, float gy, float gz,
-                                         float& rho, float& ux, float& uy, float& uz) {
-  float r = F[0];
+template <class V>
+__device__ __forceinline__ void macro_of(const V (&F)[19], V gx, V gy, V gz, V& rho, V& ux, V& uy,
+                                         V& uz) {
+  V r = F[0];
 #pragma unroll
-  for (int q = 1; q < 19; ++q) r = __fadd_rn(r, F[q]);
-  float x = __fsub_rn(F[1], F[2]);
-  x = __fadd_rn(x, F[7]); x = __fsub_rn(x, F[8]); x = __fadd_rn(x, F[9]); x = __fsub_rn(x, F[10]);
-  x = __fadd_rn(x, F[11]); x = __fsub_rn(x, F[12]); x = __fadd_rn(x, F[13]); x = __fsub_rn(x, F[14]);
-  float y = __fsub_rn(F[3], F[4]);
-  y = __fadd_rn(y, F[7]); y = __fsub_rn(y, F[8]); y = __fsub_rn(y, F[9]); y = __fadd_rn(y, F[10]);
-  y = __fadd_rn(y, F[15]); y = __fsub_rn(y, F[16]); y = __fadd_rn(y, F[17]); y = __fsub_rn(y, F[18]);
-  float z = __fsub_rn(F[5], F[6]);
-  z = __fadd_rn(z, F[11]); z = __fsub_rn(z, F[12]); z = __fsub_rn(z, F[13]); z = __fadd_rn(z, F[14]);
-  z = __fadd_rn(z, F[15]); z = __fsub_rn(z, F[16]); z = __fsub_rn(z, F[17]); z = __fadd_rn(z, F[18]);
-  x = __fdiv_rn(x, r); y = __fdiv_rn(y, r); z = __fdiv_rn(z, r);
-  x = __fadd_rn(x, __fdiv_rn(__fmul_rn(gx, 0.5f), r));
-  y = __fadd_rn(y, __fdiv_rn(__fmul_rn(gy, 0.5f), r));
-  z = __fadd_rn(z, __fdiv_rn(__fmul_rn(gz, 0.5f), r));
+  for (int q = 1; q < 19; ++q) r = vadd(r, F[q]);
+  V x = vsub(F[1], F[2]);
+  x = vadd(x, F[7]); x = vsub(x, F[8]); x = vadd(x, F[9]); x = vsub(x, F[10]);
+  x = vadd(x, F[11]); x = vsub(x, F[12]); x = vadd(x, F[13]); x = vsub(x, F[14]);
+  V y = vsub(F[3], F[4]);
+  y = vadd(y, F[7]); y = vsub(y, F[8]); y = vsub(y, F[9]); y = vadd(y, F[10]);
+  y = vadd(y, F[15]); y = vsub(y, F[16]); y = vadd(y, F[17]); y = vsub(y, F[18]);
+  V z = vsub(F[5], F[6]);
+  z = vadd(z, F[11]); z = vsub(z, F[12]); z = vsub(z, F[13]); z = vadd(z, F[14]);
+  z = vadd(z, F[15]); z = vsub(z, F[16]); z = vsub(z, F[17]); z = vadd(z, F[18]);
+  x = vdiv(x, r); y = vdiv(y, r); z = vdiv(z, r);
+  x = vadd(x, vdiv(vmul(gx, 0.5f), r));
+  y = vadd(y, vdiv(vmul(gy, 0.5f), r));
+  z = vadd(z, vdiv(vmul(gz, 0.5f), r));
   rho = r; ux = x; uy = y; uz = z;
 }
 
 // The same quantities with fused operations and one reciprocal (fast forms).
-__device__ __forceinline__ void macro_fast(const float (&F)[19], float gx, float gy, float gz,
-                                           float& rho, float& ux, float& uy, float& uz) {
-  const float P0 = F[1] + F[2], P1 = F[3] + F[4], P2 = F[5] + F[6], P3 = F[7] + F[8];
-  const float P4 = F[9] + F[10], P5 = F[11] + F[12], P6 = F[13] + F[14], P7 = F[15] + F[16];
-  const float P8 = F[17] + F[18];
-  const float r = (((F[0] + P0) + (P1 + P2)) + ((P3 + P4) + (P5 + P6))) + (P7 + P8);
-  const float D3 = F[7] - F[8], D4 = F[9] - F[10], D5 = F[11] - F[12], D6 = F[13] - F[14];
-  const float D7 = F[15] - F[16], D8 = F[17] - F[18];
-  const float jx = ((F[1] - F[2]) + (D3 + D4)) + (D5 + D6);
-  const float jy = ((F[3] - F[4]) + (D3 - D4)) + (D7 + D8);
-  const float jz = ((F[5] - F[6]) + (D5 - D6)) + (D7 - D8);
-  const float inv = __frcp_rn(r);
+template <class V>
+__device__ __forceinline__ void macro_fast(const V (&F)[19], V gx, V gy, V gz, V& rho, V& ux,
+                                           V& uy, V& uz) {
+  const V P0 = vadd(F[1], F[2]), P1 = vadd(F[3], F[4]), P2 = vadd(F[5], F[6]);
+  const V P3 = vadd(F[7], F[8]), P4 = vadd(F[9], F[10]), P5 = vadd(F[11], F[12]);
+  const V P6 = vadd(F[13], F[14]), P7 = vadd(F[15], F[16]), P8 = vadd(F[17], F[18]);
+  const V r = vadd(vadd(vadd(vadd(F[0], P0), vadd(P1, P2)), vadd(vadd(P3, P4), vadd(P5, P6))),
+                   vadd(P7, P8));
+  const V D3 = vsub(F[7], F[8]), D4 = vsub(F[9], F[10]), D5 = vsub(F[11], F[12]);
+  const V D6 = vsub(F[13], F[14]), D7 = vsub(F[15], F[16]), D8 = vsub(F[17], F[18]);
+  const V jx = vadd(vadd(vsub(F[1], F[2]), vadd(D3, D4)), vadd(D5, D6));
+  const V jy = vadd(vadd(vsub(F[3], F[4]), vsub(D3, D4)), vadd(D7, D8));
+  const V jz = vadd(vadd(vsub(F[5], F[6]), vsub(D5, D6)), vsub(D7, D8));
+  const V inv = vrcp(r);
   rho = r;
-  ux = fmaf(gx, 0.5f, jx) * inv;
-  uy = fmaf(gy, 0.5f, jy) * inv;
-  uz = fmaf(gz, 0.5f, jz) * inv;
+  ux = vmul(vfma(0.5f, gx, jx), inv);
+  uy = vmul(vfma(0.5f, gy, jy), inv);
+  uz = vmul(vfma(0.5f, gz, jz), inv);
 }
 
-template <bool kFast>
-__device__ __forceinline__ void macro_any(const float (&F)[19], float gx, float gy, float gz,
-                                          float& rho, float& ux, float& uy, float& uz) {
+template <bool kFast, class V>
+__device__ __forceinline__ void macro_any(const V (&F)[19], V gx, V gy, V gz, V& rho, V& ux,
+                                          V& uy, V& uz) {
   if (kFast) macro_fast(F, gx, gy, gz, rho, ux, uy, uz);
   else macro_of(F, gx, gy, gz, rho, ux, uy, uz);
 }
 
 // Sum of the non-zero terms e_c * v_c in x, y, z order (Taichi Vector.dot with
 // exact zero products dropped).
-__device__ __forceinline__ float edot(int q, float vx, float vy, float vz) {
-  float s = 0.0f;
+template <class V>
+__device__ __forceinline__ V edot(int q, V vx, V vy, V vz) {
+  V s = splat<V>(0.0f);
   bool first = true;
-  if (ex(q) != 0) { s = ex(q) > 0 ? vx : -vx; first = false; }
-  if (ey(q) != 0) { float t = ey(q) > 0 ? vy : -vy; s = first ? t : __fadd_rn(s, t); first = false; }
-  if (ez(q) != 0) { float t = ez(q) > 0 ? vz : -vz; s = first ? t : __fadd_rn(s, t); }
+  if (ex(q) != 0) { s = ex(q) > 0 ? vx : vneg(vx); first = false; }
+  if (ey(q) != 0) { V t = ey(q) > 0 ? vy : vneg(vy); s = first ? t : vadd(s, t); first = false; }
+  if (ez(q) != 0) { V t = ez(q) > 0 ? vz : vneg(vz); s = first ? t : vadd(s, t); }
   return s;
 }
 
-// MRT collision with Guo forcing of one fluid cell in the reference's order (lbm3d.py:276-333).
-__device__ __forceinline__ void collide_cell(const float (&F)[19], float rho, float ux, float uy,
-                                             float uz, float gx, float gy, float gz,
-                                             const float* __restrict__ S, float (&out)[19]) {
+// MRT collision with Guo forcing of one fluid cell (or two, V = float2) in the reference's
+// order (lbm3d.py:276-333).
+template <class V>
+__device__ __forceinline__ void collide_cell(const V (&F)[19], V ux, V uy, V uz, V gx, V gy, V gz,
+                                             const float* __restrict__ S, V (&out)[19]) {
   // Guo source terms t_q = w_q ((e_q - u).G + (e_q.u)(e_q.G)) (lbm3d.py:276-283).
   // (e - u_c) G_c takes three values per axis, for e = -1, 0, +1.
-  const float dx[3] = {__fmul_rn(__fsub_rn(-1.0f, ux), gx), __fmul_rn(-ux, gx),
-                       __fmul_rn(__fsub_rn(1.0f, ux), gx)};
-  const float dy[3] = {__fmul_rn(__fsub_rn(-1.0f, uy), gy), __fmul_rn(-uy, gy),
-                       __fmul_rn(__fsub_rn(1.0f, uy), gy)};
-  const float dz[3] = {__fmul_rn(__fsub_rn(-1.0f, uz), gz), __fmul_rn(-uz, gz),
-                       __fmul_rn(__fsub_rn(1.0f, uz), gz)};
-  float t[19];
+  const V dx[3] = {vmul(vsub(-1.0f, ux), gx), vmul(vneg(ux), gx), vmul(vsub(1.0f, ux), gx)};
+  const V dy[3] = {vmul(vsub(-1.0f, uy), gy), vmul(vneg(uy), gy), vmul(vsub(1.0f, uy), gy)};
+  const V dz[3] = {vmul(vsub(-1.0f, uz), gz), vmul(vneg(uz), gz), vmul(vsub(1.0f, uz), gz)};
+  V t[19];
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
-    float a = __fadd_rn(__fadd_rn(dx[ex(q) + 1], dy[ey(q) + 1]), dz[ez(q) + 1]);
-    float b = q == 0 ? 0.0f : __fmul_rn(edot(q, ux, uy, uz), edot(q, gx, gy, gz));
-    t[q] = __fmul_rn(weight_of(q), q == 0 ? a : __fadd_rn(a, b));
+    const V a = vadd(vadd(dx[ex(q) + 1], dy[ey(q) + 1]), dz[ez(q) + 1]);
+    if (q == 0) {
+      t[q] = vmul(weight_of(q), a);
+    } else {
+      const V b = vmul(edot(q, ux, uy, uz), edot(q, gx, gy, gz));
+      t[q] = vmul(weight_of(q), vadd(a, b));
+    }
   }
-  float g[19], m[19];
+  V g[19], m[19];
   mrt_forward(t, g);
   mrt_forward(F, m);
   // Relaxation towards meq (lbm3d.py:285-326). S_0 = S_3 = S_5 = S_7 = 0: those
   // moments only receive the forcing term.
-  const float uu = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
-  float meq[19];
+  const V uxx = vmul(ux, ux), uyy = vmul(uy, uy), uzz = vmul(uz, uz);
+  V meq[19];
 #pragma unroll
-  for (int k = 0; k < 19; ++k) meq[k] = 0.0f;
-  meq[1] = uu;
-  meq[9] = __fsub_rn(__fsub_rn(__fmul_rn(__fmul_rn(2.0f, ux), ux), __fmul_rn(uy, uy)),
-                     __fmul_rn(uz, uz));
-  meq[11] = __fsub_rn(__fmul_rn(uy, uy), __fmul_rn(uz, uz));
-  meq[13] = __fmul_rn(ux, uy);
-  meq[14] = __fmul_rn(uy, uz);
-  meq[15] = __fmul_rn(ux, uz);
-  (void)rho;
+  for (int k = 0; k < 19; ++k) meq[k] = splat<V>(0.0f);
+  meq[1] = vadd(vadd(uxx, uyy), uzz);
+  meq[9] = vsub(vsub(vmul(vmul(2.0f, ux), ux), uyy), uzz);
+  meq[11] = vsub(uyy, uzz);
+  meq[13] = vmul(ux, uy);
+  meq[14] = vmul(uy, uz);
+  meq[15] = vmul(ux, uz);
 #pragma unroll
   for (int k = 0; k < 19; ++k) {
     if (k == 0 || k == 3 || k == 5 || k == 7) {
-      m[k] = __fadd_rn(m[k], g[k]);
+      m[k] = vadd(m[k], g[k]);
     } else {
       const bool has_eq = (k == 1 || k == 9 || k == 11 || k == 13 || k == 14 || k == 15);
-      float d = has_eq ? __fsub_rn(m[k], meq[k]) : m[k];
-      m[k] = __fsub_rn(m[k], __fmul_rn(S[k], d));
-      m[k] = __fadd_rn(m[k], __fmul_rn(__fsub_rn(1.0f, __fmul_rn(0.5f, S[k])), g[k]));
+      const V d = has_eq ? vsub(m[k], meq[k]) : m[k];
+      m[k] = vsub(m[k], vmul(S[k], d));
+      m[k] = vadd(m[k], vmul(__fsub_rn(1.0f, __fmul_rn(0.5f, S[k])), g[k]));
     }
   }
   mrt_inverse(m, out);
@@ -258,64 +290,157 @@ struct StepArgs {
   int write_faces;
 };
 
+// Cells per thread of the step kernel: the exact form evaluates one cell per thread in
+// scalar float arithmetic; the fast forms evaluate the two cells (i, j, k) and (i, j + 1, k)
+// of a thread together in packed float2 arithmetic (half the floating-point instructions).
+// The exact form stays scalar because the assembler's optimisation of packed f32x2 code
+// was observed to change rounding (a single-use product merged into the following
+// subtraction), which would break bit-identity with the reference's float32 operations.
+template <bool kFast>
+struct StepLanes {
+  static constexpr int n = kFast ? 2 : 1;
+  using V = typename std::conditional<kFast, float2, float>::type;
+};
+
+// Minimum resident 128-thread blocks per SM of the step kernel (caps its registers at
+// 65536 / (128 * n)): scalar exact form by parity, then the packed forms.
+#ifndef FSI_LBM_MIN_BLOCKS_EXACT_EVEN
+#define FSI_LBM_MIN_BLOCKS_EXACT_EVEN 6
+#endif
+#ifndef FSI_LBM_MIN_BLOCKS_EXACT_ODD
+#define FSI_LBM_MIN_BLOCKS_EXACT_ODD 8
+#endif
+#ifndef FSI_LBM_MIN_BLOCKS_FAST
+#define FSI_LBM_MIN_BLOCKS_FAST 6
+#endif
+constexpr int kStepBlock = 128;
+
+template <bool kFast, bool kOdd>
+constexpr int step_min_blocks() {
+  return kFast ? FSI_LBM_MIN_BLOCKS_FAST
+               : (kOdd ? FSI_LBM_MIN_BLOCKS_EXACT_ODD : FSI_LBM_MIN_BLOCKS_EXACT_EVEN);
+}
+
+// Launch shape of the step kernel: x = z (contiguous), y = groups of `lanes` rows, z = x planes.
+CellLaunch step_launch(const LbmGeom& g, int lanes) {
+  int bz = ((g.nz + 31) / 32) * 32;
+  if (bz > kStepBlock) bz = kStepBlock;
+  const int rows = (g.ny + lanes - 1) / lanes;
+  int by = kStepBlock / bz;
+  if (by > rows) by = rows;
+  return CellLaunch{dim3((g.nz + bz - 1) / bz, (rows + by - 1) / by, g.nx), dim3(bz, by, 1)};
+}
+
+// Storage index that the odd step reads F_q(x) from, and that it writes f*_q(x) to.
+__device__ __forceinline__ uint32_t odd_src(const Deltas& d, uint32_t fl, int q, uint32_t n) {
+  return ((fl >> opp(q)) & 1u) ? q * n + d.c : opp(q) * n + d.nb(q, -1);
+}
+__device__ __forceinline__ uint32_t odd_dst(const Deltas& d, uint32_t fl, int q, uint32_t n) {
+  return ((fl >> q) & 1u) ? opp(q) * n + d.c : q * n + d.nb(q, +1);
+}
+
 template <int kStore, bool kFast, bool kOdd, bool kRecompute>
-__global__ void __launch_bounds__(kBlock) lbm_step_kernel(StepArgs a) {
+__global__ void __launch_bounds__(kStepBlock, (step_min_blocks<kFast, kOdd>()))
+    lbm_step_kernel(StepArgs a) {
   using St = Store<kStore>;
+  constexpr int L = StepLanes<kFast>::n;
+  using V = typename StepLanes<kFast>::V;
+  using Ln = Lanes<V>;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int j = L * (blockIdx.y * blockDim.y + threadIdx.y);
   const int i = blockIdx.z;
   if (k >= a.g.nz || j >= a.g.ny) return;
-  const Deltas d(a.g, i, j, k);
-  const uint32_t c = d.c;
-  const uint32_t fl = a.flags[c];
-  if (fl & kFlagSolid) return;
+  Deltas d[L];
+  uint32_t fl[L];
+  bool live[L];
+  bool any = false;
+#pragma unroll
+  for (int l = 0; l < L; ++l) {
+    const bool has = j + l < a.g.ny;
+    d[l] = Deltas(a.g, i, has ? j + l : j, k);
+    fl[l] = has ? a.flags[d[l].c] : kFlagSolid;
+    live[l] = !(fl[l] & kFlagSolid);
+    any = any || live[l];
+  }
+  if (!any) return;
+  // A solid (or missing) lane reads the cells of a live lane and is never stored.
+  const int src = live[0] ? 0 : L - 1;
   const uint32_t n = (uint32_t)a.g.n;
   typename St::T* __restrict__ pops = reinterpret_cast<typename St::T*>(a.pops);
 
-  float F[19];
-  if (!kOdd) {
+  V F[19];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) F[q] = St::ld(pops, q * n + c, a.shift[q]);
-  } else {
-    F[0] = St::ld(pops, c, a.shift[0]);
+  for (int q = 0; q < 19; ++q) {
+    uint32_t sl[L];
 #pragma unroll
-    for (int q = 1; q < 19; ++q) {
+    for (int l = 0; l < L; ++l) {
+      const int ll = live[l] ? l : src;
       // F_q(x) = f*_q(x - e_q) in slot opp(q) there, or f*_opp(q)(x) in slot q here when
       // x - e_q is solid (half-way bounce-back).
-      const bool bounce = (fl >> opp(q)) & 1u;
-      const uint32_t idx = bounce ? q * n + c : opp(q) * n + d.nb(q, -1);
-      F[q] = St::ld(pops, idx, a.shift[q]);
+      sl[l] = (!kOdd || q == 0) ? q * n + d[ll].c : odd_src(d[ll], fl[ll], q, n);
+    }
+    if constexpr (L == 2) {
+      F[q] = St::ld2(pops, sl[0], sl[1], a.shift[q]);
+    } else {
+      F[q] = St::ld(pops, sl[0], a.shift[q]);
     }
   }
 
-  const float gx = a.force[c], gy = a.force[n + c], gz = a.force[2 * n + c];
-  float rho, ux, uy, uz;
+  uint32_t c[L];
+#pragma unroll
+  for (int l = 0; l < L; ++l) c[l] = d[live[l] ? l : src].c;
+  V gx, gy, gz, rho, ux, uy, uz;
+#pragma unroll
+  for (int l = 0; l < L; ++l) {
+    Ln::set(gx, l, a.force[c[l]]);
+    Ln::set(gy, l, a.force[n + c[l]]);
+    Ln::set(gz, l, a.force[2 * n + c[l]]);
+  }
   if (kRecompute) {
-    macro_any<kFast>(F, a.force_prev[c], a.force_prev[n + c], a.force_prev[2 * n + c], rho, ux,
-                     uy, uz);
-    if (a.write_faces && (fl & (kFlagFaceLeft | kFlagFaceRight)))
-      a.macro[c] = make_float4(ux, uy, uz, rho);
+    V px, py, pz;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+      Ln::set(px, l, a.force_prev[c[l]]);
+      Ln::set(py, l, a.force_prev[n + c[l]]);
+      Ln::set(pz, l, a.force_prev[2 * n + c[l]]);
+    }
+    macro_any<kFast>(F, px, py, pz, rho, ux, uy, uz);
+    if (a.write_faces) {
+#pragma unroll
+      for (int l = 0; l < L; ++l)
+        if (live[l] && (fl[l] & (kFlagFaceLeft | kFlagFaceRight)))
+          a.macro[d[l].c] = make_float4(Ln::get(ux, l), Ln::get(uy, l), Ln::get(uz, l),
+                                        Ln::get(rho, l));
+    }
   } else {
-    const float4 mc = a.macro[c];
-    ux = mc.x; uy = mc.y; uz = mc.z; rho = mc.w;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+      const float4 m = a.macro[c[l]];
+      Ln::set(ux, l, m.x); Ln::set(uy, l, m.y); Ln::set(uz, l, m.z); Ln::set(rho, l, m.w);
+    }
   }
 
-  float out[19];
+  V out[19];
   if (kFast) mrt_collide_fast(F, rho, ux, uy, uz, gx, gy, gz, a.s, out);
-  else collide_cell(F, rho, ux, uy, uz, gx, gy, gz, a.s, out);
+  else collide_cell(F, ux, uy, uz, gx, gy, gz, a.s, out);
 
-  if (!kOdd) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) St::st(pops, opp(q) * n + c, out[q], a.shift[opp(q)]);
-  } else {
-    St::st(pops, c, out[0], a.shift[0]);
+  for (int q = 0; q < 19; ++q) {
+    // f*_q goes to slot opp(q) of this cell (even step, or odd-step bounce-back) or to slot q
+    // of x + e_q (odd step). w_q = w_opp(q), so either slot's storage shift is shift[q].
+    uint32_t t[L];
 #pragma unroll
-    for (int q = 1; q < 19; ++q) {
-      const bool bounce = (fl >> q) & 1u;
-      // The slot receiving f*_q holds direction q (neighbour) or opp(q) (bounce-back).
-      if (bounce) St::st(pops, opp(q) * n + c, out[q], a.shift[opp(q)]);
-      else St::st(pops, q * n + d.nb(q, +1), out[q], a.shift[q]);
+    for (int l = 0; l < L; ++l)
+      t[l] = (!kOdd || q == 0) ? opp(q) * n + d[l].c : odd_dst(d[l], fl[l], q, n);
+    if constexpr (L == 2) {
+      if (live[0] && live[1]) {
+        St::st2(pops, t[0], t[1], out[q], a.shift[q]);
+        continue;
+      }
     }
+#pragma unroll
+    for (int l = 0; l < L; ++l)
+      if (live[l]) St::st(pops, t[l], Ln::get(out[q], l), a.shift[q]);
   }
 }
 
@@ -715,7 +840,8 @@ extern "C" int fsi_lbm_step(const fsi_lbm_desc* d, void* pops, float* macro, con
   a.write_faces = (d->bc_mode_left != 0 || d->bc_mode_right != 0) ? 1 : 0;
   cudaStream_t s = as_stream(stream);
   const bool odd = (steps_done & 1) != 0;
-  dispatch_forms<StepLauncher>(d, a, odd, force_prev != nullptr, cell_launch(a.g), s);
+  const int lanes = d->arithmetic == FSI_ARITH_FAST ? 2 : 1;
+  dispatch_forms<StepLauncher>(d, a, odd, force_prev != nullptr, step_launch(a.g, lanes), s);
   if (int e = check_launch("lbm_step_kernel")) return e;
   if (a.write_faces) {
     FaceArgs f;

@@ -3,86 +3,90 @@
 // register formulas with the reference's float32 operation order.
 #pragma once
 
+#include "lbm_vec.cuh"
+
 namespace fsi {
 
 // m[k] = sum_q M[k][q] * X[q], sequential in q (lbm3d.py:269-274).
-__device__ __forceinline__ void mrt_forward(const float (&X)[19], float (&m)[19]) {
-  float two[19];
-  two[1] = __fadd_rn(X[1], X[1]);
-  two[2] = __fadd_rn(X[2], X[2]);
-  two[3] = __fadd_rn(X[3], X[3]);
-  two[4] = __fadd_rn(X[4], X[4]);
-  two[5] = __fadd_rn(X[5], X[5]);
-  two[6] = __fadd_rn(X[6], X[6]);
-  two[15] = __fadd_rn(X[15], X[15]);
-  two[16] = __fadd_rn(X[16], X[16]);
-  two[17] = __fadd_rn(X[17], X[17]);
-  two[18] = __fadd_rn(X[18], X[18]);
-  m[0] = X[0]; m[0] = __fadd_rn(m[0], X[1]); m[0] = __fadd_rn(m[0], X[2]); m[0] = __fadd_rn(m[0], X[3]); m[0] = __fadd_rn(m[0], X[4]); m[0] = __fadd_rn(m[0], X[5]); m[0] = __fadd_rn(m[0], X[6]); m[0] = __fadd_rn(m[0], X[7]); m[0] = __fadd_rn(m[0], X[8]); m[0] = __fadd_rn(m[0], X[9]); m[0] = __fadd_rn(m[0], X[10]); m[0] = __fadd_rn(m[0], X[11]); m[0] = __fadd_rn(m[0], X[12]); m[0] = __fadd_rn(m[0], X[13]); m[0] = __fadd_rn(m[0], X[14]); m[0] = __fadd_rn(m[0], X[15]); m[0] = __fadd_rn(m[0], X[16]); m[0] = __fadd_rn(m[0], X[17]); m[0] = __fadd_rn(m[0], X[18]);
-  m[1] = -X[0]; m[1] = __fadd_rn(m[1], X[7]); m[1] = __fadd_rn(m[1], X[8]); m[1] = __fadd_rn(m[1], X[9]); m[1] = __fadd_rn(m[1], X[10]); m[1] = __fadd_rn(m[1], X[11]); m[1] = __fadd_rn(m[1], X[12]); m[1] = __fadd_rn(m[1], X[13]); m[1] = __fadd_rn(m[1], X[14]); m[1] = __fadd_rn(m[1], X[15]); m[1] = __fadd_rn(m[1], X[16]); m[1] = __fadd_rn(m[1], X[17]); m[1] = __fadd_rn(m[1], X[18]);
-  m[2] = X[0]; m[2] = __fsub_rn(m[2], two[1]); m[2] = __fsub_rn(m[2], two[2]); m[2] = __fsub_rn(m[2], two[3]); m[2] = __fsub_rn(m[2], two[4]); m[2] = __fsub_rn(m[2], two[5]); m[2] = __fsub_rn(m[2], two[6]); m[2] = __fadd_rn(m[2], X[7]); m[2] = __fadd_rn(m[2], X[8]); m[2] = __fadd_rn(m[2], X[9]); m[2] = __fadd_rn(m[2], X[10]); m[2] = __fadd_rn(m[2], X[11]); m[2] = __fadd_rn(m[2], X[12]); m[2] = __fadd_rn(m[2], X[13]); m[2] = __fadd_rn(m[2], X[14]); m[2] = __fadd_rn(m[2], X[15]); m[2] = __fadd_rn(m[2], X[16]); m[2] = __fadd_rn(m[2], X[17]); m[2] = __fadd_rn(m[2], X[18]);
-  m[3] = X[1]; m[3] = __fsub_rn(m[3], X[2]); m[3] = __fadd_rn(m[3], X[7]); m[3] = __fsub_rn(m[3], X[8]); m[3] = __fadd_rn(m[3], X[9]); m[3] = __fsub_rn(m[3], X[10]); m[3] = __fadd_rn(m[3], X[11]); m[3] = __fsub_rn(m[3], X[12]); m[3] = __fadd_rn(m[3], X[13]); m[3] = __fsub_rn(m[3], X[14]);
-  m[4] = -two[1]; m[4] = __fadd_rn(m[4], two[2]); m[4] = __fadd_rn(m[4], X[7]); m[4] = __fsub_rn(m[4], X[8]); m[4] = __fadd_rn(m[4], X[9]); m[4] = __fsub_rn(m[4], X[10]); m[4] = __fadd_rn(m[4], X[11]); m[4] = __fsub_rn(m[4], X[12]); m[4] = __fadd_rn(m[4], X[13]); m[4] = __fsub_rn(m[4], X[14]);
-  m[5] = X[3]; m[5] = __fsub_rn(m[5], X[4]); m[5] = __fadd_rn(m[5], X[7]); m[5] = __fsub_rn(m[5], X[8]); m[5] = __fsub_rn(m[5], X[9]); m[5] = __fadd_rn(m[5], X[10]); m[5] = __fadd_rn(m[5], X[15]); m[5] = __fsub_rn(m[5], X[16]); m[5] = __fadd_rn(m[5], X[17]); m[5] = __fsub_rn(m[5], X[18]);
-  m[6] = -two[3]; m[6] = __fadd_rn(m[6], two[4]); m[6] = __fadd_rn(m[6], X[7]); m[6] = __fsub_rn(m[6], X[8]); m[6] = __fsub_rn(m[6], X[9]); m[6] = __fadd_rn(m[6], X[10]); m[6] = __fadd_rn(m[6], X[15]); m[6] = __fsub_rn(m[6], X[16]); m[6] = __fadd_rn(m[6], X[17]); m[6] = __fsub_rn(m[6], X[18]);
-  m[7] = X[5]; m[7] = __fsub_rn(m[7], X[6]); m[7] = __fadd_rn(m[7], X[11]); m[7] = __fsub_rn(m[7], X[12]); m[7] = __fsub_rn(m[7], X[13]); m[7] = __fadd_rn(m[7], X[14]); m[7] = __fadd_rn(m[7], X[15]); m[7] = __fsub_rn(m[7], X[16]); m[7] = __fsub_rn(m[7], X[17]); m[7] = __fadd_rn(m[7], X[18]);
-  m[8] = -two[5]; m[8] = __fadd_rn(m[8], two[6]); m[8] = __fadd_rn(m[8], X[11]); m[8] = __fsub_rn(m[8], X[12]); m[8] = __fsub_rn(m[8], X[13]); m[8] = __fadd_rn(m[8], X[14]); m[8] = __fadd_rn(m[8], X[15]); m[8] = __fsub_rn(m[8], X[16]); m[8] = __fsub_rn(m[8], X[17]); m[8] = __fadd_rn(m[8], X[18]);
-  m[9] = two[1]; m[9] = __fadd_rn(m[9], two[2]); m[9] = __fsub_rn(m[9], X[3]); m[9] = __fsub_rn(m[9], X[4]); m[9] = __fsub_rn(m[9], X[5]); m[9] = __fsub_rn(m[9], X[6]); m[9] = __fadd_rn(m[9], X[7]); m[9] = __fadd_rn(m[9], X[8]); m[9] = __fadd_rn(m[9], X[9]); m[9] = __fadd_rn(m[9], X[10]); m[9] = __fadd_rn(m[9], X[11]); m[9] = __fadd_rn(m[9], X[12]); m[9] = __fadd_rn(m[9], X[13]); m[9] = __fadd_rn(m[9], X[14]); m[9] = __fsub_rn(m[9], two[15]); m[9] = __fsub_rn(m[9], two[16]); m[9] = __fsub_rn(m[9], two[17]); m[9] = __fsub_rn(m[9], two[18]);
-  m[10] = -two[1]; m[10] = __fsub_rn(m[10], two[2]); m[10] = __fadd_rn(m[10], X[3]); m[10] = __fadd_rn(m[10], X[4]); m[10] = __fadd_rn(m[10], X[5]); m[10] = __fadd_rn(m[10], X[6]); m[10] = __fadd_rn(m[10], X[7]); m[10] = __fadd_rn(m[10], X[8]); m[10] = __fadd_rn(m[10], X[9]); m[10] = __fadd_rn(m[10], X[10]); m[10] = __fadd_rn(m[10], X[11]); m[10] = __fadd_rn(m[10], X[12]); m[10] = __fadd_rn(m[10], X[13]); m[10] = __fadd_rn(m[10], X[14]); m[10] = __fsub_rn(m[10], two[15]); m[10] = __fsub_rn(m[10], two[16]); m[10] = __fsub_rn(m[10], two[17]); m[10] = __fsub_rn(m[10], two[18]);
-  m[11] = X[3]; m[11] = __fadd_rn(m[11], X[4]); m[11] = __fsub_rn(m[11], X[5]); m[11] = __fsub_rn(m[11], X[6]); m[11] = __fadd_rn(m[11], X[7]); m[11] = __fadd_rn(m[11], X[8]); m[11] = __fadd_rn(m[11], X[9]); m[11] = __fadd_rn(m[11], X[10]); m[11] = __fsub_rn(m[11], X[11]); m[11] = __fsub_rn(m[11], X[12]); m[11] = __fsub_rn(m[11], X[13]); m[11] = __fsub_rn(m[11], X[14]);
-  m[12] = -X[3]; m[12] = __fsub_rn(m[12], X[4]); m[12] = __fadd_rn(m[12], X[5]); m[12] = __fadd_rn(m[12], X[6]); m[12] = __fadd_rn(m[12], X[7]); m[12] = __fadd_rn(m[12], X[8]); m[12] = __fadd_rn(m[12], X[9]); m[12] = __fadd_rn(m[12], X[10]); m[12] = __fsub_rn(m[12], X[11]); m[12] = __fsub_rn(m[12], X[12]); m[12] = __fsub_rn(m[12], X[13]); m[12] = __fsub_rn(m[12], X[14]);
-  m[13] = X[7]; m[13] = __fadd_rn(m[13], X[8]); m[13] = __fsub_rn(m[13], X[9]); m[13] = __fsub_rn(m[13], X[10]);
-  m[14] = X[15]; m[14] = __fadd_rn(m[14], X[16]); m[14] = __fsub_rn(m[14], X[17]); m[14] = __fsub_rn(m[14], X[18]);
-  m[15] = X[11]; m[15] = __fadd_rn(m[15], X[12]); m[15] = __fsub_rn(m[15], X[13]); m[15] = __fsub_rn(m[15], X[14]);
-  m[16] = X[7]; m[16] = __fsub_rn(m[16], X[8]); m[16] = __fadd_rn(m[16], X[9]); m[16] = __fsub_rn(m[16], X[10]); m[16] = __fsub_rn(m[16], X[11]); m[16] = __fadd_rn(m[16], X[12]); m[16] = __fsub_rn(m[16], X[13]); m[16] = __fadd_rn(m[16], X[14]);
-  m[17] = -X[7]; m[17] = __fadd_rn(m[17], X[8]); m[17] = __fadd_rn(m[17], X[9]); m[17] = __fsub_rn(m[17], X[10]); m[17] = __fadd_rn(m[17], X[15]); m[17] = __fsub_rn(m[17], X[16]); m[17] = __fadd_rn(m[17], X[17]); m[17] = __fsub_rn(m[17], X[18]);
-  m[18] = X[11]; m[18] = __fsub_rn(m[18], X[12]); m[18] = __fsub_rn(m[18], X[13]); m[18] = __fadd_rn(m[18], X[14]); m[18] = __fsub_rn(m[18], X[15]); m[18] = __fadd_rn(m[18], X[16]); m[18] = __fadd_rn(m[18], X[17]); m[18] = __fsub_rn(m[18], X[18]);
+template <class V>
+__device__ __forceinline__ void mrt_forward(const V (&X)[19], V (&m)[19]) {
+  V two[19];
+  two[1] = vadd(X[1], X[1]);
+  two[2] = vadd(X[2], X[2]);
+  two[3] = vadd(X[3], X[3]);
+  two[4] = vadd(X[4], X[4]);
+  two[5] = vadd(X[5], X[5]);
+  two[6] = vadd(X[6], X[6]);
+  two[15] = vadd(X[15], X[15]);
+  two[16] = vadd(X[16], X[16]);
+  two[17] = vadd(X[17], X[17]);
+  two[18] = vadd(X[18], X[18]);
+  m[0] = X[0]; m[0] = vadd(m[0], X[1]); m[0] = vadd(m[0], X[2]); m[0] = vadd(m[0], X[3]); m[0] = vadd(m[0], X[4]); m[0] = vadd(m[0], X[5]); m[0] = vadd(m[0], X[6]); m[0] = vadd(m[0], X[7]); m[0] = vadd(m[0], X[8]); m[0] = vadd(m[0], X[9]); m[0] = vadd(m[0], X[10]); m[0] = vadd(m[0], X[11]); m[0] = vadd(m[0], X[12]); m[0] = vadd(m[0], X[13]); m[0] = vadd(m[0], X[14]); m[0] = vadd(m[0], X[15]); m[0] = vadd(m[0], X[16]); m[0] = vadd(m[0], X[17]); m[0] = vadd(m[0], X[18]);
+  m[1] = vneg(X[0]); m[1] = vadd(m[1], X[7]); m[1] = vadd(m[1], X[8]); m[1] = vadd(m[1], X[9]); m[1] = vadd(m[1], X[10]); m[1] = vadd(m[1], X[11]); m[1] = vadd(m[1], X[12]); m[1] = vadd(m[1], X[13]); m[1] = vadd(m[1], X[14]); m[1] = vadd(m[1], X[15]); m[1] = vadd(m[1], X[16]); m[1] = vadd(m[1], X[17]); m[1] = vadd(m[1], X[18]);
+  m[2] = X[0]; m[2] = vsub(m[2], two[1]); m[2] = vsub(m[2], two[2]); m[2] = vsub(m[2], two[3]); m[2] = vsub(m[2], two[4]); m[2] = vsub(m[2], two[5]); m[2] = vsub(m[2], two[6]); m[2] = vadd(m[2], X[7]); m[2] = vadd(m[2], X[8]); m[2] = vadd(m[2], X[9]); m[2] = vadd(m[2], X[10]); m[2] = vadd(m[2], X[11]); m[2] = vadd(m[2], X[12]); m[2] = vadd(m[2], X[13]); m[2] = vadd(m[2], X[14]); m[2] = vadd(m[2], X[15]); m[2] = vadd(m[2], X[16]); m[2] = vadd(m[2], X[17]); m[2] = vadd(m[2], X[18]);
+  m[3] = X[1]; m[3] = vsub(m[3], X[2]); m[3] = vadd(m[3], X[7]); m[3] = vsub(m[3], X[8]); m[3] = vadd(m[3], X[9]); m[3] = vsub(m[3], X[10]); m[3] = vadd(m[3], X[11]); m[3] = vsub(m[3], X[12]); m[3] = vadd(m[3], X[13]); m[3] = vsub(m[3], X[14]);
+  m[4] = vneg(two[1]); m[4] = vadd(m[4], two[2]); m[4] = vadd(m[4], X[7]); m[4] = vsub(m[4], X[8]); m[4] = vadd(m[4], X[9]); m[4] = vsub(m[4], X[10]); m[4] = vadd(m[4], X[11]); m[4] = vsub(m[4], X[12]); m[4] = vadd(m[4], X[13]); m[4] = vsub(m[4], X[14]);
+  m[5] = X[3]; m[5] = vsub(m[5], X[4]); m[5] = vadd(m[5], X[7]); m[5] = vsub(m[5], X[8]); m[5] = vsub(m[5], X[9]); m[5] = vadd(m[5], X[10]); m[5] = vadd(m[5], X[15]); m[5] = vsub(m[5], X[16]); m[5] = vadd(m[5], X[17]); m[5] = vsub(m[5], X[18]);
+  m[6] = vneg(two[3]); m[6] = vadd(m[6], two[4]); m[6] = vadd(m[6], X[7]); m[6] = vsub(m[6], X[8]); m[6] = vsub(m[6], X[9]); m[6] = vadd(m[6], X[10]); m[6] = vadd(m[6], X[15]); m[6] = vsub(m[6], X[16]); m[6] = vadd(m[6], X[17]); m[6] = vsub(m[6], X[18]);
+  m[7] = X[5]; m[7] = vsub(m[7], X[6]); m[7] = vadd(m[7], X[11]); m[7] = vsub(m[7], X[12]); m[7] = vsub(m[7], X[13]); m[7] = vadd(m[7], X[14]); m[7] = vadd(m[7], X[15]); m[7] = vsub(m[7], X[16]); m[7] = vsub(m[7], X[17]); m[7] = vadd(m[7], X[18]);
+  m[8] = vneg(two[5]); m[8] = vadd(m[8], two[6]); m[8] = vadd(m[8], X[11]); m[8] = vsub(m[8], X[12]); m[8] = vsub(m[8], X[13]); m[8] = vadd(m[8], X[14]); m[8] = vadd(m[8], X[15]); m[8] = vsub(m[8], X[16]); m[8] = vsub(m[8], X[17]); m[8] = vadd(m[8], X[18]);
+  m[9] = two[1]; m[9] = vadd(m[9], two[2]); m[9] = vsub(m[9], X[3]); m[9] = vsub(m[9], X[4]); m[9] = vsub(m[9], X[5]); m[9] = vsub(m[9], X[6]); m[9] = vadd(m[9], X[7]); m[9] = vadd(m[9], X[8]); m[9] = vadd(m[9], X[9]); m[9] = vadd(m[9], X[10]); m[9] = vadd(m[9], X[11]); m[9] = vadd(m[9], X[12]); m[9] = vadd(m[9], X[13]); m[9] = vadd(m[9], X[14]); m[9] = vsub(m[9], two[15]); m[9] = vsub(m[9], two[16]); m[9] = vsub(m[9], two[17]); m[9] = vsub(m[9], two[18]);
+  m[10] = vneg(two[1]); m[10] = vsub(m[10], two[2]); m[10] = vadd(m[10], X[3]); m[10] = vadd(m[10], X[4]); m[10] = vadd(m[10], X[5]); m[10] = vadd(m[10], X[6]); m[10] = vadd(m[10], X[7]); m[10] = vadd(m[10], X[8]); m[10] = vadd(m[10], X[9]); m[10] = vadd(m[10], X[10]); m[10] = vadd(m[10], X[11]); m[10] = vadd(m[10], X[12]); m[10] = vadd(m[10], X[13]); m[10] = vadd(m[10], X[14]); m[10] = vsub(m[10], two[15]); m[10] = vsub(m[10], two[16]); m[10] = vsub(m[10], two[17]); m[10] = vsub(m[10], two[18]);
+  m[11] = X[3]; m[11] = vadd(m[11], X[4]); m[11] = vsub(m[11], X[5]); m[11] = vsub(m[11], X[6]); m[11] = vadd(m[11], X[7]); m[11] = vadd(m[11], X[8]); m[11] = vadd(m[11], X[9]); m[11] = vadd(m[11], X[10]); m[11] = vsub(m[11], X[11]); m[11] = vsub(m[11], X[12]); m[11] = vsub(m[11], X[13]); m[11] = vsub(m[11], X[14]);
+  m[12] = vneg(X[3]); m[12] = vsub(m[12], X[4]); m[12] = vadd(m[12], X[5]); m[12] = vadd(m[12], X[6]); m[12] = vadd(m[12], X[7]); m[12] = vadd(m[12], X[8]); m[12] = vadd(m[12], X[9]); m[12] = vadd(m[12], X[10]); m[12] = vsub(m[12], X[11]); m[12] = vsub(m[12], X[12]); m[12] = vsub(m[12], X[13]); m[12] = vsub(m[12], X[14]);
+  m[13] = X[7]; m[13] = vadd(m[13], X[8]); m[13] = vsub(m[13], X[9]); m[13] = vsub(m[13], X[10]);
+  m[14] = X[15]; m[14] = vadd(m[14], X[16]); m[14] = vsub(m[14], X[17]); m[14] = vsub(m[14], X[18]);
+  m[15] = X[11]; m[15] = vadd(m[15], X[12]); m[15] = vsub(m[15], X[13]); m[15] = vsub(m[15], X[14]);
+  m[16] = X[7]; m[16] = vsub(m[16], X[8]); m[16] = vadd(m[16], X[9]); m[16] = vsub(m[16], X[10]); m[16] = vsub(m[16], X[11]); m[16] = vadd(m[16], X[12]); m[16] = vsub(m[16], X[13]); m[16] = vadd(m[16], X[14]);
+  m[17] = vneg(X[7]); m[17] = vadd(m[17], X[8]); m[17] = vadd(m[17], X[9]); m[17] = vsub(m[17], X[10]); m[17] = vadd(m[17], X[15]); m[17] = vsub(m[17], X[16]); m[17] = vadd(m[17], X[17]); m[17] = vsub(m[17], X[18]);
+  m[18] = X[11]; m[18] = vsub(m[18], X[12]); m[18] = vsub(m[18], X[13]); m[18] = vadd(m[18], X[14]); m[18] = vsub(m[18], X[15]); m[18] = vadd(m[18], X[16]); m[18] = vadd(m[18], X[17]); m[18] = vsub(m[18], X[18]);
 }
 
 // f[q] = sum_k inv(M)[q][k] * m[k], sequential in k (lbm3d.py:328-333).
 // 22 rounded products; every other product is an exact power-of-two scaling.
-__device__ __forceinline__ void mrt_inverse(const float (&m)[19], float (&f)[19]) {
-  const float p0_0 = __fmul_rn(0x1.5555560000000p-2f, m[0]);
-  const float p0_1 = __fmul_rn(0x1.c71c720000000p-5f, m[0]);
-  const float p1_0 = __fmul_rn(0x1.0000000000000p-1f, m[1]);
-  const float p1_1 = __fmul_rn(0x1.5555560000000p-5f, m[1]);
-  const float p2_0 = __fmul_rn(0x1.5555560000000p-3f, m[2]);
-  const float p2_1 = __fmul_rn(0x1.c71c720000000p-5f, m[2]);
-  const float p3_0 = __fmul_rn(0x1.5555560000000p-3f, m[3]);
-  const float p4_0 = __fmul_rn(0x1.5555560000000p-3f, m[4]);
-  const float p5_0 = __fmul_rn(0x1.5555560000000p-3f, m[5]);
-  const float p6_0 = __fmul_rn(0x1.5555560000000p-3f, m[6]);
-  const float p7_0 = __fmul_rn(0x1.5555560000000p-3f, m[7]);
-  const float p8_0 = __fmul_rn(0x1.5555560000000p-3f, m[8]);
-  const float p9_0 = __fmul_rn(0x1.5555560000000p-4f, m[9]);
-  const float p10_0 = __fmul_rn(0x1.5555560000000p-4f, m[10]);
-  const float p11_0 = __fmul_rn(0x1.0000000000000p-3f, m[11]);
-  const float p12_0 = __fmul_rn(0x1.0000000000000p-3f, m[12]);
-  const float p13_0 = __fmul_rn(0x1.0000000000000p-2f, m[13]);
-  const float p14_0 = __fmul_rn(0x1.0000000000000p-2f, m[14]);
-  const float p15_0 = __fmul_rn(0x1.0000000000000p-2f, m[15]);
-  const float p16_0 = __fmul_rn(0x1.0000000000000p-3f, m[16]);
-  const float p17_0 = __fmul_rn(0x1.0000000000000p-3f, m[17]);
-  const float p18_0 = __fmul_rn(0x1.0000000000000p-3f, m[18]);
-  { float a; a = p0_0; a = __fsub_rn(a, p1_0); a = __fadd_rn(a, p2_0); f[0] = a; }
-  { float a; a = p0_1; a = __fsub_rn(a, p2_1); a = __fadd_rn(a, p3_0); a = __fsub_rn(a, p4_0); a = __fadd_rn(a, p9_0); a = __fsub_rn(a, p10_0); f[1] = a; }
-  { float a; a = p0_1; a = __fsub_rn(a, p2_1); a = __fsub_rn(a, p3_0); a = __fadd_rn(a, p4_0); a = __fadd_rn(a, p9_0); a = __fsub_rn(a, p10_0); f[2] = a; }
-  { float a; a = p0_1; a = __fsub_rn(a, p2_1); a = __fadd_rn(a, p5_0); a = __fsub_rn(a, p6_0); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p11_0); a = __fsub_rn(a, p12_0); f[3] = a; }
-  { float a; a = p0_1; a = __fsub_rn(a, p2_1); a = __fsub_rn(a, p5_0); a = __fadd_rn(a, p6_0); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p11_0); a = __fsub_rn(a, p12_0); f[4] = a; }
-  { float a; a = p0_1; a = __fsub_rn(a, p2_1); a = __fadd_rn(a, p7_0); a = __fsub_rn(a, p8_0); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p11_0); a = __fadd_rn(a, p12_0); f[5] = a; }
-  { float a; a = p0_1; a = __fsub_rn(a, p2_1); a = __fsub_rn(a, p7_0); a = __fadd_rn(a, p8_0); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p11_0); a = __fadd_rn(a, p12_0); f[6] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p13_0); a = __fadd_rn(a, p16_0); a = __fsub_rn(a, p17_0); f[7] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p13_0); a = __fsub_rn(a, p16_0); a = __fadd_rn(a, p17_0); f[8] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p13_0); a = __fadd_rn(a, p16_0); a = __fadd_rn(a, p17_0); f[9] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p13_0); a = __fsub_rn(a, p16_0); a = __fsub_rn(a, p17_0); f[10] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p15_0); a = __fsub_rn(a, p16_0); a = __fadd_rn(a, p18_0); f[11] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p15_0); a = __fadd_rn(a, p16_0); a = __fsub_rn(a, p18_0); f[12] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p15_0); a = __fsub_rn(a, p16_0); a = __fsub_rn(a, p18_0); f[13] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p3_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p4_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p11_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p12_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p15_0); a = __fadd_rn(a, p16_0); a = __fadd_rn(a, p18_0); f[14] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p14_0); a = __fadd_rn(a, p17_0); a = __fsub_rn(a, p18_0); f[15] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, p14_0); a = __fsub_rn(a, p17_0); a = __fadd_rn(a, p18_0); f[16] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p14_0); a = __fadd_rn(a, p17_0); a = __fadd_rn(a, p18_0); f[17] = a; }
-  { float a; a = __fmul_rn(p0_1, 0x1.0000000000000p-1f); a = __fadd_rn(a, p1_1); a = __fadd_rn(a, __fmul_rn(p2_1, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p5_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p6_0, 0x1.0000000000000p-2f)); a = __fadd_rn(a, __fmul_rn(p7_0, 0x1.0000000000000p-1f)); a = __fadd_rn(a, __fmul_rn(p8_0, 0x1.0000000000000p-2f)); a = __fsub_rn(a, __fmul_rn(p9_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, __fmul_rn(p10_0, 0x1.0000000000000p-1f)); a = __fsub_rn(a, p14_0); a = __fsub_rn(a, p17_0); a = __fsub_rn(a, p18_0); f[18] = a; }
+template <class V>
+__device__ __forceinline__ void mrt_inverse(const V (&m)[19], V (&f)[19]) {
+  const V p0_0 = vmul(m[0], 0x1.5555560000000p-2f);
+  const V p0_1 = vmul(m[0], 0x1.c71c720000000p-5f);
+  const V p1_0 = vmul(m[1], 0x1.0000000000000p-1f);
+  const V p1_1 = vmul(m[1], 0x1.5555560000000p-5f);
+  const V p2_0 = vmul(m[2], 0x1.5555560000000p-3f);
+  const V p2_1 = vmul(m[2], 0x1.c71c720000000p-5f);
+  const V p3_0 = vmul(m[3], 0x1.5555560000000p-3f);
+  const V p4_0 = vmul(m[4], 0x1.5555560000000p-3f);
+  const V p5_0 = vmul(m[5], 0x1.5555560000000p-3f);
+  const V p6_0 = vmul(m[6], 0x1.5555560000000p-3f);
+  const V p7_0 = vmul(m[7], 0x1.5555560000000p-3f);
+  const V p8_0 = vmul(m[8], 0x1.5555560000000p-3f);
+  const V p9_0 = vmul(m[9], 0x1.5555560000000p-4f);
+  const V p10_0 = vmul(m[10], 0x1.5555560000000p-4f);
+  const V p11_0 = vmul(m[11], 0x1.0000000000000p-3f);
+  const V p12_0 = vmul(m[12], 0x1.0000000000000p-3f);
+  const V p13_0 = vmul(m[13], 0x1.0000000000000p-2f);
+  const V p14_0 = vmul(m[14], 0x1.0000000000000p-2f);
+  const V p15_0 = vmul(m[15], 0x1.0000000000000p-2f);
+  const V p16_0 = vmul(m[16], 0x1.0000000000000p-3f);
+  const V p17_0 = vmul(m[17], 0x1.0000000000000p-3f);
+  const V p18_0 = vmul(m[18], 0x1.0000000000000p-3f);
+  { V a; a = p0_0; a = vsub(a, p1_0); a = vadd(a, p2_0); f[0] = a; }
+  { V a; a = p0_1; a = vsub(a, p2_1); a = vadd(a, p3_0); a = vsub(a, p4_0); a = vadd(a, p9_0); a = vsub(a, p10_0); f[1] = a; }
+  { V a; a = p0_1; a = vsub(a, p2_1); a = vsub(a, p3_0); a = vadd(a, p4_0); a = vadd(a, p9_0); a = vsub(a, p10_0); f[2] = a; }
+  { V a; a = p0_1; a = vsub(a, p2_1); a = vadd(a, p5_0); a = vsub(a, p6_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p11_0); a = vsub(a, p12_0); f[3] = a; }
+  { V a; a = p0_1; a = vsub(a, p2_1); a = vsub(a, p5_0); a = vadd(a, p6_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p11_0); a = vsub(a, p12_0); f[4] = a; }
+  { V a; a = p0_1; a = vsub(a, p2_1); a = vadd(a, p7_0); a = vsub(a, p8_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p11_0); a = vadd(a, p12_0); f[5] = a; }
+  { V a; a = p0_1; a = vsub(a, p2_1); a = vsub(a, p7_0); a = vadd(a, p8_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p11_0); a = vadd(a, p12_0); f[6] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p13_0); a = vadd(a, p16_0); a = vsub(a, p17_0); f[7] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p13_0); a = vsub(a, p16_0); a = vadd(a, p17_0); f[8] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p13_0); a = vadd(a, p16_0); a = vadd(a, p17_0); f[9] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p13_0); a = vsub(a, p16_0); a = vsub(a, p17_0); f[10] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p15_0); a = vsub(a, p16_0); a = vadd(a, p18_0); f[11] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p15_0); a = vadd(a, p16_0); a = vsub(a, p18_0); f[12] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p15_0); a = vsub(a, p16_0); a = vsub(a, p18_0); f[13] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p15_0); a = vadd(a, p16_0); a = vadd(a, p18_0); f[14] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p14_0); a = vadd(a, p17_0); a = vsub(a, p18_0); f[15] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p14_0); a = vsub(a, p17_0); a = vadd(a, p18_0); f[16] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p14_0); a = vadd(a, p17_0); a = vadd(a, p18_0); f[17] = a; }
+  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p14_0); a = vsub(a, p17_0); a = vsub(a, p18_0); f[18] = a; }
 }
 
 
@@ -90,79 +94,79 @@ __device__ __forceinline__ void mrt_inverse(const float (&m)[19], float (&f)[19]
 // parity-split moments from pair sums/differences, closed-form forcing moments
 // g_k = A_k.G - B_k (u.G) + u^T C_k G, parity-split inverse. Used by the FP16/BF16
 // storage forms and the FP32 fast form.
-__device__ __forceinline__ void mrt_collide_fast(const float (&F)[19], float rho, float ux,
-    float uy, float uz, float gx, float gy, float gz, const float* __restrict__ S,
-    float (&out)[19]) {
-  const float P0 = F[1] + F[2], D0 = F[1] - F[2];
-  const float P1 = F[3] + F[4], D1 = F[3] - F[4];
-  const float P2 = F[5] + F[6], D2 = F[5] - F[6];
-  const float P3 = F[7] + F[8], D3 = F[7] - F[8];
-  const float P4 = F[9] + F[10], D4 = F[9] - F[10];
-  const float P5 = F[11] + F[12], D5 = F[11] - F[12];
-  const float P6 = F[13] + F[14], D6 = F[13] - F[14];
-  const float P7 = F[15] + F[16], D7 = F[15] - F[16];
-  const float P8 = F[17] + F[18], D8 = F[17] - F[18];
-  float m0 = (((((((((F[0] + P0) + P1) + P2) + P3) + P4) + P5) + P6) + P7) + P8);
-  float m1 = ((((((-F[0] + P3) + P4) + P5) + P6) + P7) + P8);
-  float m2 = ((((((fmaf(-0x1.0000000000000p+1f, P2, fmaf(-0x1.0000000000000p+1f, P1, fmaf(-0x1.0000000000000p+1f, P0, F[0]))) + P3) + P4) + P5) + P6) + P7) + P8);
-  float m9 = fmaf(-0x1.0000000000000p+1f, P8, fmaf(-0x1.0000000000000p+1f, P7, (((((((0x1.0000000000000p+1f * P0) - P1) - P2) + P3) + P4) + P5) + P6)));
-  float m10 = fmaf(-0x1.0000000000000p+1f, P8, fmaf(-0x1.0000000000000p+1f, P7, (((((((-0x1.0000000000000p+1f * P0) + P1) + P2) + P3) + P4) + P5) + P6)));
-  float m11 = (((((P1 - P2) + P3) + P4) - P5) - P6);
-  float m12 = (((((-P1 + P2) + P3) + P4) - P5) - P6);
-  float m13 = (P3 - P4);
-  float m14 = (P7 - P8);
-  float m15 = (P5 - P6);
-  float m3 = ((((D0 + D3) + D4) + D5) + D6);
-  float m4 = (((((-0x1.0000000000000p+1f * D0) + D3) + D4) + D5) + D6);
-  float m5 = ((((D1 + D3) - D4) + D7) + D8);
-  float m6 = (((((-0x1.0000000000000p+1f * D1) + D3) - D4) + D7) + D8);
-  float m7 = ((((D2 + D5) - D6) + D7) - D8);
-  float m8 = (((((-0x1.0000000000000p+1f * D2) + D5) - D6) + D7) - D8);
-  float m16 = (((D3 + D4) - D5) - D6);
-  float m17 = (((-D3 + D4) + D7) + D8);
-  float m18 = (((D5 - D6) - D7) + D8);
-  const float uG = fmaf(ux, gx, fmaf(uy, gy, uz * gz));
-  const float pxx = ux * gx, pyy = uy * gy, pzz = uz * gz;
-  const float sxy = fmaf(ux, gy, uy * gx), syz = fmaf(uy, gz, uz * gy), sxz = fmaf(ux, gz, uz * gx);
-  const float g0 = fmaf(0x1.5555560000000p-2f, pzz, fmaf(0x1.5555560000000p-2f, pyy, fmaf(0x1.5555560000000p-2f, pxx, -uG)));
-  const float g1 = fmaf(0x1.c71c720000000p-3f, pzz, fmaf(0x1.c71c720000000p-3f, pyy, (0x1.c71c720000000p-3f * pxx)));
-  const float g3 = (0x1.5555560000000p-2f * gx);
-  const float g5 = (0x1.5555560000000p-2f * gy);
-  const float g7 = (0x1.5555560000000p-2f * gz);
-  const float g9 = fmaf(-0x1.c71c720000000p-3f, pzz, fmaf(-0x1.c71c720000000p-3f, pyy, (0x1.c71c720000000p-2f * pxx)));
-  const float g11 = fmaf(-0x1.c71c720000000p-3f, pzz, (0x1.c71c720000000p-3f * pyy));
-  const float g13 = (0x1.c71c720000000p-4f * sxy);
-  const float g14 = (0x1.c71c720000000p-4f * syz);
-  const float g15 = (0x1.c71c720000000p-4f * sxz);
-  const float uu = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
-  m0 = m0 + g0;
-  m1 = fmaf(fmaf(-0.5f, S[1], 1.0f), g1, fmaf(-S[1], (m1 - (uu)), m1));
-  m2 = fmaf(-S[2], m2, m2);
-  m3 = m3 + g3;
-  m4 = fmaf(-S[4], m4, m4);
-  m5 = m5 + g5;
-  m6 = fmaf(-S[6], m6, m6);
-  m7 = m7 + g7;
-  m8 = fmaf(-S[8], m8, m8);
-  m9 = fmaf(fmaf(-0.5f, S[9], 1.0f), g9, fmaf(-S[9], (m9 - (fmaf(2.0f * ux, ux, -fmaf(uy, uy, uz * uz)))), m9));
-  m10 = fmaf(-S[10], m10, m10);
-  m11 = fmaf(fmaf(-0.5f, S[11], 1.0f), g11, fmaf(-S[11], (m11 - (fmaf(uy, uy, -(uz * uz)))), m11));
-  m12 = fmaf(-S[12], m12, m12);
-  m13 = fmaf(fmaf(-0.5f, S[13], 1.0f), g13, fmaf(-S[13], (m13 - (ux * uy)), m13));
-  m14 = fmaf(fmaf(-0.5f, S[14], 1.0f), g14, fmaf(-S[14], (m14 - (uy * uz)), m14));
-  m15 = fmaf(fmaf(-0.5f, S[15], 1.0f), g15, fmaf(-S[15], (m15 - (ux * uz)), m15));
-  m16 = fmaf(-S[16], m16, m16);
-  m17 = fmaf(-S[17], m17, m17);
-  m18 = fmaf(-S[18], m18, m18);
-  out[0] = fmaf(0x1.5555560000000p-3f, m2, fmaf(-0x1.0000000000000p-1f, m1, (0x1.5555560000000p-2f * m0)));
-  { const float e = fmaf(-0x1.5555560000000p-4f, m10, fmaf(0x1.5555560000000p-4f, m9, fmaf(-0x1.c71c720000000p-5f, m2, (0x1.c71c720000000p-5f * m0)))), o = fmaf(-0x1.5555560000000p-3f, m4, (0x1.5555560000000p-3f * m3)); out[1] = e + o; out[2] = e - o; }
-  { const float e = fmaf(-0x1.0000000000000p-3f, m12, fmaf(0x1.0000000000000p-3f, m11, fmaf(0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(-0x1.c71c720000000p-5f, m2, (0x1.c71c720000000p-5f * m0)))))), o = fmaf(-0x1.5555560000000p-3f, m6, (0x1.5555560000000p-3f * m5)); out[3] = e + o; out[4] = e - o; }
-  { const float e = fmaf(0x1.0000000000000p-3f, m12, fmaf(-0x1.0000000000000p-3f, m11, fmaf(0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(-0x1.c71c720000000p-5f, m2, (0x1.c71c720000000p-5f * m0)))))), o = fmaf(-0x1.5555560000000p-3f, m8, (0x1.5555560000000p-3f * m7)); out[5] = e + o; out[6] = e - o; }
-  { const float e = fmaf(0x1.0000000000000p-2f, m13, fmaf(0x1.0000000000000p-4f, m12, fmaf(0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(-0x1.0000000000000p-3f, m17, fmaf(0x1.0000000000000p-3f, m16, fmaf(0x1.5555560000000p-5f, m6, fmaf(0x1.5555560000000p-4f, m5, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[7] = e + o; out[8] = e - o; }
-  { const float e = fmaf(-0x1.0000000000000p-2f, m13, fmaf(0x1.0000000000000p-4f, m12, fmaf(0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(0x1.0000000000000p-3f, m17, fmaf(0x1.0000000000000p-3f, m16, fmaf(-0x1.5555560000000p-5f, m6, fmaf(-0x1.5555560000000p-4f, m5, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[9] = e + o; out[10] = e - o; }
-  { const float e = fmaf(0x1.0000000000000p-2f, m15, fmaf(-0x1.0000000000000p-4f, m12, fmaf(-0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(0x1.0000000000000p-3f, m18, fmaf(-0x1.0000000000000p-3f, m16, fmaf(0x1.5555560000000p-5f, m8, fmaf(0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[11] = e + o; out[12] = e - o; }
-  { const float e = fmaf(-0x1.0000000000000p-2f, m15, fmaf(-0x1.0000000000000p-4f, m12, fmaf(-0x1.0000000000000p-4f, m11, fmaf(0x1.5555560000000p-6f, m10, fmaf(0x1.5555560000000p-6f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))))), o = fmaf(-0x1.0000000000000p-3f, m18, fmaf(-0x1.0000000000000p-3f, m16, fmaf(-0x1.5555560000000p-5f, m8, fmaf(-0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m4, (0x1.5555560000000p-4f * m3)))))); out[13] = e + o; out[14] = e - o; }
-  { const float e = fmaf(0x1.0000000000000p-2f, m14, fmaf(-0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))), o = fmaf(-0x1.0000000000000p-3f, m18, fmaf(0x1.0000000000000p-3f, m17, fmaf(0x1.5555560000000p-5f, m8, fmaf(0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m6, (0x1.5555560000000p-4f * m5)))))); out[15] = e + o; out[16] = e - o; }
-  { const float e = fmaf(-0x1.0000000000000p-2f, m14, fmaf(-0x1.5555560000000p-5f, m10, fmaf(-0x1.5555560000000p-5f, m9, fmaf(0x1.c71c720000000p-7f, m2, fmaf(0x1.5555560000000p-5f, m1, (0x1.c71c720000000p-6f * m0)))))), o = fmaf(0x1.0000000000000p-3f, m18, fmaf(0x1.0000000000000p-3f, m17, fmaf(-0x1.5555560000000p-5f, m8, fmaf(-0x1.5555560000000p-4f, m7, fmaf(0x1.5555560000000p-5f, m6, (0x1.5555560000000p-4f * m5)))))); out[17] = e + o; out[18] = e - o; }
+template <class V>
+__device__ __forceinline__ void mrt_collide_fast(const V (&F)[19], V rho, V ux, V uy, V uz,
+    V gx, V gy, V gz, const float* __restrict__ S, V (&out)[19]) {
+  const V P0 = vadd(F[1], F[2]), D0 = vsub(F[1], F[2]);
+  const V P1 = vadd(F[3], F[4]), D1 = vsub(F[3], F[4]);
+  const V P2 = vadd(F[5], F[6]), D2 = vsub(F[5], F[6]);
+  const V P3 = vadd(F[7], F[8]), D3 = vsub(F[7], F[8]);
+  const V P4 = vadd(F[9], F[10]), D4 = vsub(F[9], F[10]);
+  const V P5 = vadd(F[11], F[12]), D5 = vsub(F[11], F[12]);
+  const V P6 = vadd(F[13], F[14]), D6 = vsub(F[13], F[14]);
+  const V P7 = vadd(F[15], F[16]), D7 = vsub(F[15], F[16]);
+  const V P8 = vadd(F[17], F[18]), D8 = vsub(F[17], F[18]);
+  V m0 = vadd(vadd(vadd(vadd(vadd(vadd(vadd(vadd(vadd(F[0], P0), P1), P2), P3), P4), P5), P6), P7), P8);
+  V m1 = vadd(vadd(vadd(vadd(vadd(vadd(vneg(F[0]), P3), P4), P5), P6), P7), P8);
+  V m2 = vadd(vadd(vadd(vadd(vadd(vadd(vfma(-0x1.0000000000000p+1f, P2, vfma(-0x1.0000000000000p+1f, P1, vfma(-0x1.0000000000000p+1f, P0, F[0]))), P3), P4), P5), P6), P7), P8);
+  V m9 = vfma(-0x1.0000000000000p+1f, P8, vfma(-0x1.0000000000000p+1f, P7, vadd(vadd(vadd(vadd(vsub(vsub(vmul(P0, 0x1.0000000000000p+1f), P1), P2), P3), P4), P5), P6)));
+  V m10 = vfma(-0x1.0000000000000p+1f, P8, vfma(-0x1.0000000000000p+1f, P7, vadd(vadd(vadd(vadd(vadd(vadd(vmul(P0, -0x1.0000000000000p+1f), P1), P2), P3), P4), P5), P6)));
+  V m11 = vsub(vsub(vadd(vadd(vsub(P1, P2), P3), P4), P5), P6);
+  V m12 = vsub(vsub(vadd(vadd(vadd(vneg(P1), P2), P3), P4), P5), P6);
+  V m13 = vsub(P3, P4);
+  V m14 = vsub(P7, P8);
+  V m15 = vsub(P5, P6);
+  V m3 = vadd(vadd(vadd(vadd(D0, D3), D4), D5), D6);
+  V m4 = vadd(vadd(vadd(vadd(vmul(D0, -0x1.0000000000000p+1f), D3), D4), D5), D6);
+  V m5 = vadd(vadd(vsub(vadd(D1, D3), D4), D7), D8);
+  V m6 = vadd(vadd(vsub(vadd(vmul(D1, -0x1.0000000000000p+1f), D3), D4), D7), D8);
+  V m7 = vsub(vadd(vsub(vadd(D2, D5), D6), D7), D8);
+  V m8 = vsub(vadd(vsub(vadd(vmul(D2, -0x1.0000000000000p+1f), D5), D6), D7), D8);
+  V m16 = vsub(vsub(vadd(D3, D4), D5), D6);
+  V m17 = vadd(vadd(vadd(vneg(D3), D4), D7), D8);
+  V m18 = vadd(vsub(vsub(D5, D6), D7), D8);
+  const V uG = vfma(ux, gx, vfma(uy, gy, vmul(uz, gz)));
+  const V pxx = vmul(ux, gx), pyy = vmul(uy, gy), pzz = vmul(uz, gz);
+  const V sxy = vfma(ux, gy, vmul(uy, gx)), syz = vfma(uy, gz, vmul(uz, gy)), sxz = vfma(ux, gz, vmul(uz, gx));
+  const V g0 = vfma(0x1.5555560000000p-2f, pzz, vfma(0x1.5555560000000p-2f, pyy, vfma(0x1.5555560000000p-2f, pxx, vneg(uG))));
+  const V g1 = vfma(0x1.c71c720000000p-3f, pzz, vfma(0x1.c71c720000000p-3f, pyy, vmul(pxx, 0x1.c71c720000000p-3f)));
+  const V g3 = vmul(gx, 0x1.5555560000000p-2f);
+  const V g5 = vmul(gy, 0x1.5555560000000p-2f);
+  const V g7 = vmul(gz, 0x1.5555560000000p-2f);
+  const V g9 = vfma(-0x1.c71c720000000p-3f, pzz, vfma(-0x1.c71c720000000p-3f, pyy, vmul(pxx, 0x1.c71c720000000p-2f)));
+  const V g11 = vfma(-0x1.c71c720000000p-3f, pzz, vmul(pyy, 0x1.c71c720000000p-3f));
+  const V g13 = vmul(sxy, 0x1.c71c720000000p-4f);
+  const V g14 = vmul(syz, 0x1.c71c720000000p-4f);
+  const V g15 = vmul(sxz, 0x1.c71c720000000p-4f);
+  const V uu = vfma(ux, ux, vfma(uy, uy, vmul(uz, uz)));
+  m0 = vadd(m0, g0);
+  m1 = vfma(fmaf(-0.5f, S[1], 1.0f), g1, vfma(-S[1], vsub(m1, uu), m1));
+  m2 = vfma(-S[2], m2, m2);
+  m3 = vadd(m3, g3);
+  m4 = vfma(-S[4], m4, m4);
+  m5 = vadd(m5, g5);
+  m6 = vfma(-S[6], m6, m6);
+  m7 = vadd(m7, g7);
+  m8 = vfma(-S[8], m8, m8);
+  m9 = vfma(fmaf(-0.5f, S[9], 1.0f), g9, vfma(-S[9], vsub(m9, vfma(vadd(ux, ux), ux, vneg(vfma(uy, uy, vmul(uz, uz))))), m9));
+  m10 = vfma(-S[10], m10, m10);
+  m11 = vfma(fmaf(-0.5f, S[11], 1.0f), g11, vfma(-S[11], vsub(m11, vfma(uy, uy, vneg(vmul(uz, uz)))), m11));
+  m12 = vfma(-S[12], m12, m12);
+  m13 = vfma(fmaf(-0.5f, S[13], 1.0f), g13, vfma(-S[13], vsub(m13, vmul(ux, uy)), m13));
+  m14 = vfma(fmaf(-0.5f, S[14], 1.0f), g14, vfma(-S[14], vsub(m14, vmul(uy, uz)), m14));
+  m15 = vfma(fmaf(-0.5f, S[15], 1.0f), g15, vfma(-S[15], vsub(m15, vmul(ux, uz)), m15));
+  m16 = vfma(-S[16], m16, m16);
+  m17 = vfma(-S[17], m17, m17);
+  m18 = vfma(-S[18], m18, m18);
+  out[0] = vfma(0x1.5555560000000p-3f, m2, vfma(-0x1.0000000000000p-1f, m1, vmul(m0, 0x1.5555560000000p-2f)));
+  { const V e = vfma(-0x1.5555560000000p-4f, m10, vfma(0x1.5555560000000p-4f, m9, vfma(-0x1.c71c720000000p-5f, m2, vmul(m0, 0x1.c71c720000000p-5f)))), o = vfma(-0x1.5555560000000p-3f, m4, vmul(m3, 0x1.5555560000000p-3f)); out[1] = vadd(e, o); out[2] = vsub(e, o); }
+  { const V e = vfma(-0x1.0000000000000p-3f, m12, vfma(0x1.0000000000000p-3f, m11, vfma(0x1.5555560000000p-5f, m10, vfma(-0x1.5555560000000p-5f, m9, vfma(-0x1.c71c720000000p-5f, m2, vmul(m0, 0x1.c71c720000000p-5f)))))), o = vfma(-0x1.5555560000000p-3f, m6, vmul(m5, 0x1.5555560000000p-3f)); out[3] = vadd(e, o); out[4] = vsub(e, o); }
+  { const V e = vfma(0x1.0000000000000p-3f, m12, vfma(-0x1.0000000000000p-3f, m11, vfma(0x1.5555560000000p-5f, m10, vfma(-0x1.5555560000000p-5f, m9, vfma(-0x1.c71c720000000p-5f, m2, vmul(m0, 0x1.c71c720000000p-5f)))))), o = vfma(-0x1.5555560000000p-3f, m8, vmul(m7, 0x1.5555560000000p-3f)); out[5] = vadd(e, o); out[6] = vsub(e, o); }
+  { const V e = vfma(0x1.0000000000000p-2f, m13, vfma(0x1.0000000000000p-4f, m12, vfma(0x1.0000000000000p-4f, m11, vfma(0x1.5555560000000p-6f, m10, vfma(0x1.5555560000000p-6f, m9, vfma(0x1.c71c720000000p-7f, m2, vfma(0x1.5555560000000p-5f, m1, vmul(m0, 0x1.c71c720000000p-6f)))))))), o = vfma(-0x1.0000000000000p-3f, m17, vfma(0x1.0000000000000p-3f, m16, vfma(0x1.5555560000000p-5f, m6, vfma(0x1.5555560000000p-4f, m5, vfma(0x1.5555560000000p-5f, m4, vmul(m3, 0x1.5555560000000p-4f)))))); out[7] = vadd(e, o); out[8] = vsub(e, o); }
+  { const V e = vfma(-0x1.0000000000000p-2f, m13, vfma(0x1.0000000000000p-4f, m12, vfma(0x1.0000000000000p-4f, m11, vfma(0x1.5555560000000p-6f, m10, vfma(0x1.5555560000000p-6f, m9, vfma(0x1.c71c720000000p-7f, m2, vfma(0x1.5555560000000p-5f, m1, vmul(m0, 0x1.c71c720000000p-6f)))))))), o = vfma(0x1.0000000000000p-3f, m17, vfma(0x1.0000000000000p-3f, m16, vfma(-0x1.5555560000000p-5f, m6, vfma(-0x1.5555560000000p-4f, m5, vfma(0x1.5555560000000p-5f, m4, vmul(m3, 0x1.5555560000000p-4f)))))); out[9] = vadd(e, o); out[10] = vsub(e, o); }
+  { const V e = vfma(0x1.0000000000000p-2f, m15, vfma(-0x1.0000000000000p-4f, m12, vfma(-0x1.0000000000000p-4f, m11, vfma(0x1.5555560000000p-6f, m10, vfma(0x1.5555560000000p-6f, m9, vfma(0x1.c71c720000000p-7f, m2, vfma(0x1.5555560000000p-5f, m1, vmul(m0, 0x1.c71c720000000p-6f)))))))), o = vfma(0x1.0000000000000p-3f, m18, vfma(-0x1.0000000000000p-3f, m16, vfma(0x1.5555560000000p-5f, m8, vfma(0x1.5555560000000p-4f, m7, vfma(0x1.5555560000000p-5f, m4, vmul(m3, 0x1.5555560000000p-4f)))))); out[11] = vadd(e, o); out[12] = vsub(e, o); }
+  { const V e = vfma(-0x1.0000000000000p-2f, m15, vfma(-0x1.0000000000000p-4f, m12, vfma(-0x1.0000000000000p-4f, m11, vfma(0x1.5555560000000p-6f, m10, vfma(0x1.5555560000000p-6f, m9, vfma(0x1.c71c720000000p-7f, m2, vfma(0x1.5555560000000p-5f, m1, vmul(m0, 0x1.c71c720000000p-6f)))))))), o = vfma(-0x1.0000000000000p-3f, m18, vfma(-0x1.0000000000000p-3f, m16, vfma(-0x1.5555560000000p-5f, m8, vfma(-0x1.5555560000000p-4f, m7, vfma(0x1.5555560000000p-5f, m4, vmul(m3, 0x1.5555560000000p-4f)))))); out[13] = vadd(e, o); out[14] = vsub(e, o); }
+  { const V e = vfma(0x1.0000000000000p-2f, m14, vfma(-0x1.5555560000000p-5f, m10, vfma(-0x1.5555560000000p-5f, m9, vfma(0x1.c71c720000000p-7f, m2, vfma(0x1.5555560000000p-5f, m1, vmul(m0, 0x1.c71c720000000p-6f)))))), o = vfma(-0x1.0000000000000p-3f, m18, vfma(0x1.0000000000000p-3f, m17, vfma(0x1.5555560000000p-5f, m8, vfma(0x1.5555560000000p-4f, m7, vfma(0x1.5555560000000p-5f, m6, vmul(m5, 0x1.5555560000000p-4f)))))); out[15] = vadd(e, o); out[16] = vsub(e, o); }
+  { const V e = vfma(-0x1.0000000000000p-2f, m14, vfma(-0x1.5555560000000p-5f, m10, vfma(-0x1.5555560000000p-5f, m9, vfma(0x1.c71c720000000p-7f, m2, vfma(0x1.5555560000000p-5f, m1, vmul(m0, 0x1.c71c720000000p-6f)))))), o = vfma(0x1.0000000000000p-3f, m18, vfma(0x1.0000000000000p-3f, m17, vfma(-0x1.5555560000000p-5f, m8, vfma(-0x1.5555560000000p-4f, m7, vfma(0x1.5555560000000p-5f, m6, vmul(m5, 0x1.5555560000000p-4f)))))); out[17] = vadd(e, o); out[18] = vsub(e, o); }
 }
 }  // namespace fsi

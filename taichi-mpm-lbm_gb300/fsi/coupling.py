@@ -134,7 +134,11 @@ class LBMMpmCoupler:
         dt_ratio = mpm_dt / lbm_dt_value
         for substep in range(self.substeps):
             if self.enabled:
-                self.clear_particle_diagnostics()
+                # clear_particle_diagnostics() of coupling.py:147: the coupling kernel rewrites
+                # the weight and mask of every active particle, and inactive particles keep
+                # the zeros written by clear_coupling_fields() above, so only the per-substep
+                # counters need clearing here.
+                self._counters[0:5].zero_()
                 self._coupling_kernel(dt_ratio, substep == 0 and self.build_solid_volume_fraction)
             else:
                 self.mpm.clear_particle_force()
@@ -152,6 +156,64 @@ class LBMMpmCoupler:
         self.lbm.step()
         if self.enabled:
             self._coupled_step += 1
+
+    # ------------------------------------------------------- graph stepping
+    def _graph_state(self) -> tuple:
+        lbm = self.lbm
+        return (lbm._steps_done % 2, lbm._fcur, lbm._fprev, lbm._macro_fresh)
+
+    def _gamma_settled(self) -> bool:
+        ramp = int(self.config.gamma_ramp_steps)
+        return ramp <= 0 or not self.enabled or self._coupled_step + 1 >= ramp
+
+    def step_many(self, lbm_dt: float, steps: int, graph: bool = True) -> None:
+        """``steps`` calls of step(lbm_dt) (no reference counterpart).
+
+        With ``graph`` the steady part runs as replays of one captured CUDA graph of two
+        coupled steps, which removes the per-launch host cost of the ~40 launches of a step.
+        Steps during the gamma ramp (whose gamma differs per step) and a last odd step run
+        eagerly. The results are those of the eager loop: the graph replays the same kernels
+        with the same arguments, and two steps return the lattice to the same buffers and
+        parity."""
+        steps = int(steps)
+        if steps < 0:
+            raise ValueError("steps must be non-negative.")
+        self._validate_initialized()
+        if not graph or steps < 4:
+            for _ in range(steps):
+                self.step(lbm_dt)
+            return
+        # The graph bakes gamma_eff and the lattice's buffer choice: settle both eagerly.
+        while steps > 0 and (not self._gamma_settled() or self.lbm._macro_fresh
+                             or self.lbm._fcur != self.lbm._fprev):
+            self.step(lbm_dt)
+            steps -= 1
+        if steps < 2:
+            for _ in range(steps):
+                self.step(lbm_dt)
+            return
+        before = self._graph_state()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            # Capture records the two steps without running them; the host-side counters
+            # advance here, and the first replay below performs the work.
+            self.step(lbm_dt)
+            self.step(lbm_dt)
+        g.replay()
+        steps -= 2
+        if self._graph_state() != before:
+            for _ in range(steps):
+                self.step(lbm_dt)
+            return
+        while steps >= 2:
+            g.replay()
+            self.lbm._steps_done += 2
+            if self.enabled:
+                self._coupled_step += 2
+            steps -= 2
+        if steps:
+            self.step(lbm_dt)
+        del g
 
     def compute_coupling_forces(self, dt_ratio: float = 1.0) -> None:
         """Particle force and fluid reaction without stepping (coupling.py:175-196)."""

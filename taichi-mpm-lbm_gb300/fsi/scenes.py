@@ -156,3 +156,59 @@ def coupled_smoke(steps: int = 1000) -> tuple[SimulationConfig, np.ndarray, np.n
                    axis=-1).reshape(-1, 3)
     pos = (12.0 + 0.5 * (idx + rng.uniform(0.0, 1.0, idx.shape))).astype(np.float32)
     return cfg, wall_mask(nx, ny, nz), pos
+
+
+def sphere_particles(center, radius: float, ppc_axis: int, rng=None) -> np.ndarray:
+    """Particles of a ball: the sub-cell lattice of its bounding cube of cells, jittered like
+    ``cube_particles``, kept where the particle lies within ``radius`` of ``center``."""
+    edge = int(np.ceil(2 * radius))
+    lower = np.floor(np.asarray(center, np.float64) - edge / 2)
+    pts = cube_particles(lower, edge, ppc_axis, rng)
+    keep = np.linalg.norm(pts.astype(np.float64) - np.asarray(center), axis=1) <= radius
+    return pts[keep]
+
+
+def coupled_bodies(nx: int = 384, ny: int = 192, nz: int = 192, bodies: int = 48,
+                   cube_edge: int = 12, sphere_radius: float = 6.0, tau: float = 0.55,
+                   inflow: float = 0.05, seed: int = 3, substeps: int = 10):
+    """The coupled workload at scale: an nx*ny*nz channel (walls in y and z as mask planes)
+    with a velocity inlet of ``inflow`` in x at x = 0 and a pressure outlet (rho 1) at
+    x = nx-1; ``bodies`` elastic bodies, half cubes of edge ``cube_edge`` cells and half
+    balls of radius ``sphere_radius``, at non-overlapping positions from ``seed``, 8
+    particles per cell, Young's modulus U[0.02, 0.1] per body, nu 0.3, rho_s 1.2.
+    Returns (config, solid mask, positions, per-particle Young's modulus)."""
+    rng = np.random.default_rng(seed)
+    lbm = LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=viscosity_for_tau(tau), rho0=1.0,
+                    x_left=BoundaryConfig("velocity", velocity=(inflow, 0.0, 0.0)),
+                    x_right=BoundaryConfig("pressure", rho=1.0),
+                    y_left=BoundaryConfig("periodic"), y_right=BoundaryConfig("periodic"),
+                    z_left=BoundaryConfig("periodic"), z_right=BoundaryConfig("periodic"))
+    half = max(cube_edge / 2, sphere_radius)
+    margin = half + 4
+    centres = []
+    tries = 0
+    while len(centres) < bodies:
+        tries += 1
+        if tries > 1_000_000:
+            raise RuntimeError("could not place the bodies without overlap")
+        c = np.array([rng.uniform(margin + 16, nx - margin - 16), rng.uniform(margin, ny - margin),
+                      rng.uniform(margin, nz - margin)])
+        if any(np.max(np.abs(c - o)) < 2 * half + 2 for o in centres):
+            continue
+        centres.append(c)
+    pos, young = [], []
+    for b, c in enumerate(centres):
+        if b % 2 == 0:
+            p = cube_particles(np.floor(c - cube_edge / 2), cube_edge, 2, rng)
+        else:
+            p = sphere_particles(c, sphere_radius, 2, rng)
+        pos.append(p)
+        young.append(np.full(len(p), rng.uniform(0.02, 0.1), np.float32))
+    pos = np.concatenate(pos)
+    young = np.concatenate(young)
+    mpm = MPMConfig(nx=nx, ny=ny, nz=nz, max_particles=len(pos), particles_per_cell=2, dx=1.0,
+                    dt=1.0 / substeps, density=1.2, youngs_modulus=0.05, poisson_ratio=0.3,
+                    gravity=(0.0, 0.0, 0.0), boundary_width=3)
+    cfg = SimulationConfig(num_steps=2000, lbm_dt=1.0, lbm=lbm, mpm=mpm,
+                           coupling=CouplingConfig(gamma=0.1, mpm_substeps_per_lbm_step=substeps))
+    return cfg, wall_mask(nx, ny, nz), pos, young

@@ -37,10 +37,14 @@ class FSISimulation:
         return count
 
     def initialize_mpm_from_numpy(self, positions, velocities=None, particle_mass=None,
-                                  particle_volume=None) -> int:
+                                  particle_volume=None, youngs_modulus=None,
+                                  poisson_ratio=None) -> int:
+        """Load particles (simulation.py:51-59); ``youngs_modulus`` / ``poisson_ratio`` per
+        particle are the MPMSolver3D extension for bodies of different stiffness."""
         count = self.mpm.initialize_particles_from_numpy(
             positions=positions, velocities=velocities, particle_mass=particle_mass,
-            particle_volume=particle_volume)
+            particle_volume=particle_volume, youngs_modulus=youngs_modulus,
+            poisson_ratio=poisson_ratio)
         self._mpm_initialized = True
         return count
 
@@ -74,6 +78,18 @@ class FSISimulation:
             if write_output and self.output_writer.should_write(self.step_index):
                 self.write_snapshot()
         return history
+
+    def advance(self, steps: int, graph: bool = True) -> None:
+        """``steps`` coupled steps without per-step diagnostics (no reference counterpart):
+        LBMMpmCoupler.step_many, with the step counter and time advanced as by step()."""
+        self._validate_initialized()
+        count = int(steps)
+        if count <= 0:
+            raise ValueError("steps must be positive.")
+        self.coupler.step_many(self.config.lbm_dt, count, graph=graph)
+        for _ in range(count):
+            self.step_index += 1
+            self.time += self.config.lbm_dt
 
     def write_snapshot(self):
         self._validate_initialized()

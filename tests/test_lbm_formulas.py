@@ -67,9 +67,9 @@ def _fast_as_python(src: str) -> str:
         if line.startswith("{"):
             line = line.strip("{} ")
         for stmt in filter(None, (s.strip() for s in line.split(";"))):
-            stmt = stmt.replace("const float ", "").replace("float ", "")
+            stmt = re.sub(r"^(const )?V ", "", stmt)
             stmts.extend(_split_top(stmt))
-    return "\n".join(stmts).replace("fmaf(", "fma(")
+    return "\n".join(stmts).replace("splat<V>(0.0)", "0.0")
 
 
 def _collide_f64(gen, F, u, G, S):
@@ -106,7 +106,9 @@ def test_fast_collision_is_the_same_operator():
     out = [None] * 19
     env = {"F": F.T, "rho": F.sum(1), "ux": u[:, 0], "uy": u[:, 1], "uz": u[:, 2],
            "gx": G[:, 0], "gy": G[:, 1], "gz": G[:, 2], "S": S, "out": out,
-           "fma": lambda a, b, c: a * b + c}
+           "vfma": lambda a, b, c: a * b + c, "fmaf": lambda a, b, c: a * b + c,
+           "vadd": lambda a, b: a + b, "vsub": lambda a, b: a - b, "vmul": lambda a, b: a * b,
+           "vneg": lambda a: -a}
     exec(code, env)
     want = _collide_f64(gen, F, u, G, S)
     got = np.stack(out, axis=1)
