@@ -35,6 +35,9 @@ LBM_BYTES_PER_CELL = 181     # algorithmic bytes per FP32 cell update (pops 152,
 KERNEL_BYTES_PER_CELL = 168  # what the fused step moves: pops 152, flag word 4, force 12
 MPM_BYTES_PER_PARTICLE = 200  # algorithmic bytes per particle-substep (standalone)
 MPM_BYTES_PER_NODE = 32       # per touched grid node per substep
+# DRAM bytes per fluid cell and step kernel launch, from the ncu captures of the 192^3 scene
+# (dram__bytes_read.sum + dram__bytes_write.sum, odd/even launch average).
+TRAFFIC_PER_FLUID_CELL = {"f32/exact": 177.7, "f16/fast": 96.1}
 METRIC = "MLUPS & particle-steps/s on 1 GB300: plain vs FP16/learned, <=1% drag error"
 
 
@@ -362,7 +365,12 @@ def run_gpu(args) -> dict:
         },
         "roofline": {
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None,
+            "frac": round(achieved / peak, 4),
+            "traffic": (round(TRAFFIC_PER_FLUID_CELL[args.lbm_form] * fluid_cells)
+                        if args.lbm_form in TRAFFIC_PER_FLUID_CELL else None),
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of the "
+                               "192^3 capture (odd/even average per fluid cell), scaled to this "
+                               "lattice's fluid cells"),
             "kernel": "lbm_step_kernel", "peak_source": peak_kind,
             "algorithmic_bytes_per_cell": alg_bytes,
             "kernel_bytes_per_cell": moved_bytes,

@@ -308,6 +308,53 @@ int fsi_contact(const fsi_coupling_desc* desc, const fsi_mpm_desc* mpm,
 int fsi_coupling_reduce(const fsi_lbm_desc* lbm, const float* accum, const uint32_t* flags,
                         double* out, void* stream);
 
+/* ------------------------------------------------------------- batches of scenes
+ * Many independent lattices advanced together: one launch per phase covers every lattice
+ * of the batch. No reference counterpart (the reference runs one scene per FSISimulation).
+ * Lattice s owns cells [cell_offset, cell_offset + nx*ny*nz) of the batch's concatenated
+ * per-cell arrays: populations are the [19][N_s] block at element 19 * cell_offset (in the
+ * batch's storage type), force the [3][N_s] block at 3 * cell_offset, macro the [N_s][4]
+ * block at cell_offset, flags and masks start at cell_offset. The offsets are the running
+ * sums of the lattice sizes in order. Faces are periodic (x faces are not batched). */
+typedef struct fsi_batch_lattice {
+  int32_t nx, ny, nz;
+  int32_t reserved;
+  int64_t cell_offset;
+  float s[19];          /* MRT relaxation rates, as fsi_lbm_desc.s */
+  float rho0;
+  float base_force[3];  /* the lattice's body force (LBMConfig.force) */
+} fsi_batch_lattice;
+
+typedef struct fsi_batch fsi_batch; /* opaque */
+
+/* Validates the lattices (host array), copies them and the launch tiles to the device.
+ * storage / arithmetic: FSI_STORAGE_* / FSI_ARITH_* for every lattice of the batch. */
+int fsi_batch_create(const fsi_batch_lattice* lattices, int32_t count, int32_t storage,
+                     int32_t arithmetic, fsi_batch** out);
+int fsi_batch_destroy(fsi_batch* batch);
+/* Total cells of the batch (the length of the concatenated per-cell arrays). */
+int fsi_batch_cells(const fsi_batch* batch, int64_t* cells);
+
+/* fsi_lbm_build_flags / fsi_lbm_init_fields / fsi_lbm_step / fsi_lbm_update_macro /
+ * fsi_lbm_distribution over every lattice of the batch, with the same meaning per lattice.
+ * u0: device float[count][3]. diag: NULL or device double[count][2] (sum of rho over fluid
+ * cells, max |u|), zeroed here. */
+int fsi_batch_lbm_flags(const fsi_batch* batch, const int32_t* solid, uint32_t* flags,
+                        void* stream);
+int fsi_batch_lbm_init(const fsi_batch* batch, const float* u0, const uint32_t* flags,
+                       void* pops, float* macro, void* stream);
+int fsi_batch_lbm_step(const fsi_batch* batch, void* pops, float* macro, const float* force,
+                       const float* force_prev, const uint32_t* flags, int64_t steps_done,
+                       void* stream);
+int fsi_batch_lbm_macro(const fsi_batch* batch, const void* pops, const float* force,
+                        const uint32_t* flags, int64_t steps_done, float* macro, double* diag,
+                        void* stream);
+int fsi_batch_lbm_distribution(const fsi_batch* batch, const void* pops, const uint32_t* flags,
+                               int64_t steps_done, float* out, void* stream);
+/* force = the lattice's base_force on fluid cells, 0 on solid cells (reset_force). */
+int fsi_batch_lbm_base_force(const fsi_batch* batch, const uint32_t* flags, float* force,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,433 @@
+// Batches of independent scenes: one launch per phase over every lattice of the batch.
+//
+// A launch walks the batch's tiles of kTileCells consecutive cells of one lattice each
+// (tile = one thread block). Every lattice keeps its own geometry, relaxation rates and
+// storage shift in a device table; the per-cell work is the single-lattice code
+// (lbm_core.cuh) applied to that lattice's block of the concatenated arrays, so a batch
+// reproduces each lattice's standalone run bit for bit.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "fsi_common.cuh"
+#include "lbm_core.cuh"
+
+struct fsi_batch;
+
+namespace fsi {
+namespace {
+
+constexpr int kTileCells = 256;
+
+struct BatchLattice {
+  LbmGeom g;
+  long long off;  // first cell in the concatenated arrays
+  float s[19];
+  float shift[19];
+  float rho0;
+  float base[3];
+};
+
+struct Tile {
+  int lattice;
+  int first;  // first cell within the lattice
+};
+
+}  // namespace
+}  // namespace fsi
+
+struct fsi_batch {
+  fsi::BatchLattice* lat = nullptr;  // device
+  fsi::Tile* tiles = nullptr;        // device
+  int count = 0;
+  int ntiles = 0;
+  int storage = 0;
+  int arithmetic = 0;
+  long long cells = 0;
+};
+
+namespace fsi {
+namespace {
+
+// The lattice of a tile as the argument type of step_cells.
+struct LatticeView {
+  LbmGeom g;
+  void* __restrict__ pops;
+  float4* __restrict__ macro;
+  const float* __restrict__ force;
+  const float* __restrict__ force_prev;
+  const uint32_t* __restrict__ flags;
+  const float* s;
+  const float* shift;
+  int write_faces;
+};
+
+template <int kStore>
+__device__ __forceinline__ LatticeView view_of(const BatchLattice& L, void* pops, float* macro,
+                                               const float* force, const float* force_prev,
+                                               const uint32_t* flags) {
+  using T = typename Store<kStore>::T;
+  LatticeView v;
+  v.g = L.g;
+  v.pops = reinterpret_cast<T*>(pops) + 19 * L.off;
+  v.macro = reinterpret_cast<float4*>(macro) + L.off;
+  v.force = force + 3 * L.off;
+  v.force_prev = force_prev ? force_prev + 3 * L.off : nullptr;
+  v.flags = flags + L.off;
+  v.s = L.s;
+  v.shift = L.shift;
+  v.write_faces = 0;
+  return v;
+}
+
+__device__ __forceinline__ void cell_ijk(const LbmGeom& g, int c, int& i, int& j, int& k) {
+  const int nyz = g.ny * g.nz;
+  i = c / nyz;
+  const int r = c - i * nyz;
+  j = r / g.nz;
+  k = r - j * g.nz;
+}
+
+struct BatchStepArgs {
+  const BatchLattice* lat;
+  const Tile* tiles;
+  void* pops;
+  float* macro;
+  const float* force;
+  const float* force_prev;
+  const uint32_t* flags;
+};
+
+// kStepBlock threads cover a tile of kTileCells cells: the exact form takes cells t and
+// t + kStepBlock one after the other, the fast forms take them as the two packed lanes.
+template <int kStore, bool kFast, bool kOdd, bool kRecompute>
+__global__ void __launch_bounds__(kStepBlock, (step_min_blocks<kFast, kOdd>()))
+    batch_step_kernel(BatchStepArgs b) {
+  constexpr int NL = StepLanes<kFast>::n;
+  constexpr int kReps = kTileCells / (kStepBlock * NL);
+  const Tile t = b.tiles[blockIdx.x];
+  const BatchLattice& L = b.lat[t.lattice];
+  const LatticeView v = view_of<kStore>(L, b.pops, b.macro, b.force, b.force_prev, b.flags);
+  const int n = (int)L.g.n;
+#pragma unroll
+  for (int r = 0; r < kReps; ++r) {
+    int ci[NL], cj[NL], ck[NL];
+    bool has[NL];
+    bool any = false;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      const int c = t.first + threadIdx.x + (r * NL + l) * kStepBlock;
+      has[l] = c < n;
+      any = any || has[l];
+      cell_ijk(L.g, has[l] ? c : t.first, ci[l], cj[l], ck[l]);
+    }
+    if (any) step_cells<kStore, kFast, kOdd, kRecompute, LatticeView>(v, ci, cj, ck, has);
+  }
+}
+
+// update_macro of every lattice (lbm3d.py:409-425), optionally with each lattice's sum of
+// rho over fluid cells and max |u| (lbm3d.py:450-457) in diag[2 * lattice + {0, 1}].
+template <int kStore, bool kFast>
+__global__ void __launch_bounds__(kTileCells)
+    batch_macro_kernel(const BatchLattice* __restrict__ lat, const Tile* __restrict__ tiles,
+                       const void* pops_v, const float* __restrict__ force_all,
+                       const uint32_t* __restrict__ flags_all, int parity, float* macro_all,
+                       double* __restrict__ diag) {
+  const Tile t = tiles[blockIdx.x];
+  const BatchLattice& L = lat[t.lattice];
+  const int c = t.first + threadIdx.x;
+  float mass = 0.f, vmax = 0.f;
+  if (c < L.g.n) {
+    int i, j, k;
+    cell_ijk(L.g, c, i, j, k);
+    const Deltas d(L.g, i, j, k);
+    const uint32_t fl = flags_all[L.off + c];
+    float4* macro = reinterpret_cast<float4*>(macro_all) + L.off;
+    if (fl & kFlagSolid) {
+      macro[c] = make_float4(0.f, 0.f, 0.f, L.rho0);
+    } else {
+      const uint32_t n = (uint32_t)L.g.n;
+      const auto* pops = reinterpret_cast<const typename Store<kStore>::T*>(pops_v) + 19 * L.off;
+      const float* force = force_all + 3 * L.off;
+      float F[19];
+#pragma unroll
+      for (int q = 0; q < 19; ++q) F[q] = gather32<kStore>(pops, n, d, fl, q, parity, L.shift[q]);
+      float rho, ux, uy, uz;
+      macro_any<kFast>(F, force[c], force[n + c], force[2 * n + c], rho, ux, uy, uz);
+      macro[c] = make_float4(ux, uy, uz, rho);
+      mass = rho;
+      vmax = norm3_ref(ux, uy, uz);
+    }
+  }
+  if (diag) {
+    const float s[1] = {mass};
+    block_accumulate<1>(diag + 2 * t.lattice, s, diag + 2 * t.lattice + 1, vmax);
+  }
+}
+
+template <int kStore>
+__global__ void __launch_bounds__(kTileCells)
+    batch_distribution_kernel(const BatchLattice* __restrict__ lat, const Tile* __restrict__ tiles,
+                              const void* pops_v, const uint32_t* __restrict__ flags_all,
+                              int parity, float* __restrict__ out) {
+  const Tile t = tiles[blockIdx.x];
+  const BatchLattice& L = lat[t.lattice];
+  const int c = t.first + threadIdx.x;
+  if (c >= L.g.n) return;
+  int i, j, k;
+  cell_ijk(L.g, c, i, j, k);
+  const Deltas d(L.g, i, j, k);
+  const uint32_t fl = flags_all[L.off + c];
+  const int p = (fl & kFlagSolid) ? 0 : parity;
+  const auto* pops = reinterpret_cast<const typename Store<kStore>::T*>(pops_v) + 19 * L.off;
+#pragma unroll
+  for (int q = 0; q < 19; ++q)
+    out[(size_t)(L.off + c) * 19 + q] = gather32<kStore>(pops, (uint32_t)L.g.n, d, fl, q, p, L.shift[q]);
+}
+
+__global__ void __launch_bounds__(kTileCells)
+    batch_flags_kernel(const BatchLattice* __restrict__ lat, const Tile* __restrict__ tiles,
+                       const int32_t* __restrict__ solid_all, uint32_t* __restrict__ flags_all) {
+  const Tile t = tiles[blockIdx.x];
+  const BatchLattice& L = lat[t.lattice];
+  const int c = t.first + threadIdx.x;
+  if (c >= L.g.n) return;
+  int i, j, k;
+  cell_ijk(L.g, c, i, j, k);
+  const Deltas d(L.g, i, j, k);
+  const int32_t* solid = solid_all + L.off;
+  uint32_t f = solid[d.c] != 0 ? kFlagSolid : 0u;
+#pragma unroll
+  for (int q = 1; q < 19; ++q)
+    if (solid[d.nb(q, +1)] != 0) f |= 1u << q;
+  if (i == 0) f |= kFlagFaceLeft;
+  if (i == L.g.nx - 1) f |= kFlagFaceRight;
+  flags_all[L.off + c] = f;
+}
+
+template <int kStore>
+__global__ void __launch_bounds__(kTileCells)
+    batch_init_kernel(const BatchLattice* __restrict__ lat, const Tile* __restrict__ tiles,
+                      const float* __restrict__ u0, const uint32_t* __restrict__ flags_all,
+                      void* pops_v, float* macro_all) {
+  const Tile t = tiles[blockIdx.x];
+  const BatchLattice& L = lat[t.lattice];
+  const int c = t.first + threadIdx.x;
+  if (c >= L.g.n) return;
+  const bool solid = flags_all[L.off + c] & kFlagSolid;
+  const float* u = u0 + 3 * t.lattice;
+  const float ux = solid ? 0.f : u[0], uy = solid ? 0.f : u[1], uz = solid ? 0.f : u[2];
+  reinterpret_cast<float4*>(macro_all)[L.off + c] = make_float4(ux, uy, uz, L.rho0);
+  auto* pops = reinterpret_cast<typename Store<kStore>::T*>(pops_v) + 19 * L.off;
+#pragma unroll
+  for (int q = 0; q < 19; ++q)
+    Store<kStore>::st(pops, (uint32_t)(q * L.g.n + c), feq_ref(q, L.rho0, ux, uy, uz), L.shift[q]);
+}
+
+__global__ void __launch_bounds__(kTileCells)
+    batch_base_force_kernel(const BatchLattice* __restrict__ lat, const Tile* __restrict__ tiles,
+                            const uint32_t* __restrict__ flags_all, float* __restrict__ force_all) {
+  const Tile t = tiles[blockIdx.x];
+  const BatchLattice& L = lat[t.lattice];
+  const int c = t.first + threadIdx.x;
+  if (c >= L.g.n) return;
+  const bool fluid = !(flags_all[L.off + c] & kFlagSolid);
+  float* force = force_all + 3 * L.off;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) force[a * L.g.n + c] = fluid ? L.base[a] : 0.f;
+}
+
+template <int S, bool F>
+struct BatchStepLauncher {
+  static void run(const fsi_batch* b, const BatchStepArgs& a, bool odd, bool recompute,
+                  cudaStream_t s) {
+    const dim3 grid(b->ntiles), block(kStepBlock);
+    if (recompute) {
+      if (odd) batch_step_kernel<S, F, true, true><<<grid, block, 0, s>>>(a);
+      else batch_step_kernel<S, F, false, true><<<grid, block, 0, s>>>(a);
+    } else {
+      if (odd) batch_step_kernel<S, F, true, false><<<grid, block, 0, s>>>(a);
+      else batch_step_kernel<S, F, false, false><<<grid, block, 0, s>>>(a);
+    }
+  }
+};
+
+template <int S, bool F>
+struct BatchMacroLauncher {
+  static void run(const fsi_batch* b, const void* pops, const float* force, const uint32_t* flags,
+                  int parity, float* macro, double* diag, cudaStream_t s) {
+    batch_macro_kernel<S, F><<<b->ntiles, kTileCells, 0, s>>>(b->lat, b->tiles, pops, force, flags,
+                                                              parity, macro, diag);
+  }
+};
+
+template <int S, bool F>
+struct BatchDistLauncher {
+  static void run(const fsi_batch* b, const void* pops, const uint32_t* flags, int parity,
+                  float* out, cudaStream_t s) {
+    batch_distribution_kernel<S><<<b->ntiles, kTileCells, 0, s>>>(b->lat, b->tiles, pops, flags,
+                                                                  parity, out);
+  }
+};
+
+template <int S, bool F>
+struct BatchInitLauncher {
+  static void run(const fsi_batch* b, const float* u0, const uint32_t* flags, void* pops,
+                  float* macro, cudaStream_t s) {
+    batch_init_kernel<S><<<b->ntiles, kTileCells, 0, s>>>(b->lat, b->tiles, u0, flags, pops, macro);
+  }
+};
+
+template <template <int, bool> class Launcher, class... Args>
+void dispatch_batch(const fsi_batch* b, Args&&... args) {
+  switch (b->storage) {
+    case FSI_STORAGE_F16: Launcher<FSI_STORAGE_F16, true>::run(b, args...); break;
+    case FSI_STORAGE_BF16: Launcher<FSI_STORAGE_BF16, true>::run(b, args...); break;
+    default:
+      if (b->arithmetic == FSI_ARITH_FAST) Launcher<FSI_STORAGE_F32, true>::run(b, args...);
+      else Launcher<FSI_STORAGE_F32, false>::run(b, args...);
+  }
+}
+
+int check_batch(const fsi_batch* b) {
+  FSI_REQUIRE(b != nullptr && b->lat != nullptr && b->ntiles > 0, "invalid batch handle");
+  return FSI_OK;
+}
+
+}  // namespace
+}  // namespace fsi
+
+using namespace fsi;
+
+extern "C" int fsi_batch_create(const fsi_batch_lattice* lattices, int32_t count, int32_t storage,
+                                int32_t arithmetic, fsi_batch** out) {
+  FSI_REQUIRE(out != nullptr, "NULL output handle");
+  *out = nullptr;
+  FSI_REQUIRE(lattices != nullptr && count > 0, "empty batch");
+  FSI_REQUIRE(storage >= FSI_STORAGE_F32 && storage <= FSI_STORAGE_BF16, "unknown storage %d",
+              storage);
+  FSI_REQUIRE(arithmetic == FSI_ARITH_EXACT || arithmetic == FSI_ARITH_FAST,
+              "unknown arithmetic form %d", arithmetic);
+  FSI_REQUIRE(storage == FSI_STORAGE_F32 || arithmetic == FSI_ARITH_FAST,
+              "FP16/BF16 population storage uses the fast arithmetic form");
+  std::vector<BatchLattice> host(count);
+  std::vector<Tile> tiles;
+  long long off = 0;
+  for (int s = 0; s < count; ++s) {
+    const fsi_batch_lattice& in = lattices[s];
+    FSI_REQUIRE(in.nx > 4 && in.ny > 4 && in.nz > 4, "lattice %d: %dx%dx%d too small", s, in.nx,
+                in.ny, in.nz);
+    const long long n = (long long)in.nx * in.ny * in.nz;
+    FSI_REQUIRE(19ll * n < (1ll << 31), "lattice %d too large for a batch", s);
+    FSI_REQUIRE(in.cell_offset == off, "lattice %d: cell_offset %lld, expected %lld", s,
+                (long long)in.cell_offset, off);
+    FSI_REQUIRE(in.s[0] == 0.f && in.s[3] == 0.f && in.s[5] == 0.f && in.s[7] == 0.f,
+                "lattice %d: conserved moments must have zero relaxation rate", s);
+    BatchLattice& L = host[s];
+    L.g = LbmGeom{in.nx, in.ny, in.nz, n};
+    L.off = off;
+    for (int q = 0; q < 19; ++q) {
+      L.s[q] = in.s[q];
+      L.shift[q] = storage == FSI_STORAGE_F32 ? 0.f : weight_of(q) * in.rho0;
+    }
+    L.rho0 = in.rho0;
+    for (int a = 0; a < 3; ++a) L.base[a] = in.base_force[a];
+    for (long long c = 0; c < n; c += kTileCells) tiles.push_back(Tile{s, (int)c});
+    off += n;
+  }
+  FSI_REQUIRE(tiles.size() < (1u << 31), "batch has too many tiles");
+  fsi_batch* b = new fsi_batch;
+  b->count = count;
+  b->ntiles = (int)tiles.size();
+  b->storage = storage;
+  b->arithmetic = arithmetic;
+  b->cells = off;
+  if (cudaMalloc(&b->lat, sizeof(BatchLattice) * count) != cudaSuccess ||
+      cudaMalloc(&b->tiles, sizeof(Tile) * tiles.size()) != cudaSuccess ||
+      cudaMemcpy(b->lat, host.data(), sizeof(BatchLattice) * count, cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaMemcpy(b->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+    const int e = check_launch("fsi_batch_create");
+    cudaFree(b->lat);
+    cudaFree(b->tiles);
+    delete b;
+    return e ? e : FSI_ERR_CUDA;
+  }
+  *out = b;
+  return FSI_OK;
+}
+
+extern "C" int fsi_batch_destroy(fsi_batch* b) {
+  if (!b) return FSI_OK;
+  cudaFree(b->lat);
+  cudaFree(b->tiles);
+  delete b;
+  return check_launch("fsi_batch_destroy");
+}
+
+extern "C" int fsi_batch_cells(const fsi_batch* b, int64_t* cells) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(cells != nullptr, "NULL output");
+  *cells = b->cells;
+  return FSI_OK;
+}
+
+extern "C" int fsi_batch_lbm_flags(const fsi_batch* b, const int32_t* solid, uint32_t* flags,
+                                   void* stream) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(solid && flags, "NULL array");
+  batch_flags_kernel<<<b->ntiles, kTileCells, 0, as_stream(stream)>>>(b->lat, b->tiles, solid, flags);
+  return check_launch("batch_flags_kernel");
+}
+
+extern "C" int fsi_batch_lbm_init(const fsi_batch* b, const float* u0, const uint32_t* flags,
+                                  void* pops, float* macro, void* stream) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(u0 && flags && pops && macro, "NULL array");
+  dispatch_batch<BatchInitLauncher>(b, u0, flags, pops, macro, as_stream(stream));
+  return check_launch("batch_init_kernel");
+}
+
+extern "C" int fsi_batch_lbm_step(const fsi_batch* b, void* pops, float* macro, const float* force,
+                                  const float* force_prev, const uint32_t* flags,
+                                  int64_t steps_done, void* stream) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(pops && macro && force && flags, "NULL array");
+  FSI_REQUIRE(steps_done >= 0, "steps_done must be non-negative");
+  BatchStepArgs a{b->lat, b->tiles, pops, macro, force, force_prev, flags};
+  dispatch_batch<BatchStepLauncher>(b, a, (steps_done & 1) != 0, force_prev != nullptr,
+                                    as_stream(stream));
+  return check_launch("batch_step_kernel");
+}
+
+extern "C" int fsi_batch_lbm_macro(const fsi_batch* b, const void* pops, const float* force,
+                                   const uint32_t* flags, int64_t steps_done, float* macro,
+                                   double* diag, void* stream) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(pops && force && flags && macro, "NULL array");
+  cudaStream_t s = as_stream(stream);
+  if (diag && cudaMemsetAsync(diag, 0, 2 * sizeof(double) * b->count, s) != cudaSuccess)
+    return check_launch("memset");
+  dispatch_batch<BatchMacroLauncher>(b, pops, force, flags, (int)(steps_done & 1), macro, diag, s);
+  return check_launch("batch_macro_kernel");
+}
+
+extern "C" int fsi_batch_lbm_distribution(const fsi_batch* b, const void* pops,
+                                          const uint32_t* flags, int64_t steps_done, float* out,
+                                          void* stream) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(pops && flags && out, "NULL array");
+  dispatch_batch<BatchDistLauncher>(b, pops, flags, (int)(steps_done & 1), out, as_stream(stream));
+  return check_launch("batch_distribution_kernel");
+}
+
+extern "C" int fsi_batch_lbm_base_force(const fsi_batch* b, const uint32_t* flags, float* force,
+                                        void* stream) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(flags && force, "NULL array");
+  batch_base_force_kernel<<<b->ntiles, kTileCells, 0, as_stream(stream)>>>(b->lat, b->tiles, flags,
+                                                                           force);
+  return check_launch("batch_base_force_kernel");
+}

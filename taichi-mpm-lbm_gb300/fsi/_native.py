@@ -92,7 +92,19 @@ class CouplingDesc(ctypes.Structure):
     ]
 
 
+class BatchLattice(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("cell_offset", ctypes.c_int64),
+        ("s", ctypes.c_float * 19),
+        ("rho0", ctypes.c_float),
+        ("base_force", c_float3),
+    ]
+
+
 _VP = ctypes.c_void_p
+_BATCH = ctypes.c_void_p
 _SIGNATURES = {
     "fsi_abi_version": ([], ctypes.c_int),
     "fsi_last_error": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_size_t),
@@ -113,6 +125,16 @@ _SIGNATURES = {
     "fsi_coupling_assemble": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(LbmDesc), _VP, ctypes.POINTER(ctypes.c_float), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_contact": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_coupling_reduce": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_batch_create": ([ctypes.POINTER(BatchLattice), ctypes.c_int32, ctypes.c_int32,
+                          ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "fsi_batch_destroy": ([_BATCH], ctypes.c_int),
+    "fsi_batch_cells": ([_BATCH, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "fsi_batch_lbm_flags": ([_BATCH, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_batch_lbm_init": ([_BATCH, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_batch_lbm_step": ([_BATCH, _VP, _VP, _VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "fsi_batch_lbm_macro": ([_BATCH, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_batch_lbm_distribution": ([_BATCH, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "fsi_batch_lbm_base_force": ([_BATCH, _VP, _VP, _VP], ctypes.c_int),
 }
 
 

@@ -244,6 +244,11 @@ class OutputConfig:
     write_mpm_particles: bool = True
     write_coupling_fields: bool = True
 
+    # Extension: compress and write NPZ snapshots on a background thread (the fields are
+    # copied to the host synchronously; FSISimulation.run waits for the writes before it
+    # returns). The reference writes synchronously.
+    async_write: bool = False
+
     def validate(self) -> None:
         if self.output_interval <= 0:
             raise ValueError("output_interval must be positive.")

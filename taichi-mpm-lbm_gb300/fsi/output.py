@@ -27,6 +27,23 @@ class SimulationOutputWriter:
         self.config = config
         self.config.validate()
         self.output_dir = Path(config.output_dir)
+        self._pool = None
+        self._pending: list = []
+
+    def _save(self, path: Path, arrays: dict) -> None:
+        if not getattr(self.config, "async_write", False):
+            np.savez_compressed(path, **arrays)
+            return
+        if self._pool is None:
+            from concurrent.futures import ThreadPoolExecutor
+            self._pool = ThreadPoolExecutor(max_workers=1, thread_name_prefix="fsi-snapshot")
+        self._pending.append(self._pool.submit(np.savez_compressed, path, **arrays))
+
+    def flush(self) -> None:
+        """Wait for snapshots still being written in the background; re-raises their errors."""
+        pending, self._pending = self._pending, []
+        for fut in pending:
+            fut.result()
 
     def ensure_output_dir(self) -> None:
         self.output_dir.mkdir(parents=True, exist_ok=True)
@@ -88,7 +105,7 @@ class SimulationOutputWriter:
                               "partial_support_particle_count"),
                              ("coupling_clipped_particle_count", "clipped_particle_count")):
                 arrays[key] = np.array(d[src], dtype=np.int32)
-        np.savez_compressed(path, **arrays)
+        self._save(path, arrays)
         return path
 
     def write_vtk_snapshot(self, sim: "FSISimulation") -> list[Path]:

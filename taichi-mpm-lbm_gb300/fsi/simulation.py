@@ -77,6 +77,7 @@ class FSISimulation:
             history.append(self.step())
             if write_output and self.output_writer.should_write(self.step_index):
                 self.write_snapshot()
+        self.output_writer.flush()
         return history
 
     def advance(self, steps: int, graph: bool = True) -> None:

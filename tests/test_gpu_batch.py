@@ -1,0 +1,80 @@
+"""Batched lattices (fsi.batch.LatticeBatch) against standalone LBMSolver3D runs of the same
+configurations: bit-identical in the exact form (shared per-cell code), within float32
+rounding in the fast forms (the pairing of cells into packed lanes differs)."""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+import pytest
+
+from fsi.batch import LatticeBatch
+from fsi.config import LBMConfig
+from fsi.lbm3d import LBMSolver3D, dhumieres_rates
+from helpers import PERIODIC, channel_mask, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def scenes(storage="f32", arithmetic="auto"):
+    rng = np.random.default_rng(4)
+    cfgs, masks = [], []
+    for n, tau, gx in ((12, 0.6, 1e-5), (9, 0.8, 3e-6), (16, 0.55, 7e-6), (10, 0.7, 0.0)):
+        shape = (n, n - 2, n + 1)
+        cfg = LBMConfig(nx=shape[0], ny=shape[1], nz=shape[2], viscosity=(tau - 0.5) / 3.0,
+                        force=(gx, 0.0, 1e-6), initial_velocity=(1e-3, 0.0, 0.0),
+                        population_storage=storage, collision_arithmetic=arithmetic, **PERIODIC)
+        m = channel_mask(*shape)
+        m[tuple(rng.integers(2, s - 2) for s in shape)] = 1
+        cfgs.append(cfg)
+        masks.append(m)
+    cfgs[3] = dataclasses.replace(cfgs[3], mrt_rates=dhumieres_rates(0.7))
+    return cfgs, masks
+
+
+def run_both(cfgs, masks, steps):
+    batch = LatticeBatch(cfgs)
+    batch.initialize(masks)
+    singles = []
+    for c, m in zip(cfgs, masks):
+        s = LBMSolver3D(c)
+        s.initialize(m)
+        singles.append(s)
+    for _ in range(steps):
+        batch.step()
+        for s in singles:
+            s.step()
+    return batch, singles
+
+
+@pytest.mark.parametrize("steps", [1, 6, 11])
+def test_exact_batch_is_bit_identical(steps):
+    cfgs, masks = scenes()
+    batch, singles = run_both(cfgs, masks, steps)
+    for i, s in enumerate(singles):
+        np.testing.assert_array_equal(batch.distribution_numpy(i), s.distribution_numpy())
+        np.testing.assert_array_equal(batch.velocity_numpy(i), s.velocity_numpy())
+        np.testing.assert_array_equal(batch.density_numpy(i), s.density_numpy())
+    diag = batch.mass_and_speed()
+    for i, s in enumerate(singles):
+        # float32 warp partial sums, float64 across warps: summation order differs
+        assert diag[i, 0] == pytest.approx(s.total_mass(), rel=1e-7)
+        assert diag[i, 1] == pytest.approx(s.max_velocity_norm(), rel=1e-6)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
+def test_fast_batch_matches_standalone(storage):
+    cfgs, masks = scenes(storage, "fast")
+    batch, singles = run_both(cfgs, masks, 9)
+    for i, s in enumerate(singles):
+        assert rel_l2(batch.distribution_numpy(i), s.distribution_numpy()) < 1e-6
+        assert rel_l2(batch.velocity_numpy(i), s.velocity_numpy()) < 1e-3
+
+
+def test_batch_rejects_mixed_forms_and_faces():
+    cfgs, _ = scenes()
+    with pytest.raises(ValueError):
+        LatticeBatch([cfgs[0], dataclasses.replace(cfgs[1], population_storage="f16")])
+    from fsi.config import BoundaryConfig
+    with pytest.raises(NotImplementedError):
+        LatticeBatch([dataclasses.replace(cfgs[0], x_left=BoundaryConfig("velocity"))])

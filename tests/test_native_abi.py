@@ -51,6 +51,7 @@ def test_invalid_descriptor_is_rejected_without_touching_the_gpu():
 
 def test_struct_sizes_match_header_layout():
     assert ctypes.sizeof(_native.LbmDesc) == 4 * (5 + 19 + 3 + 6 + 2)
+    assert ctypes.sizeof(_native.BatchLattice) == 4 * 4 + 8 + 4 * (19 + 1 + 3) + 4  # + tail pad
     assert ctypes.sizeof(_native.MpmDesc) == 4 * 20
     assert ctypes.sizeof(_native.Particles) == 8 * 11
     assert ctypes.sizeof(_native.CouplingDesc) == 4 * 18
