@@ -355,6 +355,39 @@ int fsi_batch_lbm_distribution(const fsi_batch* batch, const void* pops, const u
 int fsi_batch_lbm_base_force(const fsi_batch* batch, const uint32_t* flags, float* force,
                              void* stream);
 
+/* The solid and coupling of each scene of a batch (one entry per lattice, same order).
+ * Particles of all scenes live in one set of fsi_particles arrays of the batch's capacity;
+ * scene s owns particles [particle_offset, particle_offset + mpm.num_particles), with
+ * particle_offset a multiple of FSI_BATCH_PARTICLE_ALIGN and the ranges in scene order.
+ * mpm.nx/ny/nz must equal the lattice's; mpm.dt is the MPM substep. coupling carries the
+ * scene's penalty parameters and gamma_eff; dt_ratio and build_fraction are per call. The
+ * MPM grid is the batch's concatenated float4 [cells] array (scene blocks at cell_offset)
+ * and the dirty map one byte per 4^3 node block, scene blocks in scene order. */
+#define FSI_BATCH_PARTICLE_ALIGN 256
+typedef struct fsi_batch_solid {
+  fsi_mpm_desc mpm;
+  fsi_coupling_desc coupling;
+  int64_t particle_offset;
+} fsi_batch_solid;
+
+/* Validates and installs the scenes' solids (host array of fsi_batch_count entries);
+ * capacity is the particle arrays' length. Writes the dirty-map length to *dirty_blocks. */
+int fsi_batch_set_solids(fsi_batch* batch, const fsi_batch_solid* solids, int64_t capacity,
+                         int64_t* dirty_blocks);
+/* Sets every scene's gamma_eff (host float[count]). */
+int fsi_batch_set_gamma(fsi_batch* batch, const float* gamma_eff);
+/* fsi_mpm_substep / fsi_coupling_forces / fsi_coupling_assemble over every scene, with the
+ * same meaning per scene. counters: device fsi_coupling_counters[count]. */
+int fsi_batch_mpm_substep(const fsi_batch* batch, const fsi_particles* particles, float* grid,
+                          uint8_t* dirty, void* stream);
+int fsi_batch_coupling_forces(const fsi_batch* batch, const fsi_particles* particles,
+                              const float* macro, const uint32_t* flags, float* accum,
+                              float* valid_weight, int32_t* coupling_mask, void* counters,
+                              float dt_ratio, int32_t build_fraction, void* stream);
+int fsi_batch_coupling_assemble(const fsi_batch* batch, const uint32_t* flags, int32_t mode,
+                                float* accum, const float* macro, float* force, float* ib_force,
+                                void* counters, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,8 +10,10 @@
 #include <cstdint>
 #include <vector>
 
+#include "coupling_core.cuh"
 #include "fsi_common.cuh"
 #include "lbm_core.cuh"
+#include "mpm_core.cuh"
 
 struct fsi_batch;
 
@@ -31,7 +33,13 @@ struct BatchLattice {
 
 struct Tile {
   int lattice;
-  int first;  // first cell within the lattice
+  int first;  // first cell (lattice tiles), particle block or node block (solid tiles)
+};
+
+struct BatchSolid {
+  Mpm m;                  // n = end of the scene's particle range, cap = batch capacity
+  long long block_off;    // first 4^3 node block of the scene in the dirty map
+  fsi_coupling_desc c;
 };
 
 }  // namespace
@@ -45,6 +53,15 @@ struct fsi_batch {
   int storage = 0;
   int arithmetic = 0;
   long long cells = 0;
+  std::vector<fsi::BatchLattice> host;
+  // solids (fsi_batch_set_solids)
+  fsi::BatchSolid* sol = nullptr;   // device
+  fsi::Tile* ptiles = nullptr;      // device: (scene, particle block of kBlock particles)
+  fsi::Tile* ctiles = nullptr;      // device: (scene, first node block of 8)
+  int nptiles = 0;
+  int nctiles = 0;
+  long long capacity = 0;
+  std::vector<fsi::BatchSolid> host_sol;
 };
 
 namespace fsi {
@@ -295,6 +312,82 @@ int check_batch(const fsi_batch* b) {
   return FSI_OK;
 }
 
+// ------------------------------------------------------------------ solids
+
+// One CTA per (scene, block of kBlock particles): the single-solver P2G / G2P bodies on the
+// scene's grid block.
+__global__ void __launch_bounds__(kBlock)
+    batch_p2g_kernel(const BatchLattice* __restrict__ lat, const BatchSolid* __restrict__ sol,
+                     const Tile* __restrict__ ptiles, PView P, float4* grid_all, uint8_t* dirty_all) {
+  const Tile t = ptiles[blockIdx.x];
+  const Mpm m = sol[t.lattice].m;
+  p2g_body(m, P, grid_all + lat[t.lattice].off, dirty_all + sol[t.lattice].block_off,
+           t.first * kBlock + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kBlock)
+    batch_g2p_kernel(const BatchLattice* __restrict__ lat, const BatchSolid* __restrict__ sol,
+                     const Tile* __restrict__ ptiles, PView P, const float4* grid_all) {
+  const Tile t = ptiles[blockIdx.x];
+  const Mpm m = sol[t.lattice].m;
+  g2p_body(m, P, grid_all + lat[t.lattice].off, t.first * kBlock + threadIdx.x);
+}
+
+// One warp per node block: CTA (scene, first block) covers kBlock / 32 blocks.
+__global__ void __launch_bounds__(kBlock)
+    batch_clear_kernel(const BatchLattice* __restrict__ lat, const BatchSolid* __restrict__ sol,
+                       const Tile* __restrict__ ctiles, float4* grid_all, uint8_t* dirty_all) {
+  const Tile t = ctiles[blockIdx.x];
+  const Mpm m = sol[t.lattice].m;
+  clear_body(m, grid_all + lat[t.lattice].off, dirty_all + sol[t.lattice].block_off,
+             (long long)t.first + (threadIdx.x >> 5));
+}
+
+__global__ void __launch_bounds__(kBlock)
+    batch_coupling_forces_kernel(const BatchLattice* __restrict__ lat,
+                                 const BatchSolid* __restrict__ sol, const Tile* __restrict__ ptiles,
+                                 ForceArgs base, float dt_ratio, int build_fraction) {
+  const Tile t = ptiles[blockIdx.x];
+  const BatchLattice& L = lat[t.lattice];
+  const BatchSolid& S = sol[t.lattice];
+  ForceArgs a = base;
+  a.c = S.c;
+  a.c.dt_ratio = dt_ratio;
+  a.c.build_fraction = build_fraction;
+  a.g = Geo{L.g.nx, L.g.ny, L.g.nz, L.g.n};
+  a.n = S.m.n;
+  a.macro = base.macro + L.off;
+  a.flags = base.flags + L.off;
+  a.accum = base.accum + L.off;
+  a.cnt = base.cnt + t.lattice;
+  coupling_forces_body(a, t.first * kBlock + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kTileCells)
+    batch_assemble_kernel(const BatchLattice* __restrict__ lat, const BatchSolid* __restrict__ sol,
+                          const Tile* __restrict__ tiles, AssembleArgs base) {
+  const Tile t = tiles[blockIdx.x];
+  const BatchLattice& L = lat[t.lattice];
+  AssembleArgs a = base;
+  a.c = sol[t.lattice].c;
+  a.g = Geo{L.g.nx, L.g.ny, L.g.nz, L.g.n};
+  a.flags = base.flags + L.off;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) a.base[i] = L.base[i];
+  a.accum = base.accum + L.off;
+  a.macro = base.macro ? base.macro + L.off : nullptr;
+  a.force = base.force ? base.force + 3 * L.off : nullptr;
+  a.ib = base.ib ? base.ib + 3 * L.off : nullptr;
+  a.cnt = base.cnt + t.lattice;
+  assemble_body(a, (long long)t.first + threadIdx.x);
+}
+
+int check_solids(const fsi_batch* b) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(b->sol != nullptr, "the batch has no solids (fsi_batch_set_solids)");
+  return FSI_OK;
+}
+
 }  // namespace
 }  // namespace fsi
 
@@ -338,6 +431,7 @@ extern "C" int fsi_batch_create(const fsi_batch_lattice* lattices, int32_t count
   }
   FSI_REQUIRE(tiles.size() < (1u << 31), "batch has too many tiles");
   fsi_batch* b = new fsi_batch;
+  b->host = host;
   b->count = count;
   b->ntiles = (int)tiles.size();
   b->storage = storage;
@@ -363,6 +457,9 @@ extern "C" int fsi_batch_destroy(fsi_batch* b) {
   if (!b) return FSI_OK;
   cudaFree(b->lat);
   cudaFree(b->tiles);
+  cudaFree(b->sol);
+  cudaFree(b->ptiles);
+  cudaFree(b->ctiles);
   delete b;
   return check_launch("fsi_batch_destroy");
 }
@@ -430,4 +527,156 @@ extern "C" int fsi_batch_lbm_base_force(const fsi_batch* b, const uint32_t* flag
   batch_base_force_kernel<<<b->ntiles, kTileCells, 0, as_stream(stream)>>>(b->lat, b->tiles, flags,
                                                                            force);
   return check_launch("batch_base_force_kernel");
+}
+
+extern "C" int fsi_batch_set_solids(fsi_batch* b, const fsi_batch_solid* solids, int64_t capacity,
+                                    int64_t* dirty_blocks) {
+  if (int e = check_batch(b)) return e;
+  FSI_REQUIRE(solids != nullptr && dirty_blocks != nullptr, "NULL argument");
+  FSI_REQUIRE(capacity > 0 && capacity < (1ll << 31), "capacity %lld out of range",
+              (long long)capacity);
+  std::vector<BatchSolid> host(b->count);
+  std::vector<Tile> ptiles, ctiles;
+  long long next = 0, block_off = 0;
+  // make_mpm validates a descriptor against particle arrays; the batch's arrays are checked
+  // per call, so stand-in (never dereferenced) pointers satisfy its NULL checks here.
+  fsi_particles dummy{};
+  float stand_in = 0.f;
+  int32_t stand_in_i = 0;
+  dummy.x = dummy.v = dummy.C = dummy.F = dummy.force = dummy.mass = dummy.volume = &stand_in;
+  dummy.active = &stand_in_i;
+  dummy.capacity = capacity;
+  for (int s = 0; s < b->count; ++s) {
+    const fsi_batch_solid& in = solids[s];
+    const BatchLattice& L = b->host[s];
+    FSI_REQUIRE(in.mpm.nx == L.g.nx && in.mpm.ny == L.g.ny && in.mpm.nz == L.g.nz,
+                "scene %d: MPM grid differs from its lattice", s);
+    FSI_REQUIRE(in.particle_offset >= next && in.particle_offset % FSI_BATCH_PARTICLE_ALIGN == 0,
+                "scene %d: particle_offset %lld not aligned or overlapping", s,
+                (long long)in.particle_offset);
+    FSI_REQUIRE(in.particle_offset + in.mpm.num_particles <= capacity,
+                "scene %d: particles beyond the capacity", s);
+    BatchSolid& S = host[s];
+    PView unused;
+    fsi_mpm_desc d = in.mpm;
+    d.num_particles = 0;
+    if (int e = make_mpm(&d, &dummy, S.m, unused)) return e;
+    S.m.n = (int)(in.particle_offset + in.mpm.num_particles);
+    S.m.cap = capacity;
+    S.block_off = block_off;
+    S.c = in.coupling;
+    for (long long p = in.particle_offset; p < S.m.n; p += kBlock)
+      ptiles.push_back(Tile{s, (int)(p / kBlock)});
+    const long long nb = (long long)S.m.nbx * S.m.nby * S.m.nbz;
+    for (long long q = 0; q < nb; q += kBlock / 32) ctiles.push_back(Tile{s, (int)q});
+    block_off += nb;
+    next = S.m.n;
+  }
+  cudaFree(b->sol); cudaFree(b->ptiles); cudaFree(b->ctiles);
+  b->sol = nullptr; b->ptiles = b->ctiles = nullptr;
+  const size_t np = ptiles.size() ? ptiles.size() : 1;
+  if (cudaMalloc(&b->sol, sizeof(BatchSolid) * b->count) != cudaSuccess ||
+      cudaMalloc(&b->ptiles, sizeof(Tile) * np) != cudaSuccess ||
+      cudaMalloc(&b->ctiles, sizeof(Tile) * ctiles.size()) != cudaSuccess ||
+      cudaMemcpy(b->sol, host.data(), sizeof(BatchSolid) * b->count, cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      (ptiles.size() && cudaMemcpy(b->ptiles, ptiles.data(), sizeof(Tile) * ptiles.size(),
+                                   cudaMemcpyHostToDevice) != cudaSuccess) ||
+      cudaMemcpy(b->ctiles, ctiles.data(), sizeof(Tile) * ctiles.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+    const int e = check_launch("fsi_batch_set_solids");
+    cudaFree(b->sol); cudaFree(b->ptiles); cudaFree(b->ctiles);
+    b->sol = nullptr; b->ptiles = b->ctiles = nullptr;
+    return e ? e : FSI_ERR_CUDA;
+  }
+  b->host_sol = host;
+  b->nptiles = (int)ptiles.size();
+  b->nctiles = (int)ctiles.size();
+  b->capacity = capacity;
+  *dirty_blocks = block_off;
+  return FSI_OK;
+}
+
+extern "C" int fsi_batch_set_gamma(fsi_batch* b, const float* gamma_eff) {
+  if (int e = check_solids(b)) return e;
+  FSI_REQUIRE(gamma_eff != nullptr, "NULL gamma");
+  for (int s = 0; s < b->count; ++s) b->host_sol[s].c.gamma_eff = gamma_eff[s];
+  if (cudaMemcpy(b->sol, b->host_sol.data(), sizeof(BatchSolid) * b->count,
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return check_launch("fsi_batch_set_gamma");
+  return FSI_OK;
+}
+
+namespace {
+int particle_view(const fsi_batch* b, const fsi_particles* p, PView& v) {
+  FSI_REQUIRE(p != nullptr, "NULL particles");
+  FSI_REQUIRE(p->capacity == b->capacity, "particle capacity %lld differs from the batch's %lld",
+              (long long)p->capacity, b->capacity);
+  FSI_REQUIRE(p->x && p->v && p->C && p->F && p->mass && p->volume && p->active && p->force,
+              "NULL particle array");
+  FSI_REQUIRE((p->mu == nullptr) == (p->lam == nullptr), "per-particle mu and lam go together");
+  v.x = p->x; v.v = p->v; v.C = p->C; v.F = p->F; v.mass = p->mass; v.vol = p->volume;
+  v.active = p->active; v.fp = p->force; v.mu = p->mu; v.lam = p->lam;
+  return FSI_OK;
+}
+}  // namespace
+
+extern "C" int fsi_batch_mpm_substep(const fsi_batch* b, const fsi_particles* particles,
+                                     float* grid, uint8_t* dirty, void* stream) {
+  if (int e = check_solids(b)) return e;
+  FSI_REQUIRE(grid && dirty, "NULL array");
+  FSI_REQUIRE(((uintptr_t)grid & 15) == 0, "grid must be 16-byte aligned");
+  PView P;
+  if (int e = particle_view(b, particles, P)) return e;
+  if (b->nptiles == 0) return FSI_OK;
+  cudaStream_t s = as_stream(stream);
+  float4* g4 = reinterpret_cast<float4*>(grid);
+  batch_p2g_kernel<<<b->nptiles, kBlock, 0, s>>>(b->lat, b->sol, b->ptiles, P, g4, dirty);
+  if (int e = check_launch("batch_p2g_kernel")) return e;
+  batch_g2p_kernel<<<b->nptiles, kBlock, 0, s>>>(b->lat, b->sol, b->ptiles, P, g4);
+  if (int e = check_launch("batch_g2p_kernel")) return e;
+  batch_clear_kernel<<<b->nctiles, kBlock, 0, s>>>(b->lat, b->sol, b->ctiles, g4, dirty);
+  return check_launch("batch_clear_kernel");
+}
+
+extern "C" int fsi_batch_coupling_forces(const fsi_batch* b, const fsi_particles* particles,
+                                         const float* macro, const uint32_t* flags, float* accum,
+                                         float* valid_weight, int32_t* coupling_mask,
+                                         void* counters, float dt_ratio, int32_t build_fraction,
+                                         void* stream) {
+  if (int e = check_solids(b)) return e;
+  FSI_REQUIRE(macro && flags && accum && valid_weight && coupling_mask && counters, "NULL array");
+  PView P;
+  if (int e = particle_view(b, particles, P)) return e;
+  if (b->nptiles == 0) return FSI_OK;
+  ForceArgs a{};
+  a.cap = b->capacity;
+  a.x = P.x; a.v = P.v; a.mass = P.mass; a.vol = P.vol; a.active = P.active; a.fp = P.fp;
+  a.macro = reinterpret_cast<const float4*>(macro);
+  a.flags = flags;
+  a.accum = reinterpret_cast<float4*>(accum);
+  a.valid_out = valid_weight;
+  a.mask_out = coupling_mask;
+  a.cnt = reinterpret_cast<Cnt*>(counters);
+  batch_coupling_forces_kernel<<<b->nptiles, kBlock, 0, as_stream(stream)>>>(
+      b->lat, b->sol, b->ptiles, a, dt_ratio, build_fraction);
+  return check_launch("batch_coupling_forces_kernel");
+}
+
+extern "C" int fsi_batch_coupling_assemble(const fsi_batch* b, const uint32_t* flags, int32_t mode,
+                                           float* accum, const float* macro, float* force,
+                                           float* ib_force, void* counters, void* stream) {
+  if (int e = check_solids(b)) return e;
+  FSI_REQUIRE(flags && accum && counters, "NULL array");
+  FSI_REQUIRE(!(mode & FSI_ASSEMBLE_IB) || (macro && ib_force), "IB needs macro and ib_force");
+  AssembleArgs a{};
+  a.flags = flags;
+  a.mode = mode;
+  a.accum = reinterpret_cast<float4*>(accum);
+  a.macro = reinterpret_cast<const float4*>(macro);
+  a.force = force;
+  a.ib = ib_force;
+  a.cnt = reinterpret_cast<Cnt*>(counters);
+  batch_assemble_kernel<<<b->ntiles, kTileCells, 0, as_stream(stream)>>>(b->lat, b->sol, b->tiles, a);
+  return check_launch("batch_assemble_kernel");
 }

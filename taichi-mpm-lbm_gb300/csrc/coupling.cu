@@ -14,232 +14,17 @@
 #include <cstdint>
 
 #include "fsi_common.cuh"
+#include "coupling_core.cuh"
 
 namespace fsi {
 namespace {
 
-constexpr int kBlock = 256;
-
-struct Cnt {
-  int32_t unsupported, partial, clipped, contact_candidates, contact_damped, ib_active, ib_clipped,
-      pad;
-  float ib_total[4];
-};
-
-struct Geo {
-  int nx, ny, nz;
-  long long n;
-};
-
-__device__ __forceinline__ float bspline_w(float fx, int i) {
-  if (i == 0) { float a = __fsub_rn(1.5f, fx); return __fmul_rn(0.5f, __fmul_rn(a, a)); }
-  if (i == 1) { float b = __fsub_rn(fx, 1.0f); return __fsub_rn(0.75f, __fmul_rn(b, b)); }
-  float c = __fsub_rn(fx, 0.5f);
-  return __fmul_rn(0.5f, __fmul_rn(c, c));
-}
-
-__device__ __forceinline__ float norm3(float a, float b, float c) {
-  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c)));
-}
-
-__device__ __forceinline__ void stencil_base(float inv_dx, const float x[3], int base[3],
-                                             float fx[3]) {
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float g = __fmul_rn(x[a], inv_dx);
-    base[a] = (int)__fsub_rn(g, 0.5f);
-    fx[a] = __fsub_rn(g, (float)base[a]);
-  }
-}
-
-struct ForceArgs {
-  fsi_coupling_desc c;
-  Geo g;
-  int n;
-  long long cap;
-  const float* __restrict__ x;
-  const float* __restrict__ v;
-  const float* __restrict__ mass;
-  const float* __restrict__ vol;
-  const int32_t* __restrict__ active;
-  float* __restrict__ fp;
-  const float4* __restrict__ macro;
-  const uint32_t* __restrict__ flags;
-  float4* __restrict__ accum;
-  float* __restrict__ valid_out;
-  int32_t* __restrict__ mask_out;
-  Cnt* __restrict__ cnt;
-};
-
-// _compute_coupling_forces_kernel, fsi/coupling.py:332-406.
 __global__ void __launch_bounds__(kBlock) coupling_forces_kernel(ForceArgs a) {
-  const int p = blockIdx.x * kBlock + threadIdx.x;
-  const bool live = p < a.n;
-  const long long cap = a.cap;
-  bool partial = false, clipped = false, unsupported = false;
-  if (live) {
-    if (a.active[p] == 0) {
-      a.fp[p] = 0.f; a.fp[cap + p] = 0.f; a.fp[2 * cap + p] = 0.f;
-    } else {
-      const float x[3] = {a.x[p], a.x[cap + p], a.x[2 * cap + p]};
-      int base[3];
-      float fx[3];
-      stencil_base(a.c.inv_dx, x, base, fx);
-      float wv[3][3];
-#pragma unroll
-      for (int ax = 0; ax < 3; ++ax)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) wv[ax][i] = bspline_w(fx[ax], i);
-      float valid = 0.f, uf[3] = {0.f, 0.f, 0.f};
-      uint32_t usable = 0;  // bit s: node s of the stencil is in-grid and fluid
-#pragma unroll
-      for (int s = 0; s < 27; ++s) {
-        const int i = s / 9, j = (s / 3) % 3, k = s % 3;
-        const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
-        if (ni < 0 || ni >= a.g.nx || nj < 0 || nj >= a.g.ny || nk < 0 || nk >= a.g.nz) continue;
-        const long long c = ((long long)ni * a.g.ny + nj) * a.g.nz + nk;
-        if (a.flags[c] & kFlagSolid) continue;
-        usable |= 1u << s;
-        const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
-        valid = __fadd_rn(valid, w);
-        const float4 mc = a.macro[c];
-        uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc.x));
-        uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc.y));
-        uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc.z));
-      }
-      a.valid_out[p] = valid;
-      if (valid > a.c.min_valid_weight) {
-        partial = valid < __fsub_rn(1.0f, 1.0e-5f);
-        float dv[3];
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-          uf[ax] = __fdiv_rn(uf[ax], valid);
-          dv[ax] = __fsub_rn(uf[ax], a.v[ax * cap + p]);
-        }
-        if (a.c.use_rel_limit) {
-          const float nrm = norm3(dv[0], dv[1], dv[2]);
-          if (nrm > a.c.rel_limit && nrm > 0.f) {
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) dv[ax] = __fmul_rn(__fdiv_rn(dv[ax], nrm), a.c.rel_limit);
-            clipped = true;
-          }
-        }
-        const float gm = __fmul_rn(a.c.gamma_eff, a.mass[p]);
-        float pf[3] = {__fmul_rn(gm, dv[0]), __fmul_rn(gm, dv[1]), __fmul_rn(gm, dv[2])};
-        if (a.c.use_force_limit) {
-          const float nrm = norm3(pf[0], pf[1], pf[2]);
-          if (nrm > a.c.force_limit && nrm > 0.f) {
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) pf[ax] = __fmul_rn(__fdiv_rn(pf[ax], nrm), a.c.force_limit);
-            clipped = true;
-          }
-        }
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) a.fp[ax * cap + p] = pf[ax];
-        a.mask_out[p] = 1;
-        const float vp = a.vol[p];
-#pragma unroll
-        for (int s = 0; s < 27; ++s) {
-          if (!(usable & (1u << s))) continue;
-          const int i = s / 9, j = (s / 3) % 3, k = s % 3;
-          const long long c =
-              ((long long)(base[0] + i) * a.g.ny + (base[1] + j)) * a.g.nz + (base[2] + k);
-          const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
-          const float nw = __fdiv_rn(w, valid);
-          float add[3];
-#pragma unroll
-          for (int ax = 0; ax < 3; ++ax)
-            add[ax] = __fdiv_rn(__fmul_rn(__fmul_rn(-nw, pf[ax]), a.c.dt_ratio), a.c.cell_volume);
-          const float ph = a.c.build_fraction ? __fdiv_rn(__fmul_rn(nw, vp), a.c.cell_volume) : 0.f;
-          red_add_v4(a.accum + c, add[0], add[1], add[2], ph);
-        }
-      } else {
-        a.fp[p] = 0.f; a.fp[cap + p] = 0.f; a.fp[2 * cap + p] = 0.f;
-        a.mask_out[p] = 0;
-        unsupported = true;
-      }
-    }
-  }
-  warp_count(&a.cnt->unsupported, unsupported);
-  warp_count(&a.cnt->partial, partial);
-  warp_count(&a.cnt->clipped, clipped);
+  coupling_forces_body(a, blockIdx.x * kBlock + threadIdx.x);
 }
 
-struct AssembleArgs {
-  fsi_coupling_desc c;
-  Geo g;
-  const uint32_t* __restrict__ flags;
-  float base[3];
-  int mode;
-  float4* __restrict__ accum;
-  const float4* __restrict__ macro;
-  float* __restrict__ force;
-  float* __restrict__ ib;
-  Cnt* __restrict__ cnt;
-};
-
-// _clamp_solid_volume_fraction_kernel + reset_force + _apply_coupling_force_to_lbm_kernel +
-// _compute/_apply_immersed_boundary_force_kernel (coupling.py:408-461, lbm3d.py:504-510).
 __global__ void __launch_bounds__(kBlock) assemble_kernel(AssembleArgs a) {
-  const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-  bool ib_active = false, ib_clipped = false;
-  float ibf[3] = {0.f, 0.f, 0.f};
-  if (c < a.g.n) {
-    const bool fluid = !(a.flags[c] & kFlagSolid);
-    float4 acc = a.accum[c];
-    if (a.mode & FSI_ASSEMBLE_CLAMP_FRACTION) {
-      acc.w = fminf(acc.w, 1.0f);
-      a.accum[c].w = acc.w;
-    }
-    float f[3] = {fluid ? a.base[0] : 0.f, fluid ? a.base[1] : 0.f, fluid ? a.base[2] : 0.f};
-    if (a.mode & FSI_ASSEMBLE_COUPLING) {
-      f[0] = fluid ? __fadd_rn(f[0], acc.x) : 0.f;
-      f[1] = fluid ? __fadd_rn(f[1], acc.y) : 0.f;
-      f[2] = fluid ? __fadd_rn(f[2], acc.z) : 0.f;
-    }
-    if (a.mode & FSI_ASSEMBLE_IB) {
-      if (a.c.ib_enabled && a.c.ib_drag > 0.f && fluid) {
-        const float phi = acc.w;
-        if (phi > 0.f && phi >= a.c.ib_threshold) {
-          const float4 mc = a.macro[c];
-          const float s = __fmul_rn(__fmul_rn(-a.c.ib_drag, phi), mc.w);
-          ibf[0] = __fmul_rn(s, mc.x); ibf[1] = __fmul_rn(s, mc.y); ibf[2] = __fmul_rn(s, mc.z);
-          const float nrm = norm3(ibf[0], ibf[1], ibf[2]);
-          if (a.c.ib_use_max && nrm > a.c.ib_max_force && nrm > 0.f) {
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) ibf[ax] = __fmul_rn(__fdiv_rn(ibf[ax], nrm), a.c.ib_max_force);
-            ib_clipped = true;
-          }
-          ib_active = true;
-        }
-      }
-#pragma unroll
-      for (int ax = 0; ax < 3; ++ax) {
-        a.ib[ax * a.g.n + c] = ibf[ax];
-        f[ax] = fluid ? __fadd_rn(f[ax], ibf[ax]) : 0.f;
-      }
-    }
-    if (a.force) {
-#pragma unroll
-      for (int ax = 0; ax < 3; ++ax) a.force[ax * a.g.n + c] = f[ax];
-    }
-  }
-  if (a.mode & FSI_ASSEMBLE_IB) {
-    warp_count(&a.cnt->ib_active, ib_active);
-    warp_count(&a.cnt->ib_clipped, ib_clipped);
-    float t[3] = {ibf[0], ibf[1], ibf[2]};
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t[ax] += __shfl_down_sync(0xffffffffu, t[ax], o);
-    }
-    const bool warp_active = __any_sync(0xffffffffu, ib_active);
-    if ((threadIdx.x & 31) == 0 && warp_active) {
-      atomicAdd(&a.cnt->ib_total[0], t[0]);
-      atomicAdd(&a.cnt->ib_total[1], t[1]);
-      atomicAdd(&a.cnt->ib_total[2], t[2]);
-    }
-  }
+  assemble_body(a, (long long)blockIdx.x * kBlock + threadIdx.x);
 }
 
 struct ContactArgs {

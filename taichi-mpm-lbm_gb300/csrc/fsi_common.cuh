@@ -41,6 +41,17 @@ __host__ __device__ constexpr int ez(int q) {
   return (q == 5 || q == 11 || q == 14 || q == 15 || q == 18) ? 1
          : (q == 6 || q == 12 || q == 13 || q == 16 || q == 17) ? -1 : 0;
 }
+// Threads per block of the one-thread-per-item kernels.
+constexpr int kBlock = 256;
+
+// Quadratic B-spline weight of offset i (mpm3d.py:227-232).
+__device__ __forceinline__ float bspline_w(float fx, int i) {
+  if (i == 0) { float a = __fsub_rn(1.5f, fx); return __fmul_rn(0.5f, __fmul_rn(a, a)); }
+  if (i == 1) { float b = __fsub_rn(fx, 1.0f); return __fsub_rn(0.75f, __fmul_rn(b, b)); }
+  float c = __fsub_rn(fx, 0.5f);
+  return __fmul_rn(0.5f, __fmul_rn(c, c));
+}
+
 __host__ __device__ constexpr int opp(int q) { return q == 0 ? 0 : ((q & 1) ? q + 1 : q - 1); }
 
 // Lattice weights as the reference stores them: float32(1/3), float32(1/18), float32(1/36).

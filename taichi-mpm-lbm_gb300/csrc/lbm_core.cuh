@@ -14,7 +14,6 @@
 namespace fsi {
 namespace {
 
-constexpr int kBlock = 256;
 
 struct LbmGeom {
   int nx, ny, nz;

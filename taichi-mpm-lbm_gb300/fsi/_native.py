@@ -103,6 +103,12 @@ class BatchLattice(ctypes.Structure):
     ]
 
 
+class BatchSolid(ctypes.Structure):
+    _fields_ = [("mpm", MpmDesc), ("coupling", CouplingDesc), ("particle_offset", ctypes.c_int64)]
+
+
+BATCH_PARTICLE_ALIGN = 256
+
 _VP = ctypes.c_void_p
 _BATCH = ctypes.c_void_p
 _SIGNATURES = {
@@ -135,6 +141,14 @@ _SIGNATURES = {
     "fsi_batch_lbm_macro": ([_BATCH, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP, _VP], ctypes.c_int),
     "fsi_batch_lbm_distribution": ([_BATCH, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "fsi_batch_lbm_base_force": ([_BATCH, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_batch_set_solids": ([_BATCH, ctypes.POINTER(BatchSolid), ctypes.c_int64,
+                              ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "fsi_batch_set_gamma": ([_BATCH, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "fsi_batch_mpm_substep": ([_BATCH, ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),
+    "fsi_batch_coupling_forces": ([_BATCH, ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP, _VP,
+                                   ctypes.c_float, ctypes.c_int32, _VP], ctypes.c_int),
+    "fsi_batch_coupling_assemble": ([_BATCH, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP],
+                                    ctypes.c_int),
 }
 
 

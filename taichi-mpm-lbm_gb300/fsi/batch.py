@@ -183,3 +183,236 @@ class LatticeBatch:
             return out
         self._ensure_macro(diag=True)
         return self._diag.cpu().numpy()
+
+
+class SceneBatch:
+    """Many independent coupled LBM-MPM scenes stepped together (no reference counterpart).
+
+    Scene s behaves as ``FSISimulation(configs[s])`` stepped with ``coupler.step(lbm_dt)``:
+    per coupled step, ``substeps`` times (coupling forces, MPM substep), then force assembly
+    and the lattice step -- with each phase one launch over all scenes. All scenes share
+    lbm_dt, the number of substeps, the population storage form and periodic faces; contact
+    is not batched. ``run(steps)`` replays a captured CUDA graph of two coupled steps once
+    every scene's gamma ramp has finished (its gamma is then a constant of the graph).
+    """
+
+    def __init__(self, configs):
+        from .config import SimulationConfig  # noqa: F401  (type of configs)
+
+        if not configs:
+            raise ValueError("a batch needs at least one scene.")
+        for c in configs:
+            c.validate()
+            if c.coupling.contact_enabled:
+                raise NotImplementedError("contact is not batched.")
+            if not c.coupling.enabled:
+                raise NotImplementedError("a scene batch couples every scene.")
+        for key in ("build_solid_volume_fraction", "immersed_boundary_enabled"):
+            if len({bool(getattr(c.coupling, key)) for c in configs}) != 1:
+                raise ValueError(f"scenes of a batch share coupling.{key}.")
+        subs = {int(c.coupling.mpm_substeps_per_lbm_step) for c in configs}
+        dts = {float(c.lbm_dt) for c in configs}
+        if len(subs) != 1 or len(dts) != 1:
+            raise ValueError("scenes of a batch share lbm_dt and mpm_substeps_per_lbm_step.")
+        self.configs = list(configs)
+        self.count = len(configs)
+        self.substeps = subs.pop()
+        self.lbm_dt = dts.pop()
+        self.lattice = LatticeBatch([c.lbm for c in configs])
+        self._device = self.lattice._device
+        self.step_index = 0
+        self._coupled_step = 0
+        self._initialized = False
+
+    # ---------------------------------------------------------------- setup
+    def initialize(self, solids, positions, youngs_modulus=None, poisson_ratio=None) -> None:
+        """solids: per-scene masks (or None); positions: per-scene float32 (n_s, 3) arrays;
+        youngs_modulus / poisson_ratio: optional per-scene scalars or per-particle arrays."""
+        from .coupling import coupling_descriptor, gamma_for_step
+        from .mpm3d import MPMSolver3D, mpm_descriptor, particle_mass_volume
+
+        if len(positions) != self.count:
+            raise ValueError("one particle set per scene is required.")
+        self.lattice.initialize(solids)
+        align = nat.BATCH_PARTICLE_ALIGN
+        counts = [int(np.asarray(p).shape[0]) for p in positions]
+        offsets, off = [], 0
+        for n in counts:
+            offsets.append(off)
+            off += (n + align - 1) // align * align
+        cap = max(off, align)
+        self.particle_counts, self.particle_offsets, self.capacity = counts, offsets, cap
+        dev, f32 = self._device, torch.float32
+        x = np.zeros((3, cap), np.float32)
+        F = np.zeros((9, cap), np.float32)
+        mass = np.zeros(cap, np.float32)
+        vol = np.zeros(cap, np.float32)
+        active = np.zeros(cap, np.int32)
+        mu = np.zeros(cap, np.float32)
+        lam = np.zeros(cap, np.float32)
+        table = (nat.BatchSolid * self.count)()
+        mpm_dt = self.lbm_dt / float(self.substeps)
+        for s, (c, pos, o, n) in enumerate(zip(self.configs, positions, offsets, counts)):
+            p = np.asarray(pos, np.float32)
+            if p.ndim != 2 or p.shape[1] != 3 or n <= 0:
+                raise ValueError(f"positions of scene {s} must have shape (n, 3), n > 0.")
+            m, v = particle_mass_volume(c.mpm)
+            x[:, o:o + n] = p.T
+            F[[0, 4, 8], o:o + n] = 1.0
+            mass[o:o + n] = np.float32(m)
+            vol[o:o + n] = np.float32(v)
+            active[o:o + n] = 1
+            E = c.mpm.youngs_modulus if youngs_modulus is None else youngs_modulus[s]
+            nu = c.mpm.poisson_ratio if poisson_ratio is None else poisson_ratio[s]
+            mu_s, lam_s = MPMSolver3D.lame_parameters(np.broadcast_to(np.asarray(E, np.float64), (n,)),
+                                                      np.broadcast_to(np.asarray(nu, np.float64), (n,)))
+            mu[o:o + n] = mu_s.astype(np.float32)
+            lam[o:o + n] = lam_s.astype(np.float32)
+            t = table[s]
+            t.mpm = mpm_descriptor(c.mpm, dt=mpm_dt)
+            t.mpm.num_particles = n
+            t.coupling = coupling_descriptor(c.coupling, c.mpm.dx)
+            t.coupling.gamma_eff = gamma_for_step(c.coupling, 0)
+            t.particle_offset = o
+        self._per_particle_material = youngs_modulus is not None or poisson_ratio is not None
+        to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        self._x, self._F = to(x), to(F)
+        self._v = torch.zeros((3, cap), dtype=f32, device=dev)
+        self._C = torch.zeros((9, cap), dtype=f32, device=dev)
+        self._mass, self._vol, self._active = to(mass), to(vol), to(active)
+        self._force = torch.zeros((3, cap), dtype=f32, device=dev)
+        self._mu, self._lam = to(mu), to(lam)
+        parts = nat.Particles()
+        for name, t in (("x", self._x), ("v", self._v), ("C", self._C), ("F", self._F),
+                        ("mass", self._mass), ("volume", self._vol), ("active", self._active),
+                        ("force", self._force)):
+            setattr(parts, name, t.data_ptr())
+        parts.capacity = cap
+        if self._per_particle_material:
+            parts.mu, parts.lam = self._mu.data_ptr(), self._lam.data_ptr()
+        self._parts = parts
+        dirty = ctypes.c_int64()
+        nat.call("fsi_batch_set_solids", self.lattice._handle, table, cap, ctypes.byref(dirty))
+        n = self.lattice.cells
+        self._grid = torch.zeros((n, 4), dtype=f32, device=dev)
+        self._dirty = torch.zeros(max(int(dirty.value), 1), dtype=torch.uint8, device=dev)
+        self._accum = torch.zeros((n, 4), dtype=f32, device=dev)
+        self._ib = torch.zeros((3 * n,), dtype=f32, device=dev)
+        self._valid = torch.zeros(cap, dtype=f32, device=dev)
+        self._mask = torch.zeros(cap, dtype=torch.int32, device=dev)
+        self._counters = torch.zeros((self.count, 12), dtype=torch.int32, device=dev)
+        self._gamma_host = np.array([gamma_for_step(c.coupling, 0) for c in self.configs],
+                                    np.float32)
+        self._initialized = True
+
+    # ------------------------------------------------------------------ step
+    def _set_gamma(self) -> None:
+        from .coupling import gamma_for_step
+
+        g = np.array([gamma_for_step(c.coupling, self._coupled_step) for c in self.configs],
+                     np.float32)
+        if not np.array_equal(g, self._gamma_host):
+            nat.call("fsi_batch_set_gamma", self.lattice._handle,
+                     g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+            self._gamma_host = g
+
+    def _gamma_settled(self) -> bool:
+        return all(int(c.coupling.gamma_ramp_steps) <= 0
+                   or self._coupled_step + 1 >= int(c.coupling.gamma_ramp_steps)
+                   for c in self.configs)
+
+    def step(self) -> None:
+        """One coupled step of every scene (coupling.py:135-173 per scene)."""
+        if not self._initialized:
+            raise RuntimeError("SceneBatch.initialize must be called before step().")
+        self._set_gamma()
+        h, st = self.lattice._handle, nat.stream_ptr()
+        self._accum.zero_()
+        self._ib.zero_()
+        self._counters.zero_()
+        self._valid.zero_()
+        self._mask.zero_()
+        dt_ratio = float(np.float32((self.lbm_dt / self.substeps) / self.lbm_dt))
+        build = [bool(c.coupling.build_solid_volume_fraction) for c in self.configs]
+        for sub in range(self.substeps):
+            self._counters[:, 0:5].zero_()
+            nat.call("fsi_batch_coupling_forces", h, self._parts, nat.ptr(self.lattice.macro),
+                     nat.ptr(self.lattice.flags), nat.ptr(self._accum), nat.ptr(self._valid),
+                     nat.ptr(self._mask), nat.ptr(self._counters), dt_ratio,
+                     int(sub == 0 and all(build)), st)
+            nat.call("fsi_batch_mpm_substep", h, self._parts, nat.ptr(self._grid),
+                     nat.ptr(self._dirty), st)
+        mode = nat.ASSEMBLE_COUPLING | (nat.ASSEMBLE_CLAMP_FRACTION if all(build) else 0)
+        if any(c.coupling.immersed_boundary_enabled for c in self.configs):
+            mode |= nat.ASSEMBLE_IB
+            self._counters[:, 5:7].zero_()
+            self._counters[:, 8:12].zero_()
+        force = self.lattice.writable_force()
+        nat.call("fsi_batch_coupling_assemble", h, nat.ptr(self.lattice.flags), mode,
+                 nat.ptr(self._accum), nat.ptr(self.lattice.macro), nat.ptr(force),
+                 nat.ptr(self._ib), nat.ptr(self._counters), st)
+        self.lattice.step()
+        self._coupled_step += 1
+        self.step_index += 1
+
+    def _graph_state(self) -> tuple:
+        L = self.lattice
+        return (L._steps_done % 2, L._fcur, L._fprev, L._macro_fresh)
+
+    def run(self, steps: int, graph: bool = True) -> None:
+        """``steps`` coupled steps of every scene; the steady part as CUDA-graph replays."""
+        steps = int(steps)
+        if steps < 0:
+            raise ValueError("steps must be non-negative.")
+        L = self.lattice
+        if graph:
+            while steps > 0 and (not self._gamma_settled() or L._macro_fresh or L._fcur != L._fprev):
+                self.step()
+                steps -= 1
+        if not graph or steps < 4:
+            for _ in range(steps):
+                self.step()
+            return
+        before = self._graph_state()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step()
+            self.step()
+        g.replay()
+        steps -= 2
+        if self._graph_state() != before:
+            for _ in range(steps):
+                self.step()
+            return
+        while steps >= 2:
+            g.replay()
+            L._steps_done += 2
+            self._coupled_step += 2
+            self.step_index += 2
+            steps -= 2
+        if steps:
+            self.step()
+
+    # ------------------------------------------------------------- accessors
+    def _rows(self, t: torch.Tensor, s: int, width: int) -> np.ndarray:
+        o, n = self.particle_offsets[s], self.particle_counts[s]
+        return t[:, o:o + n].t().reshape(n, width).cpu().numpy().copy()
+
+    def positions_numpy(self, s: int) -> np.ndarray:
+        return self._rows(self._x, s, 3)
+
+    def velocities_numpy(self, s: int) -> np.ndarray:
+        return self._rows(self._v, s, 3)
+
+    def particle_forces_numpy(self, s: int) -> np.ndarray:
+        return self._rows(self._force, s, 3)
+
+    def density_numpy(self, s: int) -> np.ndarray:
+        return self.lattice.density_numpy(s)
+
+    def velocity_numpy(self, s: int) -> np.ndarray:
+        return self.lattice.velocity_numpy(s)
+
+    def counters_numpy(self) -> np.ndarray:
+        """fsi_coupling_counters of every scene as int32[count, 12]."""
+        return self._counters.cpu().numpy()

@@ -24,6 +24,39 @@ from .mpm3d import MPMSolver3D
 _SUPPORT_TOLERANCE = 1.0e-5
 
 
+def coupling_descriptor(config: CouplingConfig, dx: float) -> nat.CouplingDesc:
+    """The C-ABI descriptor of the coupling parameters (gamma_eff, dt_ratio and
+    build_fraction are set per call)."""
+    c, d = config, nat.CouplingDesc()
+    f32 = lambda v: float(np.float32(v))  # noqa: E731
+    d.cell_volume = f32(float(dx) ** 3)
+    d.inv_dx = f32(1.0 / float(dx))
+    d.min_valid_weight = f32(c.min_valid_weight)
+    d.use_rel_limit = int(c.relative_velocity_limit is not None)
+    d.rel_limit = f32(c.relative_velocity_limit or 0.0)
+    d.use_force_limit = int(c.force_limit is not None)
+    d.force_limit = f32(c.force_limit or 0.0)
+    d.ib_enabled = int(c.immersed_boundary_enabled)
+    d.ib_drag = f32(c.immersed_boundary_drag)
+    d.ib_threshold = f32(c.immersed_boundary_fraction_threshold)
+    d.ib_use_max = int(c.immersed_boundary_max_force is not None)
+    d.ib_max_force = f32(c.immersed_boundary_max_force or 0.0)
+    d.contact_enabled = int(c.contact_enabled)
+    d.contact_threshold = f32(c.contact_fraction_threshold)
+    d.contact_damping = f32(c.contact_velocity_damping)
+    return d
+
+
+def gamma_for_step(config: CouplingConfig, coupled_step: int) -> float:
+    """_effective_gamma of coupling.py:321-330, evaluated in float32."""
+    g = np.float32(config.gamma)
+    ramp = int(config.gamma_ramp_steps)
+    if ramp > 0:
+        r = (np.float32(coupled_step) + np.float32(1.0)) / np.float32(ramp)
+        g = np.float32(g * min(np.float32(1.0), r))
+    return float(g)
+
+
 class LBMMpmCoupler:
     """Explicit partitioned penalty coupling between the LBM and MPM solvers."""
 
@@ -70,33 +103,11 @@ class LBMMpmCoupler:
             raise ValueError("MPM dx must be positive.")
 
     def _fill_desc(self) -> None:
-        c, d = self.config, self._desc
-        f32 = lambda v: float(np.float32(v))  # noqa: E731
-        d.cell_volume = f32(self.cell_volume)
-        d.inv_dx = f32(self.inv_dx)
-        d.min_valid_weight = f32(c.min_valid_weight)
-        d.use_rel_limit = int(c.relative_velocity_limit is not None)
-        d.rel_limit = f32(c.relative_velocity_limit or 0.0)
-        d.use_force_limit = int(c.force_limit is not None)
-        d.force_limit = f32(c.force_limit or 0.0)
-        d.ib_enabled = int(self.immersed_boundary_enabled)
-        d.ib_drag = f32(c.immersed_boundary_drag)
-        d.ib_threshold = f32(c.immersed_boundary_fraction_threshold)
-        d.ib_use_max = int(c.immersed_boundary_max_force is not None)
-        d.ib_max_force = f32(c.immersed_boundary_max_force or 0.0)
-        d.contact_enabled = int(self.contact_enabled)
-        d.contact_threshold = f32(c.contact_fraction_threshold)
-        d.contact_damping = f32(c.contact_velocity_damping)
+        self._desc = coupling_descriptor(self.config, self.mpm.dx)
 
     # ------------------------------------------------------------ stepping
     def _gamma_for_kernel(self) -> float:
-        """_effective_gamma of coupling.py:321-330, evaluated in float32."""
-        g = np.float32(self.config.gamma)
-        ramp = int(self.config.gamma_ramp_steps)
-        if ramp > 0:
-            r = (np.float32(self._coupled_step) + np.float32(1.0)) / np.float32(ramp)
-            g = np.float32(g * min(np.float32(1.0), r))
-        return float(g)
+        return gamma_for_step(self.config, self._coupled_step)
 
     def _coupling_kernel(self, dt_ratio: float, build_fraction: bool) -> None:
         self._desc.gamma_eff = self._gamma_for_kernel()

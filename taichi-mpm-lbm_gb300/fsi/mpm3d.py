@@ -17,6 +17,43 @@ from . import _native as nat
 from .config import MPMConfig
 
 
+def mpm_descriptor(config: MPMConfig, dt: float | None = None) -> nat.MpmDesc:
+    """The C-ABI descriptor of a solver with this configuration (num_particles 0)."""
+    d = nat.MpmDesc()
+    d.nx, d.ny, d.nz = int(config.nx), int(config.ny), int(config.nz)
+    d.num_particles = 0
+    dx = float(config.dx)
+    d.dt = float(np.float32(config.dt if dt is None else dt))
+    d.dx = float(np.float32(dx))
+    d.inv_dx = float(np.float32(1.0 / dx))
+    E, nu = config.youngs_modulus, config.poisson_ratio
+    d.mu = float(np.float32(E / (2.0 * (1.0 + nu))))  # Lame parameters, mpm3d.py:33-38
+    d.lam = float(np.float32(E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))))
+    for i in range(3):
+        d.gravity[i] = float(np.float32(config.gravity[i]))
+    d.boundary_damping = float(np.float32(config.boundary_damping))
+    d.boundary_width = int(config.boundary_width)
+    d.apic = 1 if config.apic else 0
+    # position clamp of mpm3d.py:320-328
+    d.clamp_lower = float(np.float32(0.5 * dx))
+    for i, n in enumerate((config.nx, config.ny, config.nz)):
+        d.clamp_upper[i] = float(np.float32((n - 1.5) * dx))
+    d.material = 1 if config.constitutive_model == "neo_hookean" else 0
+    return d
+
+
+def particle_mass_volume(config: MPMConfig, particle_mass=None, particle_volume=None):
+    """Per-particle (mass, volume) of mpm3d.py:135-140: volume dx^3 / ppc^3, mass rho V."""
+    volume = (float(particle_volume) if particle_volume is not None
+              else float(config.dx) ** 3 / float(config.particles_per_cell ** 3))
+    if volume <= 0.0:
+        raise ValueError("particle_volume must be positive.")
+    mass = float(particle_mass) if particle_mass is not None else float(config.density) * volume
+    if mass <= 0.0:
+        raise ValueError("particle_mass must be positive.")
+    return mass, volume
+
+
 class MPMSolver3D:
     """Standalone dense 3D elastic MLS-MPM solver (GPU)."""
 
@@ -65,25 +102,7 @@ class MPMSolver3D:
 
     # ----------------------------------------------------------------- setup
     def _make_desc(self) -> nat.MpmDesc:
-        d = nat.MpmDesc()
-        d.nx, d.ny, d.nz = self.nx, self.ny, self.nz
-        d.num_particles = 0
-        d.dt = float(np.float32(self.dt_default))
-        d.dx = float(np.float32(self.dx))
-        d.inv_dx = float(np.float32(self.inv_dx))
-        d.mu = float(np.float32(self.mu))
-        d.lam = float(np.float32(self.lam))
-        for i in range(3):
-            d.gravity[i] = float(np.float32(self.config.gravity[i]))
-        d.boundary_damping = float(np.float32(self.boundary_damping))
-        d.boundary_width = self.boundary_width
-        d.apic = 1 if self.apic else 0
-        # position clamp of mpm3d.py:320-328
-        d.clamp_lower = float(np.float32(0.5 * self.dx))
-        for i, n in enumerate((self.nx, self.ny, self.nz)):
-            d.clamp_upper[i] = float(np.float32((n - 1.5) * self.dx))
-        d.material = 1 if self.config.constitutive_model == "neo_hookean" else 0
-        return d
+        return mpm_descriptor(self.config)
 
     @staticmethod
     def lame_parameters(youngs_modulus, poisson_ratio):
@@ -169,13 +188,7 @@ class MPMSolver3D:
             vel = np.asarray(velocities, dtype=np.float32)
             if vel.shape != (count, 3):
                 raise ValueError(f"velocities must have shape {(count, 3)}, got {vel.shape}.")
-        volume = (float(particle_volume) if particle_volume is not None
-                  else self.dx ** 3 / float(self.config.particles_per_cell ** 3))
-        if volume <= 0.0:
-            raise ValueError("particle_volume must be positive.")
-        mass = float(particle_mass) if particle_mass is not None else float(self.config.density) * volume
-        if mass <= 0.0:
-            raise ValueError("particle_mass must be positive.")
+        mass, volume = particle_mass_volume(self.config, particle_mass, particle_volume)
 
         for t in (self._x, self._v, self._C, self._F, self._mass, self._volume, self._active,
                   self._force):

@@ -78,3 +78,65 @@ def test_batch_rejects_mixed_forms_and_faces():
     from fsi.config import BoundaryConfig
     with pytest.raises(NotImplementedError):
         LatticeBatch([dataclasses.replace(cfgs[0], x_left=BoundaryConfig("velocity"))])
+
+
+def coupled_scenes():
+    from fsi import scenes as sc
+    from fsi.config import CouplingConfig, MPMConfig, SimulationConfig
+    rng = np.random.default_rng(5)
+    cfgs, masks, pos, young = [], [], [], []
+    for n, tau, gx, E in ((20, 0.6, 1e-5, 0.05), (16, 0.7, 4e-6, 0.08), (24, 0.55, 7e-6, 0.03)):
+        shape = (n + 4, n, n - 2)
+        lbm = LBMConfig(nx=shape[0], ny=shape[1], nz=shape[2], viscosity=(tau - 0.5) / 3.0,
+                        force=(gx, 0.0, 0.0), **PERIODIC)
+        mpm = MPMConfig(nx=shape[0], ny=shape[1], nz=shape[2], max_particles=4096,
+                        particles_per_cell=2, dx=1.0, dt=0.1, density=1.5, youngs_modulus=E,
+                        poisson_ratio=0.3, gravity=(0.0, 0.0, 0.0), boundary_width=3)
+        cfgs.append(SimulationConfig(num_steps=10, lbm_dt=1.0, lbm=lbm, mpm=mpm,
+                                     coupling=CouplingConfig(gamma=0.1, mpm_substeps_per_lbm_step=4,
+                                                             gamma_ramp_steps=3)))
+        masks.append(sc.wall_mask(*shape))
+        lo = rng.integers(5, 8, size=3)
+        pos.append(sc.cube_particles(lo, 5, 2, rng))
+        young.append(E)
+    return cfgs, masks, pos, young
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_scene_batch_matches_standalone_simulations(graph):
+    from fsi.batch import SceneBatch
+    from fsi.simulation import FSISimulation
+    cfgs, masks, pos, _ = coupled_scenes()
+    steps = 9
+    batch = SceneBatch(cfgs)
+    batch.initialize(masks, pos)
+    batch.run(steps, graph=graph)
+    assert batch.step_index == steps
+    counters = batch.counters_numpy()
+    for s, (c, m, p) in enumerate(zip(cfgs, masks, pos)):
+        sim = FSISimulation(c)
+        sim.initialize_lbm(m)
+        sim.initialize_mpm_from_numpy(p)
+        for _ in range(steps):
+            sim.coupler.step(c.lbm_dt)
+        assert rel_l2(batch.density_numpy(s), sim.lbm.density_numpy()) < 1e-5
+        assert rel_l2(batch.velocity_numpy(s), sim.lbm.velocity_numpy()) < 2.5e-4
+        assert rel_l2(batch.positions_numpy(s), sim.mpm.positions_numpy()) < 1e-5
+        assert rel_l2(batch.velocities_numpy(s), sim.mpm.velocities_numpy()) < 1e-3
+        d = sim.coupler.coupling_diagnostics()
+        assert counters[s, 0] == d["unsupported_particle_count"]
+        assert counters[s, 1] == d["partial_support_particle_count"]
+
+
+def test_scene_batch_per_particle_stiffness():
+    """Per-scene Young's modulus given to initialize() equals the scenes' own configuration."""
+    from fsi.batch import SceneBatch
+    cfgs, masks, pos, young = coupled_scenes()
+    a = SceneBatch(cfgs)
+    a.initialize(masks, pos)
+    b = SceneBatch(cfgs)
+    b.initialize(masks, pos, youngs_modulus=young, poisson_ratio=[0.3] * 3)
+    a.run(4, graph=False)
+    b.run(4, graph=False)
+    for s in range(3):
+        assert rel_l2(b.positions_numpy(s), a.positions_numpy(s)) < 1e-6
