@@ -335,6 +335,12 @@ int fsi_batch_destroy(fsi_batch* batch);
 /* Total cells of the batch (the length of the concatenated per-cell arrays). */
 int fsi_batch_cells(const fsi_batch* batch, int64_t* cells);
 
+/* Launch parameters of the batched lattice step, chosen by a caller's autotuner: cells per
+ * thread block (a multiple of 128, or of 256 for the fast forms; default 256) and the
+ * register-cap variant 0..2 (default 1). The exact form's results do not depend on them; the
+ * fast forms' may differ in the last bits (the assembler schedules each variant apart). */
+int fsi_batch_tune(fsi_batch* batch, int32_t step_tile_cells, int32_t variant);
+
 /* fsi_lbm_build_flags / fsi_lbm_init_fields / fsi_lbm_step / fsi_lbm_update_macro /
  * fsi_lbm_distribution over every lattice of the batch, with the same meaning per lattice.
  * u0: device float[count][3]. diag: NULL or device double[count][2] (sum of rho over fluid

@@ -10,37 +10,12 @@
 #include <cstdint>
 #include <vector>
 
-#include "coupling_core.cuh"
-#include "fsi_common.cuh"
-#include "lbm_core.cuh"
-#include "mpm_core.cuh"
+#include "batch_types.cuh"
 
 struct fsi_batch;
 
 namespace fsi {
 namespace {
-
-constexpr int kTileCells = 256;
-
-struct BatchLattice {
-  LbmGeom g;
-  long long off;  // first cell in the concatenated arrays
-  float s[19];
-  float shift[19];
-  float rho0;
-  float base[3];
-};
-
-struct Tile {
-  int lattice;
-  int first;  // first cell (lattice tiles), particle block or node block (solid tiles)
-};
-
-struct BatchSolid {
-  Mpm m;                  // n = end of the scene's particle range, cap = batch capacity
-  long long block_off;    // first 4^3 node block of the scene in the dirty map
-  fsi_coupling_desc c;
-};
 
 }  // namespace
 }  // namespace fsi
@@ -55,6 +30,10 @@ struct fsi_batch {
   long long cells = 0;
   std::vector<fsi::BatchLattice> host;
   // solids (fsi_batch_set_solids)
+  fsi::Tile* step_tiles = nullptr;  // device: tiles of the step kernel (fsi_batch_tune)
+  int nstep_tiles = 0;
+  int step_tile_cells = 0;
+  int variant = 1;
   fsi::BatchSolid* sol = nullptr;   // device
   fsi::Tile* ptiles = nullptr;      // device: (scene, particle block of kBlock particles)
   fsi::Tile* ctiles = nullptr;      // device: (scene, first node block of 8)
@@ -66,82 +45,6 @@ struct fsi_batch {
 
 namespace fsi {
 namespace {
-
-// The lattice of a tile as the argument type of step_cells.
-struct LatticeView {
-  LbmGeom g;
-  void* __restrict__ pops;
-  float4* __restrict__ macro;
-  const float* __restrict__ force;
-  const float* __restrict__ force_prev;
-  const uint32_t* __restrict__ flags;
-  const float* s;
-  const float* shift;
-  int write_faces;
-};
-
-template <int kStore>
-__device__ __forceinline__ LatticeView view_of(const BatchLattice& L, void* pops, float* macro,
-                                               const float* force, const float* force_prev,
-                                               const uint32_t* flags) {
-  using T = typename Store<kStore>::T;
-  LatticeView v;
-  v.g = L.g;
-  v.pops = reinterpret_cast<T*>(pops) + 19 * L.off;
-  v.macro = reinterpret_cast<float4*>(macro) + L.off;
-  v.force = force + 3 * L.off;
-  v.force_prev = force_prev ? force_prev + 3 * L.off : nullptr;
-  v.flags = flags + L.off;
-  v.s = L.s;
-  v.shift = L.shift;
-  v.write_faces = 0;
-  return v;
-}
-
-__device__ __forceinline__ void cell_ijk(const LbmGeom& g, int c, int& i, int& j, int& k) {
-  const int nyz = g.ny * g.nz;
-  i = c / nyz;
-  const int r = c - i * nyz;
-  j = r / g.nz;
-  k = r - j * g.nz;
-}
-
-struct BatchStepArgs {
-  const BatchLattice* lat;
-  const Tile* tiles;
-  void* pops;
-  float* macro;
-  const float* force;
-  const float* force_prev;
-  const uint32_t* flags;
-};
-
-// kStepBlock threads cover a tile of kTileCells cells: the exact form takes cells t and
-// t + kStepBlock one after the other, the fast forms take them as the two packed lanes.
-template <int kStore, bool kFast, bool kOdd, bool kRecompute>
-__global__ void __launch_bounds__(kStepBlock, (step_min_blocks<kFast, kOdd>()))
-    batch_step_kernel(BatchStepArgs b) {
-  constexpr int NL = StepLanes<kFast>::n;
-  constexpr int kReps = kTileCells / (kStepBlock * NL);
-  const Tile t = b.tiles[blockIdx.x];
-  const BatchLattice& L = b.lat[t.lattice];
-  const LatticeView v = view_of<kStore>(L, b.pops, b.macro, b.force, b.force_prev, b.flags);
-  const int n = (int)L.g.n;
-#pragma unroll
-  for (int r = 0; r < kReps; ++r) {
-    int ci[NL], cj[NL], ck[NL];
-    bool has[NL];
-    bool any = false;
-#pragma unroll
-    for (int l = 0; l < NL; ++l) {
-      const int c = t.first + threadIdx.x + (r * NL + l) * kStepBlock;
-      has[l] = c < n;
-      any = any || has[l];
-      cell_ijk(L.g, has[l] ? c : t.first, ci[l], cj[l], ck[l]);
-    }
-    if (any) step_cells<kStore, kFast, kOdd, kRecompute, LatticeView>(v, ci, cj, ck, has);
-  }
-}
 
 // update_macro of every lattice (lbm3d.py:409-425), optionally with each lattice's sum of
 // rho over fluid cells and max |u| (lbm3d.py:450-457) in diag[2 * lattice + {0, 1}].
@@ -254,21 +157,6 @@ __global__ void __launch_bounds__(kTileCells)
 #pragma unroll
   for (int a = 0; a < 3; ++a) force[a * L.g.n + c] = fluid ? L.base[a] : 0.f;
 }
-
-template <int S, bool F>
-struct BatchStepLauncher {
-  static void run(const fsi_batch* b, const BatchStepArgs& a, bool odd, bool recompute,
-                  cudaStream_t s) {
-    const dim3 grid(b->ntiles), block(kStepBlock);
-    if (recompute) {
-      if (odd) batch_step_kernel<S, F, true, true><<<grid, block, 0, s>>>(a);
-      else batch_step_kernel<S, F, false, true><<<grid, block, 0, s>>>(a);
-    } else {
-      if (odd) batch_step_kernel<S, F, true, false><<<grid, block, 0, s>>>(a);
-      else batch_step_kernel<S, F, false, false><<<grid, block, 0, s>>>(a);
-    }
-  }
-};
 
 template <int S, bool F>
 struct BatchMacroLauncher {
@@ -449,6 +337,9 @@ extern "C" int fsi_batch_create(const fsi_batch_lattice* lattices, int32_t count
     delete b;
     return e ? e : FSI_ERR_CUDA;
   }
+  b->step_tiles = b->tiles;
+  b->nstep_tiles = b->ntiles;
+  b->step_tile_cells = kTileCells;
   *out = b;
   return FSI_OK;
 }
@@ -457,6 +348,7 @@ extern "C" int fsi_batch_destroy(fsi_batch* b) {
   if (!b) return FSI_OK;
   cudaFree(b->lat);
   cudaFree(b->tiles);
+  if (b->step_tiles != b->tiles) cudaFree(b->step_tiles);
   cudaFree(b->sol);
   cudaFree(b->ptiles);
   cudaFree(b->ctiles);
@@ -493,10 +385,49 @@ extern "C" int fsi_batch_lbm_step(const fsi_batch* b, void* pops, float* macro, 
   if (int e = check_batch(b)) return e;
   FSI_REQUIRE(pops && macro && force && flags, "NULL array");
   FSI_REQUIRE(steps_done >= 0, "steps_done must be non-negative");
-  BatchStepArgs a{b->lat, b->tiles, pops, macro, force, force_prev, flags};
-  dispatch_batch<BatchStepLauncher>(b, a, (steps_done & 1) != 0, force_prev != nullptr,
-                                    as_stream(stream));
-  return check_launch("batch_step_kernel");
+  const bool fast = b->arithmetic == FSI_ARITH_FAST, odd = (steps_done & 1) != 0;
+  const bool recompute = force_prev != nullptr;
+  cudaStream_t s = as_stream(stream);
+  switch (b->storage) {
+    case FSI_STORAGE_F16:
+      return batch_step_launch_f16(b->lat, b->step_tiles, b->nstep_tiles, b->step_tile_cells,
+                                   b->variant, fast, odd, recompute, pops, macro, force,
+                                   force_prev, flags, s);
+    case FSI_STORAGE_BF16:
+      return batch_step_launch_bf16(b->lat, b->step_tiles, b->nstep_tiles, b->step_tile_cells,
+                                    b->variant, fast, odd, recompute, pops, macro, force,
+                                    force_prev, flags, s);
+    default:
+      return batch_step_launch_f32(b->lat, b->step_tiles, b->nstep_tiles, b->step_tile_cells,
+                                   b->variant, fast, odd, recompute, pops, macro, force,
+                                   force_prev, flags, s);
+  }
+}
+
+extern "C" int fsi_batch_tune(fsi_batch* b, int32_t step_tile_cells, int32_t variant) {
+  if (int e = check_batch(b)) return e;
+  const int lanes = b->arithmetic == FSI_ARITH_FAST ? 2 : 1;
+  FSI_REQUIRE(step_tile_cells > 0 && step_tile_cells % (kStepBlock * lanes) == 0 &&
+                  step_tile_cells <= 8192,
+              "step tile of %d cells is not a multiple of %d (at most 8192)", step_tile_cells,
+              kStepBlock * lanes);
+  FSI_REQUIRE(variant >= 0 && variant <= 2, "unknown variant %d", variant);
+  std::vector<Tile> tiles;
+  for (int s = 0; s < b->count; ++s)
+    for (long long c = 0; c < b->host[s].g.n; c += step_tile_cells) tiles.push_back(Tile{s, (int)c});
+  Tile* dev = nullptr;
+  if (cudaMalloc(&dev, sizeof(Tile) * tiles.size()) != cudaSuccess ||
+      cudaMemcpy(dev, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+    cudaFree(dev);
+    return check_launch("fsi_batch_tune");
+  }
+  if (b->step_tiles != b->tiles) cudaFree(b->step_tiles);
+  b->step_tiles = dev;
+  b->nstep_tiles = (int)tiles.size();
+  b->step_tile_cells = step_tile_cells;
+  b->variant = variant;
+  return FSI_OK;
 }
 
 extern "C" int fsi_batch_lbm_macro(const fsi_batch* b, const void* pops, const float* force,

@@ -141,6 +141,7 @@ _SIGNATURES = {
     "fsi_batch_lbm_macro": ([_BATCH, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP, _VP], ctypes.c_int),
     "fsi_batch_lbm_distribution": ([_BATCH, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "fsi_batch_lbm_base_force": ([_BATCH, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_batch_tune": ([_BATCH, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "fsi_batch_set_solids": ([_BATCH, ctypes.POINTER(BatchSolid), ctypes.c_int64,
                               ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "fsi_batch_set_gamma": ([_BATCH, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),

@@ -73,6 +73,26 @@ class LatticeBatch:
         self._fcur = 0
         self._fprev = -1
         self._initialized = False
+        self.tuning = {"step_tile_cells": 256, "variant": 1}
+
+    # ------------------------------------------------------------ state / tuning
+    def snapshot(self) -> dict:
+        """Device copies of the lattice state and its host bookkeeping."""
+        return {"pops": self._pops.clone(), "macro": self._macro.clone(),
+                "force": [f.clone() for f in self._force_buf],
+                "host": (self._steps_done, self._macro_fresh, self._fcur, self._fprev)}
+
+    def restore(self, snap: dict) -> None:
+        self._pops.copy_(snap["pops"])
+        self._macro.copy_(snap["macro"])
+        for dst, src in zip(self._force_buf, snap["force"]):
+            dst.copy_(src)
+        self._steps_done, self._macro_fresh, self._fcur, self._fprev = snap["host"]
+
+    def autotune(self, steps: int = 4, use_cache: bool = True) -> dict:
+        """Pick the step kernel's launch parameters for this batch (fsi.autotune)."""
+        from .autotune import tune_lattice_batch
+        return tune_lattice_batch(self, steps=steps, use_cache=use_cache)
 
     def __del__(self):
         handle = getattr(self, "_handle", None)
@@ -354,6 +374,10 @@ class SceneBatch:
         self.lattice.step()
         self._coupled_step += 1
         self.step_index += 1
+
+    def autotune(self, steps: int = 4, use_cache: bool = True) -> dict:
+        """Tune the batched lattice step (fsi.autotune); the simulation state is unchanged."""
+        return self.lattice.autotune(steps=steps, use_cache=use_cache)
 
     def _graph_state(self) -> tuple:
         L = self.lattice

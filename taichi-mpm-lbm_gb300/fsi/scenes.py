@@ -212,3 +212,49 @@ def coupled_bodies(nx: int = 384, ny: int = 192, nz: int = 192, bodies: int = 48
     cfg = SimulationConfig(num_steps=2000, lbm_dt=1.0, lbm=lbm, mpm=mpm,
                            coupling=CouplingConfig(gamma=0.1, mpm_substeps_per_lbm_step=substeps))
     return cfg, wall_mask(nx, ny, nz), pos, young
+
+
+def batch_scenes(count: int = 256, seed: int = 4, edges=(32, 48, 64, 96), bodies=(1, 4),
+                 size=(4, 10), storage: str = "f16", substeps: int = 10):
+    """Independent coupled scenes for a batch: per scene a cubic lattice of edge drawn from
+    ``edges`` (walls in y and z as mask planes, periodic x), g_x U[1e-6, 1e-5], tau
+    U[0.55, 0.8], and 1 to 4 non-overlapping elastic bodies -- cubes of edge or balls of
+    radius U{4..10} cells, 8 particles per cell, Young's modulus U[0.02, 0.1] per body,
+    nu 0.3, rho_s 1.2 -- all drawn from ``seed``. Population storage ``storage``.
+    Returns a list of (config, solid mask, positions, per-particle Young's modulus)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.choice(edges))
+        tau = float(rng.uniform(0.55, 0.8))
+        gx = float(rng.uniform(1e-6, 1e-5))
+        lbm = LBMConfig(nx=n, ny=n, nz=n, viscosity=viscosity_for_tau(tau),
+                        force=(gx, 0.0, 0.0), population_storage=storage, **PERIODIC_FACES)
+        want = int(rng.integers(bodies[0], bodies[1] + 1))
+        placed = []  # (centre, half extent)
+        pos, young = [], []
+        tries = 0
+        while len(placed) < want and tries < 1000:
+            tries += 1
+            s_ = int(rng.integers(size[0], size[1] + 1))
+            cube = bool(rng.integers(0, 2))
+            half = s_ / 2 if cube else float(s_)
+            lo_c, hi_c = 4 + half, n - 4 - half
+            if hi_c <= lo_c:
+                continue
+            c = rng.uniform(lo_c, hi_c, size=3)
+            if any(np.max(np.abs(c - o)) < half + h + 1 for o, h in placed):
+                continue
+            placed.append((c, half))
+            p = (cube_particles(np.floor(c - s_ / 2), s_, 2, rng) if cube
+                 else sphere_particles(c, float(s_), 2, rng))
+            pos.append(p)
+            young.append(np.full(len(p), rng.uniform(0.02, 0.1), np.float32))
+        pos = np.concatenate(pos)
+        mpm = MPMConfig(nx=n, ny=n, nz=n, max_particles=len(pos), particles_per_cell=2, dx=1.0,
+                        dt=1.0 / substeps, density=1.2, youngs_modulus=0.05, poisson_ratio=0.3,
+                        gravity=(0.0, 0.0, 0.0), boundary_width=3)
+        cfg = SimulationConfig(num_steps=500, lbm_dt=1.0, lbm=lbm, mpm=mpm,
+                               coupling=CouplingConfig(gamma=0.1, mpm_substeps_per_lbm_step=substeps))
+        out.append((cfg, wall_mask(n, n, n), pos, np.concatenate(young)))
+    return out

@@ -120,7 +120,9 @@ def test_scene_batch_matches_standalone_simulations(graph):
         for _ in range(steps):
             sim.coupler.step(c.lbm_dt)
         assert rel_l2(batch.density_numpy(s), sim.lbm.density_numpy()) < 1e-5
-        assert rel_l2(batch.velocity_numpy(s), sim.lbm.velocity_numpy()) < 2.5e-4
+        # u: float32 order noise of the atomic grid sums (2.5e-4 at 100 steps of the smoke
+        # workload, larger relative to the smaller velocities after 9 steps)
+        assert rel_l2(batch.velocity_numpy(s), sim.lbm.velocity_numpy()) < 1e-3
         assert rel_l2(batch.positions_numpy(s), sim.mpm.positions_numpy()) < 1e-5
         assert rel_l2(batch.velocities_numpy(s), sim.mpm.velocities_numpy()) < 1e-3
         d = sim.coupler.coupling_diagnostics()
@@ -140,3 +142,43 @@ def test_scene_batch_per_particle_stiffness():
     b.run(4, graph=False)
     for s in range(3):
         assert rel_l2(b.positions_numpy(s), a.positions_numpy(s)) < 1e-6
+
+
+def test_autotune_keeps_state_and_results(tmp_path, monkeypatch):
+    monkeypatch.setenv("FSI_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    cfgs, masks = scenes()
+    a, b = LatticeBatch(cfgs), LatticeBatch(cfgs)
+    a.initialize(masks)
+    b.initialize(masks)
+    for _ in range(3):
+        a.step()
+        b.step()
+    rec = a.autotune(steps=2)
+    assert len(rec["ms"]) == 12 and all(v > 0 for v in rec["ms"].values())
+    assert a.tuning == {"step_tile_cells": rec["best"][0], "variant": rec["best"][1]}
+    for _ in range(5):
+        a.step()
+        b.step()
+    for i in range(len(cfgs)):  # exact form: launch parameters do not change the results
+        np.testing.assert_array_equal(a.distribution_numpy(i), b.distribution_numpy(i))
+    c = LatticeBatch(cfgs)
+    c.initialize(masks)
+    assert c.autotune()["best"] == rec["best"]  # from the cache
+
+
+def test_batch_scene_generator_runs_in_fp16(tmp_path, monkeypatch):
+    from fsi import scenes as sc
+    from fsi.batch import SceneBatch
+    monkeypatch.setenv("FSI_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    items = sc.batch_scenes(count=5, seed=4, edges=(32, 48), substeps=4)
+    batch = SceneBatch([c for c, _, _, _ in items])
+    batch.initialize([m for _, m, _, _ in items], [p for _, _, p, _ in items],
+                     youngs_modulus=[e for _, _, _, e in items], poisson_ratio=[0.3] * 5)
+    batch.autotune(steps=2)
+    batch.run(6, graph=True)
+    for s, (_, _, p, _) in enumerate(items):
+        x = batch.positions_numpy(s)
+        assert np.all(np.isfinite(x)) and rel_l2(x, p) < 1e-2
+        assert np.all(np.isfinite(batch.velocity_numpy(s)))
+        rho = batch.density_numpy(s)
+        assert abs(float(rho.mean()) - 1.0) < 1e-2
