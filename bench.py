@@ -247,6 +247,71 @@ def time_coupled(args, world, stream) -> dict:
     return out
 
 
+def time_batched(args, world, stream) -> dict:
+    """The batched workload: 256 independent coupled scenes (lattice edges 32-96, 1-4 bodies,
+    seed 4) in FP16 deviation storage, advanced together by SceneBatch.run (one launch per
+    phase over all scenes, CUDA graph), after autotuning; beside it the same per-scene work
+    done one scene at a time (FSISimulation, eager) on the first 8 scenes."""
+    import torch
+    from fsi import scenes
+    from fsi.batch import SceneBatch
+    from fsi.simulation import FSISimulation
+
+    items = scenes.batch_scenes(count=args.batch_scenes)
+    cfgs = [c for c, _, _, _ in items]
+    batch = SceneBatch(cfgs)
+    batch.initialize([m for _, m, _, _ in items], [p for _, _, p, _ in items],
+                     youngs_modulus=[e for _, _, _, e in items],
+                     poisson_ratio=[0.3] * len(items))
+    rec = batch.autotune(steps=3)
+    batch.run(4)
+    steps = 10
+    barrier(world)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    batch.run(steps)
+    b.record(stream)
+    barrier(world)
+    ms = max_over_ranks(a.elapsed_time(b), world) / steps
+    cells = batch.lattice.cells
+    particles = sum(batch.particle_counts)
+    sub = batch.substeps
+    # one scene at a time (eager FSISimulation steps) on a sample of the same scenes
+    sample = items[:8]
+    single_ms = 0.0
+    single_cells = 0
+    for cfg, mask, pos, young in sample:
+        sim = FSISimulation(cfg)
+        sim.initialize_lbm(mask)
+        sim.initialize_mpm_from_numpy(pos, youngs_modulus=young, poisson_ratio=0.3)
+        for _ in range(2):
+            sim.coupler.step(cfg.lbm_dt)
+        a.record(stream)
+        for _ in range(3):
+            sim.coupler.step(cfg.lbm_dt)
+        b.record(stream)
+        torch.cuda.synchronize()
+        single_ms += a.elapsed_time(b) / 3
+        single_cells += cfg.lbm.nx * cfg.lbm.ny * cfg.lbm.nz
+        del sim
+    single_mlups = single_cells / (single_ms * 1e-3) / 1e6
+    out = {
+        "scenes": len(items), "cells": cells, "particles": particles, "substeps": sub,
+        "storage": "f16", "ms_per_coupled_step": round(ms, 4),
+        "scene_steps_per_s": round(len(items) * 1e3 / ms * world, 1),
+        "mlups": round(cells / (ms * 1e-3) / 1e6 * world, 1),
+        "particle_steps_per_s": round(particles * sub / (ms * 1e-3) * world, 1),
+        "autotune": {"best_step_tile_cells": rec["best"][0], "best_variant": rec["best"][1]},
+        "one_at_a_time": {"scenes": len(sample), "mlups": round(single_mlups, 1),
+                          "mode": "FSISimulation coupler.step, eager, one scene after another"},
+        "speedup_vs_one_at_a_time": round(cells / (ms * 1e-3) / 1e6 / single_mlups, 2),
+        "gpu_launches": steps * (4 * sub + 3),
+    }
+    del batch
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args) -> dict:
     import torch
     from fsi import scenes
@@ -302,6 +367,8 @@ def run_gpu(args) -> dict:
         forms = time_lbm_forms(lcfg, mask, args, world, stream) if not args.no_forms else {}
         # --- coupled steps -------------------------------------------------------
         coupled = time_coupled(args, world, stream) if not args.no_coupled else {}
+        # --- many scenes at once ------------------------------------------------
+        batched = time_batched(args, world, stream) if args.batch_scenes > 0 else {}
     lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
     lbm_launches = args.steps
     mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
@@ -383,10 +450,12 @@ def run_gpu(args) -> dict:
         },
         "lbm_forms": forms,
         "coupled": coupled,
+        "batched": batched,
         # lattice steps + 3 MPM launches per substep + 3 launches per end-to-end step
         # (force op, step, fused macro + diagnostics) + one step per form per step + coupled
         "gpu_launches": (lbm_launches + 3 * args.steps + 3 * args.steps + len(forms) * args.steps
-                         + sum(c["gpu_launches"] for c in coupled.values())),
+                         + sum(c["gpu_launches"] for c in coupled.values())
+                         + batched.get("gpu_launches", 0)),
         "clocks": clocks.summary(),
     }
     if world > 1:
@@ -481,6 +550,8 @@ def main() -> None:
                     choices=["f32/exact", "f32/fast", "f16/fast", "bf16/fast"],
                     help="population storage / collision arithmetic of the headline lattice")
     ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-step timings")
+    ap.add_argument("--batch-scenes", type=int, default=256,
+                    help="scenes of the batched workload (0 skips it)")
     ap.add_argument("--no-coupled-scale", action="store_true",
                     help="time only the small coupled workload")
     ap.add_argument("--no-forms", action="store_true",

@@ -122,6 +122,7 @@ __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) 
         for (int ax = 0; ax < 3; ++ax) a.fp[ax * cap + p] = pf[ax];
         a.mask_out[p] = 1;
         const float vp = a.vol[p];
+        const bool unit_cell = a.c.cell_volume == 1.0f;
 #pragma unroll
         for (int s = 0; s < 27; ++s) {
           if (!(usable & (1u << s))) continue;
@@ -132,9 +133,16 @@ __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) 
           const float nw = __fdiv_rn(w, valid);
           float add[3];
 #pragma unroll
-          for (int ax = 0; ax < 3; ++ax)
-            add[ax] = __fdiv_rn(__fmul_rn(__fmul_rn(-nw, pf[ax]), a.c.dt_ratio), a.c.cell_volume);
-          const float ph = a.c.build_fraction ? __fdiv_rn(__fmul_rn(nw, vp), a.c.cell_volume) : 0.f;
+          for (int ax = 0; ax < 3; ++ax) {
+            add[ax] = __fmul_rn(__fmul_rn(-nw, pf[ax]), a.c.dt_ratio);
+            // x / 1 is exactly x: skip the division for unit cells (dx = 1).
+            if (!unit_cell) add[ax] = __fdiv_rn(add[ax], a.c.cell_volume);
+          }
+          float ph = 0.f;
+          if (a.c.build_fraction) {
+            ph = __fmul_rn(nw, vp);
+            if (!unit_cell) ph = __fdiv_rn(ph, a.c.cell_volume);
+          }
           red_add_v4(a.accum + c, add[0], add[1], add[2], ph);
         }
       } else {
