@@ -394,6 +394,85 @@ int fsi_batch_coupling_assemble(const fsi_batch* batch, const uint32_t* flags, i
                                 float* accum, const float* macro, float* force, float* ib_force,
                                 void* counters, void* stream);
 
+/* ------------------------------------------------------------ learned closure
+ * A per-cell MLP (621 -> 64 -> 64 -> 64 -> 19, GELU, BF16 weights, FP32 accumulation) that
+ * corrects the post-stream populations of a lattice run on a grid 2x coarser than the one it
+ * was trained on, on the tcgen05 tensor cores. No reference counterpart. Lattices must use
+ * FP32 population storage. Features of a cell: for each of its 27 neighbours (periodic wrap,
+ * offsets (dx, dy, dz) in {-1,0,1}^3 with dz fastest) the 19 populations as
+ * (f_q - w_q rho0) * pop_scale, the occupancy (1 solid) and the force * force_scale:
+ * 27 * 23 = 621 values, zero-padded to 640 columns. */
+#define FSI_CLOSURE_FEATURES 640
+
+/* Feature rows (BF16 [m][640]) of the cells listed in `cells` (device int32[m]). */
+int fsi_closure_features(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
+                         const float* force, int64_t steps_done, const int32_t* cells, int32_t m,
+                         float pop_scale, float force_scale, void* x, void* stream);
+
+/* C = A B^T with BF16 K-major operands A [m][lda], B [n][ldb] (row-major, 16-byte aligned,
+ * lda and ldb multiples of 8) on the tensor cores, K split into k_chunk pieces over the grid,
+ * and one epilogue:
+ *   0  C[r][c] = acc                        (FP32, ldc)
+ *   1  C[r][c] += acc atomically            (FP32, ldc; for split-K weight gradients)
+ *   2  z = acc + bias[c]; zout[r][c] = z (if not NULL); h[r][c] = ht[c][r] = gelu(z) (BF16)
+ *   3  h[r][c] = ht[c][r] = acc * gelu'(zin[r][c])                                (BF16)
+ * (h, zout, zin are [m][n]; ht is [n][ldht] or NULL.) err: device int, set non-zero if a
+ * wait on the tensor cores timed out. */
+typedef struct fsi_closure_gemm_desc {
+  const void* a;
+  const void* b;
+  int32_t lda, ldb;
+  int32_t m, n, k, k_chunk;
+  int32_t mode;
+  int32_t ldc;
+  float* c;
+  const float* bias;
+  void* h;
+  void* ht;
+  int32_t ldht;
+  int32_t reserved;
+  float* zout;
+  const float* zin;
+  int32_t* err;
+} fsi_closure_gemm_desc;
+int fsi_closure_gemm(const fsi_closure_gemm_desc* desc, void* stream);
+
+/* Network of the fused inference: BF16 w1 [64][640], w2 [64][64], w3 [64][64], w4 [32][64]
+ * (rows 19..31 zero), FP32 bias = b1[64] b2[64] b3[64] b4[32]; correction = y / out_scale. */
+typedef struct fsi_closure_weights {
+  const void* w1;
+  const void* w2;
+  const void* w3;
+  const void* w4;
+  const float* bias;
+  float pop_scale;
+  float force_scale;
+  float out_scale;
+  int32_t reserved;
+} fsi_closure_weights;
+
+/* Fused inference over every cell: features built in shared memory, the four layers on the
+ * tensor cores with the weights resident, corrections corr [19][N] (0 on solid cells). */
+int fsi_closure_infer(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
+                      const float* force, int64_t steps_done, const fsi_closure_weights* weights,
+                      float* corr, int32_t* err, void* stream);
+/* f_q += corr_q - w_q sum_p corr_p on fluid cells (moves no mass). */
+int fsi_closure_apply(const fsi_lbm_desc* desc, float* pops, const uint32_t* flags,
+                      int64_t steps_done, const float* corr, void* stream);
+/* Mean post-stream populations of the fluid children of each coarse cell, out [Nc][19]. */
+int fsi_closure_restrict(const fsi_lbm_desc* fine, const float* pops, const uint32_t* flags,
+                         int64_t steps_done, const fsi_lbm_desc* coarse, float* out,
+                         void* stream);
+/* Training: mean-square loss of y [m][32] + b4 against target [m][19], its gradient dy
+ * (BF16 [m][32]) and transpose dyt ([32][ldt]); loss (device double) accumulates. */
+int fsi_closure_loss(const float* y, const float* target, const float* b4, int32_t m, void* dy,
+                     void* dyt, int32_t ldt, double* loss, void* stream);
+/* out[c] += sum_r g[r][c] for BF16 g [m][n]. */
+int fsi_closure_colsum(const void* g, int32_t m, int32_t n, float* out, void* stream);
+/* One Adam step (bias-corrected) of n parameters. */
+int fsi_closure_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
+                     float beta1, float beta2, float eps, int32_t step, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

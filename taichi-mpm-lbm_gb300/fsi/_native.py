@@ -107,6 +107,29 @@ class BatchSolid(ctypes.Structure):
     _fields_ = [("mpm", MpmDesc), ("coupling", CouplingDesc), ("particle_offset", ctypes.c_int64)]
 
 
+class ClosureGemmDesc(ctypes.Structure):
+    _fields_ = [
+        ("a", ctypes.c_void_p), ("b", ctypes.c_void_p),
+        ("lda", ctypes.c_int32), ("ldb", ctypes.c_int32),
+        ("m", ctypes.c_int32), ("n", ctypes.c_int32), ("k", ctypes.c_int32),
+        ("k_chunk", ctypes.c_int32), ("mode", ctypes.c_int32), ("ldc", ctypes.c_int32),
+        ("c", ctypes.c_void_p), ("bias", ctypes.c_void_p),
+        ("h", ctypes.c_void_p), ("ht", ctypes.c_void_p),
+        ("ldht", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("zout", ctypes.c_void_p), ("zin", ctypes.c_void_p), ("err", ctypes.c_void_p),
+    ]
+
+
+class ClosureWeights(ctypes.Structure):
+    _fields_ = [
+        ("w1", ctypes.c_void_p), ("w2", ctypes.c_void_p), ("w3", ctypes.c_void_p),
+        ("w4", ctypes.c_void_p), ("bias", ctypes.c_void_p),
+        ("pop_scale", ctypes.c_float), ("force_scale", ctypes.c_float),
+        ("out_scale", ctypes.c_float), ("reserved", ctypes.c_int32),
+    ]
+
+
+GEMM_STORE, GEMM_ATOMIC, GEMM_GELU_FWD, GEMM_GELU_BWD = 0, 1, 2, 3
 BATCH_PARTICLE_ALIGN = 256
 
 _VP = ctypes.c_void_p
@@ -142,6 +165,19 @@ _SIGNATURES = {
     "fsi_batch_lbm_distribution": ([_BATCH, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "fsi_batch_lbm_base_force": ([_BATCH, _VP, _VP, _VP], ctypes.c_int),
     "fsi_batch_tune": ([_BATCH, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "fsi_closure_features": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64, _VP,
+                              ctypes.c_int32, ctypes.c_float, ctypes.c_float, _VP, _VP], ctypes.c_int),
+    "fsi_closure_gemm": ([ctypes.POINTER(ClosureGemmDesc), _VP], ctypes.c_int),
+    "fsi_closure_infer": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64,
+                           ctypes.POINTER(ClosureWeights), _VP, _VP, _VP], ctypes.c_int),
+    "fsi_closure_apply": ([ctypes.POINTER(LbmDesc), _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "fsi_closure_restrict": ([ctypes.POINTER(LbmDesc), _VP, _VP, ctypes.c_int64,
+                              ctypes.POINTER(LbmDesc), _VP, _VP], ctypes.c_int),
+    "fsi_closure_loss": ([_VP, _VP, _VP, ctypes.c_int32, _VP, _VP, ctypes.c_int32, _VP, _VP],
+                         ctypes.c_int),
+    "fsi_closure_colsum": ([_VP, ctypes.c_int32, ctypes.c_int32, _VP, _VP], ctypes.c_int),
+    "fsi_closure_adam": ([_VP, _VP, _VP, _VP, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, ctypes.c_float, ctypes.c_int32, _VP], ctypes.c_int),
     "fsi_batch_set_solids": ([_BATCH, ctypes.POINTER(BatchSolid), ctypes.c_int64,
                               ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "fsi_batch_set_gamma": ([_BATCH, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),

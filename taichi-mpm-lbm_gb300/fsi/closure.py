@@ -1,0 +1,393 @@
+"""Learned coarse-grid closure (no reference counterpart).
+
+A lattice run on a grid 2x coarser than a reference ("fine") run, with lattice units kept
+(acoustic scaling: dx and dt double, so velocities in lattice units are unchanged, the
+lattice viscosity halves and a body force doubles), is corrected after every step by a
+per-cell MLP: 621 features of the cell's 3^3 neighbourhood (19 populations, occupancy and
+3 force components per neighbour) -> 64 -> 64 -> 64 -> 19 corrections of the post-stream
+populations, GELU activations, BF16 weights with FP32 accumulation. Training pairs come
+from restricted fine runs of the plain solver: the correction is what the coarse step
+misses, R(f(t + 2 dt_f)) - C(R(f(t))), with R the 2x2x2 restriction and C one coarse step.
+
+Every matrix product (forward, backward and weight gradients) runs on the tcgen05 tensor
+cores through ``fsi_closure_gemm``; inference during stepping is one fused kernel
+(``fsi_closure_infer``). ``ClosureSimulation`` watches mass drift and the local Mach number
+and falls back to the plain fine-grid solver (prolongating the coarse state) when a guard
+trips.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .config import LBMConfig
+from .lbm3d import LBMSolver3D
+
+FEATURES = 640  # 621 used
+HIDDEN = 64
+OUT = 19
+OUT_PAD = 32
+_CS = 1.0 / math.sqrt(3.0)
+
+
+# ----------------------------------------------------------------- grids
+def coarse_config(fine: LBMConfig) -> LBMConfig:
+    """The 2x coarser lattice in acoustic scaling: half the cells per axis, half the lattice
+    viscosity, twice the body force, FP32 populations in the exact form."""
+    for n in (fine.nx, fine.ny, fine.nz):
+        if n % 2:
+            raise ValueError("the fine lattice needs even sizes.")
+    return dataclasses.replace(fine, nx=fine.nx // 2, ny=fine.ny // 2, nz=fine.nz // 2,
+                               viscosity=fine.viscosity / 2.0,
+                               force=tuple(2.0 * g for g in fine.force),
+                               population_storage="f32", collision_arithmetic="exact",
+                               mrt_rates=None)
+
+
+def coarse_mask(fine_mask: np.ndarray) -> np.ndarray:
+    """A coarse cell is solid when at least 4 of its 8 children are."""
+    m = np.asarray(fine_mask) > 0
+    nx, ny, nz = m.shape
+    c = m.reshape(nx // 2, 2, ny // 2, 2, nz // 2, 2).sum(axis=(1, 3, 5))
+    return (c >= 4).astype(np.int32)
+
+
+def restrict(fine: LBMSolver3D, coarse: LBMSolver3D) -> torch.Tensor:
+    """Mean post-stream populations of the fluid children, [Nc, 19] (device)."""
+    out = torch.empty((coarse.n_cells, OUT), dtype=torch.float32, device=fine._device)
+    nat.call("fsi_closure_restrict", fine._desc, nat.ptr(fine._pops), nat.ptr(fine.flags),
+             fine.steps_done, coarse._desc, nat.ptr(out), nat.stream_ptr())
+    return out
+
+
+def prolongate(coarse_f: torch.Tensor, shape) -> torch.Tensor:
+    """Each fine cell takes its parent's populations, [Nf, 19]."""
+    nx, ny, nz = shape
+    f = coarse_f.reshape(nx // 2, ny // 2, nz // 2, OUT)
+    f = f.repeat_interleave(2, 0).repeat_interleave(2, 1).repeat_interleave(2, 2)
+    return f.reshape(-1, OUT).contiguous()
+
+
+# ------------------------------------------------------------------- net
+def _gemm(a, b, lda, ldb, m, n, k, mode, err, c=None, ldc=0, bias=None, h=None, ht=None,
+          ldht=0, zout=None, zin=None, k_chunk=None):
+    d = nat.ClosureGemmDesc()
+    d.a, d.b = a.data_ptr(), b.data_ptr()
+    d.lda, d.ldb, d.m, d.n, d.k = lda, ldb, m, n, k
+    d.k_chunk = k_chunk or ((k + 63) // 64 * 64)
+    d.mode = mode
+    d.ldc = ldc
+    for name, t in (("c", c), ("bias", bias), ("h", h), ("ht", ht), ("zout", zout), ("zin", zin)):
+        setattr(d, name, None if t is None else t.data_ptr())
+    d.ldht = ldht
+    d.err = err.data_ptr()
+    nat.call("fsi_closure_gemm", ctypes.byref(d), nat.stream_ptr())
+
+
+class ClosureMLP:
+    """Parameters (FP32 master, BF16 copies), Adam state and the tensor-core passes."""
+
+    def __init__(self, seed: int = 0, device=None):
+        self.device = device or nat.device()
+        nat.load()
+        g = torch.Generator().manual_seed(seed)
+        sizes = [(HIDDEN, FEATURES), (HIDDEN,), (HIDDEN, HIDDEN), (HIDDEN,), (HIDDEN, HIDDEN),
+                 (HIDDEN,), (OUT_PAD, HIDDEN), (OUT_PAD,)]
+        total = sum(int(np.prod(s)) for s in sizes)
+        self.params = torch.zeros(total, dtype=torch.float32, device=self.device)
+        self.grads = torch.zeros_like(self.params)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.views, self.gviews, off = [], [], 0
+        for s in sizes:
+            n = int(np.prod(s))
+            self.views.append(self.params[off:off + n].view(*s))
+            self.gviews.append(self.grads[off:off + n].view(*s))
+            off += n
+        W1, _, W2, _, W3, _, W4, _ = self.views
+        for W, fan_in in ((W1, 621), (W2, HIDDEN), (W3, HIDDEN), (W4, HIDDEN)):
+            W.copy_(torch.randn(W.shape, generator=g) * math.sqrt(2.0 / fan_in))
+        W1[:, 621:] = 0.0
+        W4[OUT:] = 0.0
+        W4.mul_(0.1)
+        self.pop_scale = self.force_scale = self.out_scale = 1.0
+        self.step_count = 0
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.refresh()
+
+    def refresh(self) -> None:
+        """BF16 copies of the weights and the transposes used by the backward pass."""
+        W1, b1, W2, b2, W3, b3, W4, b4 = self.views
+        bf = torch.bfloat16
+        self.w1, self.w2, self.w3, self.w4 = (W.to(bf).contiguous() for W in (W1, W2, W3, W4))
+        self.w2t, self.w3t = W2.t().contiguous().to(bf), W3.t().contiguous().to(bf)
+        self.w4t = W4.t().contiguous().to(bf)  # [64][32]
+        self.bias = torch.cat([b1, b2, b3, b4]).contiguous()
+
+    def weights_struct(self) -> nat.ClosureWeights:
+        w = nat.ClosureWeights()
+        w.w1, w.w2, w.w3, w.w4 = (t.data_ptr() for t in (self.w1, self.w2, self.w3, self.w4))
+        w.bias = self.bias.data_ptr()
+        w.pop_scale, w.force_scale, w.out_scale = self.pop_scale, self.force_scale, self.out_scale
+        return w
+
+    # -- forward / backward over a batch of feature rows (BF16 [m][640]) ------------
+    def forward(self, x: torch.Tensor, keep: bool = False):
+        m = x.shape[0]
+        dev, bf = self.device, torch.bfloat16
+        b1, b2, b3 = self.views[1], self.views[3], self.views[5]
+        acts = {}
+        h_in = x
+        for i, (w, b) in enumerate(((self.w1, b1), (self.w2, b2), (self.w3, b3)), start=1):
+            k = w.shape[1]
+            h = torch.empty((m, HIDDEN), dtype=bf, device=dev)
+            ht = torch.empty((HIDDEN, m), dtype=bf, device=dev) if keep else None
+            z = torch.empty((m, HIDDEN), dtype=torch.float32, device=dev) if keep else None
+            _gemm(h_in, w, k, k, m, HIDDEN, k, nat.GEMM_GELU_FWD, self.err, bias=b, h=h, ht=ht,
+                  ldht=m, zout=z)
+            acts[i] = (h, ht, z)
+            h_in = h
+        y = torch.empty((m, OUT_PAD), dtype=torch.float32, device=dev)
+        _gemm(h_in, self.w4, HIDDEN, HIDDEN, m, OUT_PAD, HIDDEN, nat.GEMM_STORE, self.err, c=y,
+              ldc=OUT_PAD)
+        return (y, acts) if keep else y
+
+    def predict(self, x: torch.Tensor) -> torch.Tensor:
+        """Network output (normalised corrections) [m][19], FP32."""
+        return self.forward(x)[:, :OUT] + self.views[7][:OUT]
+
+    def backward(self, x: torch.Tensor, y: torch.Tensor, acts: dict, target: torch.Tensor,
+                 xt: torch.Tensor | None = None, k_chunk: int = 4096) -> float:
+        """Gradients of the mean-square loss into self.grads; returns the loss."""
+        m = x.shape[0]
+        dev, bf = self.device, torch.bfloat16
+        self.grads.zero_()
+        loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        dy = torch.empty((m, OUT_PAD), dtype=bf, device=dev)
+        dyt = torch.empty((OUT_PAD, m), dtype=bf, device=dev)
+        nat.call("fsi_closure_loss", nat.ptr(y), nat.ptr(target), nat.ptr(self.views[7]), m,
+                 nat.ptr(dy), nat.ptr(dyt), m, nat.ptr(loss), nat.stream_ptr())
+        gW1, gb1, gW2, gb2, gW3, gb3, gW4, gb4 = self.gviews
+        kc = k_chunk
+        # output layer
+        h3, h3t, z3 = acts[3]
+        _gemm(dyt, h3t, m, m, OUT_PAD, HIDDEN, m, nat.GEMM_ATOMIC, self.err, c=gW4, ldc=HIDDEN,
+              k_chunk=kc)
+        nat.call("fsi_closure_colsum", nat.ptr(dy), m, OUT_PAD, nat.ptr(gb4), nat.stream_ptr())
+        # hidden layers, from the top
+        g_in, g_ld, w_t = dy, OUT_PAD, self.w4t
+        for layer, (gW, gb) in ((3, (gW3, gb3)), (2, (gW2, gb2)), (1, (gW1, gb1))):
+            h, ht, z = acts[layer]
+            dz = torch.empty((m, HIDDEN), dtype=bf, device=dev)
+            dzt = torch.empty((HIDDEN, m), dtype=bf, device=dev)
+            _gemm(g_in, w_t, g_ld, g_ld, m, HIDDEN, g_ld, nat.GEMM_GELU_BWD, self.err, h=dz, ht=dzt,
+                  ldht=m, zin=z)
+            below_t = xt if layer == 1 else acts[layer - 1][1]
+            n_below = FEATURES if layer == 1 else HIDDEN
+            _gemm(dzt, below_t, m, m, HIDDEN, n_below, m, nat.GEMM_ATOMIC, self.err, c=gW,
+                  ldc=n_below, k_chunk=kc)
+            nat.call("fsi_closure_colsum", nat.ptr(dz), m, HIDDEN, nat.ptr(gb), nat.stream_ptr())
+            g_in, g_ld = dz, HIDDEN
+            w_t = self.w3t if layer == 3 else self.w2t
+        gW4[OUT:] = 0.0
+        gb4[OUT:] = 0.0
+        gW1[:, 621:] = 0.0
+        return float(loss.item())
+
+    def adam_step(self, lr: float = 1e-3, beta1: float = 0.9, beta2: float = 0.999,
+                  eps: float = 1e-8) -> None:
+        self.step_count += 1
+        nat.call("fsi_closure_adam", nat.ptr(self.params), nat.ptr(self.grads), nat.ptr(self.m),
+                 nat.ptr(self.v), self.params.numel(), lr, beta1, beta2, eps, self.step_count,
+                 nat.stream_ptr())
+        self.refresh()
+
+    def check(self) -> None:
+        if int(self.err.item()) != 0:
+            raise nat.NativeError(f"tensor-core wait timed out (code {int(self.err.item())})")
+
+    def state_dict(self) -> dict:
+        return {"params": self.params.cpu(), "scales": (self.pop_scale, self.force_scale,
+                                                        self.out_scale)}
+
+    def load_state_dict(self, state: dict) -> None:
+        self.params.copy_(state["params"])
+        self.pop_scale, self.force_scale, self.out_scale = state["scales"]
+        self.refresh()
+
+
+# ------------------------------------------------------------------ data
+def features(lbm: LBMSolver3D, cells: torch.Tensor, pop_scale: float, force_scale: float):
+    """BF16 feature rows [m][640] of the given cells (int32 device tensor) of `lbm`."""
+    m = int(cells.numel())
+    x = torch.empty((m, FEATURES), dtype=torch.bfloat16, device=lbm._device)
+    nat.call("fsi_closure_features", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags),
+             nat.ptr(lbm.force), lbm.steps_done, nat.ptr(cells), m, pop_scale, force_scale,
+             nat.ptr(x), nat.stream_ptr())
+    return x
+
+
+def training_pairs(fine_cfg: LBMConfig, fine_mask: np.ndarray, warmup: int, snapshots: int,
+                   every: int = 2):
+    """Run the plain fine solver and collect (coarse post-step state, correction target)
+    pairs: for each snapshot, the coarse solver is loaded with the restricted fine state,
+    takes one step, and the target is the restricted fine state two fine steps later minus
+    the coarse result. Yields (coarse solver after its step, fluid cells, target [m][19])."""
+    fine = LBMSolver3D(fine_cfg)
+    fine.initialize(fine_mask)
+    ccfg = coarse_config(fine_cfg)
+    coarse = LBMSolver3D(ccfg)
+    cmask = coarse_mask(fine_mask)
+    coarse.initialize(cmask)
+    fluid = torch.nonzero(torch.from_numpy(cmask.reshape(-1) == 0)).reshape(-1).to(
+        torch.int32).to(fine._device)
+    for _ in range(warmup):
+        fine.step()
+    for _ in range(snapshots):
+        r0 = restrict(fine, coarse)
+        fine.step()
+        fine.step()
+        r1 = restrict(fine, coarse)
+        coarse.load_populations(r0)
+        coarse.step()
+        cstate = torch.from_numpy(coarse.distribution_numpy().reshape(-1, OUT)).to(fine._device)
+        target = (r1 - cstate)[fluid.long()]
+        yield coarse, fluid, target
+        for _ in range(every - 2):
+            fine.step()
+
+
+class ClosureTrainer:
+    """Collects training rows from restricted fine runs and fits a ClosureMLP."""
+
+    def __init__(self, net: ClosureMLP):
+        self.net = net
+        self.rows_x: list[torch.Tensor] = []
+        self.rows_t: list[torch.Tensor] = []
+        self._pending = []  # (coarse state copy, cells, raw target) before scales are known
+
+    def add_run(self, fine_cfg: LBMConfig, fine_mask: np.ndarray, warmup: int = 40,
+                snapshots: int = 10, every: int = 4) -> None:
+        for coarse, cells, target in training_pairs(fine_cfg, fine_mask, warmup, snapshots, every):
+            self._pending.append((coarse.state_dict(), coarse.config, cells, target.clone()))
+
+    def _fit_scales(self) -> None:
+        devs, forces, targets = [], [], []
+        for state, cfg, cells, target in self._pending:
+            f = state["pops"]
+            w = torch.tensor([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, device=f.device).view(OUT, 1)
+            devs.append((f - w * cfg.rho0)[:, cells.long()].flatten())
+            forces.append(torch.tensor(cfg.force).abs().max())
+            targets.append(target.flatten())
+        self.net.pop_scale = float(1.0 / max(torch.cat(devs).std().item(), 1e-12))
+        self.net.force_scale = float(1.0 / max(max(float(f) for f in forces), 1e-12))
+        self.net.out_scale = float(1.0 / max(torch.cat(targets).std().item(), 1e-20))
+
+    def build(self) -> int:
+        """Feature rows of every collected pair with the fitted scales; returns the row count."""
+        self._fit_scales()
+        for state, cfg, cells, target in self._pending:
+            lbm = LBMSolver3D(cfg)
+            lbm.load_state_dict(state)
+            self.rows_x.append(features(lbm, cells, self.net.pop_scale, self.net.force_scale))
+            self.rows_t.append((target * self.net.out_scale).float())
+        self._pending.clear()
+        self.x = torch.cat(self.rows_x)
+        self.t = torch.cat(self.rows_t).contiguous()
+        self.rows_x.clear()
+        self.rows_t.clear()
+        return int(self.x.shape[0])
+
+    def fit(self, steps: int = 500, batch: int = 16384, lr: float = 2e-3, seed: int = 0) -> list[float]:
+        """Adam on random mini-batches (multiples of 128 rows); returns the loss history."""
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        n = self.x.shape[0]
+        batch = max(128, min(batch, n) // 128 * 128)
+        hist = []
+        for it in range(steps):
+            idx = torch.randint(0, n, (batch,), generator=g).to(self.x.device)
+            x = self.x[idx].contiguous()
+            xt = x.t().contiguous()
+            t = self.t[idx].contiguous()
+            y, acts = self.net.forward(x, keep=True)
+            hist.append(self.net.backward(x, y, acts, t, xt=xt))
+            self.net.adam_step(lr=lr * (0.5 ** (it / max(steps, 1) * 3)))
+        self.net.check()
+        return hist
+
+
+# ------------------------------------------------------------ simulation
+class ClosureSimulation:
+    """The coarse lattice with the learned correction after every step; guards on mass drift
+    and local Mach number fall back to the plain fine-grid solver."""
+
+    def __init__(self, fine_cfg: LBMConfig, fine_mask: np.ndarray, net: ClosureMLP,
+                 mass_tol: float = 1e-3, mach_tol: float = 0.3, check_every: int = 10):
+        self.fine_cfg = fine_cfg
+        self.fine_mask = np.asarray(fine_mask)
+        self.net = net
+        self.coarse = LBMSolver3D(coarse_config(fine_cfg))
+        self.coarse.initialize(coarse_mask(fine_mask))
+        self.corr = torch.zeros((OUT, self.coarse.n_cells), dtype=torch.float32,
+                                device=self.coarse._device)
+        self.mass_tol, self.mach_tol, self.check_every = mass_tol, mach_tol, check_every
+        self.mass0 = self.coarse.total_mass()
+        self.fine: LBMSolver3D | None = None
+        self.fallback_step: int | None = None
+        self.fallback_reason = ""
+        self.coarse_steps = 0
+        self._weights = net.weights_struct()
+
+    @property
+    def on_fine_grid(self) -> bool:
+        return self.fine is not None
+
+    def _guard(self) -> str:
+        mass = self.coarse.total_mass()
+        if abs(mass - self.mass0) > self.mass_tol * abs(self.mass0):
+            return f"mass drift {abs(mass - self.mass0) / abs(self.mass0):.2e}"
+        mach = self.coarse.max_velocity_norm() / _CS
+        if not math.isfinite(mach) or mach > self.mach_tol:
+            return f"local Mach {mach:.3f}"
+        return ""
+
+    def _fall_back(self, reason: str) -> None:
+        f = torch.from_numpy(self.coarse.distribution_numpy().reshape(-1, OUT)).to(self.coarse._device)
+        self.fine = LBMSolver3D(self.fine_cfg)
+        self.fine.initialize(self.fine_mask)
+        self.fine.load_populations(prolongate(f, (self.fine_cfg.nx, self.fine_cfg.ny, self.fine_cfg.nz)))
+        self.fallback_step = self.coarse_steps
+        self.fallback_reason = reason
+
+    def step(self) -> None:
+        """One coarse step (= two fine steps of time), or two fine steps after a fallback."""
+        if self.fine is not None:
+            self.fine.step()
+            self.fine.step()
+            return
+        c = self.coarse
+        c.step()
+        nat.call("fsi_closure_infer", c._desc, nat.ptr(c._pops), nat.ptr(c.flags), nat.ptr(c.force),
+                 c.steps_done, ctypes.byref(self._weights), nat.ptr(self.corr),
+                 nat.ptr(self.net.err), nat.stream_ptr())
+        nat.call("fsi_closure_apply", c._desc, nat.ptr(c._pops), nat.ptr(c.flags), c.steps_done,
+                 nat.ptr(self.corr), nat.stream_ptr())
+        c._mass_speed_cache = None
+        self.coarse_steps += 1
+        if self.check_every and self.coarse_steps % self.check_every == 0:
+            reason = self._guard()
+            if reason:
+                self._fall_back(reason)
+
+    def velocity_numpy(self) -> np.ndarray:
+        """Velocity on the coarse grid (restricting the fine field after a fallback)."""
+        if self.fine is None:
+            return self.coarse.velocity_numpy()
+        u = self.fine.velocity_numpy()
+        nx, ny, nz = (n // 2 for n in u.shape[:3])
+        return u.reshape(nx, 2, ny, 2, nz, 2, 3).mean(axis=(1, 3, 5))

@@ -343,6 +343,21 @@ class LBMSolver3D:
             raise ValueError(f"force_np shape must be {expected}, got {arr.shape}.")
         return np.ascontiguousarray(arr)
 
+    def load_populations(self, f: torch.Tensor | np.ndarray) -> None:
+        """Replace the populations by ``f`` in the reference layout [nx, ny, nz, 19] (or
+        [N, 19]) and restart the step count (no reference counterpart; used to start a
+        lattice from a restricted or prolongated state). rho and u are recomputed from ``f``
+        and the current force at the next step."""
+        if self.config.population_storage != "f32":
+            raise NotImplementedError("load_populations needs FP32 population storage.")
+        t = torch.as_tensor(f, dtype=torch.float32, device=self._device).reshape(self.n_cells, _Q)
+        self._pops.copy_(t.t())
+        self._steps_done = 0
+        self._fprev = self._fcur
+        self._macro_fresh = False
+        self._mass_speed_cache = None
+        self._initialized = True
+
     # ------------------------------------------------------- checkpointing
     def state_dict(self) -> dict:
         """Complete lattice state (device tensors are cloned; no reference counterpart)."""

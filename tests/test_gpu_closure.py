@@ -1,0 +1,235 @@
+"""Learned coarse-grid closure (fsi.closure): the tcgen05 GEMM epilogues, the features, the
+fused inference and the gradients against the CPU restatement (oracle/closure_oracle.py),
+training, the gain over the coarse run without the network, and the guard fallback."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from fsi import _native as nat
+from fsi import closure as cl
+from fsi.config import LBMConfig
+from fsi.lbm3d import LBMSolver3D
+from helpers import PERIODIC, channel_mask, rel_l2
+from oracle import closure_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def bf(a: np.ndarray) -> torch.Tensor:
+    return torch.from_numpy(np.asarray(a, np.float32)).cuda().to(torch.bfloat16)
+
+
+def host(t: torch.Tensor) -> np.ndarray:
+    return t.float().cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.parametrize("m,n,k", [(300, 64, 640), (128, 32, 64), (257, 128, 96), (64, 640, 1024)])
+def test_gemm_store_and_atomic(m, n, k):
+    rng = np.random.default_rng(m + n + k)
+    a, b = bf(rng.standard_normal((m, k))), bf(rng.standard_normal((n, k)))
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    want = host(a) @ host(b).T
+    c = torch.zeros((m, n), dtype=torch.float32, device="cuda")
+    cl._gemm(a, b, k, k, m, n, k, nat.GEMM_STORE, err, c=c, ldc=n)
+    np.testing.assert_allclose(c.cpu().numpy(), want, rtol=1e-5, atol=1e-4)
+    c.zero_()
+    cl._gemm(a, b, k, k, m, n, k, nat.GEMM_ATOMIC, err, c=c, ldc=n, k_chunk=64)  # split-K
+    np.testing.assert_allclose(c.cpu().numpy(), want, rtol=1e-5, atol=1e-4)
+    assert int(err.item()) == 0
+
+
+def test_gemm_gelu_epilogues():
+    rng = np.random.default_rng(7)
+    m, n, k = 384, 64, 640
+    a, b = bf(rng.standard_normal((m, k)) * 0.1), bf(rng.standard_normal((n, k)) * 0.1)
+    bias = torch.from_numpy(rng.standard_normal(n).astype(np.float32)).cuda()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    h = torch.empty((m, n), dtype=torch.bfloat16, device="cuda")
+    ht = torch.empty((n, m), dtype=torch.bfloat16, device="cuda")
+    z = torch.empty((m, n), dtype=torch.float32, device="cuda")
+    cl._gemm(a, b, k, k, m, n, k, nat.GEMM_GELU_FWD, err, bias=bias, h=h, ht=ht, ldht=m, zout=z)
+    zw = host(a) @ host(b).T + bias.double().cpu().numpy()
+    np.testing.assert_allclose(z.cpu().numpy(), zw, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(host(h), O.gelu(zw), rtol=1e-2, atol=1e-2)
+    np.testing.assert_array_equal(host(ht), host(h).T)
+    g = bf(rng.standard_normal((m, 32)))
+    w = bf(rng.standard_normal((n, 32)))
+    d = torch.empty((m, n), dtype=torch.bfloat16, device="cuda")
+    dt = torch.empty((n, m), dtype=torch.bfloat16, device="cuda")
+    cl._gemm(g, w, 32, 32, m, n, 32, nat.GEMM_GELU_BWD, err, h=d, ht=dt, ldht=m, zin=z)
+    want = (host(g) @ host(w).T) * O.gelu_grad(z.double().cpu().numpy())
+    np.testing.assert_allclose(host(d), want, rtol=1e-2, atol=1e-2)
+    np.testing.assert_array_equal(host(dt), host(d).T)
+    assert int(err.item()) == 0
+
+
+def small_lattice(seed=0, steps=5):
+    cfg = LBMConfig(nx=10, ny=9, nz=8, viscosity=0.05, force=(1e-4, 2e-5, 0.0), **PERIODIC)
+    mask = channel_mask(10, 9, 8)
+    mask[4:6, 3:5, 3:5] = 1
+    lbm = LBMSolver3D(cfg)
+    lbm.initialize(mask)
+    for _ in range(steps):
+        lbm.step()
+    return lbm, mask
+
+
+def numpy_features(lbm, mask, cells, pop_scale, force_scale):
+    f = lbm.distribution_numpy()
+    g = lbm.force_numpy()
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
+    nx, ny, nz = mask.shape
+    out = np.zeros((len(cells), 640))
+    for r, c in enumerate(cells):
+        i, j, k = c // (ny * nz), (c // nz) % ny, c % nz
+        col = 0
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    a, b, e = (i + dx) % nx, (j + dy) % ny, (k + dz) % nz
+                    solid = mask[a, b, e] > 0
+                    pops = np.zeros(19) if solid else (f[a, b, e] - w * np.float32(lbm.config.rho0)) * pop_scale
+                    out[r, col:col + 19] = pops
+                    out[r, col + 19] = 1.0 if solid else 0.0
+                    out[r, col + 20:col + 23] = g[a, b, e] * force_scale
+                    col += 23
+    return out
+
+
+def test_features_match_numpy():
+    lbm, mask = small_lattice()
+    cells = np.array([0, 17, 123, 300, 555, 719])
+    x = cl.features(lbm, torch.from_numpy(cells.astype(np.int32)).cuda(), 30.0, 1e3)
+    want = numpy_features(lbm, mask, cells, 30.0, 1e3)
+    np.testing.assert_allclose(host(x), O.bf16(want.astype(np.float32)), rtol=0, atol=1e-6)
+
+
+def test_fused_inference_matches_unfused_passes():
+    lbm, mask = small_lattice()
+    net = cl.ClosureMLP(seed=3)
+    net.pop_scale, net.force_scale, net.out_scale = 30.0, 1e3, 250.0
+    corr = torch.zeros((19, lbm.n_cells), dtype=torch.float32, device="cuda")
+    w = net.weights_struct()
+    nat.call("fsi_closure_infer", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags),
+             nat.ptr(lbm.force), lbm.steps_done, w, nat.ptr(corr), nat.ptr(net.err),
+             nat.stream_ptr())
+    net.check()
+    fluid = np.nonzero(mask.reshape(-1) == 0)[0]
+    cells = torch.from_numpy(fluid.astype(np.int32)).cuda()
+    x = cl.features(lbm, cells, net.pop_scale, net.force_scale)
+    pad = (-len(fluid)) % 128
+    xp = torch.cat([x, torch.zeros((pad, 640), dtype=x.dtype, device="cuda")])
+    y = net.predict(xp)[:len(fluid)] / net.out_scale
+    got = corr[:, torch.from_numpy(fluid).cuda()].t()
+    assert rel_l2(got.cpu().numpy(), y.cpu().numpy()) < 2e-3
+    solid = np.nonzero(mask.reshape(-1))[0]
+    assert float(corr[:, torch.from_numpy(solid).cuda()].abs().max()) == 0.0
+
+
+def test_gradients_match_the_oracle():
+    rng = np.random.default_rng(11)
+    net = cl.ClosureMLP(seed=5)
+    m = 256
+    xh = O.bf16(rng.standard_normal((m, 640)).astype(np.float32) * 0.5)
+    xh[:, 621:] = 0.0
+    target = rng.standard_normal((m, 19)) * 0.5
+    x = torch.from_numpy(xh.astype(np.float32)).cuda().to(torch.bfloat16)
+    y, acts = net.forward(x, keep=True)
+    t = torch.from_numpy(target.astype(np.float32)).cuda()
+    loss = net.backward(x, y, acts, t, xt=x.t().contiguous())
+    net.check()
+    P = [v.double().cpu().numpy() for v in net.views]
+    yw, aw = O.forward(xh, P[0], P[1], P[2], P[3], P[4], P[5], P[6])
+    np.testing.assert_allclose(y.cpu().numpy(), yw, rtol=2e-2, atol=2e-3)
+    lw, gw = O.backward(xh, yw, aw, target, P[2], P[4], P[6], P[7])
+    assert loss == pytest.approx(lw, rel=1e-3)
+    names = ["W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4"]
+    for name, g in zip(names, net.gviews):
+        want = gw[name]
+        got = g.double().cpu().numpy()
+        if name == "W4":
+            want, got = want[:19], got[:19]
+        if name == "b4":
+            want, got = want[:19], got[:19]
+        if name == "W1":
+            want, got = want[:, :621], got[:, :621]
+        assert rel_l2(got, want) < 3e-2, name
+
+
+def test_training_fits_a_teacher_network():
+    rng = np.random.default_rng(2)
+    teacher = cl.ClosureMLP(seed=9)
+    m = 8192
+    xh = rng.standard_normal((m, 640)).astype(np.float32)
+    xh[:, 621:] = 0
+    x = torch.from_numpy(xh).cuda().to(torch.bfloat16)
+    t = teacher.predict(x).contiguous()
+    student = cl.ClosureMLP(seed=1)
+    tr = cl.ClosureTrainer(student)
+    tr.x, tr.t = x, t
+    hist = tr.fit(steps=300, batch=4096, lr=3e-3)
+    assert hist[-1] < 0.2 * hist[0], (hist[0], hist[-1])
+
+
+def channel_scene(seed, n=(32, 16, 16)):
+    from fsi import scenes
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = n
+    mask = scenes.wall_mask(nx, ny, nz)
+    for _ in range(3):
+        c = [rng.uniform(4, nx - 4), rng.uniform(5, ny - 5), rng.uniform(5, nz - 5)]
+        scenes.add_sphere(mask, c, rng.uniform(2.0, 3.5))
+    cfg = LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=(0.6 - 0.5) / 3.0, force=(2e-5, 0.0, 0.0),
+                    **PERIODIC)
+    return cfg, mask
+
+
+def coarse_errors(cfg, mask, net, steps=40):
+    """rel-L2 velocity error of the plain coarse run and of the closure run against the
+    restricted fine run, after `steps` coarse steps."""
+    fine = LBMSolver3D(cfg)
+    fine.initialize(mask)
+    ccfg = cl.coarse_config(cfg)
+    plain = LBMSolver3D(ccfg)
+    plain.initialize(cl.coarse_mask(mask))
+    sim = cl.ClosureSimulation(cfg, mask, net, check_every=0)
+    for _ in range(steps):
+        fine.step()
+        fine.step()
+        plain.step()
+        sim.step()
+    ref = cl.restrict(fine, plain)
+    tmp = LBMSolver3D(ccfg)
+    tmp.initialize(cl.coarse_mask(mask))
+    tmp.load_populations(ref)
+    u_ref = tmp.velocity_numpy()
+    return rel_l2(plain.velocity_numpy(), u_ref), rel_l2(sim.velocity_numpy(), u_ref)
+
+
+def test_trained_closure_beats_the_plain_coarse_run():
+    net = cl.ClosureMLP(seed=0)
+    tr = cl.ClosureTrainer(net)
+    for seed in (100, 101, 102, 103):
+        cfg, mask = channel_scene(seed)
+        tr.add_run(cfg, mask, warmup=20, snapshots=12, every=4)
+    rows = tr.build()
+    assert rows > 10_000
+    hist = tr.fit(steps=400, batch=8192, lr=2e-3)
+    assert hist[-1] < hist[0]
+    cfg, mask = channel_scene(300)  # held out
+    e_plain, e_closure = coarse_errors(cfg, mask, net)
+    assert e_closure < e_plain, (e_plain, e_closure)
+
+
+def test_guard_falls_back_to_the_fine_grid():
+    cfg, mask = channel_scene(7)
+    net = cl.ClosureMLP(seed=0)
+    sim = cl.ClosureSimulation(cfg, mask, net, mach_tol=1e-12, check_every=3)
+    for _ in range(5):
+        sim.step()
+    assert sim.on_fine_grid and sim.fallback_step == 3 and "Mach" in sim.fallback_reason
+    assert sim.fine.steps_done == 4
+    u = sim.velocity_numpy()
+    assert u.shape == (16, 8, 8, 3) and np.all(np.isfinite(u))
