@@ -312,6 +312,92 @@ def time_batched(args, world, stream) -> dict:
     return out
 
 
+def time_closure(args, world, stream) -> dict:
+    """Learned coarse-grid closure: steps/s of the coarse 192x96x96 lattice with the fused
+    tcgen05 inference and correction after every step, against the plain fine 384x192x192
+    lattice (2 fine steps = 1 coarse step of simulated time), on the bodies channel geometry
+    (static body masks); and the accuracy of a network trained here on restricted fine runs
+    of small channel scenes (seeds 100-103), evaluated on a held-out scene (seed 300)."""
+    import torch
+    from fsi import closure as cl
+    from fsi import scenes
+    from fsi.lbm3d import LBMSolver3D
+
+    # --- training and accuracy on small scenes --------------------------------
+    def channel(seed, n=(48, 24, 24)):
+        rng = np.random.default_rng(seed)
+        nx, ny, nz = n
+        mask = scenes.wall_mask(nx, ny, nz)
+        for _ in range(4):
+            c = [rng.uniform(5, nx - 5), rng.uniform(6, ny - 6), rng.uniform(6, nz - 6)]
+            scenes.add_sphere(mask, c, rng.uniform(2.5, 4.5))
+        cfg = scenes.LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=(0.6 - 0.5) / 3.0,
+                               force=(2e-5, 0.0, 0.0), **scenes.PERIODIC_FACES)
+        return cfg, mask
+
+    t0 = time.perf_counter()
+    net = cl.ClosureMLP(seed=0)
+    trainer = cl.ClosureTrainer(net)
+    for seed in (100, 101, 102, 103):
+        cfg, mask = channel(seed)
+        trainer.add_run(cfg, mask, warmup=30, snapshots=16, every=4)
+    rows = trainer.build()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    hist = trainer.fit(steps=600, batch=16384, lr=2e-3)
+    b.record(stream)
+    torch.cuda.synchronize()
+    train_ms = a.elapsed_time(b) / 600
+    train_s = time.perf_counter() - t0
+    cfg, mask = channel(300)
+    acc = cl.evaluate(cfg, mask, net, coarse_steps=60)
+
+    # --- speed on the bodies channel geometry ------------------------------------
+    bcfg, bsolid, _, _ = scenes.coupled_bodies()
+    fine_cfg = scenes.LBMConfig(nx=bcfg.lbm.nx, ny=bcfg.lbm.ny, nz=bcfg.lbm.nz,
+                                viscosity=bcfg.lbm.viscosity, force=(1e-5, 0.0, 0.0),
+                                **scenes.PERIODIC_FACES)
+    fine = LBMSolver3D(fine_cfg)
+    fine.initialize(bsolid)
+    sim = cl.ClosureSimulation(fine_cfg, bsolid, net, check_every=0)
+    for _ in range(3):
+        fine.step()
+        sim.step()
+    steps = 10
+    a.record(stream)
+    for _ in range(2 * steps):
+        fine.step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    fine_ms = a.elapsed_time(b) / steps  # per coarse-step interval of simulated time
+    a.record(stream)
+    for _ in range(steps):
+        sim.step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    coarse_ms = a.elapsed_time(b) / steps
+    net.check()
+    cells_c = sim.coarse.n_cells
+    mlp_flops = 2.0 * (640 * 64 + 64 * 64 * 2 + 64 * 32) * cells_c
+    out = {
+        "fine_lattice": [fine_cfg.nx, fine_cfg.ny, fine_cfg.nz],
+        "coarse_lattice": [fine_cfg.nx // 2, fine_cfg.ny // 2, fine_cfg.nz // 2],
+        "fine_ms_per_2_steps": round(fine_ms, 4), "closure_ms_per_step": round(coarse_ms, 4),
+        "speedup_vs_fine": round(fine_ms / coarse_ms, 2),
+        "mlp_tflops_per_s_in_step": round(mlp_flops / (coarse_ms * 1e-3) / 1e12, 1),
+        "training": {"rows": rows, "steps": 600, "batch": 16384, "ms_per_step": round(train_ms, 3),
+                     "loss_first": round(hist[0], 5), "loss_last": round(hist[-1], 5),
+                     "wall_s_incl_data": round(train_s, 1)},
+        "accuracy_heldout_48x24x24": {k: (round(v, 5) if isinstance(v, float) else v)
+                                       for k, v in acc.items()},
+        "gpu_launches": steps * 3 + 2 * steps,
+    }
+    del fine, sim
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args) -> dict:
     import torch
     from fsi import scenes
@@ -369,6 +455,8 @@ def run_gpu(args) -> dict:
         coupled = time_coupled(args, world, stream) if not args.no_coupled else {}
         # --- many scenes at once ------------------------------------------------
         batched = time_batched(args, world, stream) if args.batch_scenes > 0 else {}
+        # --- learned coarse-grid closure ------------------------------------------
+        learned = time_closure(args, world, stream) if not args.no_closure else {}
     lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
     lbm_launches = args.steps
     mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
@@ -451,11 +539,12 @@ def run_gpu(args) -> dict:
         "lbm_forms": forms,
         "coupled": coupled,
         "batched": batched,
+        "learned_closure": learned,
         # lattice steps + 3 MPM launches per substep + 3 launches per end-to-end step
         # (force op, step, fused macro + diagnostics) + one step per form per step + coupled
         "gpu_launches": (lbm_launches + 3 * args.steps + 3 * args.steps + len(forms) * args.steps
                          + sum(c["gpu_launches"] for c in coupled.values())
-                         + batched.get("gpu_launches", 0)),
+                         + batched.get("gpu_launches", 0) + learned.get("gpu_launches", 0)),
         "clocks": clocks.summary(),
     }
     if world > 1:
@@ -550,6 +639,7 @@ def main() -> None:
                     choices=["f32/exact", "f32/fast", "f16/fast", "bf16/fast"],
                     help="population storage / collision arithmetic of the headline lattice")
     ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-step timings")
+    ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure section")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched workload (0 skips it)")
     ap.add_argument("--no-coupled-scale", action="store_true",

@@ -261,15 +261,23 @@ struct InferArgs {
   int* err;
 };
 
-constexpr int kInferThreads = 256;
+constexpr int kInferThreads = 512;
 constexpr int kHalfK = kK1 / 2;  // layer-1 input built in two halves of 320
+// A tile is a 2 x 8 x 8 block of cells (128 rows); its 3^3 neighbourhoods lie in a
+// 4 x 10 x 10 halo block whose 23 feature values per cell are staged in shared memory once.
+constexpr int kTX = 2, kTY = 8, kTZ = 8;
+constexpr int kHX = kTX + 2, kHY = kTY + 2, kHZ = kTZ + 2;
+constexpr int kHalo = kHX * kHY * kHZ;
+constexpr int kHaloStride = 23;  // bf16 per halo cell (odd: rows of a warp hit distinct banks)
 constexpr size_t kOffW1 = 0;
 constexpr size_t kOffW2 = kOffW1 + 64 * kK1 * 2;
 constexpr size_t kOffW3 = kOffW2 + 64 * 64 * 2;
 constexpr size_t kOffW4 = kOffW3 + 64 * 64 * 2;
 constexpr size_t kOffA = kOffW4 + kOutPad * 64 * 2;
 constexpr size_t kOffH = kOffA + 128 * kHalfK * 2;
-constexpr size_t kInferSmem = kOffH + 128 * 64 * 2;
+constexpr size_t kOffHalo = kOffH + 128 * 64 * 2;
+constexpr size_t kInferSmem = kOffHalo + (kHalo * kHaloStride + 8) * 2;
+static_assert(kInferSmem <= 227 * 1024 - 2048, "fused inference tile exceeds shared memory");
 
 __device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfloat16* src, int rows,
                                               int kc) {
@@ -280,28 +288,38 @@ __device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfl
   }
 }
 
-// Bias + GELU of TMEM columns [col, col + 32) of this warp's 32 rows into the H tile.
-__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bias, int half,
+// Bias + GELU of TMEM columns [quarter * 16, quarter * 16 + 16) of this warp's 32 rows into H.
+__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bias, int quarter,
                                                 unsigned char* h, int row) {
+  float v[16];
+  tc::tmem_ld16(taddr + quarter * 16, v);
+  uint32_t w[8];
 #pragma unroll
-  for (int c0 = 0; c0 < 32; c0 += 16) {
-    float v[16];
-    tc::tmem_ld16(taddr + half * 32 + c0, v);
-#pragma unroll
-    for (int i = 0; i < 16; i += 2) {
-      const int col = half * 32 + c0 + i;
-      const __nv_bfloat162 pr = __floats2bfloat162_rn(gelu(v[i] + bias[col]), gelu(v[i + 1] + bias[col + 1]));
-      *reinterpret_cast<__nv_bfloat162*>(h + tc::kmajor_offset(row, col, 64)) = pr;
-    }
+  for (int i = 0; i < 16; i += 2) {
+    const int col = quarter * 16 + i;
+    const __nv_bfloat162 pr = __floats2bfloat162_rn(gelu(v[i] + bias[col]), gelu(v[i + 1] + bias[col + 1]));
+    w[i / 2] = *reinterpret_cast<const uint32_t*>(&pr);
   }
+  *reinterpret_cast<uint4*>(h + tc::kmajor_offset(row, quarter * 16, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
+  *reinterpret_cast<uint4*>(h + tc::kmajor_offset(row, quarter * 16 + 8, 64)) = make_uint4(w[4], w[5], w[6], w[7]);
 }
+
+__device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float sb[64 * 3 + kOutPad];
+  // Offset (in bf16) of feature column k within a row's neighbourhood, relative to the halo
+  // cell at the row's (-1, -1, -1) corner; columns past 621 read a zero slot.
+  __shared__ int16_t kmap[kK1];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tbase;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  for (int k = t; k < kK1; k += kInferThreads) {
+    const int o = k / 23, f = k - (k / 23) * 23;
+    kmap[k] = k < kFeat ? (int16_t)((((o / 9) * kHY + (o / 3) % 3) * kHZ + o % 3) * kHaloStride + f)
+                        : (int16_t)(kHalo * kHaloStride);
+  }
   stage_weights(smem + kOffW1, a.w1, 64, kK1);
   stage_weights(smem + kOffW2, a.w2, 64, 64);
   stage_weights(smem + kOffW3, a.w3, 64, 64);
@@ -317,15 +335,19 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
   const uint32_t sA = tc::smem_addr(smem + kOffA), sH = tc::smem_addr(smem + kOffH);
   const uint32_t sW1 = tc::smem_addr(smem + kOffW1), sW2 = tc::smem_addr(smem + kOffW2);
   const uint32_t sW3 = tc::smem_addr(smem + kOffW3), sW4 = tc::smem_addr(smem + kOffW4);
+  __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem + kOffHalo);
   const LbmGeom& g = a.f.g;
-  const long long ntiles = (g.n + 127) / 128;
+  const int ntx = (g.nx + kTX - 1) / kTX, nty = (g.ny + kTY - 1) / kTY, ntz = (g.nz + kTZ - 1) / kTZ;
+  const long long ntiles = (long long)ntx * nty * ntz;
   uint32_t phase = 0;
   bool ok = true;
-  const int row = t & 127, half = t >> 7;              // feature builder role
-  const int lrow = 32 * (warp & 3) + lane, lhalf = warp >> 2;  // epilogue role (TMEM lane)
+  const int row = t & 127, part = t >> 7;                      // feature builder role
+  const int rx = row / (kTY * kTZ), ry = (row / kTZ) % kTY, rz = row % kTZ;
+  const int rowbase = ((rx * kHY + ry) * kHZ + rz) * kHaloStride;
+  const int lrow = 32 * (warp & 3) + lane, lq = warp >> 2;     // epilogue role (TMEM lane)
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
 
-  // Issues the MMAs of one layer and waits for them; false on timeout.
+  // Issues the MMAs of one layer and waits for them; false on timeout (CTA-uniform).
   auto run_layer = [&](uint32_t dcol, uint32_t a_addr, int akc, uint32_t b_addr, int bkc,
                        int kslice0, int nsl, int n, bool accumulate) -> bool {
     tc::fence_smem_for_async();
@@ -341,49 +363,50 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
     const bool r = tc::mbar_wait(&bar, phase & 1, a.err, 3);
     ++phase;
     tc::fence_after_sync();
-    return __syncthreads_and(r) != 0;  // one decision for the CTA (block-wide barriers follow)
+    return __syncthreads_and(r) != 0;
   };
 
   for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    const long long c = tile * 128 + row;
-    const bool valid = c < g.n;
-    int ci = 0, cj = 0, ck = 0;
-    if (valid) {
-      const int nyz = g.ny * g.nz;
-      ci = (int)(c / nyz); cj = (int)((c / g.nz) % g.ny); ck = (int)(c % g.nz);
-    }
-    // Layer 1 in two halves of K.
-    for (int p = 0; p < 2 && ok; ++p) {
-      const int k0 = p * kHalfK + half * (kHalfK / 2), k1 = k0 + kHalfK / 2;
-      unsigned char* A = smem + kOffA;
-      int o = k0 / 23;
+    const int tx = (int)(tile / ((long long)nty * ntz)), ty = (int)((tile / ntz) % nty), tz = (int)(tile % ntz);
+    const int x0 = tx * kTX, y0 = ty * kTY, z0 = tz * kTZ;
+    // Stage the halo block's feature vectors (the previous tile's reads are complete: its
+    // last layer waited on the tensor cores and synchronised the CTA).
+    for (int h = t; h < kHalo; h += kInferThreads) {
+      const int hx = h / (kHY * kHZ), hy = (h / kHZ) % kHY, hz = h % kHZ;
       float v[23];
-      int have = -1;
-      for (int k = k0; k < k1; ++k) {
-        float x = 0.f;
-        if (k < kFeat && valid) {
-          o = k / 23;
-          if (o != have) {
-            int ni, nj, nk;
-            wrap_neighbour(g, ci, cj, ck, o, ni, nj, nk);
-            neighbour_features(a.f, ni, nj, nk, v);
-            have = o;
-          }
-          x = v[k - o * 23];
+      neighbour_features(a.f, wrap(x0 + hx - 1, g.nx), wrap(y0 + hy - 1, g.ny), wrap(z0 + hz - 1, g.nz), v);
+#pragma unroll
+      for (int f = 0; f < 23; ++f) halo[h * kHaloStride + f] = __float2bfloat16_rn(v[f]);
+    }
+    if (t == 0) halo[kHalo * kHaloStride] = __float2bfloat16_rn(0.f);  // the zero slot
+    __syncthreads();
+    // Layer 1 in two halves of K: 8-column pieces of this row's feature vector.
+    for (int p = 0; p < 2 && ok; ++p) {
+      unsigned char* A = smem + kOffA;
+      const int k0 = p * kHalfK + part * (kHalfK / 4);
+      const unsigned short* hb = reinterpret_cast<const unsigned short*>(halo);
+      for (int kk = k0; kk < k0 + kHalfK / 4; kk += 8) {
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          const int i0 = kmap[kk + e], i1 = kmap[kk + e + 1];
+          const uint32_t lo = hb[i0 < kHalo * kHaloStride ? rowbase + i0 : i0];
+          const uint32_t hi = hb[i1 < kHalo * kHaloStride ? rowbase + i1 : i1];
+          w[e / 2] = lo | (hi << 16);
         }
-        *reinterpret_cast<__nv_bfloat16*>(A + tc::kmajor_offset(row, k - p * kHalfK, kHalfK)) =
-            __float2bfloat16_rn(x);
+        *reinterpret_cast<uint4*>(A + tc::kmajor_offset(row, kk - p * kHalfK, kHalfK)) =
+            make_uint4(w[0], w[1], w[2], w[3]);
       }
       ok = run_layer(0, sA, kHalfK, sW1, kK1, p * (kHalfK / 16), kHalfK / 16, 64, p > 0);
     }
     if (!ok) break;
-    hidden_epilogue(tmem + lane_base, sb, lhalf, smem + kOffH, lrow);
+    hidden_epilogue(tmem + lane_base, sb, lq, smem + kOffH, lrow);
     ok = run_layer(64, sH, 64, sW2, 64, 0, 4, 64, false);
     if (!ok) break;
-    hidden_epilogue(tmem + lane_base + 64, sb + 64, lhalf, smem + kOffH, lrow);
+    hidden_epilogue(tmem + lane_base + 64, sb + 64, lq, smem + kOffH, lrow);
     ok = run_layer(128, sH, 64, sW3, 64, 0, 4, 64, false);
     if (!ok) break;
-    hidden_epilogue(tmem + lane_base + 128, sb + 128, lhalf, smem + kOffH, lrow);
+    hidden_epilogue(tmem + lane_base + 128, sb + 128, lq, smem + kOffH, lrow);
     ok = run_layer(192, sH, 64, sW4, 64, 0, 4, kOutPad, false);
     if (!ok) break;
     // Output layer: warps 0-3 own the 128 rows; 19 of the 32 columns are used.
@@ -391,8 +414,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
       float y[32];
       tc::tmem_ld16(tmem + lane_base + 192, *reinterpret_cast<float(*)[16]>(y));
       tc::tmem_ld16(tmem + lane_base + 208, *reinterpret_cast<float(*)[16]>(y + 16));
-      const long long cc = tile * 128 + lrow;
-      if (cc < g.n) {
+      const int ox = x0 + lrow / (kTY * kTZ), oy = y0 + (lrow / kTZ) % kTY, oz = z0 + lrow % kTZ;
+      if (ox < g.nx && oy < g.ny && oz < g.nz) {
+        const long long cc = ((long long)ox * g.ny + oy) * g.nz + oz;
         const bool fluid = !(a.f.flags[cc] & kFlagSolid);
 #pragma unroll
         for (int q = 0; q < kOut; ++q)
@@ -605,7 +629,8 @@ extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long tiles = (a.f.g.n + 127) / 128;
+  const long long tiles = (long long)((a.f.g.nx + kTX - 1) / kTX) * ((a.f.g.ny + kTY - 1) / kTY) *
+                          ((a.f.g.nz + kTZ - 1) / kTZ);
   const int grid = (int)(tiles < sms ? tiles : sms);
   cudaFuncSetAttribute(closure_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kInferSmem);

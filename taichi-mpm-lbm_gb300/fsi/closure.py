@@ -391,3 +391,41 @@ class ClosureSimulation:
         u = self.fine.velocity_numpy()
         nx, ny, nz = (n // 2 for n in u.shape[:3])
         return u.reshape(nx, 2, ny, 2, nz, 2, 3).mean(axis=(1, 3, 5))
+
+
+def evaluate(fine_cfg: LBMConfig, fine_mask: np.ndarray, net: ClosureMLP, coarse_steps: int,
+             flow_axis: int = 0) -> dict:
+    """Error of the coarse runs against the restricted plain fine run after ``coarse_steps``
+    coarse steps (2 * coarse_steps fine steps): rel-L2 velocity of the plain coarse run and
+    of the closure run, and the relative error of the mean flow along ``flow_axis`` (the
+    channel's flow rate, the body-drag balance of a force-driven channel)."""
+    fine = LBMSolver3D(fine_cfg)
+    fine.initialize(fine_mask)
+    ccfg = coarse_config(fine_cfg)
+    cmask = coarse_mask(fine_mask)
+    plain = LBMSolver3D(ccfg)
+    plain.initialize(cmask)
+    sim = ClosureSimulation(fine_cfg, fine_mask, net)
+    for _ in range(coarse_steps):
+        fine.step()
+        fine.step()
+        plain.step()
+        sim.step()
+    ref = LBMSolver3D(ccfg)
+    ref.initialize(cmask)
+    ref.load_populations(restrict(fine, plain))
+    u_ref, u_plain, u_cl = ref.velocity_numpy(), plain.velocity_numpy(), sim.velocity_numpy()
+    fluid = cmask == 0
+
+    def l2(u):
+        return float(np.linalg.norm((u - u_ref)[fluid]) / max(np.linalg.norm(u_ref[fluid]), 1e-30))
+
+    def flow(u):
+        return float(u[..., flow_axis][fluid].mean())
+
+    q_ref = flow(u_ref)
+    return {"coarse_steps": coarse_steps, "velocity_l2_plain": l2(u_plain),
+            "velocity_l2_closure": l2(u_cl),
+            "flow_rate_error_plain": abs(flow(u_plain) - q_ref) / abs(q_ref),
+            "flow_rate_error_closure": abs(flow(u_cl) - q_ref) / abs(q_ref),
+            "fallback": sim.fallback_reason or None}
