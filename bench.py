@@ -379,7 +379,7 @@ def time_closure(args, world, stream) -> dict:
     coarse_ms = a.elapsed_time(b) / steps
     net.check()
     cells_c = sim.coarse.n_cells
-    mlp_flops = 2.0 * (640 * 64 + 64 * 64 * 2 + 64 * 32) * cells_c
+    mlp_flops = 2.0 * (656 * 64 + 64 * 64 * 2 + 64 * 32) * cells_c
     out = {
         "fine_lattice": [fine_cfg.nx, fine_cfg.ny, fine_cfg.nz],
         "coarse_lattice": [fine_cfg.nx // 2, fine_cfg.ny // 2, fine_cfg.nz // 2],

@@ -395,16 +395,17 @@ int fsi_batch_coupling_assemble(const fsi_batch* batch, const uint32_t* flags, i
                                 void* counters, void* stream);
 
 /* ------------------------------------------------------------ learned closure
- * A per-cell MLP (621 -> 64 -> 64 -> 64 -> 19, GELU, BF16 weights, FP32 accumulation) that
+ * A per-cell MLP (656 -> 64 -> 64 -> 64 -> 19, GELU, BF16 weights, FP32 accumulation) that
  * corrects the post-stream populations of a lattice run on a grid 2x coarser than the one it
  * was trained on, on the tcgen05 tensor cores. No reference counterpart. Lattices must use
  * FP32 population storage. Features of a cell: for each of its 27 neighbours (periodic wrap,
  * offsets (dx, dy, dz) in {-1,0,1}^3 with dz fastest) the 19 populations as
  * (f_q - w_q rho0) * pop_scale, the occupancy (1 solid) and the force * force_scale:
- * 27 * 23 = 621 values, zero-padded to 640 columns. */
-#define FSI_CLOSURE_FEATURES 640
+ * 27 * 23 = 621 values, neighbour o in columns [24 o, 24 o + 23), column 24 o + 23 and columns
+ * 648..655 zero: 656 columns. */
+#define FSI_CLOSURE_FEATURES 656
 
-/* Feature rows (BF16 [m][640]) of the cells listed in `cells` (device int32[m]). */
+/* Feature rows (BF16 [m][656]) of the cells listed in `cells` (device int32[m]). */
 int fsi_closure_features(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
                          const float* force, int64_t steps_done, const int32_t* cells, int32_t m,
                          float pop_scale, float force_scale, void* x, void* stream);
@@ -437,7 +438,7 @@ typedef struct fsi_closure_gemm_desc {
 } fsi_closure_gemm_desc;
 int fsi_closure_gemm(const fsi_closure_gemm_desc* desc, void* stream);
 
-/* Network of the fused inference: BF16 w1 [64][640], w2 [64][64], w3 [64][64], w4 [32][64]
+/* Network of the fused inference: BF16 w1 [64][656], w2 [64][64], w3 [64][64], w4 [32][64]
  * (rows 19..31 zero), FP32 bias = b1[64] b2[64] b3[64] b4[32]; correction = y / out_scale. */
 typedef struct fsi_closure_weights {
   const void* w1;
@@ -452,7 +453,8 @@ typedef struct fsi_closure_weights {
 } fsi_closure_weights;
 
 /* Fused inference over every cell: features built in shared memory, the four layers on the
- * tensor cores with the weights resident, corrections corr [19][N] (0 on solid cells). */
+ * tensor cores with the weights resident, corrections corr [19][N] (0 on solid cells).
+ * Network: BF16 w1 [64][656]. */
 int fsi_closure_infer(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
                       const float* force, int64_t steps_done, const fsi_closure_weights* weights,
                       float* corr, int32_t* err, void* stream);

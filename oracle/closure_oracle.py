@@ -2,7 +2,7 @@
 learned-closure MLP of fsi/closure.py, used only by the tests as the checker of the
 tensor-core GEMMs, the fused inference and the gradients.
 
-Network: 640 -> 64 -> 64 -> 64 -> 32 (19 used), GELU (tanh form of Hendrycks & Gimpel
+Network: 656 -> 64 -> 64 -> 64 -> 32 (19 used), GELU (tanh form of Hendrycks & Gimpel
 2016), BF16 weights and activations, FP32/float64 accumulation. There is no reference
 counterpart to pin it to: the device path is checked against this restatement.
 """
@@ -32,7 +32,7 @@ def gelu_grad(z):
 
 
 def forward(x, W1, b1, W2, b2, W3, b3, W4):
-    """x: [m, 640] (already BF16 values); returns y [m, 32] and the activations."""
+    """x: [m, 656] (already BF16 values); returns y [m, 32] and the activations."""
     acts = []
     h = np.asarray(x, np.float64)
     for W, b in ((W1, b1), (W2, b2), (W3, b3)):

@@ -1,4 +1,4 @@
-// Learned coarse-grid closure: a per-cell MLP (621 -> 64 -> 64 -> 64 -> 19, GELU) that
+// Learned coarse-grid closure: a per-cell MLP (656 -> 64 -> 64 -> 64 -> 19, GELU) that
 // corrects the populations of a lattice running on a 2x coarser grid, on the fifth-
 // generation tensor cores (tcgen05, BF16 operands, FP32 accumulation in tensor memory).
 // No reference counterpart.
@@ -6,10 +6,12 @@
 // Features of a cell x: for each of the 27 cells y of its 3^3 neighbourhood (periodic wrap,
 // offsets in (dx, dy, dz) order, dz fastest) the 19 post-stream populations as scaled
 // deviations (f_q(y) - w_q rho0) * pop_scale, the occupancy of y (1 solid, 0 fluid) and the
-// 3 force components of y * force_scale: 27 * 23 = 621 values, zero-padded to K = 640.
+// 3 force components of y * force_scale: 27 * 23 = 621 values. Column layout: neighbour o's
+// 23 values in columns [24 o, 24 o + 23), column 24 o + 23 zero, columns 648..655 zero
+// (K = 656), so every neighbour group is three aligned 16-byte pieces.
 //
 // Kernels:
-//   closure_features_kernel: the feature rows of a list of cells, BF16 [M][640] (training).
+//   closure_features_kernel: the feature rows of a list of cells, BF16 [M][656] (training).
 //   gemm_kernel: C = A B^T for K-major BF16 A [M][K], B [N][K] (row-major in global memory),
 //     128-row tiles, split-K over blockIdx.y, two-stage cp.async pipeline into shared memory
 //     (canonical no-swizzle core-matrix layout), tcgen05.mma into tensor memory, and a fused
@@ -33,8 +35,8 @@
 namespace fsi {
 namespace {
 
-constexpr int kFeat = 621;
-constexpr int kK1 = 640;
+constexpr int kGroup = 24;           // columns per neighbour (23 values + 1 zero)
+constexpr int kK1 = 27 * kGroup + 8;  // 656
 constexpr int kOut = 19;
 constexpr int kOutPad = 32;
 
@@ -85,7 +87,7 @@ __device__ __forceinline__ void wrap_neighbour(const LbmGeom& g, int i, int j, i
   nk = nk < 0 ? nk + g.nz : (nk >= g.nz ? nk - g.nz : nk);
 }
 
-// Feature rows of cells[m] (BF16, [M][640]); one thread per (row, neighbour).
+// Feature rows of cells[m] (BF16, [M][656]); one thread per (row, neighbour).
 __global__ void __launch_bounds__(256) closure_features_kernel(FeatArgs a,
                                                                 const int32_t* __restrict__ cells,
                                                                 int m, __nv_bfloat16* __restrict__ x) {
@@ -94,7 +96,7 @@ __global__ void __launch_bounds__(256) closure_features_kernel(FeatArgs a,
   const int row = (int)(t / 28), o = (int)(t % 28);
   __nv_bfloat16* out = x + (size_t)row * kK1;
   if (o == 27) {  // padding columns
-    for (int c = kFeat; c < kK1; ++c) out[c] = __float2bfloat16(0.f);
+    for (int c = 27 * kGroup; c < kK1; ++c) out[c] = __float2bfloat16(0.f);
     return;
   }
   const int c = cells[row];
@@ -105,7 +107,8 @@ __global__ void __launch_bounds__(256) closure_features_kernel(FeatArgs a,
   float v[23];
   neighbour_features(a, ni, nj, nk, v);
 #pragma unroll
-  for (int f = 0; f < 23; ++f) out[o * 23 + f] = __float2bfloat16_rn(v[f]);
+  for (int f = 0; f < 23; ++f) out[o * kGroup + f] = __float2bfloat16_rn(v[f]);
+  out[o * kGroup + 23] = __float2bfloat16_rn(0.f);
 }
 
 // ------------------------------------------------------------------ GEMM
@@ -251,7 +254,7 @@ __global__ void __launch_bounds__(128) gemm_kernel(GemmArgs g) {
 // ------------------------------------------------------------ fused inference
 struct InferArgs {
   FeatArgs f;
-  const __nv_bfloat16* __restrict__ w1;  // [64][640]
+  const __nv_bfloat16* __restrict__ w1;  // [64][656]
   const __nv_bfloat16* __restrict__ w2;  // [64][64]
   const __nv_bfloat16* __restrict__ w3;  // [64][64]
   const __nv_bfloat16* __restrict__ w4;  // [32][64], rows >= 19 zero
@@ -262,21 +265,22 @@ struct InferArgs {
 };
 
 constexpr int kInferThreads = 512;
-constexpr int kHalfK = kK1 / 2;  // layer-1 input built in two halves of 320
+// Layer 1 runs in three passes over neighbour groups 0-9, 10-19 and 20-26 (+ 8 zero columns):
+// 240, 240 and 176 columns of the A tile.
+constexpr int kPassCols = 240;
 // A tile is a 2 x 8 x 8 block of cells (128 rows); its 3^3 neighbourhoods lie in a
-// 4 x 10 x 10 halo block whose 23 feature values per cell are staged in shared memory once.
+// 4 x 10 x 10 halo block whose feature groups are staged in shared memory once.
 constexpr int kTX = 2, kTY = 8, kTZ = 8;
 constexpr int kHX = kTX + 2, kHY = kTY + 2, kHZ = kTZ + 2;
 constexpr int kHalo = kHX * kHY * kHZ;
-constexpr int kHaloStride = 23;  // bf16 per halo cell (odd: rows of a warp hit distinct banks)
 constexpr size_t kOffW1 = 0;
 constexpr size_t kOffW2 = kOffW1 + 64 * kK1 * 2;
 constexpr size_t kOffW3 = kOffW2 + 64 * 64 * 2;
 constexpr size_t kOffW4 = kOffW3 + 64 * 64 * 2;
 constexpr size_t kOffA = kOffW4 + kOutPad * 64 * 2;
-constexpr size_t kOffH = kOffA + 128 * kHalfK * 2;
+constexpr size_t kOffH = kOffA + 128 * kPassCols * 2;
 constexpr size_t kOffHalo = kOffH + 128 * 64 * 2;
-constexpr size_t kInferSmem = kOffHalo + (kHalo * kHaloStride + 8) * 2;
+constexpr size_t kInferSmem = kOffHalo + (kHalo + 1) * kGroup * 2;  // + one zero group
 static_assert(kInferSmem <= 227 * 1024 - 2048, "fused inference tile exceeds shared memory");
 
 __device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfloat16* src, int rows,
@@ -309,17 +313,9 @@ __device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >=
 __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float sb[64 * 3 + kOutPad];
-  // Offset (in bf16) of feature column k within a row's neighbourhood, relative to the halo
-  // cell at the row's (-1, -1, -1) corner; columns past 621 read a zero slot.
-  __shared__ int16_t kmap[kK1];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tbase;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  for (int k = t; k < kK1; k += kInferThreads) {
-    const int o = k / 23, f = k - (k / 23) * 23;
-    kmap[k] = k < kFeat ? (int16_t)((((o / 9) * kHY + (o / 3) % 3) * kHZ + o % 3) * kHaloStride + f)
-                        : (int16_t)(kHalo * kHaloStride);
-  }
   stage_weights(smem + kOffW1, a.w1, 64, kK1);
   stage_weights(smem + kOffW2, a.w2, 64, 64);
   stage_weights(smem + kOffW3, a.w3, 64, 64);
@@ -341,9 +337,6 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
   const long long ntiles = (long long)ntx * nty * ntz;
   uint32_t phase = 0;
   bool ok = true;
-  const int row = t & 127, part = t >> 7;                      // feature builder role
-  const int rx = row / (kTY * kTZ), ry = (row / kTZ) % kTY, rz = row % kTZ;
-  const int rowbase = ((rx * kHY + ry) * kHZ + rz) * kHaloStride;
   const int lrow = 32 * (warp & 3) + lane, lq = warp >> 2;     // epilogue role (TMEM lane)
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
 
@@ -366,38 +359,50 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
     return __syncthreads_and(r) != 0;
   };
 
+  if (t < 3) reinterpret_cast<uint4*>(halo + kHalo * kGroup)[t] = make_uint4(0, 0, 0, 0);  // zero group
   for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int tx = (int)(tile / ((long long)nty * ntz)), ty = (int)((tile / ntz) % nty), tz = (int)(tile % ntz);
     const int x0 = tx * kTX, y0 = ty * kTY, z0 = tz * kTZ;
-    // Stage the halo block's feature vectors (the previous tile's reads are complete: its
-    // last layer waited on the tensor cores and synchronised the CTA).
+    // Stage the halo block's feature vectors (the previous tile's reads of the halo are
+    // complete: its last layer waited on the tensor cores and synchronised the CTA).
     for (int h = t; h < kHalo; h += kInferThreads) {
       const int hx = h / (kHY * kHZ), hy = (h / kHZ) % kHY, hz = h % kHZ;
       float v[23];
       neighbour_features(a.f, wrap(x0 + hx - 1, g.nx), wrap(y0 + hy - 1, g.ny), wrap(z0 + hz - 1, g.nz), v);
+      uint32_t w[12];
 #pragma unroll
-      for (int f = 0; f < 23; ++f) halo[h * kHaloStride + f] = __float2bfloat16_rn(v[f]);
-    }
-    if (t == 0) halo[kHalo * kHaloStride] = __float2bfloat16_rn(0.f);  // the zero slot
-    __syncthreads();
-    // Layer 1 in two halves of K: 8-column pieces of this row's feature vector.
-    for (int p = 0; p < 2 && ok; ++p) {
-      unsigned char* A = smem + kOffA;
-      const int k0 = p * kHalfK + part * (kHalfK / 4);
-      const unsigned short* hb = reinterpret_cast<const unsigned short*>(halo);
-      for (int kk = k0; kk < k0 + kHalfK / 4; kk += 8) {
-        uint32_t w[4];
-#pragma unroll
-        for (int e = 0; e < 8; e += 2) {
-          const int i0 = kmap[kk + e], i1 = kmap[kk + e + 1];
-          const uint32_t lo = hb[i0 < kHalo * kHaloStride ? rowbase + i0 : i0];
-          const uint32_t hi = hb[i1 < kHalo * kHaloStride ? rowbase + i1 : i1];
-          w[e / 2] = lo | (hi << 16);
-        }
-        *reinterpret_cast<uint4*>(A + tc::kmajor_offset(row, kk - p * kHalfK, kHalfK)) =
-            make_uint4(w[0], w[1], w[2], w[3]);
+      for (int f = 0; f < 22; f += 2) {
+        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[f], v[f + 1]);
+        w[f / 2] = *reinterpret_cast<const uint32_t*>(&pr);
       }
-      ok = run_layer(0, sA, kHalfK, sW1, kK1, p * (kHalfK / 16), kHalfK / 16, 64, p > 0);
+      {
+        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[22], 0.f);
+        w[11] = *reinterpret_cast<const uint32_t*>(&pr);
+      }
+      uint4* dst = reinterpret_cast<uint4*>(halo + h * kGroup);
+      dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+      dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+      dst[2] = make_uint4(w[8], w[9], w[10], w[11]);
+    }
+    __syncthreads();
+    // Layer 1 in three passes of neighbour groups: each group is three 16-byte pieces.
+    for (int p = 0; p < 3 && ok; ++p) {
+      unsigned char* A = smem + kOffA;
+      const int o0 = p * 10, ng = p < 2 ? 10 : 7;
+      const int cols = p < 2 ? kPassCols : 7 * kGroup + 8;
+      const int pieces = cols / 8;  // ng groups x 3 pieces (+1 zero piece in the last pass)
+      for (int it = t; it < 128 * pieces; it += kInferThreads) {
+        const int r = it & 127, pc = it >> 7;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (pc < ng * 3) {
+          const int o = o0 + pc / 3;
+          const int rrx = r / (kTY * kTZ), rry = (r / kTZ) % kTY, rrz = r % kTZ;
+          const int hc = ((rrx + o / 9) * kHY + rry + (o / 3) % 3) * kHZ + rrz + o % 3;
+          val = reinterpret_cast<const uint4*>(halo + hc * kGroup)[pc % 3];
+        }
+        *reinterpret_cast<uint4*>(A + tc::kmajor_offset(r, pc * 8, cols)) = val;
+      }
+      ok = run_layer(0, sA, cols, sW1, kK1, o0 * kGroup / 16, cols / 16, 64, p > 0);
     }
     if (!ok) break;
     hidden_epilogue(tmem + lane_base, sb, lq, smem + kOffH, lrow);

@@ -4,7 +4,8 @@ A lattice run on a grid 2x coarser than a reference ("fine") run, with lattice u
 (acoustic scaling: dx and dt double, so velocities in lattice units are unchanged, the
 lattice viscosity halves and a body force doubles), is corrected after every step by a
 per-cell MLP: 621 features of the cell's 3^3 neighbourhood (19 populations, occupancy and
-3 force components per neighbour) -> 64 -> 64 -> 64 -> 19 corrections of the post-stream
+3 force components per neighbour, laid out in 27 groups of 24 columns, 656 columns in all)
+-> 64 -> 64 -> 64 -> 19 corrections of the post-stream
 populations, GELU activations, BF16 weights with FP32 accumulation. Training pairs come
 from restricted fine runs of the plain solver: the correction is what the coarse step
 misses, R(f(t + 2 dt_f)) - C(R(f(t))), with R the 2x2x2 restriction and C one coarse step.
@@ -28,7 +29,9 @@ from . import _native as nat
 from .config import LBMConfig
 from .lbm3d import LBMSolver3D
 
-FEATURES = 640  # 621 used
+FEATURES = 656  # 27 groups of 24 columns (23 values + 1 zero) + 8 zero columns
+# feature columns that always hold zero (the last of each group, and the tail)
+_ZERO_COLS = [c for c in range(FEATURES) if c >= 27 * 24 or c % 24 == 23]
 HIDDEN = 64
 OUT = 19
 OUT_PAD = 32
@@ -112,7 +115,7 @@ class ClosureMLP:
         W1, _, W2, _, W3, _, W4, _ = self.views
         for W, fan_in in ((W1, 621), (W2, HIDDEN), (W3, HIDDEN), (W4, HIDDEN)):
             W.copy_(torch.randn(W.shape, generator=g) * math.sqrt(2.0 / fan_in))
-        W1[:, 621:] = 0.0
+        W1[:, _ZERO_COLS] = 0.0
         W4[OUT:] = 0.0
         W4.mul_(0.1)
         self.pop_scale = self.force_scale = self.out_scale = 1.0
@@ -136,7 +139,7 @@ class ClosureMLP:
         w.pop_scale, w.force_scale, w.out_scale = self.pop_scale, self.force_scale, self.out_scale
         return w
 
-    # -- forward / backward over a batch of feature rows (BF16 [m][640]) ------------
+    # -- forward / backward over a batch of feature rows (BF16 [m][656]) ------------
     def forward(self, x: torch.Tensor, keep: bool = False):
         m = x.shape[0]
         dev, bf = self.device, torch.bfloat16
@@ -196,7 +199,7 @@ class ClosureMLP:
             w_t = self.w3t if layer == 3 else self.w2t
         gW4[OUT:] = 0.0
         gb4[OUT:] = 0.0
-        gW1[:, 621:] = 0.0
+        gW1[:, _ZERO_COLS] = 0.0
         return float(loss.item())
 
     def adam_step(self, lr: float = 1e-3, beta1: float = 0.9, beta2: float = 0.999,
@@ -223,7 +226,7 @@ class ClosureMLP:
 
 # ------------------------------------------------------------------ data
 def features(lbm: LBMSolver3D, cells: torch.Tensor, pop_scale: float, force_scale: float):
-    """BF16 feature rows [m][640] of the given cells (int32 device tensor) of `lbm`."""
+    """BF16 feature rows [m][656] of the given cells (int32 device tensor) of `lbm`."""
     m = int(cells.numel())
     x = torch.empty((m, FEATURES), dtype=torch.bfloat16, device=lbm._device)
     nat.call("fsi_closure_features", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags),

@@ -25,7 +25,7 @@ def host(t: torch.Tensor) -> np.ndarray:
     return t.float().cpu().numpy().astype(np.float64)
 
 
-@pytest.mark.parametrize("m,n,k", [(300, 64, 640), (128, 32, 64), (257, 128, 96), (64, 640, 1024)])
+@pytest.mark.parametrize("m,n,k", [(300, 64, 656), (128, 32, 64), (257, 128, 96), (64, 656, 1024)])
 def test_gemm_store_and_atomic(m, n, k):
     rng = np.random.default_rng(m + n + k)
     a, b = bf(rng.standard_normal((m, k))), bf(rng.standard_normal((n, k)))
@@ -42,7 +42,7 @@ def test_gemm_store_and_atomic(m, n, k):
 
 def test_gemm_gelu_epilogues():
     rng = np.random.default_rng(7)
-    m, n, k = 384, 64, 640
+    m, n, k = 384, 64, 656
     a, b = bf(rng.standard_normal((m, k)) * 0.1), bf(rng.standard_normal((n, k)) * 0.1)
     bias = torch.from_numpy(rng.standard_normal(n).astype(np.float32)).cuda()
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -81,7 +81,7 @@ def numpy_features(lbm, mask, cells, pop_scale, force_scale):
     g = lbm.force_numpy()
     w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
     nx, ny, nz = mask.shape
-    out = np.zeros((len(cells), 640))
+    out = np.zeros((len(cells), 656))
     for r, c in enumerate(cells):
         i, j, k = c // (ny * nz), (c // nz) % ny, c % nz
         col = 0
@@ -94,7 +94,7 @@ def numpy_features(lbm, mask, cells, pop_scale, force_scale):
                     out[r, col:col + 19] = pops
                     out[r, col + 19] = 1.0 if solid else 0.0
                     out[r, col + 20:col + 23] = g[a, b, e] * force_scale
-                    col += 23
+                    col += 24
     return out
 
 
@@ -120,7 +120,7 @@ def test_fused_inference_matches_unfused_passes():
     cells = torch.from_numpy(fluid.astype(np.int32)).cuda()
     x = cl.features(lbm, cells, net.pop_scale, net.force_scale)
     pad = (-len(fluid)) % 128
-    xp = torch.cat([x, torch.zeros((pad, 640), dtype=x.dtype, device="cuda")])
+    xp = torch.cat([x, torch.zeros((pad, 656), dtype=x.dtype, device="cuda")])
     y = net.predict(xp)[:len(fluid)] / net.out_scale
     got = corr[:, torch.from_numpy(fluid).cuda()].t()
     assert rel_l2(got.cpu().numpy(), y.cpu().numpy()) < 2e-3
@@ -132,8 +132,8 @@ def test_gradients_match_the_oracle():
     rng = np.random.default_rng(11)
     net = cl.ClosureMLP(seed=5)
     m = 256
-    xh = O.bf16(rng.standard_normal((m, 640)).astype(np.float32) * 0.5)
-    xh[:, 621:] = 0.0
+    xh = O.bf16(rng.standard_normal((m, 656)).astype(np.float32) * 0.5)
+    xh[:, cl._ZERO_COLS] = 0.0
     target = rng.standard_normal((m, 19)) * 0.5
     x = torch.from_numpy(xh.astype(np.float32)).cuda().to(torch.bfloat16)
     y, acts = net.forward(x, keep=True)
@@ -154,7 +154,8 @@ def test_gradients_match_the_oracle():
         if name == "b4":
             want, got = want[:19], got[:19]
         if name == "W1":
-            want, got = want[:, :621], got[:, :621]
+            keep = [c for c in range(656) if c not in set(cl._ZERO_COLS)]
+            want, got = want[:, keep], got[:, keep]
         assert rel_l2(got, want) < 3e-2, name
 
 
@@ -162,8 +163,8 @@ def test_training_fits_a_teacher_network():
     rng = np.random.default_rng(2)
     teacher = cl.ClosureMLP(seed=9)
     m = 8192
-    xh = rng.standard_normal((m, 640)).astype(np.float32)
-    xh[:, 621:] = 0
+    xh = rng.standard_normal((m, 656)).astype(np.float32)
+    xh[:, cl._ZERO_COLS] = 0
     x = torch.from_numpy(xh).cuda().to(torch.bfloat16)
     t = teacher.predict(x).contiguous()
     student = cl.ClosureMLP(seed=1)
