@@ -165,7 +165,7 @@ class ClosureMLP:
         return self.forward(x)[:, :OUT] + self.views[7][:OUT]
 
     def backward(self, x: torch.Tensor, y: torch.Tensor, acts: dict, target: torch.Tensor,
-                 xt: torch.Tensor | None = None, k_chunk: int = 4096) -> float:
+                 xt: torch.Tensor | None = None, k_chunk: int = 1024) -> float:
         """Gradients of the mean-square loss into self.grads; returns the loss."""
         m = x.shape[0]
         dev, bf = self.device, torch.bfloat16
