@@ -18,9 +18,10 @@
 //     epilogue: store FP32 / add FP32 atomically / bias + GELU forward (BF16 activations,
 //     their transpose and the FP32 pre-activation) / GELU backward (BF16 gradient and its
 //     transpose).
-//   closure_infer_kernel: the fused inference pass: features built by the threads straight
-//     into shared memory, the four layers on the tensor cores with the weights resident in
-//     shared memory, and the 19 outputs written as corrections per cell.
+//   closure_infer_kernel: the fused inference pass: layer 1 as an implicit 3x3x3
+//     convolution over per-cell feature rows staged once in shared memory, the four layers
+//     on the tensor cores with the weights resident in shared memory, two tiles in flight,
+//     and the 19 outputs written as corrections per cell.
 //   closure_apply_kernel: f_q(x) += correction, mass-conserving (sum_q w-weighted projection).
 //   loss / Adam kernels for training.
 #include <cuda_bf16.h>
@@ -40,15 +41,24 @@ constexpr int kK1 = 27 * kGroup + 8;  // 656
 constexpr int kOut = 19;
 constexpr int kOutPad = 32;
 
-// GELU, tanh form of Hendrycks & Gimpel (2016): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))).
+// GELU, tanh form of Hendrycks & Gimpel (2016): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
+// with tanh from the hardware approximation (tanh.approx.f32, relative error about 2^-11,
+// below the BF16 rounding of the activations). Training and inference use the same form.
 constexpr float kGeluC0 = 0.7978845608028654f;
 constexpr float kGeluC1 = 0.044715f;
+constexpr float kGeluC01 = kGeluC0 * kGeluC1;
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ float gelu(float z) {
-  const float t = tanhf(kGeluC0 * (z + kGeluC1 * z * z * z));
-  return 0.5f * z * (1.0f + t);
+  const float t = tanh_approx(z * fmaf(kGeluC01, z * z, kGeluC0));
+  const float hz = 0.5f * z;
+  return fmaf(hz, t, hz);
 }
 __device__ __forceinline__ float gelu_grad(float z) {
-  const float t = tanhf(kGeluC0 * (z + kGeluC1 * z * z * z));
+  const float t = tanh_approx(z * fmaf(kGeluC01, z * z, kGeluC0));
   return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * kGeluC0 * (1.0f + 3.0f * kGeluC1 * z * z);
 }
 
@@ -252,6 +262,61 @@ __global__ void __launch_bounds__(128) gemm_kernel(GemmArgs g) {
 
 
 // ------------------------------------------------------------ fused inference
+//
+// Layer 1 is a 3 x 3 x 3 convolution of per-cell vectors of 24 channels (the 23 feature
+// values of a cell + one zero), so it runs as an implicit GEMM: the 24-channel rows of a
+// block of cells are staged in shared memory once, and each of the 27 neighbour offsets is
+// an MMA whose A operand is the same rows shifted by that offset.
+//
+// Rows are laid out for this: three channel chunks (channels 0-7, 8-15, 16-23), each an
+// array of rows at a 16-byte stride, so the core matrices of 8 rows x 16 bytes follow one
+// another (stride byte offset 128) and chunk c + 1 lies kChunkBytes after chunk c (leading
+// byte offset). A row shift is a start-address shift of 16 bytes. Per offset o, one K = 16
+// MMA covers channels 0-15; channels 16-23 of two offsets a < b of the same x-plane share
+// one MMA whose second K half starts (row_b - row_a) * 16 bytes after the first. That is
+// 27 + 3 * 5 = 42 MMAs of M = 128, N = 64, K = 16 per tile of 128 rows.
+//
+// Cells are walked in columns: 32 cells along z x 11 lines along y, streamed along x. An
+// x-plane of a column is a 34 x 13 halo block (442 rows, z fastest); planes sit in a ring
+// of four slots (x - 1, x, x + 1 in use, x + 2 being filled). The output rows of a plane
+// are the 374 rows of lines 1..11, covered by three M tiles of 128 consecutive rows; rows
+// on the z halo (and past line 11) are computed and discarded.
+//
+// Each CTA (one per SM, 512 threads) takes a contiguous range of (column, x) plane steps.
+// Two tiles are in flight: while the epilogues of tile t (bias + GELU of layers 1-3,
+// output of layer 4) run on the CUDA cores, the tensor cores run layer 1 of tile t + 1,
+// issued in three chunks of 14 MMAs between the small layers of tile t. The next x-plane
+// is loaded into registers during the first tile of a plane step and stored to its slot
+// after the second, so its global-memory latency overlaps two tiles of work.
+constexpr int kLine = 34;                             // halo line along z: 32 cells + 2
+constexpr int kLineCells = 32;
+constexpr int kLines = 11;                            // output lines along y per column
+constexpr int kPlaneRows = kLine * (kLines + 2);      // 442
+constexpr int kPlaneTiles = (kLine * kLines + 127) / 128;  // 3
+constexpr int kSlots = 4;
+constexpr int kPadLo = 1, kPadHi = 48;
+constexpr int kChunkRows = kPadLo + kSlots * kPlaneRows + kPadHi;
+constexpr int kChunkBytes = kChunkRows * 16;
+constexpr int kL1Mmas = 27 + 3 * 5;                   // 42
+constexpr int kL1Chunk = kL1Mmas / 3;                 // 14 MMAs per issue
+constexpr int kInferThreads = 512;
+static_assert(kPlaneRows <= kInferThreads, "one staging row per thread");
+static_assert(kPlaneTiles == 3, "the next plane is loaded in tile 0 and stored after tile 1");
+static_assert(kL1Chunk * 3 == kL1Mmas, "layer 1 is issued in three equal chunks");
+// Highest row read: the last tile's last row, offset +35, and the +16-byte second half of
+// the unpaired offset of a plane.
+static_assert(kLine + 128 * kPlaneTiles + kLine + 2 <= kPlaneRows + kPadHi, "row padding");
+static_assert(kChunkBytes < (1 << 18), "leading byte offset field");
+
+constexpr size_t kOffW1 = 0;                                  // 42 slices of 64 x 16
+constexpr size_t kOffW2 = kOffW1 + (size_t)kL1Mmas * 64 * 16 * 2;
+constexpr size_t kOffW3 = kOffW2 + 64 * 64 * 2;
+constexpr size_t kOffW4 = kOffW3 + 64 * 64 * 2;
+constexpr size_t kOffH = kOffW4 + kOutPad * 64 * 2;
+constexpr size_t kOffRows = kOffH + 128 * 64 * 2;
+constexpr size_t kInferSmem = kOffRows + 3 * (size_t)kChunkBytes;
+static_assert(kInferSmem <= 227 * 1024 - 2048, "fused inference exceeds shared memory");
+
 struct InferArgs {
   FeatArgs f;
   const __nv_bfloat16* __restrict__ w1;  // [64][656]
@@ -262,26 +327,9 @@ struct InferArgs {
   float out_scale;                       // correction = y / out_scale
   float* __restrict__ corr;              // [19][N]
   int* err;
+  int nyb, nzb;                          // columns: ceil(ny / 11) x ceil(nz / 32)
+  long long work;                        // plane steps: columns * nx
 };
-
-constexpr int kInferThreads = 512;
-// Layer 1 runs in three passes over neighbour groups 0-9, 10-19 and 20-26 (+ 8 zero columns):
-// 240, 240 and 176 columns of the A tile.
-constexpr int kPassCols = 240;
-// A tile is a 2 x 8 x 8 block of cells (128 rows); its 3^3 neighbourhoods lie in a
-// 4 x 10 x 10 halo block whose feature groups are staged in shared memory once.
-constexpr int kTX = 2, kTY = 8, kTZ = 8;
-constexpr int kHX = kTX + 2, kHY = kTY + 2, kHZ = kTZ + 2;
-constexpr int kHalo = kHX * kHY * kHZ;
-constexpr size_t kOffW1 = 0;
-constexpr size_t kOffW2 = kOffW1 + 64 * kK1 * 2;
-constexpr size_t kOffW3 = kOffW2 + 64 * 64 * 2;
-constexpr size_t kOffW4 = kOffW3 + 64 * 64 * 2;
-constexpr size_t kOffA = kOffW4 + kOutPad * 64 * 2;
-constexpr size_t kOffH = kOffA + 128 * kPassCols * 2;
-constexpr size_t kOffHalo = kOffH + 128 * 64 * 2;
-constexpr size_t kInferSmem = kOffHalo + (kHalo + 1) * kGroup * 2;  // + one zero group
-static_assert(kInferSmem <= 227 * 1024 - 2048, "fused inference tile exceeds shared memory");
 
 __device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfloat16* src, int rows,
                                               int kc) {
@@ -290,6 +338,39 @@ __device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfl
     *reinterpret_cast<uint4*>(dst + tc::kmajor_offset(r, k, kc)) =
         *reinterpret_cast<const uint4*>(src + (size_t)r * kc + k);
   }
+}
+
+// Row offset of neighbour o (dx, dy, dz in {-1, 0, 1}, o = 9 (dx+1) + 3 (dy+1) + dz + 1)
+// within its x-plane.
+__host__ __device__ constexpr int tap_dy(int o) { return (o / 3) % 3 - 1; }
+__host__ __device__ constexpr int tap_dz(int o) { return o % 3 - 1; }
+__host__ __device__ constexpr int tap_off(int o) { return kLine * tap_dy(o) + tap_dz(o); }
+
+// Layer-1 weight slices: slice s < 27 holds W1 columns [24 s, 24 s + 16) (channels 0-15 of
+// neighbour s); slice 27 + 5 p + j holds channels 16-23 of neighbours 9 p + 2 j and
+// 9 p + 2 j + 1 (j < 4), or of neighbour 9 p + 8 and zeros (j = 4).
+__device__ __forceinline__ void stage_w1(unsigned char* dst, const __nv_bfloat16* w1) {
+  for (int p = threadIdx.x; p < kL1Mmas * 64 * 2; p += blockDim.x) {
+    const int s = p >> 7, r = (p >> 1) & 63, half = p & 1;
+    int col;
+    if (s < 27) {
+      col = kGroup * s + 8 * half;
+    } else {
+      const int u = s - 27, plane = u / 5, j = u % 5;
+      col = (j == 4 && half) ? -1 : kGroup * (9 * plane + 2 * j + half) + 16;
+    }
+    const uint4 v = col < 0 ? make_uint4(0, 0, 0, 0)
+                            : *reinterpret_cast<const uint4*>(w1 + (size_t)r * kK1 + col);
+    *reinterpret_cast<uint4*>(dst + (size_t)s * 2048 + tc::kmajor_offset(r, 8 * half, 16)) = v;
+  }
+}
+
+__device__ __forceinline__ float2 gelu2(float2 z) {
+  const float2 z2 = vmul(z, z);
+  const float2 u = vmul(z, vfma(z2, splat<float2>(kGeluC01), splat<float2>(kGeluC0)));
+  const float2 t = make_float2(tanh_approx(u.x), tanh_approx(u.y));
+  const float2 hz = vmul(z, splat<float2>(0.5f));
+  return vfma(hz, t, hz);
 }
 
 // Bias + GELU of TMEM columns [quarter * 16, quarter * 16 + 16) of this warp's 32 rows into H.
@@ -301,7 +382,8 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bia
 #pragma unroll
   for (int i = 0; i < 16; i += 2) {
     const int col = quarter * 16 + i;
-    const __nv_bfloat162 pr = __floats2bfloat162_rn(gelu(v[i] + bias[col]), gelu(v[i + 1] + bias[col + 1]));
+    const float2 g = gelu2(vadd(make_float2(v[i], v[i + 1]), make_float2(bias[col], bias[col + 1])));
+    const __nv_bfloat162 pr = __floats2bfloat162_rn(g.x, g.y);
     w[i / 2] = *reinterpret_cast<const uint32_t*>(&pr);
   }
   *reinterpret_cast<uint4*>(h + tc::kmajor_offset(row, quarter * 16, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -309,129 +391,252 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bia
 }
 
 __device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+__device__ __forceinline__ int wrap_any(int v, int n) {
+  const int m = v % n;
+  return m < 0 ? m + n : m;
+}
+
+// One halo row of an x-plane: where it lies in the lattice, and its raw values.
+struct HaloRow {
+  float pop[19];
+  float frc[3];
+  bool solid;
+};
+
+__device__ __forceinline__ uint32_t halo_cell(const LbmGeom& g, int x, int y0, int z0, int r) {
+  const int hy = r / kLine, hz = r - hy * kLine;
+  const int j = wrap_any(y0 + hy - 1, g.ny), k = wrap_any(z0 + hz - 1, g.nz);
+  return (uint32_t)(((long long)x * g.ny + j) * g.nz + k);
+}
+
+// Issues the global loads of halo row r of plane x (flags `fl` already known).
+__device__ __forceinline__ void load_row(const FeatArgs& a, int x, int y0, int z0, int r, uint32_t fl,
+                                         HaloRow& h) {
+  const int hy = r / kLine, hz = r - hy * kLine;
+  const Deltas d(a.g, x, wrap_any(y0 + hy - 1, a.g.ny), wrap_any(z0 + hz - 1, a.g.nz));
+  const uint32_t n = (uint32_t)a.g.n;
+  h.solid = fl & kFlagSolid;
+#pragma unroll
+  for (int q = 0; q < 19; ++q)
+    h.pop[q] = h.solid ? 0.f : gather32<FSI_STORAGE_F32>(a.pops, n, d, fl, q, a.parity, 0.f);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) h.frc[c] = a.force[c * n + d.c];
+}
+
+// Converts a loaded halo row to its 24 BF16 channels and stores them at `row` of the chunks.
+__device__ __forceinline__ void store_row(const FeatArgs& a, const HaloRow& h, unsigned char* rows,
+                                          int row) {
+  float v[24];
+#pragma unroll
+  for (int q = 0; q < 19; ++q) v[q] = h.solid ? 0.f : (h.pop[q] - weight_of(q) * a.rho0) * a.pop_scale;
+  v[19] = h.solid ? 1.f : 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) v[20 + c] = h.frc[c] * a.force_scale;
+  v[23] = 0.f;
+  uint32_t w[12];
+#pragma unroll
+  for (int i = 0; i < 24; i += 2) {
+    const __nv_bfloat162 pr = __floats2bfloat162_rn(v[i], v[i + 1]);
+    w[i / 2] = *reinterpret_cast<const uint32_t*>(&pr);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    *reinterpret_cast<uint4*>(rows + (size_t)c * kChunkBytes + (size_t)row * 16) =
+        make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+}
 
 __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float sb[64 * 3 + kOutPad];
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bar_l1, bar_l;
   __shared__ uint32_t tbase;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  stage_weights(smem + kOffW1, a.w1, 64, kK1);
+  stage_w1(smem + kOffW1, a.w1);
   stage_weights(smem + kOffW2, a.w2, 64, 64);
   stage_weights(smem + kOffW3, a.w3, 64, 64);
   stage_weights(smem + kOffW4, a.w4, kOutPad, 64);
   for (int i = t; i < 64 * 3 + kOutPad; i += kInferThreads) sb[i] = a.b[i];
-  if (warp == 0) tc::tmem_alloc(&tbase, 256);
-  if (t == 0) tc::mbar_init(&bar, 1);
+  // Padding rows stay zero (they feed discarded rows only, but must be finite).
+  for (int i = t; i < 3 * (kPadLo + kPadHi); i += kInferThreads) {
+    const int c = i / (kPadLo + kPadHi), p = i % (kPadLo + kPadHi);
+    const int row = p < kPadLo ? p : kPadLo + kSlots * kPlaneRows + (p - kPadLo);
+    *reinterpret_cast<uint4*>(smem + kOffRows + (size_t)c * kChunkBytes + (size_t)row * 16) =
+        make_uint4(0, 0, 0, 0);
+  }
+  if (warp == 0) tc::tmem_alloc(&tbase, 512);
+  if (t == 0) { tc::mbar_init(&bar_l1, 1); tc::mbar_init(&bar_l, 1); }
   tc::fence_smem_for_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tbase;
-  const uint32_t sA = tc::smem_addr(smem + kOffA), sH = tc::smem_addr(smem + kOffH);
+  unsigned char* rows = smem + kOffRows;
+  const uint32_t sRows = tc::smem_addr(rows), sH = tc::smem_addr(smem + kOffH);
   const uint32_t sW1 = tc::smem_addr(smem + kOffW1), sW2 = tc::smem_addr(smem + kOffW2);
   const uint32_t sW3 = tc::smem_addr(smem + kOffW3), sW4 = tc::smem_addr(smem + kOffW4);
-  __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem + kOffHalo);
   const LbmGeom& g = a.f.g;
-  const int ntx = (g.nx + kTX - 1) / kTX, nty = (g.ny + kTY - 1) / kTY, ntz = (g.nz + kTZ - 1) / kTZ;
-  const long long ntiles = (long long)ntx * nty * ntz;
-  uint32_t phase = 0;
-  bool ok = true;
-  const int lrow = 32 * (warp & 3) + lane, lq = warp >> 2;     // epilogue role (TMEM lane)
+  const int lrow = 32 * (warp & 3) + lane, lq = warp >> 2;  // epilogue role (TMEM lane)
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+  constexpr uint32_t kIdesc64 = tc::idesc_bf16(128, 64), kIdesc32 = tc::idesc_bf16(128, kOutPad);
 
-  // Issues the MMAs of one layer and waits for them; false on timeout (CTA-uniform).
-  auto run_layer = [&](uint32_t dcol, uint32_t a_addr, int akc, uint32_t b_addr, int bkc,
-                       int kslice0, int nsl, int n, bool accumulate) -> bool {
+  // Layer-1 MMAs [14 c, 14 c + 14) of the tile at plane step q, M tile m, into TMEM column d.
+  auto issue_l1 = [&](int c, int q, int m, uint32_t d) {
+    const int base = kLine + 128 * m;
+    for (int s = kL1Chunk * c; s < kL1Chunk * (c + 1); ++s) {
+      uint64_t adesc;
+      if (s < 27) {
+        const int row = kPadLo + ((q + s / 9) & 3) * kPlaneRows + base + tap_off(s);
+        adesc = tc::smem_desc(sRows + (uint32_t)row * 16u, (uint32_t)kChunkBytes, 128u);
+      } else {
+        const int u = s - 27, plane = u / 5, j = u % 5, o = 9 * plane + 2 * j;
+        const int row = kPadLo + ((q + plane) & 3) * kPlaneRows + base + tap_off(o);
+        const uint32_t lbo = j < 4 ? (uint32_t)(tap_off(o + 1) - tap_off(o)) * 16u : 16u;
+        adesc = tc::smem_desc(sRows + 2u * (uint32_t)kChunkBytes + (uint32_t)row * 16u, lbo, 128u);
+      }
+      tc::mma_bf16(d, adesc, tc::smem_desc(sW1 + (uint32_t)s * 2048u, 128u, 256u), kIdesc64, s > 0);
+    }
+  };
+  // One hidden or output layer: A = H (128 x 64), B = weights at w (n x 64).
+  auto issue_layer = [&](uint32_t w, uint32_t idesc, uint32_t d) {
+    for (int s = 0; s < 4; ++s)
+      tc::mma_bf16(d, tc::tile_desc(sH, 64, s), tc::tile_desc(w, 64, s), idesc, s > 0);
+  };
+
+  const long long work = a.work;
+  const long long w0 = work * blockIdx.x / gridDim.x, w1 = work * (blockIdx.x + 1) / gridDim.x;
+  uint32_t n_l1 = 0, n_l = 0;   // phases of the two barriers waited for so far
+  uint32_t c_l1 = 0, c_l = 0;   // commits to them (thread 0)
+  int last_bar = -1;            // barrier of the most recent commit (thread 0)
+  bool ok = true, dok = true;   // dok: the last output-layer wait of this thread
+  HaloRow pre;                  // next x-plane's row of this thread, in flight
+  uint32_t fl_next = 0;         // flags of the row after that
+  for (long long p0 = w0; p0 < w1 && ok;) {
+    const long long col = p0 / g.nx;
+    const int xs = (int)(p0 - col * g.nx);
+    const int nq = (int)min((long long)(g.nx - xs), w1 - p0);  // plane steps in this segment
+    const int yb = (int)(col / a.nzb), zb = (int)(col - (long long)yb * a.nzb);
+    const int y0 = yb * kLines, z0 = zb * kLineCells;
+    // Prime the ring with planes xs - 1, xs, xs + 1 (ordinals 0-2; ordinal u is plane
+    // xs - 1 + u in slot u & 3).
+    __syncthreads();  // the previous segment's last tile has read its rows
+    for (int i = t; i < 3 * kPlaneRows; i += kInferThreads) {
+      const int u = i / kPlaneRows, r = i - u * kPlaneRows;
+      const int x = wrap(xs - 1 + u, g.nx);
+      HaloRow h;
+      load_row(a.f, x, y0, z0, r, a.f.flags[halo_cell(g, x, y0, z0, r)], h);
+      store_row(a.f, h, rows, kPadLo + u * kPlaneRows + r);
+    }
+    if (t < kPlaneRows && nq > 1) fl_next = a.f.flags[halo_cell(g, wrap(xs + 2, g.nx), y0, z0, t)];
     tc::fence_smem_for_async();
     tc::fence_before_sync();
     __syncthreads();
     if (t == 0) {
       tc::fence_after_sync();
-      for (int s = 0; s < nsl; ++s)
-        tc::mma_bf16(tmem + dcol, tc::tile_desc(a_addr, akc, s), tc::tile_desc(b_addr, bkc, kslice0 + s),
-                     tc::idesc_bf16(128, n), accumulate || s > 0);
-      tc::mma_commit(&bar);
+      for (int c = 0; c < 3; ++c) issue_l1(c, 0, 0, tmem + ((n_l1 & 1) << 8));
+      tc::mma_commit(&bar_l1);
+      ++c_l1;
+      last_bar = 0;
     }
-    const bool r = tc::mbar_wait(&bar, phase & 1, a.err, 3);
-    ++phase;
-    tc::fence_after_sync();
-    return __syncthreads_and(r) != 0;
-  };
-
-  if (t < 3) reinterpret_cast<uint4*>(halo + kHalo * kGroup)[t] = make_uint4(0, 0, 0, 0);  // zero group
-  for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    const int tx = (int)(tile / ((long long)nty * ntz)), ty = (int)((tile / ntz) % nty), tz = (int)(tile % ntz);
-    const int x0 = tx * kTX, y0 = ty * kTY, z0 = tz * kTZ;
-    // Stage the halo block's feature vectors (the previous tile's reads of the halo are
-    // complete: its last layer waited on the tensor cores and synchronised the CTA).
-    for (int h = t; h < kHalo; h += kInferThreads) {
-      const int hx = h / (kHY * kHZ), hy = (h / kHZ) % kHY, hz = h % kHZ;
-      float v[23];
-      neighbour_features(a.f, wrap(x0 + hx - 1, g.nx), wrap(y0 + hy - 1, g.ny), wrap(z0 + hz - 1, g.nz), v);
-      uint32_t w[12];
-#pragma unroll
-      for (int f = 0; f < 22; f += 2) {
-        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[f], v[f + 1]);
-        w[f / 2] = *reinterpret_cast<const uint32_t*>(&pr);
+    const int ntile = kPlaneTiles * nq;
+    for (int ti = 0; ti < ntile; ++ti) {
+      const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
+      const bool next = ti + 1 < ntile;
+      const int nq1 = (ti + 1) / kPlaneTiles, nm1 = (ti + 1) - nq1 * kPlaneTiles;
+      const uint32_t tb = tmem + ((n_l1 & 1) << 8), tn = tmem + (((n_l1 + 1) & 1) << 8);
+      if (m == 0 && q + 1 < nq && t < kPlaneRows) {
+        // Ordinal q + 3 (plane xs + q + 2) into registers; flags of ordinal q + 4.
+        load_row(a.f, wrap(xs + q + 2, g.nx), y0, z0, t, fl_next, pre);
+        if (q + 2 < nq) fl_next = a.f.flags[halo_cell(g, wrap(xs + q + 3, g.nx), y0, z0, t)];
       }
-      {
-        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[22], 0.f);
-        w[11] = *reinterpret_cast<const uint32_t*>(&pr);
+      // Phase A: layer-1 epilogue; issue layer 2 and the first chunk of the next tile.
+      bool w = tc::mbar_wait(&bar_l1, n_l1 & 1, a.err, 3);
+      ++n_l1;
+      tc::fence_after_sync();
+      hidden_epilogue(tb + lane_base, sb, lq, smem + kOffH, lrow);
+      tc::fence_smem_for_async();
+      tc::fence_before_sync();
+      if (!(ok = __syncthreads_and(w && dok) != 0)) break;
+      if (t == 0) {
+        tc::fence_after_sync();
+        issue_layer(sW2, kIdesc64, tb + 64);
+        tc::mma_commit(&bar_l);
+        ++c_l;
+        last_bar = 1;
+        if (next) issue_l1(0, nq1, nm1, tn);
       }
-      uint4* dst = reinterpret_cast<uint4*>(halo + h * kGroup);
-      dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-      dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
-      dst[2] = make_uint4(w[8], w[9], w[10], w[11]);
-    }
-    __syncthreads();
-    // Layer 1 in three passes of neighbour groups: each group is three 16-byte pieces.
-    for (int p = 0; p < 3 && ok; ++p) {
-      unsigned char* A = smem + kOffA;
-      const int o0 = p * 10, ng = p < 2 ? 10 : 7;
-      const int cols = p < 2 ? kPassCols : 7 * kGroup + 8;
-      const int pieces = cols / 8;  // ng groups x 3 pieces (+1 zero piece in the last pass)
-      for (int it = t; it < 128 * pieces; it += kInferThreads) {
-        const int r = it & 127, pc = it >> 7;
-        uint4 val = make_uint4(0, 0, 0, 0);
-        if (pc < ng * 3) {
-          const int o = o0 + pc / 3;
-          const int rrx = r / (kTY * kTZ), rry = (r / kTZ) % kTY, rrz = r % kTZ;
-          const int hc = ((rrx + o / 9) * kHY + rry + (o / 3) % 3) * kHZ + rrz + o % 3;
-          val = reinterpret_cast<const uint4*>(halo + hc * kGroup)[pc % 3];
+      // Phase B: layer-2 epilogue; layer 3 and the second chunk.
+      w = tc::mbar_wait(&bar_l, n_l & 1, a.err, 4);
+      ++n_l;
+      tc::fence_after_sync();
+      hidden_epilogue(tb + lane_base + 64, sb + 64, lq, smem + kOffH, lrow);
+      tc::fence_smem_for_async();
+      tc::fence_before_sync();
+      if (!(ok = __syncthreads_and(w) != 0)) break;
+      if (t == 0) {
+        tc::fence_after_sync();
+        issue_layer(sW3, kIdesc64, tb + 128);
+        tc::mma_commit(&bar_l);
+        ++c_l;
+        if (next) issue_l1(1, nq1, nm1, tn);
+      }
+      // Phase C: layer-3 epilogue; output layer and the last chunk.
+      w = tc::mbar_wait(&bar_l, n_l & 1, a.err, 5);
+      ++n_l;
+      tc::fence_after_sync();
+      hidden_epilogue(tb + lane_base + 128, sb + 128, lq, smem + kOffH, lrow);
+      tc::fence_smem_for_async();
+      tc::fence_before_sync();
+      if (!(ok = __syncthreads_and(w) != 0)) break;
+      if (t == 0) {
+        tc::fence_after_sync();
+        issue_layer(sW4, kIdesc32, tb + 192);
+        tc::mma_commit(&bar_l);
+        ++c_l;
+        last_bar = 1;
+        if (next) {
+          issue_l1(2, nq1, nm1, tn);
+          tc::mma_commit(&bar_l1);
+          ++c_l1;
+          last_bar = 0;
         }
-        *reinterpret_cast<uint4*>(A + tc::kmajor_offset(r, pc * 8, cols)) = val;
       }
-      ok = run_layer(0, sA, cols, sW1, kK1, o0 * kGroup / 16, cols / 16, 64, p > 0);
-    }
-    if (!ok) break;
-    hidden_epilogue(tmem + lane_base, sb, lq, smem + kOffH, lrow);
-    ok = run_layer(64, sH, 64, sW2, 64, 0, 4, 64, false);
-    if (!ok) break;
-    hidden_epilogue(tmem + lane_base + 64, sb + 64, lq, smem + kOffH, lrow);
-    ok = run_layer(128, sH, 64, sW3, 64, 0, 4, 64, false);
-    if (!ok) break;
-    hidden_epilogue(tmem + lane_base + 128, sb + 128, lq, smem + kOffH, lrow);
-    ok = run_layer(192, sH, 64, sW4, 64, 0, 4, kOutPad, false);
-    if (!ok) break;
-    // Output layer: warps 0-3 own the 128 rows; 19 of the 32 columns are used.
-    if (warp < 4) {
-      float y[32];
-      tc::tmem_ld16(tmem + lane_base + 192, *reinterpret_cast<float(*)[16]>(y));
-      tc::tmem_ld16(tmem + lane_base + 208, *reinterpret_cast<float(*)[16]>(y + 16));
-      const int ox = x0 + lrow / (kTY * kTZ), oy = y0 + (lrow / kTZ) % kTY, oz = z0 + lrow % kTZ;
-      if (ox < g.nx && oy < g.ny && oz < g.nz) {
-        const long long cc = ((long long)ox * g.ny + oy) * g.nz + oz;
-        const bool fluid = !(a.f.flags[cc] & kFlagSolid);
+      // Phase D: outputs (warps with lq < 2 hold columns 0-31; 19 are used).
+      w = tc::mbar_wait(&bar_l, n_l & 1, a.err, 6);
+      ++n_l;
+      tc::fence_after_sync();
+      if (lq < 2) {
+        float y[16];
+        tc::tmem_ld16(tb + lane_base + 192 + 16 * lq, y);
+        const int pr = kLine + 128 * m + lrow;       // row within the plane
+        const int hy = pr / kLine, hz = pr - hy * kLine;
+        const int oy = y0 + hy - 1, oz = z0 + hz - 1, ox = xs + q;
+        if (w && hy >= 1 && hy <= kLines && hz >= 1 && hz <= kLineCells && oy < g.ny && oz < g.nz) {
+          const long long cc = ((long long)ox * g.ny + oy) * g.nz + oz;
+          const int row = kPadLo + ((q + 1) & 3) * kPlaneRows + pr;
+          const unsigned short occ =
+              *reinterpret_cast<const unsigned short*>(rows + 2 * (size_t)kChunkBytes + (size_t)row * 16 + 6);
+          const bool fluid = occ == 0;
 #pragma unroll
-        for (int q = 0; q < kOut; ++q)
-          a.corr[(size_t)q * g.n + cc] = fluid ? (y[q] + sb[192 + q]) / a.out_scale : 0.f;
+          for (int i = 0; i < 16; ++i) {
+            const int qo = 16 * lq + i;
+            if (qo < kOut) a.corr[(size_t)qo * g.n + cc] = fluid ? (y[i] + sb[192 + qo]) / a.out_scale : 0.f;
+          }
+        }
       }
+      if (m == 1 && q + 1 < nq && t < kPlaneRows) store_row(a.f, pre, rows, kPadLo + ((q + 3) & 3) * kPlaneRows + t);
+      dok = w;  // made CTA-uniform at the next barrier
     }
+    p0 += nq;
+    ok = __syncthreads_and(ok && dok) != 0;
+  }
+  if (!ok && last_bar >= 0 && t == 0) {
+    // Let the MMAs in flight finish before the tensor memory is released (bounded).
+    if (last_bar == 0) tc::mbar_wait(&bar_l1, (c_l1 - 1) & 1, nullptr, 0);
+    else tc::mbar_wait(&bar_l, (c_l - 1) & 1, nullptr, 0);
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // f_q(x) += c_q - w_q sum_p c_p on fluid cells (the correction moves no mass).
@@ -631,12 +836,13 @@ extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const
   a.out_scale = w->out_scale;
   a.corr = corr;
   a.err = err;
+  a.nyb = (a.f.g.ny + kLines - 1) / kLines;
+  a.nzb = (a.f.g.nz + kLineCells - 1) / kLineCells;
+  a.work = (long long)a.nyb * a.nzb * a.f.g.nx;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long tiles = (long long)((a.f.g.nx + kTX - 1) / kTX) * ((a.f.g.ny + kTY - 1) / kTY) *
-                          ((a.f.g.nz + kTZ - 1) / kTZ);
-  const int grid = (int)(tiles < sms ? tiles : sms);
+  const int grid = (int)(a.work < sms ? a.work : sms);
   cudaFuncSetAttribute(closure_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kInferSmem);
   closure_infer_kernel<<<grid, kInferThreads, kInferSmem, as_stream(stream)>>>(a);
