@@ -452,12 +452,16 @@ typedef struct fsi_closure_weights {
   int32_t reserved;
 } fsi_closure_weights;
 
-/* Fused inference over every cell: features built in shared memory, the four layers on the
- * tensor cores with the weights resident, corrections corr [19][N] (0 on solid cells).
- * Network: BF16 w1 [64][656]. */
+/* Bytes of the scratch `rows` buffer fsi_closure_infer needs for this lattice (the BF16
+ * feature rows of every cell on a lattice padded to whole inference columns), or -1. */
+int64_t fsi_closure_rows_bytes(const fsi_lbm_desc* desc);
+/* Fused inference over every cell: the cells' feature rows written to `rows` (16-byte
+ * aligned, fsi_closure_rows_bytes bytes), then layer 1 as a 3x3x3 convolution and the four
+ * layers on the tensor cores with the weights resident in shared memory; corrections
+ * corr [19][N] (0 on solid cells). Network: BF16 w1 [64][656]. */
 int fsi_closure_infer(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
                       const float* force, int64_t steps_done, const fsi_closure_weights* weights,
-                      float* corr, int32_t* err, void* stream);
+                      void* rows, float* corr, int32_t* err, void* stream);
 /* f_q += corr_q - w_q sum_p corr_p on fluid cells (moves no mass). */
 int fsi_closure_apply(const fsi_lbm_desc* desc, float* pops, const uint32_t* flags,
                       int64_t steps_done, const float* corr, void* stream);

@@ -276,18 +276,24 @@ __global__ void __launch_bounds__(128) gemm_kernel(GemmArgs g) {
 // one MMA whose second K half starts (row_b - row_a) * 16 bytes after the first. That is
 // 27 + 3 * 5 = 42 MMAs of M = 128, N = 64, K = 16 per tile of 128 rows.
 //
-// Cells are walked in columns: 32 cells along z x 11 lines along y, streamed along x. An
-// x-plane of a column is a 34 x 13 halo block (442 rows, z fastest); planes sit in a ring
-// of four slots (x - 1, x, x + 1 in use, x + 2 being filled). The output rows of a plane
-// are the 374 rows of lines 1..11, covered by three M tiles of 128 consecutive rows; rows
-// on the z halo (and past line 11) are computed and discarded.
+// closure_rows_kernel first writes every cell's 24 BF16 channels to global memory in the
+// same chunked layout, on a lattice padded by one periodic image in y and z (and to whole
+// columns), so that each halo line of the inference blocks is a contiguous 544-byte run
+// per chunk. Cells are walked in columns: 32 cells along z x 11 lines along y, streamed
+// along x. An x-plane of a column is a 34 x 13 halo block (442 rows, z fastest), fetched
+// into a ring of four slots (x - 1, x, x + 1 in use, x + 2 in flight) by 39 bulk copies
+// (cp.async.bulk) that complete on the slot's mbarrier. The output rows of a plane are the
+// 374 rows of lines 1..11, covered by three M tiles of 128 consecutive rows; rows on the z
+// halo (and past line 11) are computed and discarded.
 //
-// Each CTA (one per SM, 512 threads) takes a contiguous range of (column, x) plane steps.
-// Two tiles are in flight: while the epilogues of tile t (bias + GELU of layers 1-3,
-// output of layer 4) run on the CUDA cores, the tensor cores run layer 1 of tile t + 1,
-// issued in three chunks of 14 MMAs between the small layers of tile t. The next x-plane
-// is loaded into registers during the first tile of a plane step and stored to its slot
-// after the second, so its global-memory latency overlaps two tiles of work.
+// Each CTA (one per SM) takes a contiguous range of (column, x) plane steps. Warp 16 issues
+// the bulk copies and the MMAs; warps 0-15 run the epilogues (warp w reads TMEM lanes
+// 32 (w % 4) .. + 31 and columns 16 (w / 4) .. + 15). Two tiles are in flight: while the
+// epilogues of tile t (bias + GELU of layers 1-3, output of layer 4) run on the CUDA cores,
+// the tensor cores run layer 1 of tile t + 1, issued in three chunks of 14 MMAs between the
+// small layers of tile t. Hand-overs are mbarriers in both directions (MMA commits to the
+// epilogue warps; one arrival per epilogue warp to the issuer), so no CTA-wide barrier
+// sits inside the loop.
 constexpr int kLine = 34;                             // halo line along z: 32 cells + 2
 constexpr int kLineCells = 32;
 constexpr int kLines = 11;                            // output lines along y per column
@@ -299,9 +305,12 @@ constexpr int kChunkRows = kPadLo + kSlots * kPlaneRows + kPadHi;
 constexpr int kChunkBytes = kChunkRows * 16;
 constexpr int kL1Mmas = 27 + 3 * 5;                   // 42
 constexpr int kL1Chunk = kL1Mmas / 3;                 // 14 MMAs per issue
-constexpr int kInferThreads = 512;
-static_assert(kPlaneRows <= kInferThreads, "one staging row per thread");
-static_assert(kPlaneTiles == 3, "the next plane is loaded in tile 0 and stored after tile 1");
+constexpr int kEpiWarps = 16;                         // epilogue warps (4 per TMEM lane quarter)
+constexpr int kWorkers = 32 * kEpiWarps;
+constexpr int kColGroups = 64 / 16 / (kEpiWarps / 4);  // 16-column groups per warp and layer
+constexpr int kInferThreads = kWorkers + 32;          // + the copy / MMA issuing warp
+constexpr uint32_t kLineBytes = kLine * 16;           // one halo line of one chunk
+constexpr uint32_t kPlaneBytes = 3u * (kLines + 2) * kLineBytes;
 static_assert(kL1Chunk * 3 == kL1Mmas, "layer 1 is issued in three equal chunks");
 // Highest row read: the last tile's last row, offset +35, and the +16-byte second half of
 // the unpaired offset of a plane.
@@ -317,19 +326,70 @@ constexpr size_t kOffRows = kOffH + 128 * 64 * 2;
 constexpr size_t kInferSmem = kOffRows + 3 * (size_t)kChunkBytes;
 static_assert(kInferSmem <= 227 * 1024 - 2048, "fused inference exceeds shared memory");
 
+// Padded row lattice of the inference: nx x ny_pad x nz_pad rows per chunk; padded row
+// (x, jp, kp) holds cell (x, (jp - 1) mod ny, (kp - 1) mod nz).
+struct RowGeom {
+  int nyb, nzb;           // columns: ceil(ny / 11) x ceil(nz / 32)
+  int ny_pad, nz_pad;     // 11 nyb + 2, 32 nzb + 2
+  long long chunk_rows;   // nx * ny_pad * nz_pad
+};
+
+inline RowGeom row_geom(const LbmGeom& g) {
+  RowGeom r;
+  r.nyb = (g.ny + kLines - 1) / kLines;
+  r.nzb = (g.nz + kLineCells - 1) / kLineCells;
+  r.ny_pad = kLines * r.nyb + 2;
+  r.nz_pad = kLineCells * r.nzb + 2;
+  r.chunk_rows = (long long)g.nx * r.ny_pad * r.nz_pad;
+  return r;
+}
+
 struct InferArgs {
   FeatArgs f;
-  const __nv_bfloat16* __restrict__ w1;  // [64][656]
-  const __nv_bfloat16* __restrict__ w2;  // [64][64]
-  const __nv_bfloat16* __restrict__ w3;  // [64][64]
-  const __nv_bfloat16* __restrict__ w4;  // [32][64], rows >= 19 zero
-  const float* __restrict__ b;           // b1[64] b2[64] b3[64] b4[32]
-  float out_scale;                       // correction = y / out_scale
-  float* __restrict__ corr;              // [19][N]
+  RowGeom rg;
+  const unsigned char* __restrict__ grows;  // [3][chunk_rows][16 B] from closure_rows_kernel
+  const __nv_bfloat16* __restrict__ w1;     // [64][656]
+  const __nv_bfloat16* __restrict__ w2;     // [64][64]
+  const __nv_bfloat16* __restrict__ w3;     // [64][64]
+  const __nv_bfloat16* __restrict__ w4;     // [32][64], rows >= 19 zero
+  const float* __restrict__ b;              // b1[64] b2[64] b3[64] b4[32]
+  float out_scale;                          // correction = y / out_scale
+  float* __restrict__ corr;                 // [19][N]
   int* err;
-  int nyb, nzb;                          // columns: ceil(ny / 11) x ceil(nz / 32)
-  long long work;                        // plane steps: columns * nx
+  long long work;                           // plane steps: columns * nx
 };
+
+__device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+__device__ __forceinline__ int wrap_any(int v, int n) {
+  const int m = v % n;
+  return m < 0 ? m + n : m;
+}
+
+// The 24 BF16 channels of every padded row (one thread per row).
+__global__ void __launch_bounds__(kBlock) closure_rows_kernel(FeatArgs a, RowGeom rg,
+                                                              unsigned char* __restrict__ grows) {
+  const long long r = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (r >= rg.chunk_rows) return;
+  const int kp = (int)(r % rg.nz_pad);
+  const long long xj = r / rg.nz_pad;
+  const int jp = (int)(xj % rg.ny_pad), x = (int)(xj / rg.ny_pad);
+  float v[23];
+  neighbour_features(a, x, wrap_any(jp - 1, a.g.ny), wrap_any(kp - 1, a.g.nz), v);
+  uint32_t w[12];
+#pragma unroll
+  for (int i = 0; i < 22; i += 2) {
+    const __nv_bfloat162 pr = __floats2bfloat162_rn(v[i], v[i + 1]);
+    w[i / 2] = *reinterpret_cast<const uint32_t*>(&pr);
+  }
+  {
+    const __nv_bfloat162 pr = __floats2bfloat162_rn(v[22], 0.f);
+    w[11] = *reinterpret_cast<const uint32_t*>(&pr);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    *reinterpret_cast<uint4*>(grows + ((size_t)c * rg.chunk_rows + r) * 16) =
+        make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+}
 
 __device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfloat16* src, int rows,
                                               int kc) {
@@ -390,66 +450,83 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bia
   *reinterpret_cast<uint4*>(h + tc::kmajor_offset(row, quarter * 16 + 8, 64)) = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
-__device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
-__device__ __forceinline__ int wrap_any(int v, int n) {
-  const int m = v % n;
-  return m < 0 ? m + n : m;
+constexpr uint32_t kIdesc64 = tc::idesc_bf16(128, 64), kIdesc32 = tc::idesc_bf16(128, kOutPad);
+
+__device__ __forceinline__ uint64_t opaque(uint64_t v) {
+  asm volatile("mov.b64 %0, %0;" : "+l"(v));
+  return v;
 }
 
-// One halo row of an x-plane: where it lies in the lattice, and its raw values.
-struct HaloRow {
-  float pop[19];
-  float frc[3];
-  bool solid;
-};
-
-__device__ __forceinline__ uint32_t halo_cell(const LbmGeom& g, int x, int y0, int z0, int r) {
-  const int hy = r / kLine, hz = r - hy * kLine;
-  const int j = wrap_any(y0 + hy - 1, g.ny), k = wrap_any(z0 + hz - 1, g.nz);
-  return (uint32_t)(((long long)x * g.ny + j) * g.nz + k);
-}
-
-// Issues the global loads of halo row r of plane x (flags `fl` already known).
-__device__ __forceinline__ void load_row(const FeatArgs& a, int x, int y0, int z0, int r, uint32_t fl,
-                                         HaloRow& h) {
-  const int hy = r / kLine, hz = r - hy * kLine;
-  const Deltas d(a.g, x, wrap_any(y0 + hy - 1, a.g.ny), wrap_any(z0 + hz - 1, a.g.nz));
-  const uint32_t n = (uint32_t)a.g.n;
-  h.solid = fl & kFlagSolid;
+// Layer-1 MMAs [14 C, 14 C + 14) of one tile, into TMEM column d. Descriptors are built by
+// adding compile-time offsets to base descriptors: `rows` addresses row 0 of channel chunk 0
+// (leading byte offset 0, stride byte offset 128), `w1` weight slice 0; the start-address
+// field counts 16-byte units, so a row shift adds the row count. r0, r1, r2: the tile's first
+// output row in the x-planes dx = -1, 0, +1.
+template <int C>
+__device__ __forceinline__ void issue_l1_chunk(uint32_t d, uint64_t rows, int r0, int r1, int r2,
+                                               uint64_t w1) {
 #pragma unroll
-  for (int q = 0; q < 19; ++q)
-    h.pop[q] = h.solid ? 0.f : gather32<FSI_STORAGE_F32>(a.pops, n, d, fl, q, a.parity, 0.f);
-#pragma unroll
-  for (int c = 0; c < 3; ++c) h.frc[c] = a.force[c * n + d.c];
-}
-
-// Converts a loaded halo row to its 24 BF16 channels and stores them at `row` of the chunks.
-__device__ __forceinline__ void store_row(const FeatArgs& a, const HaloRow& h, unsigned char* rows,
-                                          int row) {
-  float v[24];
-#pragma unroll
-  for (int q = 0; q < 19; ++q) v[q] = h.solid ? 0.f : (h.pop[q] - weight_of(q) * a.rho0) * a.pop_scale;
-  v[19] = h.solid ? 1.f : 0.f;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) v[20 + c] = h.frc[c] * a.force_scale;
-  v[23] = 0.f;
-  uint32_t w[12];
-#pragma unroll
-  for (int i = 0; i < 24; i += 2) {
-    const __nv_bfloat162 pr = __floats2bfloat162_rn(v[i], v[i + 1]);
-    w[i / 2] = *reinterpret_cast<const uint32_t*>(&pr);
+  for (int s = kL1Chunk * C; s < kL1Chunk * (C + 1); ++s) {
+    // Each descriptor is derived from an opaque copy of the bases right before its MMA, so
+    // the compiler does not compute all of them ahead (they would not fit in registers).
+    const uint64_t rows_s = opaque(rows), w1_s = opaque(w1);
+    uint64_t a;
+    if (s < 27) {
+      const int rp = s < 9 ? r0 : (s < 18 ? r1 : r2);
+      a = rows_s + ((uint64_t)(kChunkBytes >> 4) << 16) + (uint64_t)(rp + tap_off(s));
+    } else {
+      const int u = s - 27, plane = u / 5, j = u % 5, o = 9 * plane + 2 * j;
+      const int rp = plane == 0 ? r0 : (plane == 1 ? r1 : r2);
+      const uint64_t lbo = j < 4 ? (uint64_t)(tap_off(o + 1) - tap_off(o)) : 1u;  // 16-byte units
+      a = rows_s + (lbo << 16) + (uint64_t)((2 * kChunkBytes) >> 4) + (uint64_t)(rp + tap_off(o));
+    }
+    tc::mma_bf16(d, a, w1_s + (uint64_t)(s * (2048 >> 4)), kIdesc64, s > 0);
   }
+}
+
+// One hidden or output layer: A = H (128 x 64, K-major), B = the layer's weights.
+__device__ __forceinline__ void issue_layer(uint32_t d, uint64_t h, uint64_t w, uint32_t idesc) {
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
-    *reinterpret_cast<uint4*>(rows + (size_t)c * kChunkBytes + (size_t)row * 16) =
-        make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+  for (int s = 0; s < 4; ++s) tc::mma_bf16(d, h + (uint64_t)(16 * s), w + (uint64_t)(16 * s), idesc, s > 0);
+}
+
+// Bulk copy of `bytes` from global to shared memory, completing on `bar` (16-byte aligned).
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(tc::smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void expect_bytes(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Plane x of the column at (y0, z0) into ring slot `slot`: 39 line copies (3 chunks x 13
+// lines of 544 bytes) completing on `bar`.
+__device__ __forceinline__ void fill_plane(const unsigned char* grows, long long chunk_rows, int ny_pad,
+                                           int nz_pad, uint32_t s_rows, uint64_t* bar, int slot, int x,
+                                           int y0, int z0) {
+  expect_bytes(bar, kPlaneBytes);
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    const unsigned char* src = grows + ((size_t)c * chunk_rows + ((size_t)x * ny_pad + y0) * nz_pad + z0) * 16;
+    uint32_t dst = s_rows + (uint32_t)c * kChunkBytes + (uint32_t)(kPadLo + slot * kPlaneRows) * 16u;
+#pragma unroll 1
+    for (int hy = 0; hy < kLines + 2; ++hy) {
+      bulk_copy(dst, src, kLineBytes, bar);
+      src += (size_t)nz_pad * 16;
+      dst += kLineBytes;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float sb[64 * 3 + kOutPad];
-  __shared__ __align__(8) uint64_t bar_l1, bar_l;
+  __shared__ __align__(8) uint64_t bar_l1, bar_l, bar_h, bar_rows[kSlots];
   __shared__ uint32_t tbase;
+  __shared__ int abort_flag;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   stage_w1(smem + kOffW1, a.w1);
   stage_weights(smem + kOffW2, a.w2, 64, 64);
@@ -464,175 +541,183 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
         make_uint4(0, 0, 0, 0);
   }
   if (warp == 0) tc::tmem_alloc(&tbase, 512);
-  if (t == 0) { tc::mbar_init(&bar_l1, 1); tc::mbar_init(&bar_l, 1); }
+  if (t == 0) {
+    tc::mbar_init(&bar_l1, 1);
+    tc::mbar_init(&bar_l, 1);
+    tc::mbar_init(&bar_h, kWorkers / 32);
+    for (int s = 0; s < kSlots; ++s) tc::mbar_init(&bar_rows[s], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   tc::fence_smem_for_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tbase;
-  unsigned char* rows = smem + kOffRows;
-  const uint32_t sRows = tc::smem_addr(rows), sH = tc::smem_addr(smem + kOffH);
-  const uint32_t sW1 = tc::smem_addr(smem + kOffW1), sW2 = tc::smem_addr(smem + kOffW2);
-  const uint32_t sW3 = tc::smem_addr(smem + kOffW3), sW4 = tc::smem_addr(smem + kOffW4);
+  volatile int* abort = &abort_flag;
   const LbmGeom& g = a.f.g;
-  const int lrow = 32 * (warp & 3) + lane, lq = warp >> 2;  // epilogue role (TMEM lane)
-  const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-  constexpr uint32_t kIdesc64 = tc::idesc_bf16(128, 64), kIdesc32 = tc::idesc_bf16(128, kOutPad);
-
-  // Layer-1 MMAs [14 c, 14 c + 14) of the tile at plane step q, M tile m, into TMEM column d.
-  auto issue_l1 = [&](int c, int q, int m, uint32_t d) {
-    const int base = kLine + 128 * m;
-    for (int s = kL1Chunk * c; s < kL1Chunk * (c + 1); ++s) {
-      uint64_t adesc;
-      if (s < 27) {
-        const int row = kPadLo + ((q + s / 9) & 3) * kPlaneRows + base + tap_off(s);
-        adesc = tc::smem_desc(sRows + (uint32_t)row * 16u, (uint32_t)kChunkBytes, 128u);
-      } else {
-        const int u = s - 27, plane = u / 5, j = u % 5, o = 9 * plane + 2 * j;
-        const int row = kPadLo + ((q + plane) & 3) * kPlaneRows + base + tap_off(o);
-        const uint32_t lbo = j < 4 ? (uint32_t)(tap_off(o + 1) - tap_off(o)) * 16u : 16u;
-        adesc = tc::smem_desc(sRows + 2u * (uint32_t)kChunkBytes + (uint32_t)row * 16u, lbo, 128u);
-      }
-      tc::mma_bf16(d, adesc, tc::smem_desc(sW1 + (uint32_t)s * 2048u, 128u, 256u), kIdesc64, s > 0);
-    }
-  };
-  // One hidden or output layer: A = H (128 x 64), B = weights at w (n x 64).
-  auto issue_layer = [&](uint32_t w, uint32_t idesc, uint32_t d) {
-    for (int s = 0; s < 4; ++s)
-      tc::mma_bf16(d, tc::tile_desc(sH, 64, s), tc::tile_desc(w, 64, s), idesc, s > 0);
-  };
-
+  const RowGeom& rg = a.rg;
   const long long work = a.work;
   const long long w0 = work * blockIdx.x / gridDim.x, w1 = work * (blockIdx.x + 1) / gridDim.x;
-  uint32_t n_l1 = 0, n_l = 0;   // phases of the two barriers waited for so far
-  uint32_t c_l1 = 0, c_l = 0;   // commits to them (thread 0)
-  int last_bar = -1;            // barrier of the most recent commit (thread 0)
-  bool ok = true, dok = true;   // dok: the last output-layer wait of this thread
-  HaloRow pre;                  // next x-plane's row of this thread, in flight
-  uint32_t fl_next = 0;         // flags of the row after that
-  for (long long p0 = w0; p0 < w1 && ok;) {
-    const long long col = p0 / g.nx;
-    const int xs = (int)(p0 - col * g.nx);
-    const int nq = (int)min((long long)(g.nx - xs), w1 - p0);  // plane steps in this segment
-    const int yb = (int)(col / a.nzb), zb = (int)(col - (long long)yb * a.nzb);
-    const int y0 = yb * kLines, z0 = zb * kLineCells;
-    // Prime the ring with planes xs - 1, xs, xs + 1 (ordinals 0-2; ordinal u is plane
-    // xs - 1 + u in slot u & 3).
-    __syncthreads();  // the previous segment's last tile has read its rows
-    for (int i = t; i < 3 * kPlaneRows; i += kInferThreads) {
-      const int u = i / kPlaneRows, r = i - u * kPlaneRows;
-      const int x = wrap(xs - 1 + u, g.nx);
-      HaloRow h;
-      load_row(a.f, x, y0, z0, r, a.f.flags[halo_cell(g, x, y0, z0, r)], h);
-      store_row(a.f, h, rows, kPadLo + u * kPlaneRows + r);
-    }
-    if (t < kPlaneRows && nq > 1) fl_next = a.f.flags[halo_cell(g, wrap(xs + 2, g.nx), y0, z0, t)];
-    tc::fence_smem_for_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    if (t == 0) {
-      tc::fence_after_sync();
-      for (int c = 0; c < 3; ++c) issue_l1(c, 0, 0, tmem + ((n_l1 & 1) << 8));
-      tc::mma_commit(&bar_l1);
-      ++c_l1;
-      last_bar = 0;
-    }
-    const int ntile = kPlaneTiles * nq;
-    for (int ti = 0; ti < ntile; ++ti) {
-      const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
-      const bool next = ti + 1 < ntile;
-      const int nq1 = (ti + 1) / kPlaneTiles, nm1 = (ti + 1) - nq1 * kPlaneTiles;
-      const uint32_t tb = tmem + ((n_l1 & 1) << 8), tn = tmem + (((n_l1 + 1) & 1) << 8);
-      if (m == 0 && q + 1 < nq && t < kPlaneRows) {
-        // Ordinal q + 3 (plane xs + q + 2) into registers; flags of ordinal q + 4.
-        load_row(a.f, wrap(xs + q + 2, g.nx), y0, z0, t, fl_next, pre);
-        if (q + 2 < nq) fl_next = a.f.flags[halo_cell(g, wrap(xs + q + 3, g.nx), y0, z0, t)];
-      }
-      // Phase A: layer-1 epilogue; issue layer 2 and the first chunk of the next tile.
-      bool w = tc::mbar_wait(&bar_l1, n_l1 & 1, a.err, 3);
-      ++n_l1;
-      tc::fence_after_sync();
-      hidden_epilogue(tb + lane_base, sb, lq, smem + kOffH, lrow);
-      tc::fence_smem_for_async();
-      tc::fence_before_sync();
-      if (!(ok = __syncthreads_and(w && dok) != 0)) break;
-      if (t == 0) {
-        tc::fence_after_sync();
-        issue_layer(sW2, kIdesc64, tb + 64);
-        tc::mma_commit(&bar_l);
-        ++c_l;
-        last_bar = 1;
-        if (next) issue_l1(0, nq1, nm1, tn);
-      }
-      // Phase B: layer-2 epilogue; layer 3 and the second chunk.
-      w = tc::mbar_wait(&bar_l, n_l & 1, a.err, 4);
-      ++n_l;
-      tc::fence_after_sync();
-      hidden_epilogue(tb + lane_base + 64, sb + 64, lq, smem + kOffH, lrow);
-      tc::fence_smem_for_async();
-      tc::fence_before_sync();
-      if (!(ok = __syncthreads_and(w) != 0)) break;
-      if (t == 0) {
-        tc::fence_after_sync();
-        issue_layer(sW3, kIdesc64, tb + 128);
-        tc::mma_commit(&bar_l);
-        ++c_l;
-        if (next) issue_l1(1, nq1, nm1, tn);
-      }
-      // Phase C: layer-3 epilogue; output layer and the last chunk.
-      w = tc::mbar_wait(&bar_l, n_l & 1, a.err, 5);
-      ++n_l;
-      tc::fence_after_sync();
-      hidden_epilogue(tb + lane_base + 128, sb + 128, lq, smem + kOffH, lrow);
-      tc::fence_smem_for_async();
-      tc::fence_before_sync();
-      if (!(ok = __syncthreads_and(w) != 0)) break;
-      if (t == 0) {
-        tc::fence_after_sync();
-        issue_layer(sW4, kIdesc32, tb + 192);
-        tc::mma_commit(&bar_l);
-        ++c_l;
-        last_bar = 1;
-        if (next) {
-          issue_l1(2, nq1, nm1, tn);
-          tc::mma_commit(&bar_l1);
-          ++c_l1;
-          last_bar = 0;
+
+  if (warp == kWorkers / 32) {
+    // ---------------------------------------------------- row copies and MMA issue
+    if (lane == 0) {
+      const uint32_t sRows = tc::smem_addr(smem + kOffRows);
+      const uint64_t dRows = tc::smem_desc(sRows, 0u, 128u);
+      const uint64_t dW1 = tc::smem_desc(tc::smem_addr(smem + kOffW1), 128u, 256u);
+      const uint64_t dH = tc::tile_desc(tc::smem_addr(smem + kOffH), 64, 0);
+      const uint64_t dW2 = tc::tile_desc(tc::smem_addr(smem + kOffW2), 64, 0);
+      const uint64_t dW3 = tc::tile_desc(tc::smem_addr(smem + kOffW3), 64, 0);
+      const uint64_t dW4 = tc::tile_desc(tc::smem_addr(smem + kOffW4), 64, 0);
+      uint32_t n_h = 0, c_l1 = 0, c_l = 0, rows_phase = 0;
+      int last_bar = -1;
+      bool ok = true;
+#define FSI_WAIT_H(code) (ok = tc::mbar_wait_abortable(&bar_h, n_h & 1, abort, a.err, (code)), ++n_h, tc::fence_after_sync(), ok)
+#define FSI_WAIT_ROWS(s) (ok = tc::mbar_wait_abortable(&bar_rows[(s)], (rows_phase >> (s)) & 1u, abort, a.err, 12), rows_phase ^= 1u << (s), ok)
+      for (long long p0 = w0; p0 < w1 && ok;) {
+        const long long col = p0 / g.nx;
+        const int xs = (int)(p0 - col * g.nx);
+        const int nq = (int)min((long long)(g.nx - xs), w1 - p0);
+        const int yb = (int)(col / rg.nzb), zb = (int)(col - (long long)yb * rg.nzb);
+        const int y0 = yb * kLines, z0 = zb * kLineCells;
+        // The previous segment's MMAs have read their slots.
+        if (c_l > 0 && !(ok = tc::mbar_wait_abortable(&bar_l, (c_l - 1) & 1, abort, a.err, 13))) break;
+        // Ordinal u = plane xs - 1 + u, in slot u & 3.
+        for (int u = 0; u < 3; ++u) fill_plane(a.grows, a.rg.chunk_rows, a.rg.ny_pad, a.rg.nz_pad, sRows, &bar_rows[u], u, wrap(xs - 1 + u, g.nx), y0, z0);
+        if (nq > 1) fill_plane(a.grows, a.rg.chunk_rows, a.rg.ny_pad, a.rg.nz_pad, sRows, &bar_rows[3], 3, wrap(xs + 2, g.nx), y0, z0);
+        if (!FSI_WAIT_ROWS(0) || !FSI_WAIT_ROWS(1) || !FSI_WAIT_ROWS(2)) break;
+        {
+          const uint32_t d = tmem + ((c_l1 & 1) << 8);
+          const int r1 = kPadLo + 1 * kPlaneRows + kLine, r2 = kPadLo + 2 * kPlaneRows + kLine;
+          issue_l1_chunk<0>(d, dRows, kPadLo + kLine, r1, r2, dW1);
+          issue_l1_chunk<1>(d, dRows, kPadLo + kLine, r1, r2, dW1);
+          issue_l1_chunk<2>(d, dRows, kPadLo + kLine, r1, r2, dW1);
         }
+        tc::mma_commit(&bar_l1);
+        ++c_l1;
+        last_bar = 0;
+        const int ntile = kPlaneTiles * nq;
+        for (int ti = 0; ti < ntile; ++ti) {
+          const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
+          const uint32_t tb = tmem + (((c_l1 - 1) & 1) << 8), tn = tmem + ((c_l1 & 1) << 8);
+          const bool next = ti + 1 < ntile;
+          const int q1 = (ti + 1) / kPlaneTiles, m1 = (ti + 1) - q1 * kPlaneTiles;
+          const int base1 = kPadLo + kLine + 128 * m1;
+          const int r0 = base1 + (q1 & 3) * kPlaneRows, r1 = base1 + ((q1 + 1) & 3) * kPlaneRows,
+                    r2 = base1 + ((q1 + 2) & 3) * kPlaneRows;
+          if (!FSI_WAIT_H(9)) break;  // layer-1 epilogue done (so layer 1 of this tile is)
+          issue_layer(tb + 64, dH, dW2, kIdesc64);
+          tc::mma_commit(&bar_l);
+          ++c_l;
+          last_bar = 1;
+          // Plane step q - 1 is complete: its oldest plane's slot takes plane xs + q + 2.
+          if (m == 0 && q >= 1 && q + 1 < nq)
+            fill_plane(a.grows, a.rg.chunk_rows, a.rg.ny_pad, a.rg.nz_pad, sRows, &bar_rows[(q + 3) & 3], (q + 3) & 3, wrap(xs + q + 2, g.nx), y0, z0);
+          if (next && m1 == 0 && !FSI_WAIT_ROWS((q1 + 2) & 3)) break;
+          if (next) issue_l1_chunk<0>(tn, dRows, r0, r1, r2, dW1);
+          if (!FSI_WAIT_H(10)) break;  // layer-2 epilogue done
+          issue_layer(tb + 128, dH, dW3, kIdesc64);
+          tc::mma_commit(&bar_l);
+          ++c_l;
+          if (next) issue_l1_chunk<1>(tn, dRows, r0, r1, r2, dW1);
+          if (!FSI_WAIT_H(11)) break;  // layer-3 epilogue done
+          issue_layer(tb + 192, dH, dW4, kIdesc32);
+          tc::mma_commit(&bar_l);
+          ++c_l;
+          last_bar = 1;
+          if (next) {
+            issue_l1_chunk<2>(tn, dRows, r0, r1, r2, dW1);
+            tc::mma_commit(&bar_l1);
+            ++c_l1;
+            last_bar = 0;
+          }
+        }
+        p0 += nq;
       }
-      // Phase D: outputs (warps with lq < 2 hold columns 0-31; 19 are used).
-      w = tc::mbar_wait(&bar_l, n_l & 1, a.err, 6);
-      ++n_l;
-      tc::fence_after_sync();
-      if (lq < 2) {
-        float y[16];
-        tc::tmem_ld16(tb + lane_base + 192 + 16 * lq, y);
-        const int pr = kLine + 128 * m + lrow;       // row within the plane
+      if (!ok) {
+        // Let the copies and MMAs in flight finish before the CTA exits (bounded waits).
+        for (int s = 0; s < kSlots; ++s) tc::mbar_wait(&bar_rows[s], (rows_phase >> s) & 1u, nullptr, 0);
+        if (last_bar == 0) tc::mbar_wait(&bar_l1, (c_l1 - 1) & 1, nullptr, 0);
+        else if (last_bar == 1) tc::mbar_wait(&bar_l, (c_l - 1) & 1, nullptr, 0);
+      }
+#undef FSI_WAIT_H
+#undef FSI_WAIT_ROWS
+    }
+  } else {
+    // ------------------------------------------------------------------ epilogues
+    const int lrow = 32 * (warp & 3) + lane, lq = warp >> 2;  // TMEM lane, column block
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+    unsigned char* H = smem + kOffH;
+    const float inv_out = 1.0f / a.out_scale;
+    uint32_t n_l1 = 0, n_l = 0;
+    bool ok = true;
+    // Warp-uniform bounded wait (every lane takes the same branch afterwards), and the hand-over
+    // of this warp's H rows (and TMEM reads) to the issuer.
+#define FSI_WWAIT(bar, parity, code) (__all_sync(0xffffffffu, tc::mbar_wait_abortable((bar), (parity), abort, a.err, (code))) != 0)
+#define FSI_HAND_OVER()                              \
+  do {                                                \
+    tc::fence_smem_for_async();                       \
+    tc::fence_before_sync();                          \
+    __syncwarp();                                     \
+    if (lane == 0) tc::mbar_arrive(&bar_h);           \
+  } while (0)
+    for (long long p0 = w0; p0 < w1 && ok;) {
+      const long long col = p0 / g.nx;
+      const int xs = (int)(p0 - col * g.nx);
+      const int nq = (int)min((long long)(g.nx - xs), w1 - p0);
+      const int yb = (int)(col / rg.nzb), zb = (int)(col - (long long)yb * rg.nzb);
+      const int y0 = yb * kLines, z0 = zb * kLineCells;
+      const int ntile = kPlaneTiles * nq;
+      for (int ti = 0; ti < ntile && ok; ++ti) {
+        const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
+        // This thread's output cell (if its row is one) and its occupancy, fetched early.
+        const int pr = kLine + 128 * m + lrow;
         const int hy = pr / kLine, hz = pr - hy * kLine;
-        const int oy = y0 + hy - 1, oz = z0 + hz - 1, ox = xs + q;
-        if (w && hy >= 1 && hy <= kLines && hz >= 1 && hz <= kLineCells && oy < g.ny && oz < g.nz) {
-          const long long cc = ((long long)ox * g.ny + oy) * g.nz + oz;
-          const int row = kPadLo + ((q + 1) & 3) * kPlaneRows + pr;
-          const unsigned short occ =
-              *reinterpret_cast<const unsigned short*>(rows + 2 * (size_t)kChunkBytes + (size_t)row * 16 + 6);
-          const bool fluid = occ == 0;
+        const int oy = y0 + hy - 1, oz = z0 + hz - 1;
+        const bool valid = lq < 2 && hy <= kLines && hz >= 1 && hz <= kLineCells && oy < g.ny && oz < g.nz;
+        const long long cc = ((long long)(xs + q) * g.ny + oy) * g.nz + oz;
+        const uint32_t fl = valid ? a.f.flags[cc] : kFlagSolid;
+        const uint32_t tb = tmem + ((n_l1 & 1) << 8) + lane_base;
+        if (!(ok = FSI_WWAIT(&bar_l1, n_l1 & 1, 3))) break;
+        ++n_l1;
+        tc::fence_after_sync();
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int qo = 16 * lq + i;
-            if (qo < kOut) a.corr[(size_t)qo * g.n + cc] = fluid ? (y[i] + sb[192 + qo]) / a.out_scale : 0.f;
+        for (int cg = 0; cg < kColGroups; ++cg) hidden_epilogue(tb, sb, kColGroups * lq + cg, H, lrow);
+        FSI_HAND_OVER();
+        if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 4))) break;
+        ++n_l;
+        tc::fence_after_sync();
+#pragma unroll
+        for (int cg = 0; cg < kColGroups; ++cg) hidden_epilogue(tb + 64, sb + 64, kColGroups * lq + cg, H, lrow);
+        FSI_HAND_OVER();
+        if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 5))) break;
+        ++n_l;
+        tc::fence_after_sync();
+#pragma unroll
+        for (int cg = 0; cg < kColGroups; ++cg) hidden_epilogue(tb + 128, sb + 128, kColGroups * lq + cg, H, lrow);
+        FSI_HAND_OVER();
+        if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 6))) break;
+        ++n_l;
+        tc::fence_after_sync();
+        // Outputs: columns 0-31, of which 19 are used (16 per warp, warps with lq < 2).
+        if (lq < 2) {
+          float y[16];
+          tc::tmem_ld16(tb + 192 + 16 * lq, y);
+          if (valid) {
+            const float keep = (fl & kFlagSolid) ? 0.f : inv_out;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const int qo = 16 * lq + i;
+              if (qo < kOut) a.corr[(size_t)qo * g.n + cc] = (y[i] + sb[192 + qo]) * keep;
+            }
           }
         }
       }
-      if (m == 1 && q + 1 < nq && t < kPlaneRows) store_row(a.f, pre, rows, kPadLo + ((q + 3) & 3) * kPlaneRows + t);
-      dok = w;  // made CTA-uniform at the next barrier
+      p0 += nq;
     }
-    p0 += nq;
-    ok = __syncthreads_and(ok && dok) != 0;
-  }
-  if (!ok && last_bar >= 0 && t == 0) {
-    // Let the MMAs in flight finish before the tensor memory is released (bounded).
-    if (last_bar == 0) tc::mbar_wait(&bar_l1, (c_l1 - 1) & 1, nullptr, 0);
-    else tc::mbar_wait(&bar_l, (c_l - 1) & 1, nullptr, 0);
+#undef FSI_WWAIT
+#undef FSI_HAND_OVER
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -818,16 +903,24 @@ extern "C" int fsi_closure_gemm(const fsi_closure_gemm_desc* d, void* stream) {
   return check_launch("gemm_kernel");
 }
 
+extern "C" int64_t fsi_closure_rows_bytes(const fsi_lbm_desc* d) {
+  if (check_closure_lattice(d)) return -1;
+  return 3 * row_geom(geom_of(d)).chunk_rows * 16;
+}
+
 extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags,
                                  const float* force, int64_t steps_done,
-                                 const fsi_closure_weights* w, float* corr, int32_t* err,
+                                 const fsi_closure_weights* w, void* rows, float* corr, int32_t* err,
                                  void* stream) {
   if (int e = check_closure_lattice(d)) return e;
-  FSI_REQUIRE(pops && flags && force && w && corr && err, "NULL array");
+  FSI_REQUIRE(pops && flags && force && w && rows && corr && err, "NULL array");
+  FSI_REQUIRE(((uintptr_t)rows & 15) == 0, "rows must be 16-byte aligned");
   FSI_REQUIRE(w->w1 && w->w2 && w->w3 && w->w4 && w->bias, "NULL weights");
   FSI_REQUIRE(w->out_scale != 0.f, "out_scale must be non-zero");
   InferArgs a;
   a.f = feat_args(d, pops, flags, force, steps_done, w->pop_scale, w->force_scale);
+  a.rg = row_geom(a.f.g);
+  a.grows = reinterpret_cast<const unsigned char*>(rows);
   a.w1 = reinterpret_cast<const __nv_bfloat16*>(w->w1);
   a.w2 = reinterpret_cast<const __nv_bfloat16*>(w->w2);
   a.w3 = reinterpret_cast<const __nv_bfloat16*>(w->w3);
@@ -836,16 +929,18 @@ extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const
   a.out_scale = w->out_scale;
   a.corr = corr;
   a.err = err;
-  a.nyb = (a.f.g.ny + kLines - 1) / kLines;
-  a.nzb = (a.f.g.nz + kLineCells - 1) / kLineCells;
-  a.work = (long long)a.nyb * a.nzb * a.f.g.nx;
+  a.work = (long long)a.rg.nyb * a.rg.nzb * a.f.g.nx;
+  cudaStream_t s = as_stream(stream);
+  closure_rows_kernel<<<grid_for(a.rg.chunk_rows, kBlock), kBlock, 0, s>>>(
+      a.f, a.rg, reinterpret_cast<unsigned char*>(rows));
+  if (int e = check_launch("closure_rows_kernel")) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int grid = (int)(a.work < sms ? a.work : sms);
   cudaFuncSetAttribute(closure_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kInferSmem);
-  closure_infer_kernel<<<grid, kInferThreads, kInferSmem, as_stream(stream)>>>(a);
+  closure_infer_kernel<<<grid, kInferThreads, kInferSmem, s>>>(a);
   return check_launch("closure_infer_kernel");
 }
 

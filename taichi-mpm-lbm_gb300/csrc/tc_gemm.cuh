@@ -10,8 +10,8 @@
 // LBO) and those adjacent along M/N are Kc * 16 bytes apart (stride byte offset, SBO).
 // One MMA consumes K = 16 (two core matrices along K); the next K slice starts 256 bytes on.
 //
-// Every wait on an mbarrier is bounded: after kSpinLimit polls it gives up, records an
-// error code in a caller-provided flag and returns false, so a kernel can release its
+// Every wait on an mbarrier is bounded: after kWaitCycles clock cycles it gives up, records
+// an error code in a caller-provided flag and returns false, so a kernel can release its
 // tensor memory and return instead of hanging.
 #pragma once
 
@@ -22,7 +22,11 @@
 namespace fsi {
 namespace tc {
 
-constexpr uint32_t kSpinLimit = 1u << 24;
+// Bound of every wait: about one second at the 2 GHz SM clock.
+constexpr long long kWaitCycles = 1ll << 31;
+// Suspend-time hint of one poll (ns): a waiting thread sleeps instead of spinning, leaving
+// the issue slots to the warps that work.
+constexpr uint32_t kSuspendNs = 20000;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -63,22 +67,55 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
 }
 
-// Waits for the phase with parity `parity` to complete; false (and *err set) on timeout.
+// One bounded poll of the phase with parity `parity`: the thread is suspended (it issues
+// nothing) until the phase completes or kSuspendNs elapse.
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;}"
+      : "=r"(done)
+      : "r"(a), "r"(parity), "r"(kSuspendNs)
+      : "memory");
+  return done != 0;
+}
+
+// Waits for the phase with parity `parity` to complete; false (and *err set) after
+// kWaitCycles SM clock cycles.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
   const uint32_t a = smem_addr(bar);
-  for (uint32_t i = 0; i < kSpinLimit; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(a, parity)) {
+    if (clock64() - t0 > kWaitCycles) {
+      if (err) atomicExch(err, code);
+      return false;
+    }
   }
-  if (err) atomicExch(err, code);
-  return false;
+  return true;
+}
+
+// Arrives once on `bar` (release semantics at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// As mbar_wait, but also gives up (without recording an error) once *abort is non-zero,
+// and sets *abort when it times out itself, so that the other roles of a warp-specialised
+// kernel stop waiting for it.
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, uint32_t parity,
+                                                    volatile int* abort, int* err, int code) {
+  const uint32_t a = smem_addr(bar);
+  const long long t0 = clock64();
+  while (!mbar_try(a, parity)) {
+    if (*abort) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      *abort = 1;
+      if (err) atomicExch(err, code);
+      return false;
+    }
+  }
+  return true;
 }
 
 // ----------------------------------------------------------- tensor memory

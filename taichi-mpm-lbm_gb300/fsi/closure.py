@@ -325,6 +325,22 @@ class ClosureTrainer:
 
 
 # ------------------------------------------------------------ simulation
+def rows_buffer(lbm: LBMSolver3D) -> torch.Tensor:
+    """Scratch for the feature rows the fused inference stages (``fsi_closure_rows_bytes``)."""
+    nbytes = int(nat.load().fsi_closure_rows_bytes(lbm._desc))
+    if nbytes <= 0:
+        raise ValueError(f"lattice unsupported by the closure: {nat.last_error()}")
+    return torch.empty(nbytes, dtype=torch.uint8, device=lbm._device)
+
+
+def infer(lbm: LBMSolver3D, weights: nat.ClosureWeights, corr: torch.Tensor, rows: torch.Tensor,
+          err: torch.Tensor) -> None:
+    """Corrections corr [19][N] of every cell of ``lbm`` by the fused tensor-core inference."""
+    nat.call("fsi_closure_infer", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags), nat.ptr(lbm.force),
+             lbm.steps_done, ctypes.byref(weights), nat.ptr(rows), nat.ptr(corr), nat.ptr(err),
+             nat.stream_ptr())
+
+
 class ClosureSimulation:
     """The coarse lattice with the learned correction after every step; guards on mass drift
     and local Mach number fall back to the plain fine-grid solver."""
@@ -345,6 +361,7 @@ class ClosureSimulation:
         self.fallback_reason = ""
         self.coarse_steps = 0
         self._weights = net.weights_struct()
+        self._rows = rows_buffer(self.coarse)
 
     @property
     def on_fine_grid(self) -> bool:
@@ -375,9 +392,7 @@ class ClosureSimulation:
             return
         c = self.coarse
         c.step()
-        nat.call("fsi_closure_infer", c._desc, nat.ptr(c._pops), nat.ptr(c.flags), nat.ptr(c.force),
-                 c.steps_done, ctypes.byref(self._weights), nat.ptr(self.corr),
-                 nat.ptr(self.net.err), nat.stream_ptr())
+        infer(c, self._weights, self.corr, self._rows, self.net.err)
         nat.call("fsi_closure_apply", c._desc, nat.ptr(c._pops), nat.ptr(c.flags), c.steps_done,
                  nat.ptr(self.corr), nat.stream_ptr())
         c._mass_speed_cache = None

@@ -111,10 +111,7 @@ def test_fused_inference_matches_unfused_passes():
     net = cl.ClosureMLP(seed=3)
     net.pop_scale, net.force_scale, net.out_scale = 30.0, 1e3, 250.0
     corr = torch.zeros((19, lbm.n_cells), dtype=torch.float32, device="cuda")
-    w = net.weights_struct()
-    nat.call("fsi_closure_infer", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags),
-             nat.ptr(lbm.force), lbm.steps_done, w, nat.ptr(corr), nat.ptr(net.err),
-             nat.stream_ptr())
+    cl.infer(lbm, net.weights_struct(), corr, cl.rows_buffer(lbm), net.err)
     net.check()
     fluid = np.nonzero(mask.reshape(-1) == 0)[0]
     cells = torch.from_numpy(fluid.astype(np.int32)).cuda()
