@@ -24,8 +24,10 @@
 //     and the 19 outputs written as corrections per cell.
 //   closure_apply_kernel: f_q(x) += correction, mass-conserving (sum_q w-weighted projection).
 //   loss / Adam kernels for training.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstdint>
 
@@ -278,11 +280,10 @@ __global__ void __launch_bounds__(128) gemm_kernel(GemmArgs g) {
 //
 // closure_rows_kernel first writes every cell's 24 BF16 channels to global memory in the
 // same chunked layout, on a lattice padded by one periodic image in y and z (and to whole
-// columns), so that each halo line of the inference blocks is a contiguous 544-byte run
-// per chunk. Cells are walked in columns: 32 cells along z x 11 lines along y, streamed
+// columns). Cells are walked in columns: 32 cells along z x 11 lines along y, streamed
 // along x. An x-plane of a column is a 34 x 13 halo block (442 rows, z fastest), fetched
-// into a ring of four slots (x - 1, x, x + 1 in use, x + 2 in flight) by 39 bulk copies
-// (cp.async.bulk) that complete on the slot's mbarrier. The output rows of a plane are the
+// into a ring of four slots (x - 1, x, x + 1 in use, x + 2 in flight) by three TMA tensor
+// copies (one box of 8 channels x 34 x 13 per chunk) that complete on the slot's mbarrier. The output rows of a plane are the
 // 374 rows of lines 1..11, covered by three M tiles of 128 consecutive rows; rows on the z
 // halo (and past line 11) are computed and discarded.
 //
@@ -300,8 +301,9 @@ constexpr int kLines = 11;                            // output lines along y pe
 constexpr int kPlaneRows = kLine * (kLines + 2);      // 442
 constexpr int kPlaneTiles = (kLine * kLines + 127) / 128;  // 3
 constexpr int kSlots = 4;
-constexpr int kPadLo = 1, kPadHi = 48;
-constexpr int kChunkRows = kPadLo + kSlots * kPlaneRows + kPadHi;
+constexpr int kSlotRows = 448;                        // a plane, padded to 128-byte boundaries
+constexpr int kPadLo = 8, kPadHi = 48;
+constexpr int kChunkRows = kPadLo + kSlots * kSlotRows + kPadHi;
 constexpr int kChunkBytes = kChunkRows * 16;
 constexpr int kL1Mmas = 27 + 3 * 5;                   // 42
 constexpr int kL1Chunk = kL1Mmas / 3;                 // 14 MMAs per issue
@@ -309,12 +311,14 @@ constexpr int kEpiWarps = 16;                         // epilogue warps (4 per T
 constexpr int kWorkers = 32 * kEpiWarps;
 constexpr int kColGroups = 64 / 16 / (kEpiWarps / 4);  // 16-column groups per warp and layer
 constexpr int kInferThreads = kWorkers + 32;          // + the copy / MMA issuing warp
-constexpr uint32_t kLineBytes = kLine * 16;           // one halo line of one chunk
-constexpr uint32_t kPlaneBytes = 3u * (kLines + 2) * kLineBytes;
+constexpr uint32_t kPlaneBytes = 3u * kPlaneRows * 16u;  // one plane: three tensor-copy boxes
 static_assert(kL1Chunk * 3 == kL1Mmas, "layer 1 is issued in three equal chunks");
 // Highest row read: the last tile's last row, offset +35, and the +16-byte second half of
 // the unpaired offset of a plane.
-static_assert(kLine + 128 * kPlaneTiles + kLine + 2 <= kPlaneRows + kPadHi, "row padding");
+static_assert(kLine + 128 * kPlaneTiles + kLine + 2 <= kSlotRows + kPadHi, "row padding");
+static_assert(kSlotRows >= kPlaneRows && (kSlotRows * 16) % 128 == 0 && (kPadLo * 16) % 128 == 0 &&
+                  kChunkBytes % 128 == 0,
+              "tensor-copy destinations are 128-byte aligned");
 static_assert(kChunkBytes < (1 << 18), "leading byte offset field");
 
 constexpr size_t kOffW1 = 0;                                  // 42 slices of 64 x 16
@@ -365,26 +369,50 @@ __device__ __forceinline__ int wrap_any(int v, int n) {
   return m < 0 ? m + n : m;
 }
 
-// The 24 BF16 channels of every padded row (one thread per row).
-__global__ void __launch_bounds__(kBlock) closure_rows_kernel(FeatArgs a, RowGeom rg,
-                                                              unsigned char* __restrict__ grows) {
-  const long long r = (long long)blockIdx.x * kBlock + threadIdx.x;
-  if (r >= rg.chunk_rows) return;
-  const int kp = (int)(r % rg.nz_pad);
-  const long long xj = r / rg.nz_pad;
-  const int jp = (int)(xj % rg.ny_pad), x = (int)(xj / rg.ny_pad);
-  float v[23];
-  neighbour_features(a, x, wrap_any(jp - 1, a.g.ny), wrap_any(kp - 1, a.g.nz), v);
+// The 24 BF16 channels of every padded row: thread (kp, jp, x) of a grid of 128-thread
+// blocks over (z, y, x). All loads are issued before the flags are needed: the populations
+// are gathered from the slots a fluid neighbourhood uses, and only the few directions whose
+// upwind neighbour is solid (bounce-back) read their own slot afterwards.
+__global__ void __launch_bounds__(128) closure_rows_kernel(FeatArgs a, RowGeom rg,
+                                                           unsigned char* __restrict__ grows) {
+  const int kp = blockIdx.x * 128 + threadIdx.x;
+  if (kp >= rg.nz_pad) return;
+  const int jp = blockIdx.y, x = blockIdx.z;
+  const LbmGeom& g = a.g;
+  const Deltas d(g, x, wrap_any(jp - 1, g.ny), wrap_any(kp - 1, g.nz));
+  const uint32_t n = (uint32_t)g.n;
+  const uint32_t fl = a.flags[d.c];
+  float f[19], frc[3];
+  f[0] = a.pops[d.c];
+  if (a.parity == 0) {
+#pragma unroll
+    for (int q = 1; q < 19; ++q) f[q] = a.pops[q * n + d.c];
+  } else {
+#pragma unroll
+    for (int q = 1; q < 19; ++q) f[q] = a.pops[opp(q) * n + d.nb(q, -1)];
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) frc[c] = a.force[c * n + d.c];
+  const bool solid = fl & kFlagSolid;
+  if (a.parity != 0 && !solid && (fl & ~kFlagSolid)) {
+#pragma unroll
+    for (int q = 1; q < 19; ++q)
+      if ((fl >> opp(q)) & 1u) f[q] = a.pops[q * n + d.c];
+  }
+  float v[24];
+#pragma unroll
+  for (int q = 0; q < 19; ++q) v[q] = solid ? 0.f : (f[q] - weight_of(q) * a.rho0) * a.pop_scale;
+  v[19] = solid ? 1.f : 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) v[20 + c] = frc[c] * a.force_scale;
+  v[23] = 0.f;
   uint32_t w[12];
 #pragma unroll
-  for (int i = 0; i < 22; i += 2) {
+  for (int i = 0; i < 24; i += 2) {
     const __nv_bfloat162 pr = __floats2bfloat162_rn(v[i], v[i + 1]);
     w[i / 2] = *reinterpret_cast<const uint32_t*>(&pr);
   }
-  {
-    const __nv_bfloat162 pr = __floats2bfloat162_rn(v[22], 0.f);
-    w[11] = *reinterpret_cast<const uint32_t*>(&pr);
-  }
+  const size_t r = ((size_t)x * rg.ny_pad + jp) * rg.nz_pad + kp;
 #pragma unroll
   for (int c = 0; c < 3; ++c)
     *reinterpret_cast<uint4*>(grows + ((size_t)c * rg.chunk_rows + r) * 16) =
@@ -490,38 +518,29 @@ __device__ __forceinline__ void issue_layer(uint32_t d, uint64_t h, uint64_t w, 
   for (int s = 0; s < 4; ++s) tc::mma_bf16(d, h + (uint64_t)(16 * s), w + (uint64_t)(16 * s), idesc, s > 0);
 }
 
-// Bulk copy of `bytes` from global to shared memory, completing on `bar` (16-byte aligned).
-__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "l"(src), "r"(bytes), "r"(tc::smem_addr(bar))
-      : "memory");
-}
 __device__ __forceinline__ void expect_bytes(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_addr(bar)), "r"(bytes)
                : "memory");
 }
 
-// Plane x of the column at (y0, z0) into ring slot `slot`: 39 line copies (3 chunks x 13
-// lines of 544 bytes) completing on `bar`.
-__device__ __forceinline__ void fill_plane(const unsigned char* grows, long long chunk_rows, int ny_pad,
-                                           int nz_pad, uint32_t s_rows, uint64_t* bar, int slot, int x,
-                                           int y0, int z0) {
+// Plane x of the column at (y0, z0) into ring slot `slot`: one tensor copy per channel chunk
+// (box: 8 channels x 34 rows along z x 13 lines along y) completing on `bar`.
+__device__ __forceinline__ void fill_plane(const CUtensorMap* map, uint32_t s_rows, uint64_t* bar, int slot,
+                                           int x, int y0, int z0) {
   expect_bytes(bar, kPlaneBytes);
-#pragma unroll 1
+#pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const unsigned char* src = grows + ((size_t)c * chunk_rows + ((size_t)x * ny_pad + y0) * nz_pad + z0) * 16;
-    uint32_t dst = s_rows + (uint32_t)c * kChunkBytes + (uint32_t)(kPadLo + slot * kPlaneRows) * 16u;
-#pragma unroll 1
-    for (int hy = 0; hy < kLines + 2; ++hy) {
-      bulk_copy(dst, src, kLineBytes, bar);
-      src += (size_t)nz_pad * 16;
-      dst += kLineBytes;
-    }
+    const uint32_t dst = s_rows + (uint32_t)c * kChunkBytes + (uint32_t)(kPadLo + slot * kSlotRows) * 16u;
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(z0), "r"(y0), "r"(x), "r"(c), "r"(tc::smem_addr(bar))
+        : "memory");
   }
 }
 
-__global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferArgs a) {
+__global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferArgs a,
+                                                                        const __grid_constant__ CUtensorMap rows_map) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float sb[64 * 3 + kOutPad];
   __shared__ __align__(8) uint64_t bar_l1, bar_l, bar_h, bar_rows[kSlots];
@@ -533,10 +552,14 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
   stage_weights(smem + kOffW3, a.w3, 64, 64);
   stage_weights(smem + kOffW4, a.w4, kOutPad, 64);
   for (int i = t; i < 64 * 3 + kOutPad; i += kInferThreads) sb[i] = a.b[i];
-  // Padding rows stay zero (they feed discarded rows only, but must be finite).
-  for (int i = t; i < 3 * (kPadLo + kPadHi); i += kInferThreads) {
-    const int c = i / (kPadLo + kPadHi), p = i % (kPadLo + kPadHi);
-    const int row = p < kPadLo ? p : kPadLo + kSlots * kPlaneRows + (p - kPadLo);
+  // Rows no copy writes (padding) stay zero: they feed discarded rows only, but must be finite.
+  constexpr int kGap = kSlotRows - kPlaneRows;
+  for (int i = t; i < 3 * (kPadLo + kPadHi + kSlots * kGap); i += kInferThreads) {
+    const int c = i / (kPadLo + kPadHi + kSlots * kGap), p = i % (kPadLo + kPadHi + kSlots * kGap);
+    int row;
+    if (p < kPadLo) row = p;
+    else if (p < kPadLo + kPadHi) row = kPadLo + kSlots * kSlotRows + (p - kPadLo);
+    else row = kPadLo + ((p - kPadLo - kPadHi) / kGap) * kSlotRows + kPlaneRows + (p - kPadLo - kPadHi) % kGap;
     *reinterpret_cast<uint4*>(smem + kOffRows + (size_t)c * kChunkBytes + (size_t)row * 16) =
         make_uint4(0, 0, 0, 0);
   }
@@ -584,12 +607,12 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
         // The previous segment's MMAs have read their slots.
         if (c_l > 0 && !(ok = tc::mbar_wait_abortable(&bar_l, (c_l - 1) & 1, abort, a.err, 13))) break;
         // Ordinal u = plane xs - 1 + u, in slot u & 3.
-        for (int u = 0; u < 3; ++u) fill_plane(a.grows, a.rg.chunk_rows, a.rg.ny_pad, a.rg.nz_pad, sRows, &bar_rows[u], u, wrap(xs - 1 + u, g.nx), y0, z0);
-        if (nq > 1) fill_plane(a.grows, a.rg.chunk_rows, a.rg.ny_pad, a.rg.nz_pad, sRows, &bar_rows[3], 3, wrap(xs + 2, g.nx), y0, z0);
+        for (int u = 0; u < 3; ++u) fill_plane(&rows_map, sRows, &bar_rows[u], u, wrap(xs - 1 + u, g.nx), y0, z0);
+        if (nq > 1) fill_plane(&rows_map, sRows, &bar_rows[3], 3, wrap(xs + 2, g.nx), y0, z0);
         if (!FSI_WAIT_ROWS(0) || !FSI_WAIT_ROWS(1) || !FSI_WAIT_ROWS(2)) break;
         {
           const uint32_t d = tmem + ((c_l1 & 1) << 8);
-          const int r1 = kPadLo + 1 * kPlaneRows + kLine, r2 = kPadLo + 2 * kPlaneRows + kLine;
+          const int r1 = kPadLo + 1 * kSlotRows + kLine, r2 = kPadLo + 2 * kSlotRows + kLine;
           issue_l1_chunk<0>(d, dRows, kPadLo + kLine, r1, r2, dW1);
           issue_l1_chunk<1>(d, dRows, kPadLo + kLine, r1, r2, dW1);
           issue_l1_chunk<2>(d, dRows, kPadLo + kLine, r1, r2, dW1);
@@ -604,8 +627,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
           const bool next = ti + 1 < ntile;
           const int q1 = (ti + 1) / kPlaneTiles, m1 = (ti + 1) - q1 * kPlaneTiles;
           const int base1 = kPadLo + kLine + 128 * m1;
-          const int r0 = base1 + (q1 & 3) * kPlaneRows, r1 = base1 + ((q1 + 1) & 3) * kPlaneRows,
-                    r2 = base1 + ((q1 + 2) & 3) * kPlaneRows;
+          const int r0 = base1 + (q1 & 3) * kSlotRows, r1 = base1 + ((q1 + 1) & 3) * kSlotRows,
+                    r2 = base1 + ((q1 + 2) & 3) * kSlotRows;
           if (!FSI_WAIT_H(9)) break;  // layer-1 epilogue done (so layer 1 of this tile is)
           issue_layer(tb + 64, dH, dW2, kIdesc64);
           tc::mma_commit(&bar_l);
@@ -613,7 +636,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
           last_bar = 1;
           // Plane step q - 1 is complete: its oldest plane's slot takes plane xs + q + 2.
           if (m == 0 && q >= 1 && q + 1 < nq)
-            fill_plane(a.grows, a.rg.chunk_rows, a.rg.ny_pad, a.rg.nz_pad, sRows, &bar_rows[(q + 3) & 3], (q + 3) & 3, wrap(xs + q + 2, g.nx), y0, z0);
+            fill_plane(&rows_map, sRows, &bar_rows[(q + 3) & 3], (q + 3) & 3, wrap(xs + q + 2, g.nx), y0, z0);
           if (next && m1 == 0 && !FSI_WAIT_ROWS((q1 + 2) & 3)) break;
           if (next) issue_l1_chunk<0>(tn, dRows, r0, r1, r2, dW1);
           if (!FSI_WAIT_H(10)) break;  // layer-2 epilogue done
@@ -931,16 +954,39 @@ extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const
   a.err = err;
   a.work = (long long)a.rg.nyb * a.rg.nzb * a.f.g.nx;
   cudaStream_t s = as_stream(stream);
-  closure_rows_kernel<<<grid_for(a.rg.chunk_rows, kBlock), kBlock, 0, s>>>(
+  FSI_REQUIRE(a.rg.ny_pad <= 65535 && a.f.g.nx <= 65535, "lattice too large for the row pass");
+  closure_rows_kernel<<<dim3((a.rg.nz_pad + 127) / 128, a.rg.ny_pad, a.f.g.nx), 128, 0, s>>>(
       a.f, a.rg, reinterpret_cast<unsigned char*>(rows));
   if (int e = check_launch("closure_rows_kernel")) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int grid = (int)(a.work < sms ? a.work : sms);
+  // Tensor map of the padded rows: dims (8 channels, nz_pad, ny_pad, nx, 3 chunks).
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", reinterpret_cast<void**>(&encode),
+                                                           12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !encode) {
+      encode = nullptr;
+      set_error("cuTensorMapEncodeTiled unavailable (%s)", cudaGetErrorString(e));
+      return FSI_ERR_CUDA;
+    }
+  }
+  CUtensorMap map;
+  const cuuint64_t dims[5] = {8, (cuuint64_t)a.rg.nz_pad, (cuuint64_t)a.rg.ny_pad, (cuuint64_t)a.f.g.nx, 3};
+  const cuuint64_t strides[4] = {16, (cuuint64_t)a.rg.nz_pad * 16, (cuuint64_t)a.rg.ny_pad * a.rg.nz_pad * 16,
+                                 (cuuint64_t)a.rg.chunk_rows * 16};
+  const cuuint32_t box[5] = {8, kLine, kLines + 2, 1, 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  const CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, rows, dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  FSI_REQUIRE(cr == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
   cudaFuncSetAttribute(closure_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kInferSmem);
-  closure_infer_kernel<<<grid, kInferThreads, kInferSmem, s>>>(a);
+  closure_infer_kernel<<<grid, kInferThreads, kInferSmem, s>>>(a, map);
   return check_launch("closure_infer_kernel");
 }
 
