@@ -287,14 +287,17 @@ __global__ void __launch_bounds__(128) gemm_kernel(GemmArgs g) {
 // 374 rows of lines 1..11, covered by three M tiles of 128 consecutive rows; rows on the z
 // halo (and past line 11) are computed and discarded.
 //
-// Each CTA (one per SM) takes a contiguous range of (column, x) plane steps. Warp 16 issues
-// the bulk copies and the MMAs; warps 0-15 run the epilogues (warp w reads TMEM lanes
-// 32 (w % 4) .. + 31 and columns 16 (w / 4) .. + 15). Two tiles are in flight: while the
-// epilogues of tile t (bias + GELU of layers 1-3, output of layer 4) run on the CUDA cores,
-// the tensor cores run layer 1 of tile t + 1, issued in three chunks of 14 MMAs between the
-// small layers of tile t. Hand-overs are mbarriers in both directions (MMA commits to the
-// epilogue warps; one arrival per epilogue warp to the issuer), so no CTA-wide barrier
-// sits inside the loop.
+// Each CTA (one per SM) takes a contiguous range of (column, x) plane steps. Warps 0-15 run
+// the epilogues (warp w reads TMEM lanes 32 (w % 4) .. + 31 and columns 16 (w / 4) .. + 15);
+// one thread of warp 16 issues the plane copies and layers 2-4 of each tile as its layer-1,
+// -2 and -3 epilogues finish; one thread of warp 17 issues layer 1 (42 MMAs) of the tiles
+// ahead, as soon as the tensor-memory half and the planes a tile needs are free and loaded.
+// Two tiles are in flight (TMEM halves 0 and 256): the tensor cores run layer 1 of tile
+// t + 1 while the epilogues of tile t run on the CUDA cores, and the small layers of tile t
+// never queue behind a thread that is blocked issuing layer 1. Every hand-over is an
+// mbarrier, so no CTA-wide barrier sits inside the loop; barriers written more than once
+// per tile by a role that can run ahead (layer-1 commits, layer-1 epilogue arrivals) come
+// in pairs indexed by the TMEM half, so a waiter is never two phases behind.
 constexpr int kLine = 34;                             // halo line along z: 32 cells + 2
 constexpr int kLineCells = 32;
 constexpr int kLines = 11;                            // output lines along y per column
@@ -310,7 +313,8 @@ constexpr int kL1Chunk = kL1Mmas / 3;                 // 14 MMAs per issue
 constexpr int kEpiWarps = 16;                         // epilogue warps (4 per TMEM lane quarter)
 constexpr int kWorkers = 32 * kEpiWarps;
 constexpr int kColGroups = 64 / 16 / (kEpiWarps / 4);  // 16-column groups per warp and layer
-constexpr int kInferThreads = kWorkers + 32;          // + the copy / MMA issuing warp
+constexpr int kChainWarp = kEpiWarps, kL1Warp = kEpiWarps + 1;
+constexpr int kInferThreads = kWorkers + 64;          // + the two MMA-issuing warps
 constexpr uint32_t kPlaneBytes = 3u * kPlaneRows * 16u;  // one plane: three tensor-copy boxes
 static_assert(kL1Chunk * 3 == kL1Mmas, "layer 1 is issued in three equal chunks");
 // Highest row read: the last tile's last row, offset +35, and the +16-byte second half of
@@ -543,7 +547,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
                                                                         const __grid_constant__ CUtensorMap rows_map) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float sb[64 * 3 + kOutPad];
-  __shared__ __align__(8) uint64_t bar_l1, bar_l, bar_h, bar_rows[kSlots];
+  __shared__ __align__(8) uint64_t bar_l1[2], bar_e1[2], bar_l, bar_h, bar_rows[kSlots];
   __shared__ uint32_t tbase;
   __shared__ int abort_flag;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -565,7 +569,10 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
   }
   if (warp == 0) tc::tmem_alloc(&tbase, 512);
   if (t == 0) {
-    tc::mbar_init(&bar_l1, 1);
+    for (int h = 0; h < 2; ++h) {
+      tc::mbar_init(&bar_l1[h], 1);
+      tc::mbar_init(&bar_e1[h], kWorkers / 32);
+    }
     tc::mbar_init(&bar_l, 1);
     tc::mbar_init(&bar_h, kWorkers / 32);
     for (int s = 0; s < kSlots; ++s) tc::mbar_init(&bar_rows[s], 1);
@@ -583,88 +590,104 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
   const long long work = a.work;
   const long long w0 = work * blockIdx.x / gridDim.x, w1 = work * (blockIdx.x + 1) / gridDim.x;
 
-  if (warp == kWorkers / 32) {
-    // ---------------------------------------------------- row copies and MMA issue
+  const uint32_t sRows = tc::smem_addr(smem + kOffRows);
+  if (warp == kChainWarp) {
+    // ------------------------------------------------ plane copies, layers 2-4
     if (lane == 0) {
-      const uint32_t sRows = tc::smem_addr(smem + kOffRows);
-      const uint64_t dRows = tc::smem_desc(sRows, 0u, 128u);
-      const uint64_t dW1 = tc::smem_desc(tc::smem_addr(smem + kOffW1), 128u, 256u);
       const uint64_t dH = tc::tile_desc(tc::smem_addr(smem + kOffH), 64, 0);
       const uint64_t dW2 = tc::tile_desc(tc::smem_addr(smem + kOffW2), 64, 0);
       const uint64_t dW3 = tc::tile_desc(tc::smem_addr(smem + kOffW3), 64, 0);
       const uint64_t dW4 = tc::tile_desc(tc::smem_addr(smem + kOffW4), 64, 0);
-      uint32_t n_h = 0, c_l1 = 0, c_l = 0, rows_phase = 0;
-      int last_bar = -1;
+      uint32_t n_h = 0, c_l = 0, tile = 0, fills = 0;  // fills: parity of copies issued per slot
       bool ok = true;
 #define FSI_WAIT_H(code) (ok = tc::mbar_wait_abortable(&bar_h, n_h & 1, abort, a.err, (code)), ++n_h, tc::fence_after_sync(), ok)
-#define FSI_WAIT_ROWS(s) (ok = tc::mbar_wait_abortable(&bar_rows[(s)], (rows_phase >> (s)) & 1u, abort, a.err, 12), rows_phase ^= 1u << (s), ok)
+#define FSI_FILL(slot, x)                                                            \
+  do {                                                                               \
+    fill_plane(&rows_map, sRows, &bar_rows[(slot)], (slot), (x), y0, z0);           \
+    fills ^= 1u << (slot);                                                           \
+  } while (0)
       for (long long p0 = w0; p0 < w1 && ok;) {
         const long long col = p0 / g.nx;
         const int xs = (int)(p0 - col * g.nx);
         const int nq = (int)min((long long)(g.nx - xs), w1 - p0);
         const int yb = (int)(col / rg.nzb), zb = (int)(col - (long long)yb * rg.nzb);
         const int y0 = yb * kLines, z0 = zb * kLineCells;
-        // The previous segment's MMAs have read their slots.
-        if (c_l > 0 && !(ok = tc::mbar_wait_abortable(&bar_l, (c_l - 1) & 1, abort, a.err, 13))) break;
-        // Ordinal u = plane xs - 1 + u, in slot u & 3.
-        for (int u = 0; u < 3; ++u) fill_plane(&rows_map, sRows, &bar_rows[u], u, wrap(xs - 1 + u, g.nx), y0, z0);
-        if (nq > 1) fill_plane(&rows_map, sRows, &bar_rows[3], 3, wrap(xs + 2, g.nx), y0, z0);
-        if (!FSI_WAIT_ROWS(0) || !FSI_WAIT_ROWS(1) || !FSI_WAIT_ROWS(2)) break;
-        {
-          const uint32_t d = tmem + ((c_l1 & 1) << 8);
-          const int r1 = kPadLo + 1 * kSlotRows + kLine, r2 = kPadLo + 2 * kSlotRows + kLine;
-          issue_l1_chunk<0>(d, dRows, kPadLo + kLine, r1, r2, dW1);
-          issue_l1_chunk<1>(d, dRows, kPadLo + kLine, r1, r2, dW1);
-          issue_l1_chunk<2>(d, dRows, kPadLo + kLine, r1, r2, dW1);
-        }
-        tc::mma_commit(&bar_l1);
-        ++c_l1;
-        last_bar = 0;
+        // Every MMA reading the ring has completed: the last tile's layer-1 epilogue has been
+        // handed over, and layer 1 of the next segment waits for these copies. Ordinal u is
+        // plane xs - 1 + u, in slot u & 3.
+        for (int u = 0; u < 3; ++u) FSI_FILL(u, wrap(xs - 1 + u, g.nx));
+        if (nq > 1) FSI_FILL(3, wrap(xs + 2, g.nx));
         const int ntile = kPlaneTiles * nq;
-        for (int ti = 0; ti < ntile; ++ti) {
+        for (int ti = 0; ti < ntile; ++ti, ++tile) {
           const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
-          const uint32_t tb = tmem + (((c_l1 - 1) & 1) << 8), tn = tmem + ((c_l1 & 1) << 8);
-          const bool next = ti + 1 < ntile;
-          const int q1 = (ti + 1) / kPlaneTiles, m1 = (ti + 1) - q1 * kPlaneTiles;
-          const int base1 = kPadLo + kLine + 128 * m1;
-          const int r0 = base1 + (q1 & 3) * kSlotRows, r1 = base1 + ((q1 + 1) & 3) * kSlotRows,
-                    r2 = base1 + ((q1 + 2) & 3) * kSlotRows;
-          if (!FSI_WAIT_H(9)) break;  // layer-1 epilogue done (so layer 1 of this tile is)
+          const uint32_t tb = tmem + ((tile & 1) << 8);
+          if (!FSI_WAIT_H(9)) break;  // layer-1 epilogue done
           issue_layer(tb + 64, dH, dW2, kIdesc64);
           tc::mma_commit(&bar_l);
           ++c_l;
-          last_bar = 1;
-          // Plane step q - 1 is complete: its oldest plane's slot takes plane xs + q + 2.
-          if (m == 0 && q >= 1 && q + 1 < nq)
-            fill_plane(&rows_map, sRows, &bar_rows[(q + 3) & 3], (q + 3) & 3, wrap(xs + q + 2, g.nx), y0, z0);
-          if (next && m1 == 0 && !FSI_WAIT_ROWS((q1 + 2) & 3)) break;
-          if (next) issue_l1_chunk<0>(tn, dRows, r0, r1, r2, dW1);
+          // Layer 1 of plane step q is complete, so is that of plane step q - 1: its oldest
+          // plane's slot takes plane xs + q + 2.
+          if (m == 0 && q >= 1 && q + 1 < nq) FSI_FILL((q + 3) & 3, wrap(xs + q + 2, g.nx));
           if (!FSI_WAIT_H(10)) break;  // layer-2 epilogue done
           issue_layer(tb + 128, dH, dW3, kIdesc64);
           tc::mma_commit(&bar_l);
           ++c_l;
-          if (next) issue_l1_chunk<1>(tn, dRows, r0, r1, r2, dW1);
           if (!FSI_WAIT_H(11)) break;  // layer-3 epilogue done
           issue_layer(tb + 192, dH, dW4, kIdesc32);
           tc::mma_commit(&bar_l);
           ++c_l;
-          last_bar = 1;
-          if (next) {
-            issue_l1_chunk<2>(tn, dRows, r0, r1, r2, dW1);
-            tc::mma_commit(&bar_l1);
-            ++c_l1;
-            last_bar = 0;
-          }
         }
         p0 += nq;
       }
       if (!ok) {
-        // Let the copies and MMAs in flight finish before the CTA exits (bounded waits).
-        for (int s = 0; s < kSlots; ++s) tc::mbar_wait(&bar_rows[s], (rows_phase >> s) & 1u, nullptr, 0);
-        if (last_bar == 0) tc::mbar_wait(&bar_l1, (c_l1 - 1) & 1, nullptr, 0);
-        else if (last_bar == 1) tc::mbar_wait(&bar_l, (c_l - 1) & 1, nullptr, 0);
+        // Let the copies and MMAs this thread issued finish before the CTA exits (bounded).
+        for (int sl = 0; sl < kSlots; ++sl) tc::mbar_wait(&bar_rows[sl], ((fills >> sl) & 1u) ^ 1u, nullptr, 0);
+        if (c_l > 0) tc::mbar_wait(&bar_l, (c_l - 1) & 1, nullptr, 0);
       }
 #undef FSI_WAIT_H
+#undef FSI_FILL
+    }
+  } else if (warp == kL1Warp) {
+    // ------------------------------------------------------------------ layer 1
+    if (lane == 0) {
+      const uint64_t dRows = tc::smem_desc(sRows, 0u, 128u);
+      const uint64_t dW1 = tc::smem_desc(tc::smem_addr(smem + kOffW1), 128u, 256u);
+      uint32_t tile = 0, rows_phase = 0, issued = 0;
+      bool ok = true;
+#define FSI_WAIT_ROWS(sl) (ok = tc::mbar_wait_abortable(&bar_rows[(sl)], (rows_phase >> (sl)) & 1u, abort, a.err, 12), rows_phase ^= 1u << (sl), ok)
+      for (long long p0 = w0; p0 < w1 && ok;) {
+        const long long col = p0 / g.nx;
+        const int nq = (int)min((long long)(g.nx - (int)(p0 - col * g.nx)), w1 - p0);
+        const int ntile = kPlaneTiles * nq;
+        for (int ti = 0; ti < ntile; ++ti, ++tile) {
+          const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
+          const uint32_t h = tile & 1;
+          // The TMEM half's previous tile (tile - 2) has been read by its layer-1 epilogue.
+          if (tile >= 2 && !(ok = tc::mbar_wait_abortable(&bar_e1[h], ((tile - 2) >> 1) & 1u, abort, a.err, 14))) break;
+          // The planes of this plane step are loaded.
+          if (ti == 0) {
+            if (!FSI_WAIT_ROWS(0) || !FSI_WAIT_ROWS(1) || !FSI_WAIT_ROWS(2)) break;
+          } else if (m == 0 && !FSI_WAIT_ROWS((q + 2) & 3)) {
+            break;
+          }
+          tc::fence_after_sync();
+          const int base = kPadLo + kLine + 128 * m;
+          const int r0 = base + (q & 3) * kSlotRows, r1 = base + ((q + 1) & 3) * kSlotRows,
+                    r2 = base + ((q + 2) & 3) * kSlotRows;
+          const uint32_t d = tmem + (h << 8);
+          issue_l1_chunk<0>(d, dRows, r0, r1, r2, dW1);
+          issue_l1_chunk<1>(d, dRows, r0, r1, r2, dW1);
+          issue_l1_chunk<2>(d, dRows, r0, r1, r2, dW1);
+          tc::mma_commit(&bar_l1[h]);
+          ++issued;
+        }
+        p0 += nq;
+      }
+      if (!ok && issued > 0) {
+        // Let the last layer 1 issued (tile issued - 1; tiles go in order) finish (bounded).
+        const uint32_t lt = issued - 1;
+        tc::mbar_wait(&bar_l1[lt & 1], (lt >> 1) & 1u, nullptr, 0);
+      }
 #undef FSI_WAIT_ROWS
     }
   } else {
@@ -701,13 +724,15 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
         const bool valid = lq < 2 && hy <= kLines && hz >= 1 && hz <= kLineCells && oy < g.ny && oz < g.nz;
         const long long cc = ((long long)(xs + q) * g.ny + oy) * g.nz + oz;
         const uint32_t fl = valid ? a.f.flags[cc] : kFlagSolid;
-        const uint32_t tb = tmem + ((n_l1 & 1) << 8) + lane_base;
-        if (!(ok = FSI_WWAIT(&bar_l1, n_l1 & 1, 3))) break;
+        const uint32_t h = n_l1 & 1;
+        const uint32_t tb = tmem + (h << 8) + lane_base;
+        if (!(ok = FSI_WWAIT(&bar_l1[h], (n_l1 >> 1) & 1u, 3))) break;
         ++n_l1;
         tc::fence_after_sync();
 #pragma unroll
         for (int cg = 0; cg < kColGroups; ++cg) hidden_epilogue(tb, sb, kColGroups * lq + cg, H, lrow);
         FSI_HAND_OVER();
+        if (lane == 0) tc::mbar_arrive(&bar_e1[h]);  // this half's layer-1 accumulator is free
         if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 4))) break;
         ++n_l;
         tc::fence_after_sync();
