@@ -462,6 +462,13 @@ int64_t fsi_closure_rows_bytes(const fsi_lbm_desc* desc);
 int fsi_closure_infer(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
                       const float* force, int64_t steps_done, const fsi_closure_weights* weights,
                       void* rows, float* corr, int32_t* err, void* stream);
+/* fsi_closure_infer followed by fsi_closure_apply in one pass: each fluid cell's
+ * mass-conserving correction is added to its populations in place (the arithmetic of
+ * fsi_closure_apply), without a correction array. */
+int fsi_closure_infer_apply(const fsi_lbm_desc* desc, float* pops, const uint32_t* flags,
+                            const float* force, int64_t steps_done,
+                            const fsi_closure_weights* weights, void* rows, int32_t* err,
+                            void* stream);
 /* f_q += corr_q - w_q sum_p corr_p on fluid cells (moves no mass). */
 int fsi_closure_apply(const fsi_lbm_desc* desc, float* pops, const uint32_t* flags,
                       int64_t steps_done, const float* corr, void* stream);

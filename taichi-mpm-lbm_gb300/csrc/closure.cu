@@ -362,7 +362,8 @@ struct InferArgs {
   const __nv_bfloat16* __restrict__ w4;     // [32][64], rows >= 19 zero
   const float* __restrict__ b;              // b1[64] b2[64] b3[64] b4[32]
   float out_scale;                          // correction = y / out_scale
-  float* __restrict__ corr;                 // [19][N]
+  float* __restrict__ corr;                 // [19][N] (kApply = false)
+  float* __restrict__ pops;                 // populations corrected in place (kApply = true)
   int* err;
   long long work;                           // plane steps: columns * nx
 };
@@ -543,6 +544,11 @@ __device__ __forceinline__ void fill_plane(const CUtensorMap* map, uint32_t s_ro
   }
 }
 
+// kApply = false: corrections to a.corr. kApply = true: each cell's mass-conserving correction
+// f_q += c_q - w_q sum_p c_p added to its populations in place (the arithmetic of
+// closure_apply_kernel); the kernel reads only the staged rows, never the populations, so
+// no other cell's inputs change.
+template <bool kApply>
 __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferArgs a,
                                                                         const __grid_constant__ CUtensorMap rows_map) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -721,9 +727,21 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
         const int pr = kLine + 128 * m + lrow;
         const int hy = pr / kLine, hz = pr - hy * kLine;
         const int oy = y0 + hy - 1, oz = z0 + hz - 1;
-        const bool valid = lq < 2 && hy <= kLines && hz >= 1 && hz <= kLineCells && oy < g.ny && oz < g.nz;
+        const bool valid = lq < (kApply ? 1 : 2) && hy <= kLines && hz >= 1 && hz <= kLineCells && oy < g.ny &&
+                           oz < g.nz;
         const long long cc = ((long long)(xs + q) * g.ny + oy) * g.nz + oz;
         const uint32_t fl = valid ? a.f.flags[cc] : kFlagSolid;
+        // In place: the cell's 19 populations, loaded now so the output epilogue only adds.
+        float fq[kApply ? kOut : 1];
+        uint32_t slq[kApply ? kOut : 1];
+        if (kApply && valid) {
+          const Deltas dc(g, xs + q, oy, oz);
+#pragma unroll
+          for (int qo = 0; qo < kOut; ++qo) {
+            slq[qo] = slot32((uint32_t)g.n, dc, fl, qo, a.f.parity);
+            fq[qo] = a.pops[slq[qo]];
+          }
+        }
         const uint32_t h = n_l1 & 1;
         const uint32_t tb = tmem + (h << 8) + lane_base;
         if (!(ok = FSI_WWAIT(&bar_l1[h], (n_l1 >> 1) & 1u, 3))) break;
@@ -748,8 +766,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
         if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 6))) break;
         ++n_l;
         tc::fence_after_sync();
-        // Outputs: columns 0-31, of which 19 are used (16 per warp, warps with lq < 2).
-        if (lq < 2) {
+        // Outputs: warps with lq < 2 hold columns 0-31, of which 19 are used; in place, the
+        // warps with lq == 0 take all 32 columns of their rows.
+        if (!kApply && lq < 2) {
           float y[16];
           tc::tmem_ld16(tb + 192 + 16 * lq, y);
           if (valid) {
@@ -759,6 +778,21 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
               const int qo = 16 * lq + i;
               if (qo < kOut) a.corr[(size_t)qo * g.n + cc] = (y[i] + sb[192 + qo]) * keep;
             }
+          }
+        }
+        if (kApply && lq == 0) {
+          float y[32];
+          tc::tmem_ld16(tb + 192, *reinterpret_cast<float(*)[16]>(y));
+          tc::tmem_ld16(tb + 208, *reinterpret_cast<float(*)[16]>(y + 16));
+          if (valid && !(fl & kFlagSolid)) {
+            float cq[kOut], sum = 0.f;
+#pragma unroll
+            for (int qo = 0; qo < kOut; ++qo) {
+              cq[qo] = (y[qo] + sb[192 + qo]) * inv_out;
+              sum += cq[qo];
+            }
+#pragma unroll
+            for (int qo = 0; qo < kOut; ++qo) a.pops[slq[qo]] = fq[qo] + (cq[qo] - weight_of(qo) * sum);
           }
         }
       }
@@ -956,12 +990,16 @@ extern "C" int64_t fsi_closure_rows_bytes(const fsi_lbm_desc* d) {
   return 3 * row_geom(geom_of(d)).chunk_rows * 16;
 }
 
-extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags,
-                                 const float* force, int64_t steps_done,
-                                 const fsi_closure_weights* w, void* rows, float* corr, int32_t* err,
-                                 void* stream) {
+namespace fsi {
+namespace {
+
+// The row pass, then the fused inference (corrections to corr, or applied to pops_out).
+template <bool kApply>
+int launch_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags, const float* force,
+                 int64_t steps_done, const fsi_closure_weights* w, void* rows, float* corr, float* pops_out,
+                 int32_t* err, void* stream) {
   if (int e = check_closure_lattice(d)) return e;
-  FSI_REQUIRE(pops && flags && force && w && rows && corr && err, "NULL array");
+  FSI_REQUIRE(pops && flags && force && w && rows && err && (kApply || corr), "NULL array");
   FSI_REQUIRE(((uintptr_t)rows & 15) == 0, "rows must be 16-byte aligned");
   FSI_REQUIRE(w->w1 && w->w2 && w->w3 && w->w4 && w->bias, "NULL weights");
   FSI_REQUIRE(w->out_scale != 0.f, "out_scale must be non-zero");
@@ -976,6 +1014,7 @@ extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const
   a.b = w->bias;
   a.out_scale = w->out_scale;
   a.corr = corr;
+  a.pops = pops_out;
   a.err = err;
   a.work = (long long)a.rg.nyb * a.rg.nzb * a.f.g.nx;
   cudaStream_t s = as_stream(stream);
@@ -1009,10 +1048,28 @@ extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   FSI_REQUIRE(cr == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
-  cudaFuncSetAttribute(closure_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(closure_infer_kernel<kApply>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kInferSmem);
-  closure_infer_kernel<<<grid, kInferThreads, kInferSmem, s>>>(a, map);
+  closure_infer_kernel<kApply><<<grid, kInferThreads, kInferSmem, s>>>(a, map);
   return check_launch("closure_infer_kernel");
+}
+
+
+}  // namespace
+}  // namespace fsi
+
+extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags,
+                                 const float* force, int64_t steps_done,
+                                 const fsi_closure_weights* w, void* rows, float* corr, int32_t* err,
+                                 void* stream) {
+  return launch_infer<false>(d, pops, flags, force, steps_done, w, rows, corr, nullptr, err, stream);
+}
+
+extern "C" int fsi_closure_infer_apply(const fsi_lbm_desc* d, float* pops, const uint32_t* flags,
+                                       const float* force, int64_t steps_done,
+                                       const fsi_closure_weights* w, void* rows, int32_t* err,
+                                       void* stream) {
+  return launch_infer<true>(d, pops, flags, force, steps_done, w, rows, nullptr, pops, err, stream);
 }
 
 extern "C" int fsi_closure_apply(const fsi_lbm_desc* d, float* pops, const uint32_t* flags,

@@ -41,14 +41,15 @@ _CS = 1.0 / math.sqrt(3.0)
 # ----------------------------------------------------------------- grids
 def coarse_config(fine: LBMConfig) -> LBMConfig:
     """The 2x coarser lattice in acoustic scaling: half the cells per axis, half the lattice
-    viscosity, twice the body force, FP32 populations in the exact form."""
+    viscosity, twice the body force, FP32 populations with the reduced-operation collision
+    (the learned correction is trained against this same coarse step)."""
     for n in (fine.nx, fine.ny, fine.nz):
         if n % 2:
             raise ValueError("the fine lattice needs even sizes.")
     return dataclasses.replace(fine, nx=fine.nx // 2, ny=fine.ny // 2, nz=fine.nz // 2,
                                viscosity=fine.viscosity / 2.0,
                                force=tuple(2.0 * g for g in fine.force),
-                               population_storage="f32", collision_arithmetic="exact",
+                               population_storage="f32", collision_arithmetic="fast",
                                mrt_rates=None)
 
 
@@ -341,6 +342,16 @@ def infer(lbm: LBMSolver3D, weights: nat.ClosureWeights, corr: torch.Tensor, row
              nat.stream_ptr())
 
 
+def infer_apply(lbm: LBMSolver3D, weights: nat.ClosureWeights, rows: torch.Tensor,
+                err: torch.Tensor) -> None:
+    """The fused inference with each cell's mass-conserving correction added to its populations
+    in place (``infer`` then ``fsi_closure_apply``, in one pass)."""
+    nat.call("fsi_closure_infer_apply", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags),
+             nat.ptr(lbm.force), lbm.steps_done, ctypes.byref(weights), nat.ptr(rows), nat.ptr(err),
+             nat.stream_ptr())
+    lbm._mass_speed_cache = None
+
+
 class ClosureSimulation:
     """The coarse lattice with the learned correction after every step; guards on mass drift
     and local Mach number fall back to the plain fine-grid solver."""
@@ -352,8 +363,6 @@ class ClosureSimulation:
         self.net = net
         self.coarse = LBMSolver3D(coarse_config(fine_cfg))
         self.coarse.initialize(coarse_mask(fine_mask))
-        self.corr = torch.zeros((OUT, self.coarse.n_cells), dtype=torch.float32,
-                                device=self.coarse._device)
         self.mass_tol, self.mach_tol, self.check_every = mass_tol, mach_tol, check_every
         self.mass0 = self.coarse.total_mass()
         self.fine: LBMSolver3D | None = None
@@ -392,10 +401,7 @@ class ClosureSimulation:
             return
         c = self.coarse
         c.step()
-        infer(c, self._weights, self.corr, self._rows, self.net.err)
-        nat.call("fsi_closure_apply", c._desc, nat.ptr(c._pops), nat.ptr(c.flags), c.steps_done,
-                 nat.ptr(self.corr), nat.stream_ptr())
-        c._mass_speed_cache = None
+        infer_apply(c, self._weights, self._rows, self.net.err)
         self.coarse_steps += 1
         if self.check_every and self.coarse_steps % self.check_every == 0:
             reason = self._guard()

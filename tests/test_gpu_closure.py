@@ -125,6 +125,28 @@ def test_fused_inference_matches_unfused_passes():
     assert float(corr[:, torch.from_numpy(solid).cuda()].abs().max()) == 0.0
 
 
+def test_in_place_inference_equals_inference_then_apply():
+    """fsi_closure_infer_apply gives bit for bit the populations of fsi_closure_infer followed
+    by fsi_closure_apply (both parities of the AA layout)."""
+    for steps in (4, 5):
+        lbm, mask = small_lattice(steps=steps)
+        net = cl.ClosureMLP(seed=5)
+        net.pop_scale, net.force_scale, net.out_scale = 30.0, 1e3, 250.0
+        w = net.weights_struct()
+        rows = cl.rows_buffer(lbm)
+        before = lbm._pops.clone()
+        corr = torch.zeros((19, lbm.n_cells), dtype=torch.float32, device="cuda")
+        cl.infer(lbm, w, corr, rows, net.err)
+        nat.call("fsi_closure_apply", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags), lbm.steps_done,
+                 nat.ptr(corr), nat.stream_ptr())
+        want = lbm._pops.clone()
+        lbm._pops.copy_(before)
+        cl.infer_apply(lbm, w, rows, net.err)
+        net.check()
+        assert torch.equal(lbm._pops, want), steps
+        assert not torch.equal(want, before)
+
+
 def test_gradients_match_the_oracle():
     rng = np.random.default_rng(11)
     net = cl.ClosureMLP(seed=5)
