@@ -312,7 +312,8 @@ constexpr int kL1Mmas = 27 + 3 * 5;                   // 42
 constexpr int kL1Chunk = kL1Mmas / 3;                 // 14 MMAs per issue
 constexpr int kEpiWarps = 16;                         // epilogue warps (4 per TMEM lane quarter)
 constexpr int kWorkers = 32 * kEpiWarps;
-constexpr int kColGroups = 64 / 16 / (kEpiWarps / 4);  // 16-column groups per warp and layer
+constexpr int kGroupWarps = kEpiWarps / 2;            // two epilogue groups, alternate tiles
+constexpr size_t kHBytes = 128 * 64 * 2;              // one activation tile
 constexpr int kChainWarp = kEpiWarps, kL1Warp = kEpiWarps + 1;
 constexpr int kInferThreads = kWorkers + 64;          // + the two MMA-issuing warps
 constexpr uint32_t kPlaneBytes = 3u * kPlaneRows * 16u;  // one plane: three tensor-copy boxes
@@ -330,7 +331,7 @@ constexpr size_t kOffW2 = kOffW1 + (size_t)kL1Mmas * 64 * 16 * 2;
 constexpr size_t kOffW3 = kOffW2 + 64 * 64 * 2;
 constexpr size_t kOffW4 = kOffW3 + 64 * 64 * 2;
 constexpr size_t kOffH = kOffW4 + kOutPad * 64 * 2;
-constexpr size_t kOffRows = kOffH + 128 * 64 * 2;
+constexpr size_t kOffRows = kOffH + 2 * kHBytes;     // an activation tile per group
 constexpr size_t kInferSmem = kOffRows + 3 * (size_t)kChunkBytes;
 static_assert(kInferSmem <= 227 * 1024 - 2048, "fused inference exceeds shared memory");
 
@@ -544,6 +545,117 @@ __device__ __forceinline__ void fill_plane(const CUtensorMap* map, uint32_t s_ro
   }
 }
 
+// The tiles of one CTA, by segment: a segment is a run of plane steps within one column.
+struct Segment {
+  int p0;                 // first plane step
+  int xs, nq, y0, z0;     // first x, plane steps, column origin
+  uint32_t first, ntile;  // CTA tile index of the first tile, tiles
+};
+
+__device__ __forceinline__ Segment segment_at(int p0, int w1, uint32_t first, const LbmGeom& g, const RowGeom& rg) {
+  Segment s;
+  s.p0 = p0;
+  const int col = p0 / g.nx;
+  s.xs = p0 - col * g.nx;
+  s.nq = min(g.nx - s.xs, w1 - p0);
+  const int yb = col / rg.nzb, zb = col - yb * rg.nzb;
+  s.y0 = yb * kLines;
+  s.z0 = zb * kLineCells;
+  s.first = first;
+  s.ntile = (uint32_t)(kPlaneTiles * s.nq);
+  return s;
+}
+
+// Moves s forward to the segment holding CTA tile t.
+__device__ __forceinline__ void seek(Segment& s, uint32_t t, int w1, const LbmGeom& g, const RowGeom& rg) {
+  while (t >= s.first + s.ntile) s = segment_at(s.p0 + s.nq, w1, s.first + s.ntile, g, rg);
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;}"
+      : "=r"(done)
+      : "r"(tc::smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Chain-issuer state of one epilogue group: its next tile, the epilogue of that tile it
+// waits for (0-2), phases of its hand-over barrier waited and commits to its layer barrier.
+struct Group {
+  uint32_t tile, stage = 0, n_h = 0, c_l = 0;
+  Segment seg;
+};
+
+struct ChainCtx {
+  const CUtensorMap* map;
+  uint32_t s_rows;
+  uint64_t* bar_rows;
+  uint32_t tmem;
+  uint64_t w2, w3, w4;
+  int w1;
+  uint32_t ntiles;
+};
+
+// The first planes of segment s (ordinal u = plane xs - 1 + u, slot u & 3).
+__device__ __forceinline__ void fill_segment_start(const CUtensorMap* map, uint32_t s_rows, uint64_t* bar_rows,
+                                                   uint32_t& fills, const Segment& s, int nx) {
+  for (int u = 0; u < 3; ++u) {
+    fill_plane(map, s_rows, &bar_rows[u], u, wrap(s.xs - 1 + u, nx), s.y0, s.z0);
+    fills ^= 1u << u;
+  }
+  if (s.nq > 1) {
+    fill_plane(map, s_rows, &bar_rows[3], 3, wrap(s.xs + 2, nx), s.y0, s.z0);
+    fills ^= 1u << 3;
+  }
+}
+
+// If group H has handed over its next epilogue, issues the layer that follows it (and, after
+// a layer-1 epilogue, the plane copies that tile frees); returns whether it did.
+template <int H>
+__device__ __forceinline__ bool serve(Group& gr, uint64_t& bar_h, uint64_t& bar_l, uint64_t dh, const ChainCtx& cx,
+                                      uint32_t& fills, const LbmGeom& g, const RowGeom& rg) {
+  if (gr.tile >= cx.ntiles || !mbar_test(&bar_h, gr.n_h & 1)) return false;
+  ++gr.n_h;
+  tc::fence_after_sync();
+  const uint32_t tb = cx.tmem + ((uint32_t)H << 8);
+  if (gr.stage == 0) {  // layer-1 epilogue done: layer 2, plane copies
+    issue_layer(tb + 64, dh, cx.w2, kIdesc64);
+    tc::mma_commit(&bar_l);
+    ++gr.c_l;
+    seek(gr.seg, gr.tile, cx.w1, g, rg);
+    const Segment& s = gr.seg;
+    const int ti = (int)(gr.tile - s.first), q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
+    // Layer 1 of this tile is complete, so is every earlier one: plane step q - 1's oldest
+    // plane gives its slot to plane xs + q + 2; after a segment's last tile, the next
+    // segment's first planes go in.
+    if (m == 0 && q >= 1 && q + 1 < s.nq) {
+      const int sl = (q + 3) & 3;
+      fill_plane(cx.map, cx.s_rows, &cx.bar_rows[sl], sl, wrap(s.xs + q + 2, g.nx), s.y0, s.z0);
+      fills ^= 1u << sl;
+    }
+    if ((uint32_t)ti + 1 == s.ntile && s.p0 + s.nq < cx.w1)
+      fill_segment_start(cx.map, cx.s_rows, cx.bar_rows, fills, segment_at(s.p0 + s.nq, cx.w1, s.first + s.ntile, g, rg),
+                         g.nx);
+    gr.stage = 1;
+  } else if (gr.stage == 1) {
+    issue_layer(tb + 128, dh, cx.w3, kIdesc64);
+    tc::mma_commit(&bar_l);
+    ++gr.c_l;
+    gr.stage = 2;
+  } else {
+    issue_layer(tb + 192, dh, cx.w4, kIdesc32);
+    tc::mma_commit(&bar_l);
+    ++gr.c_l;
+    gr.stage = 0;
+    gr.tile += 2;
+  }
+  return true;
+}
+
 // kApply = false: corrections to a.corr. kApply = true: each cell's mass-conserving correction
 // f_q += c_q - w_q sum_p c_p added to its populations in place (the arithmetic of
 // closure_apply_kernel); the kernel reads only the staged rows, never the populations, so
@@ -553,7 +665,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
                                                                         const __grid_constant__ CUtensorMap rows_map) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float sb[64 * 3 + kOutPad];
-  __shared__ __align__(8) uint64_t bar_l1[2], bar_e1[2], bar_l, bar_h, bar_rows[kSlots];
+  // Per epilogue group / TMEM half h: bar_l1[h] layer 1 done, bar_e1[h] its accumulator read,
+  // bar_h[h] an epilogue handed over, bar_l[h] a layer 2-4 done.
+  __shared__ __align__(8) uint64_t bar_l1[2], bar_e1[2], bar_h[2], bar_l[2], bar_rows[kSlots];
   __shared__ uint32_t tbase;
   __shared__ int abort_flag;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -577,10 +691,10 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
   if (t == 0) {
     for (int h = 0; h < 2; ++h) {
       tc::mbar_init(&bar_l1[h], 1);
-      tc::mbar_init(&bar_e1[h], kWorkers / 32);
+      tc::mbar_init(&bar_e1[h], kGroupWarps);
+      tc::mbar_init(&bar_h[h], kGroupWarps);
+      tc::mbar_init(&bar_l[h], 1);
     }
-    tc::mbar_init(&bar_l, 1);
-    tc::mbar_init(&bar_h, kWorkers / 32);
     for (int s = 0; s < kSlots; ++s) tc::mbar_init(&bar_rows[s], 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -593,65 +707,58 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
   volatile int* abort = &abort_flag;
   const LbmGeom& g = a.f.g;
   const RowGeom& rg = a.rg;
-  const long long work = a.work;
-  const long long w0 = work * blockIdx.x / gridDim.x, w1 = work * (blockIdx.x + 1) / gridDim.x;
+  // This CTA's plane steps [w0, w1) (the host keeps the count below 2^31 / 3).
+  const int w0 = (int)((long long)a.work * blockIdx.x / gridDim.x);
+  const int w1 = (int)((long long)a.work * (blockIdx.x + 1) / gridDim.x);
+  const uint32_t ntiles = (uint32_t)(kPlaneTiles * (w1 - w0));
 
   const uint32_t sRows = tc::smem_addr(smem + kOffRows);
   if (warp == kChainWarp) {
     // ------------------------------------------------ plane copies, layers 2-4
     if (lane == 0) {
-      const uint64_t dH = tc::tile_desc(tc::smem_addr(smem + kOffH), 64, 0);
+      const uint64_t dH0 = tc::tile_desc(tc::smem_addr(smem + kOffH), 64, 0);
+      const uint64_t dH1 = tc::tile_desc(tc::smem_addr(smem + kOffH + kHBytes), 64, 0);
       const uint64_t dW2 = tc::tile_desc(tc::smem_addr(smem + kOffW2), 64, 0);
       const uint64_t dW3 = tc::tile_desc(tc::smem_addr(smem + kOffW3), 64, 0);
       const uint64_t dW4 = tc::tile_desc(tc::smem_addr(smem + kOffW4), 64, 0);
-      uint32_t n_h = 0, c_l = 0, tile = 0, fills = 0;  // fills: parity of copies issued per slot
+      uint32_t fills = 0;  // parity of the copies issued per slot
       bool ok = true;
-#define FSI_WAIT_H(code) (ok = tc::mbar_wait_abortable(&bar_h, n_h & 1, abort, a.err, (code)), ++n_h, tc::fence_after_sync(), ok)
-#define FSI_FILL(slot, x)                                                            \
-  do {                                                                               \
-    fill_plane(&rows_map, sRows, &bar_rows[(slot)], (slot), (x), y0, z0);           \
-    fills ^= 1u << (slot);                                                           \
-  } while (0)
-      for (long long p0 = w0; p0 < w1 && ok;) {
-        const long long col = p0 / g.nx;
-        const int xs = (int)(p0 - col * g.nx);
-        const int nq = (int)min((long long)(g.nx - xs), w1 - p0);
-        const int yb = (int)(col / rg.nzb), zb = (int)(col - (long long)yb * rg.nzb);
-        const int y0 = yb * kLines, z0 = zb * kLineCells;
-        // Every MMA reading the ring has completed: the last tile's layer-1 epilogue has been
-        // handed over, and layer 1 of the next segment waits for these copies. Ordinal u is
-        // plane xs - 1 + u, in slot u & 3.
-        for (int u = 0; u < 3; ++u) FSI_FILL(u, wrap(xs - 1 + u, g.nx));
-        if (nq > 1) FSI_FILL(3, wrap(xs + 2, g.nx));
-        const int ntile = kPlaneTiles * nq;
-        for (int ti = 0; ti < ntile; ++ti, ++tile) {
-          const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
-          const uint32_t tb = tmem + ((tile & 1) << 8);
-          if (!FSI_WAIT_H(9)) break;  // layer-1 epilogue done
-          issue_layer(tb + 64, dH, dW2, kIdesc64);
-          tc::mma_commit(&bar_l);
-          ++c_l;
-          // Layer 1 of plane step q is complete, so is that of plane step q - 1: its oldest
-          // plane's slot takes plane xs + q + 2.
-          if (m == 0 && q >= 1 && q + 1 < nq) FSI_FILL((q + 3) & 3, wrap(xs + q + 2, g.nx));
-          if (!FSI_WAIT_H(10)) break;  // layer-2 epilogue done
-          issue_layer(tb + 128, dH, dW3, kIdesc64);
-          tc::mma_commit(&bar_l);
-          ++c_l;
-          if (!FSI_WAIT_H(11)) break;  // layer-3 epilogue done
-          issue_layer(tb + 192, dH, dW4, kIdesc32);
-          tc::mma_commit(&bar_l);
-          ++c_l;
+      Group gr0, gr1;
+      gr0.tile = 0;
+      gr1.tile = 1;
+      if (ntiles > 0) {
+        // The first segment's planes: ordinal u is plane xs - 1 + u, in slot u & 3.
+        const Segment s0 = segment_at(w0, w1, 0, g, rg);
+        fill_segment_start(&rows_map, sRows, bar_rows, fills, s0, g.nx);
+        gr0.seg = s0;
+        gr1.seg = s0;
+      }
+      const ChainCtx cx{&rows_map, sRows, bar_rows, tmem, dW2, dW3, dW4, w1, ntiles};
+      long long t_idle = clock64();
+      // Serve the two epilogue groups in the order their hand-overs arrive.
+      while (gr0.tile < ntiles || gr1.tile < ntiles) {
+        const bool p0 = serve<0>(gr0, bar_h[0], bar_l[0], dH0, cx, fills, g, rg);
+        const bool p1 = serve<1>(gr1, bar_h[1], bar_l[1], dH1, cx, fills, g, rg);
+        if (p0 || p1) {
+          t_idle = clock64();
+        } else if (*abort) {
+          ok = false;
+          break;
+        } else if (clock64() - t_idle > tc::kWaitCycles) {
+          *abort = 1;
+          atomicExch(a.err, 9);
+          ok = false;
+          break;
+        } else {
+          __nanosleep(20);
         }
-        p0 += nq;
       }
       if (!ok) {
         // Let the copies and MMAs this thread issued finish before the CTA exits (bounded).
         for (int sl = 0; sl < kSlots; ++sl) tc::mbar_wait(&bar_rows[sl], ((fills >> sl) & 1u) ^ 1u, nullptr, 0);
-        if (c_l > 0) tc::mbar_wait(&bar_l, (c_l - 1) & 1, nullptr, 0);
+        if (gr0.c_l > 0) tc::mbar_wait(&bar_l[0], (gr0.c_l - 1) & 1, nullptr, 0);
+        if (gr1.c_l > 0) tc::mbar_wait(&bar_l[1], (gr1.c_l - 1) & 1, nullptr, 0);
       }
-#undef FSI_WAIT_H
-#undef FSI_FILL
     }
   } else if (warp == kL1Warp) {
     // ------------------------------------------------------------------ layer 1
@@ -661,9 +768,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
       uint32_t tile = 0, rows_phase = 0, issued = 0;
       bool ok = true;
 #define FSI_WAIT_ROWS(sl) (ok = tc::mbar_wait_abortable(&bar_rows[(sl)], (rows_phase >> (sl)) & 1u, abort, a.err, 12), rows_phase ^= 1u << (sl), ok)
-      for (long long p0 = w0; p0 < w1 && ok;) {
-        const long long col = p0 / g.nx;
-        const int nq = (int)min((long long)(g.nx - (int)(p0 - col * g.nx)), w1 - p0);
+      for (int p0 = w0; p0 < w1 && ok;) {
+        const int nq = min(g.nx - p0 % g.nx, w1 - p0);
         const int ntile = kPlaneTiles * nq;
         for (int ti = 0; ti < ntile; ++ti, ++tile) {
           const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
@@ -698,9 +804,13 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
     }
   } else {
     // ------------------------------------------------------------------ epilogues
-    const int lrow = 32 * (warp & 3) + lane, lq = warp >> 2;  // TMEM lane, column block
+    // Group h = warp / 8 takes the tiles of parity h (TMEM half h, its own H tile); within
+    // a group, warp w reads TMEM lanes 32 (w % 4) .. + 31 and columns 32 cb .. + 31,
+    // cb = (w % 8) / 4.
+    const int h = warp / kGroupWarps, cb = (warp % kGroupWarps) >> 2;
+    const int lrow = 32 * (warp & 3) + lane;
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-    unsigned char* H = smem + kOffH;
+    unsigned char* H = smem + kOffH + h * kHBytes;
     const float inv_out = 1.0f / a.out_scale;
     uint32_t n_l1 = 0, n_l = 0;
     bool ok = true;
@@ -712,91 +822,80 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
     tc::fence_smem_for_async();                       \
     tc::fence_before_sync();                          \
     __syncwarp();                                     \
-    if (lane == 0) tc::mbar_arrive(&bar_h);           \
+    if (lane == 0) tc::mbar_arrive(&bar_h[h]);        \
   } while (0)
-    for (long long p0 = w0; p0 < w1 && ok;) {
-      const long long col = p0 / g.nx;
-      const int xs = (int)(p0 - col * g.nx);
-      const int nq = (int)min((long long)(g.nx - xs), w1 - p0);
-      const int yb = (int)(col / rg.nzb), zb = (int)(col - (long long)yb * rg.nzb);
-      const int y0 = yb * kLines, z0 = zb * kLineCells;
-      const int ntile = kPlaneTiles * nq;
-      for (int ti = 0; ti < ntile && ok; ++ti) {
-        const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
-        // This thread's output cell (if its row is one) and its occupancy, fetched early.
-        const int pr = kLine + 128 * m + lrow;
-        const int hy = pr / kLine, hz = pr - hy * kLine;
-        const int oy = y0 + hy - 1, oz = z0 + hz - 1;
-        const bool valid = lq < (kApply ? 1 : 2) && hy <= kLines && hz >= 1 && hz <= kLineCells && oy < g.ny &&
-                           oz < g.nz;
-        const long long cc = ((long long)(xs + q) * g.ny + oy) * g.nz + oz;
-        const uint32_t fl = valid ? a.f.flags[cc] : kFlagSolid;
-        // In place: the cell's 19 populations, loaded now so the output epilogue only adds.
-        float fq[kApply ? kOut : 1];
-        uint32_t slq[kApply ? kOut : 1];
-        if (kApply && valid) {
-          const Deltas dc(g, xs + q, oy, oz);
+    Segment s = segment_at(w0, w1, 0, g, rg);
+    for (uint32_t tt = (uint32_t)h; tt < ntiles && ok; tt += 2) {
+      seek(s, tt, w1, g, rg);
+      const int ti = (int)(tt - s.first), q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
+      // This thread's output cell (if its row is one) and its occupancy, fetched early.
+      const int pr = kLine + 128 * m + lrow;
+      const int hy = pr / kLine, hz = pr - hy * kLine;
+      const int oy = s.y0 + hy - 1, oz = s.z0 + hz - 1;
+      const bool valid = (kApply ? cb == 0 : true) && hy <= kLines && hz >= 1 && hz <= kLineCells &&
+                         oy < g.ny && oz < g.nz;
+      const long long cc = ((long long)(s.xs + q) * g.ny + oy) * g.nz + oz;
+      const uint32_t fl = valid ? a.f.flags[cc] : kFlagSolid;
+      // In place: the cell's 19 populations, loaded now so the output epilogue only adds.
+      float fq[kApply ? kOut : 1];
+      if (kApply && valid) {
+        const Deltas dc(g, s.xs + q, oy, oz);
+#pragma unroll
+        for (int qo = 0; qo < kOut; ++qo) fq[qo] = a.pops[slot32((uint32_t)g.n, dc, fl, qo, a.f.parity)];
+      }
+      const uint32_t tb = tmem + ((uint32_t)h << 8) + lane_base;
+      if (!(ok = FSI_WWAIT(&bar_l1[h], n_l1 & 1u, 3))) break;
+      ++n_l1;
+      tc::fence_after_sync();
+      hidden_epilogue(tb, sb, 2 * cb, H, lrow);
+      hidden_epilogue(tb, sb, 2 * cb + 1, H, lrow);
+      FSI_HAND_OVER();
+      if (lane == 0) tc::mbar_arrive(&bar_e1[h]);  // this half's layer-1 accumulator is free
+      if (!(ok = FSI_WWAIT(&bar_l[h], n_l & 1, 4))) break;
+      ++n_l;
+      tc::fence_after_sync();
+      hidden_epilogue(tb + 64, sb + 64, 2 * cb, H, lrow);
+      hidden_epilogue(tb + 64, sb + 64, 2 * cb + 1, H, lrow);
+      FSI_HAND_OVER();
+      if (!(ok = FSI_WWAIT(&bar_l[h], n_l & 1, 5))) break;
+      ++n_l;
+      tc::fence_after_sync();
+      hidden_epilogue(tb + 128, sb + 128, 2 * cb, H, lrow);
+      hidden_epilogue(tb + 128, sb + 128, 2 * cb + 1, H, lrow);
+      FSI_HAND_OVER();
+      if (!(ok = FSI_WWAIT(&bar_l[h], n_l & 1, 6))) break;
+      ++n_l;
+      tc::fence_after_sync();
+      // Outputs: columns 0-31, 19 used. Corrections: 16 per warp (cb); in place: the warps
+      // with cb == 0 take all 32 columns of their rows.
+      if (!kApply) {
+        float y[16];
+        tc::tmem_ld16(tb + 192 + 16 * cb, y);
+        if (valid) {
+          const float keep = (fl & kFlagSolid) ? 0.f : inv_out;
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int qo = 16 * cb + i;
+            if (qo < kOut) a.corr[(size_t)qo * g.n + cc] = (y[i] + sb[192 + qo]) * keep;
+          }
+        }
+      } else if (cb == 0) {
+        float y[32];
+        tc::tmem_ld16(tb + 192, *reinterpret_cast<float(*)[16]>(y));
+        tc::tmem_ld16(tb + 208, *reinterpret_cast<float(*)[16]>(y + 16));
+        if (valid && !(fl & kFlagSolid)) {
+          float cq[kOut], sum = 0.f;
 #pragma unroll
           for (int qo = 0; qo < kOut; ++qo) {
-            slq[qo] = slot32((uint32_t)g.n, dc, fl, qo, a.f.parity);
-            fq[qo] = a.pops[slq[qo]];
+            cq[qo] = (y[qo] + sb[192 + qo]) * inv_out;
+            sum += cq[qo];
           }
-        }
-        const uint32_t h = n_l1 & 1;
-        const uint32_t tb = tmem + (h << 8) + lane_base;
-        if (!(ok = FSI_WWAIT(&bar_l1[h], (n_l1 >> 1) & 1u, 3))) break;
-        ++n_l1;
-        tc::fence_after_sync();
+          const Deltas dc(g, s.xs + q, oy, oz);
 #pragma unroll
-        for (int cg = 0; cg < kColGroups; ++cg) hidden_epilogue(tb, sb, kColGroups * lq + cg, H, lrow);
-        FSI_HAND_OVER();
-        if (lane == 0) tc::mbar_arrive(&bar_e1[h]);  // this half's layer-1 accumulator is free
-        if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 4))) break;
-        ++n_l;
-        tc::fence_after_sync();
-#pragma unroll
-        for (int cg = 0; cg < kColGroups; ++cg) hidden_epilogue(tb + 64, sb + 64, kColGroups * lq + cg, H, lrow);
-        FSI_HAND_OVER();
-        if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 5))) break;
-        ++n_l;
-        tc::fence_after_sync();
-#pragma unroll
-        for (int cg = 0; cg < kColGroups; ++cg) hidden_epilogue(tb + 128, sb + 128, kColGroups * lq + cg, H, lrow);
-        FSI_HAND_OVER();
-        if (!(ok = FSI_WWAIT(&bar_l, n_l & 1, 6))) break;
-        ++n_l;
-        tc::fence_after_sync();
-        // Outputs: warps with lq < 2 hold columns 0-31, of which 19 are used; in place, the
-        // warps with lq == 0 take all 32 columns of their rows.
-        if (!kApply && lq < 2) {
-          float y[16];
-          tc::tmem_ld16(tb + 192 + 16 * lq, y);
-          if (valid) {
-            const float keep = (fl & kFlagSolid) ? 0.f : inv_out;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-              const int qo = 16 * lq + i;
-              if (qo < kOut) a.corr[(size_t)qo * g.n + cc] = (y[i] + sb[192 + qo]) * keep;
-            }
-          }
-        }
-        if (kApply && lq == 0) {
-          float y[32];
-          tc::tmem_ld16(tb + 192, *reinterpret_cast<float(*)[16]>(y));
-          tc::tmem_ld16(tb + 208, *reinterpret_cast<float(*)[16]>(y + 16));
-          if (valid && !(fl & kFlagSolid)) {
-            float cq[kOut], sum = 0.f;
-#pragma unroll
-            for (int qo = 0; qo < kOut; ++qo) {
-              cq[qo] = (y[qo] + sb[192 + qo]) * inv_out;
-              sum += cq[qo];
-            }
-#pragma unroll
-            for (int qo = 0; qo < kOut; ++qo) a.pops[slq[qo]] = fq[qo] + (cq[qo] - weight_of(qo) * sum);
-          }
+          for (int qo = 0; qo < kOut; ++qo)
+            a.pops[slot32((uint32_t)g.n, dc, fl, qo, a.f.parity)] = fq[qo] + (cq[qo] - weight_of(qo) * sum);
         }
       }
-      p0 += nq;
     }
 #undef FSI_WWAIT
 #undef FSI_HAND_OVER
@@ -1017,6 +1116,7 @@ int launch_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags
   a.pops = pops_out;
   a.err = err;
   a.work = (long long)a.rg.nyb * a.rg.nzb * a.f.g.nx;
+  FSI_REQUIRE(a.work < (1ll << 31) / kPlaneTiles, "lattice too large for the closure inference");
   cudaStream_t s = as_stream(stream);
   FSI_REQUIRE(a.rg.ny_pad <= 65535 && a.f.g.nx <= 65535, "lattice too large for the row pass");
   closure_rows_kernel<<<dim3((a.rg.nz_pad + 127) / 128, a.rg.ny_pad, a.f.g.nx), 128, 0, s>>>(
