@@ -400,15 +400,20 @@ int fsi_batch_coupling_assemble(const fsi_batch* batch, const uint32_t* flags, i
  * was trained on, on the tcgen05 tensor cores. No reference counterpart. Lattices must use
  * FP32 population storage. Features of a cell: for each of its 27 neighbours (periodic wrap,
  * offsets (dx, dy, dz) in {-1,0,1}^3 with dz fastest) the 19 populations as
- * (f_q - w_q rho0) * pop_scale, the occupancy (1 solid) and the force * force_scale:
+ * (f_q - w_q rho0) * pop_scale, the occupancy (solid fraction, or 1 solid) and the
+ * force * force_scale:
  * 27 * 23 = 621 values, neighbour o in columns [24 o, 24 o + 23), column 24 o + 23 and columns
  * 648..655 zero: 656 columns. */
 #define FSI_CLOSURE_FEATURES 656
 
-/* Feature rows (BF16 [m][656]) of the cells listed in `cells` (device int32[m]). */
+/* Feature rows (BF16 [m][656]) of the cells listed in `cells` (device int32[m]). The
+ * occupancy feature is solid_fraction[cell] (device float[N], the share of a coarse cell's
+ * fine children that are solid) when given, else 1 for solid and 0 for fluid cells; the
+ * inference entries below take the same argument. */
 int fsi_closure_features(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
-                         const float* force, int64_t steps_done, const int32_t* cells, int32_t m,
-                         float pop_scale, float force_scale, void* x, void* stream);
+                         const float* force, const float* solid_fraction, int64_t steps_done,
+                         const int32_t* cells, int32_t m, float pop_scale, float force_scale,
+                         void* x, void* stream);
 
 /* C = A B^T with BF16 K-major operands A [m][lda], B [n][ldb] (row-major, 16-byte aligned,
  * lda and ldb multiples of 8) on the tensor cores, K split into k_chunk pieces over the grid,
@@ -460,13 +465,14 @@ int64_t fsi_closure_rows_bytes(const fsi_lbm_desc* desc);
  * layers on the tensor cores with the weights resident in shared memory; corrections
  * corr [19][N] (0 on solid cells). Network: BF16 w1 [64][656]. */
 int fsi_closure_infer(const fsi_lbm_desc* desc, const float* pops, const uint32_t* flags,
-                      const float* force, int64_t steps_done, const fsi_closure_weights* weights,
+                      const float* force, const float* solid_fraction, int64_t steps_done,
+                      const fsi_closure_weights* weights,
                       void* rows, float* corr, int32_t* err, void* stream);
 /* fsi_closure_infer followed by fsi_closure_apply in one pass: each fluid cell's
  * mass-conserving correction is added to its populations in place (the arithmetic of
  * fsi_closure_apply), without a correction array. */
 int fsi_closure_infer_apply(const fsi_lbm_desc* desc, float* pops, const uint32_t* flags,
-                            const float* force, int64_t steps_done,
+                            const float* force, const float* solid_fraction, int64_t steps_done,
                             const fsi_closure_weights* weights, void* rows, int32_t* err,
                             void* stream);
 /* f_q += corr_q - w_q sum_p corr_p on fluid cells (moves no mass). */

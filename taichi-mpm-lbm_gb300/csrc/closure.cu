@@ -5,7 +5,9 @@
 //
 // Features of a cell x: for each of the 27 cells y of its 3^3 neighbourhood (periodic wrap,
 // offsets in (dx, dy, dz) order, dz fastest) the 19 post-stream populations as scaled
-// deviations (f_q(y) - w_q rho0) * pop_scale, the occupancy of y (1 solid, 0 fluid) and the
+// deviations (f_q(y) - w_q rho0) * pop_scale, the occupancy of y (its solid fraction when
+// given -- the share of a coarse cell's fine children that are solid --, else 1 solid /
+// 0 fluid) and the
 // 3 force components of y * force_scale: 27 * 23 = 621 values. Column layout: neighbour o's
 // 23 values in columns [24 o, 24 o + 23), column 24 o + 23 zero, columns 648..655 zero
 // (K = 656), so every neighbour group is three aligned 16-byte pieces.
@@ -69,6 +71,7 @@ struct FeatArgs {
   const float* __restrict__ pops;  // FP32 populations [19][N], AA layout of `parity`
   const uint32_t* __restrict__ flags;
   const float* __restrict__ force;  // [3][N]
+  const float* __restrict__ frac;   // [N] solid fraction of each cell, or NULL (occupancy 0/1)
   int parity;
   float rho0, pop_scale, force_scale;
 };
@@ -85,7 +88,7 @@ __device__ __forceinline__ void neighbour_features(const FeatArgs& a, int i, int
     const float f = gather32<FSI_STORAGE_F32>(a.pops, n, d, fl, q, solid ? 0 : a.parity, 0.f);
     v[q] = solid ? 0.f : (f - weight_of(q) * a.rho0) * a.pop_scale;
   }
-  v[19] = solid ? 1.f : 0.f;
+  v[19] = a.frac ? a.frac[d.c] : (solid ? 1.f : 0.f);
 #pragma unroll
   for (int c = 0; c < 3; ++c) v[20 + c] = a.force[c * n + d.c] * a.force_scale;
 }
@@ -408,7 +411,7 @@ __global__ void __launch_bounds__(128) closure_rows_kernel(FeatArgs a, RowGeom r
   float v[24];
 #pragma unroll
   for (int q = 0; q < 19; ++q) v[q] = solid ? 0.f : (f[q] - weight_of(q) * a.rho0) * a.pop_scale;
-  v[19] = solid ? 1.f : 0.f;
+  v[19] = a.frac ? a.frac[d.c] : (solid ? 1.f : 0.f);
 #pragma unroll
   for (int c = 0; c < 3; ++c) v[20 + c] = frc[c] * a.force_scale;
   v[23] = 0.f;
@@ -1008,8 +1011,10 @@ __global__ void __launch_bounds__(kBlock) closure_adam_kernel(float* __restrict_
 }
 
 FeatArgs feat_args(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags,
-                   const float* force, int64_t steps_done, float pop_scale, float force_scale) {
+                   const float* force, const float* frac, int64_t steps_done, float pop_scale,
+                   float force_scale) {
   FeatArgs f;
+  f.frac = frac;
   f.g = geom_of(d);
   f.pops = pops;
   f.flags = flags;
@@ -1035,12 +1040,13 @@ int check_closure_lattice(const fsi_lbm_desc* d) {
 using namespace fsi;
 
 extern "C" int fsi_closure_features(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags,
-                                    const float* force, int64_t steps_done, const int32_t* cells,
+                                    const float* force, const float* solid_fraction, int64_t steps_done,
+                                    const int32_t* cells,
                                     int32_t m, float pop_scale, float force_scale, void* x,
                                     void* stream) {
   if (int e = check_closure_lattice(d)) return e;
   FSI_REQUIRE(pops && flags && force && cells && x && m > 0, "NULL array or empty cell list");
-  const FeatArgs f = feat_args(d, pops, flags, force, steps_done, pop_scale, force_scale);
+  const FeatArgs f = feat_args(d, pops, flags, force, solid_fraction, steps_done, pop_scale, force_scale);
   closure_features_kernel<<<grid_for(28ll * m, 256), 256, 0, as_stream(stream)>>>(
       f, cells, m, reinterpret_cast<__nv_bfloat16*>(x));
   return check_launch("closure_features_kernel");
@@ -1095,7 +1101,7 @@ namespace {
 // The row pass, then the fused inference (corrections to corr, or applied to pops_out).
 template <bool kApply>
 int launch_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags, const float* force,
-                 int64_t steps_done, const fsi_closure_weights* w, void* rows, float* corr, float* pops_out,
+                 const float* frac, int64_t steps_done, const fsi_closure_weights* w, void* rows, float* corr, float* pops_out,
                  int32_t* err, void* stream) {
   if (int e = check_closure_lattice(d)) return e;
   FSI_REQUIRE(pops && flags && force && w && rows && err && (kApply || corr), "NULL array");
@@ -1103,7 +1109,7 @@ int launch_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags
   FSI_REQUIRE(w->w1 && w->w2 && w->w3 && w->w4 && w->bias, "NULL weights");
   FSI_REQUIRE(w->out_scale != 0.f, "out_scale must be non-zero");
   InferArgs a;
-  a.f = feat_args(d, pops, flags, force, steps_done, w->pop_scale, w->force_scale);
+  a.f = feat_args(d, pops, flags, force, frac, steps_done, w->pop_scale, w->force_scale);
   a.rg = row_geom(a.f.g);
   a.grows = reinterpret_cast<const unsigned char*>(rows);
   a.w1 = reinterpret_cast<const __nv_bfloat16*>(w->w1);
@@ -1159,17 +1165,19 @@ int launch_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags
 }  // namespace fsi
 
 extern "C" int fsi_closure_infer(const fsi_lbm_desc* d, const float* pops, const uint32_t* flags,
-                                 const float* force, int64_t steps_done,
+                                 const float* force, const float* solid_fraction, int64_t steps_done,
                                  const fsi_closure_weights* w, void* rows, float* corr, int32_t* err,
                                  void* stream) {
-  return launch_infer<false>(d, pops, flags, force, steps_done, w, rows, corr, nullptr, err, stream);
+  return launch_infer<false>(d, pops, flags, force, solid_fraction, steps_done, w, rows, corr, nullptr, err,
+                             stream);
 }
 
 extern "C" int fsi_closure_infer_apply(const fsi_lbm_desc* d, float* pops, const uint32_t* flags,
-                                       const float* force, int64_t steps_done,
+                                       const float* force, const float* solid_fraction, int64_t steps_done,
                                        const fsi_closure_weights* w, void* rows, int32_t* err,
                                        void* stream) {
-  return launch_infer<true>(d, pops, flags, force, steps_done, w, rows, nullptr, pops, err, stream);
+  return launch_infer<true>(d, pops, flags, force, solid_fraction, steps_done, w, rows, nullptr, pops, err,
+                            stream);
 }
 
 extern "C" int fsi_closure_apply(const fsi_lbm_desc* d, float* pops, const uint32_t* flags,

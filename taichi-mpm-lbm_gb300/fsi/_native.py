@@ -165,13 +165,13 @@ _SIGNATURES = {
     "fsi_batch_lbm_distribution": ([_BATCH, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "fsi_batch_lbm_base_force": ([_BATCH, _VP, _VP, _VP], ctypes.c_int),
     "fsi_batch_tune": ([_BATCH, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
-    "fsi_closure_features": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64, _VP,
+    "fsi_closure_features": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, ctypes.c_int64, _VP,
                               ctypes.c_int32, ctypes.c_float, ctypes.c_float, _VP, _VP], ctypes.c_int),
     "fsi_closure_gemm": ([ctypes.POINTER(ClosureGemmDesc), _VP], ctypes.c_int),
     "fsi_closure_rows_bytes": ([ctypes.POINTER(LbmDesc)], ctypes.c_int64),
-    "fsi_closure_infer_apply": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64,
+    "fsi_closure_infer_apply": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, ctypes.c_int64,
                                  ctypes.POINTER(ClosureWeights), _VP, _VP, _VP], ctypes.c_int),
-    "fsi_closure_infer": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64,
+    "fsi_closure_infer": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, ctypes.c_int64,
                            ctypes.POINTER(ClosureWeights), _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_closure_apply": ([ctypes.POINTER(LbmDesc), _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "fsi_closure_restrict": ([ctypes.POINTER(LbmDesc), _VP, _VP, ctypes.c_int64,

@@ -61,6 +61,16 @@ def coarse_mask(fine_mask: np.ndarray) -> np.ndarray:
     return (c >= 4).astype(np.int32)
 
 
+def solid_fraction(fine_mask: np.ndarray, device=None) -> torch.Tensor:
+    """Share of each coarse cell's 8 fine children that are solid (float32 [Nc], device): the
+    occupancy feature of the network, which keeps the sub-cell geometry the coarse mask
+    loses."""
+    m = np.asarray(fine_mask) > 0
+    nx, ny, nz = m.shape
+    f = m.reshape(nx // 2, 2, ny // 2, 2, nz // 2, 2).mean(axis=(1, 3, 5)).astype(np.float32)
+    return torch.from_numpy(f.reshape(-1)).to(device if device is not None else nat.device())
+
+
 def restrict(fine: LBMSolver3D, coarse: LBMSolver3D) -> torch.Tensor:
     """Mean post-stream populations of the fluid children, [Nc, 19] (device)."""
     out = torch.empty((coarse.n_cells, OUT), dtype=torch.float32, device=fine._device)
@@ -96,8 +106,11 @@ def _gemm(a, b, lda, ldb, m, n, k, mode, err, c=None, ldc=0, bias=None, h=None, 
 class ClosureMLP:
     """Parameters (FP32 master, BF16 copies), Adam state and the tensor-core passes."""
 
-    def __init__(self, seed: int = 0, device=None):
+    def __init__(self, seed: int = 0, device=None, use_fraction: bool = True):
         self.device = device or nat.device()
+        # Occupancy feature: the solid fraction of each coarse cell (from the fine mask) when
+        # True, else the coarse cell's 0/1 flag.
+        self.use_fraction = use_fraction
         nat.load()
         g = torch.Generator().manual_seed(seed)
         sizes = [(HIDDEN, FEATURES), (HIDDEN,), (HIDDEN, HIDDEN), (HIDDEN,), (HIDDEN, HIDDEN),
@@ -217,22 +230,30 @@ class ClosureMLP:
 
     def state_dict(self) -> dict:
         return {"params": self.params.cpu(), "scales": (self.pop_scale, self.force_scale,
-                                                        self.out_scale)}
+                                                        self.out_scale),
+                "use_fraction": self.use_fraction}
 
     def load_state_dict(self, state: dict) -> None:
         self.params.copy_(state["params"])
         self.pop_scale, self.force_scale, self.out_scale = state["scales"]
+        self.use_fraction = bool(state.get("use_fraction", False))
         self.refresh()
 
 
 # ------------------------------------------------------------------ data
-def features(lbm: LBMSolver3D, cells: torch.Tensor, pop_scale: float, force_scale: float):
-    """BF16 feature rows [m][656] of the given cells (int32 device tensor) of `lbm`."""
+def _ptr_or_null(t: torch.Tensor | None):
+    return None if t is None else nat.ptr(t)
+
+
+def features(lbm: LBMSolver3D, cells: torch.Tensor, pop_scale: float, force_scale: float,
+             frac: torch.Tensor | None = None):
+    """BF16 feature rows [m][656] of the given cells (int32 device tensor) of `lbm`; the
+    occupancy feature is ``frac`` (solid fraction per cell) when given, else 0/1."""
     m = int(cells.numel())
     x = torch.empty((m, FEATURES), dtype=torch.bfloat16, device=lbm._device)
     nat.call("fsi_closure_features", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags),
-             nat.ptr(lbm.force), lbm.steps_done, nat.ptr(cells), m, pop_scale, force_scale,
-             nat.ptr(x), nat.stream_ptr())
+             nat.ptr(lbm.force), _ptr_or_null(frac), lbm.steps_done, nat.ptr(cells), m, pop_scale,
+             force_scale, nat.ptr(x), nat.stream_ptr())
     return x
 
 
@@ -277,12 +298,13 @@ class ClosureTrainer:
 
     def add_run(self, fine_cfg: LBMConfig, fine_mask: np.ndarray, warmup: int = 40,
                 snapshots: int = 10, every: int = 4) -> None:
+        frac = solid_fraction(fine_mask, self.net.device) if self.net.use_fraction else None
         for coarse, cells, target in training_pairs(fine_cfg, fine_mask, warmup, snapshots, every):
-            self._pending.append((coarse.state_dict(), coarse.config, cells, target.clone()))
+            self._pending.append((coarse.state_dict(), coarse.config, cells, target.clone(), frac))
 
     def _fit_scales(self) -> None:
         devs, forces, targets = [], [], []
-        for state, cfg, cells, target in self._pending:
+        for state, cfg, cells, target, _ in self._pending:
             f = state["pops"]
             w = torch.tensor([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, device=f.device).view(OUT, 1)
             devs.append((f - w * cfg.rho0)[:, cells.long()].flatten())
@@ -295,10 +317,10 @@ class ClosureTrainer:
     def build(self) -> int:
         """Feature rows of every collected pair with the fitted scales; returns the row count."""
         self._fit_scales()
-        for state, cfg, cells, target in self._pending:
+        for state, cfg, cells, target, frac in self._pending:
             lbm = LBMSolver3D(cfg)
             lbm.load_state_dict(state)
-            self.rows_x.append(features(lbm, cells, self.net.pop_scale, self.net.force_scale))
+            self.rows_x.append(features(lbm, cells, self.net.pop_scale, self.net.force_scale, frac))
             self.rows_t.append((target * self.net.out_scale).float())
         self._pending.clear()
         self.x = torch.cat(self.rows_x)
@@ -335,20 +357,20 @@ def rows_buffer(lbm: LBMSolver3D) -> torch.Tensor:
 
 
 def infer(lbm: LBMSolver3D, weights: nat.ClosureWeights, corr: torch.Tensor, rows: torch.Tensor,
-          err: torch.Tensor) -> None:
+          err: torch.Tensor, frac: torch.Tensor | None = None) -> None:
     """Corrections corr [19][N] of every cell of ``lbm`` by the fused tensor-core inference."""
     nat.call("fsi_closure_infer", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags), nat.ptr(lbm.force),
-             lbm.steps_done, ctypes.byref(weights), nat.ptr(rows), nat.ptr(corr), nat.ptr(err),
-             nat.stream_ptr())
+             _ptr_or_null(frac), lbm.steps_done, ctypes.byref(weights), nat.ptr(rows), nat.ptr(corr),
+             nat.ptr(err), nat.stream_ptr())
 
 
 def infer_apply(lbm: LBMSolver3D, weights: nat.ClosureWeights, rows: torch.Tensor,
-                err: torch.Tensor) -> None:
+                err: torch.Tensor, frac: torch.Tensor | None = None) -> None:
     """The fused inference with each cell's mass-conserving correction added to its populations
     in place (``infer`` then ``fsi_closure_apply``, in one pass)."""
     nat.call("fsi_closure_infer_apply", lbm._desc, nat.ptr(lbm._pops), nat.ptr(lbm.flags),
-             nat.ptr(lbm.force), lbm.steps_done, ctypes.byref(weights), nat.ptr(rows), nat.ptr(err),
-             nat.stream_ptr())
+             nat.ptr(lbm.force), _ptr_or_null(frac), lbm.steps_done, ctypes.byref(weights), nat.ptr(rows),
+             nat.ptr(err), nat.stream_ptr())
     lbm._mass_speed_cache = None
 
 
@@ -371,6 +393,7 @@ class ClosureSimulation:
         self.coarse_steps = 0
         self._weights = net.weights_struct()
         self._rows = rows_buffer(self.coarse)
+        self._frac = solid_fraction(fine_mask, self.coarse._device) if net.use_fraction else None
 
     @property
     def on_fine_grid(self) -> bool:
@@ -401,7 +424,7 @@ class ClosureSimulation:
             return
         c = self.coarse
         c.step()
-        infer_apply(c, self._weights, self._rows, self.net.err)
+        infer_apply(c, self._weights, self._rows, self.net.err, self._frac)
         self.coarse_steps += 1
         if self.check_every and self.coarse_steps % self.check_every == 0:
             reason = self._guard()

@@ -76,7 +76,7 @@ def small_lattice(seed=0, steps=5):
     return lbm, mask
 
 
-def numpy_features(lbm, mask, cells, pop_scale, force_scale):
+def numpy_features(lbm, mask, cells, pop_scale, force_scale, frac=None):
     f = lbm.distribution_numpy()
     g = lbm.force_numpy()
     w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
@@ -92,7 +92,7 @@ def numpy_features(lbm, mask, cells, pop_scale, force_scale):
                     solid = mask[a, b, e] > 0
                     pops = np.zeros(19) if solid else (f[a, b, e] - w * np.float32(lbm.config.rho0)) * pop_scale
                     out[r, col:col + 19] = pops
-                    out[r, col + 19] = 1.0 if solid else 0.0
+                    out[r, col + 19] = (frac[a, b, e] if frac is not None else (1.0 if solid else 0.0))
                     out[r, col + 20:col + 23] = g[a, b, e] * force_scale
                     col += 24
     return out
@@ -104,6 +104,32 @@ def test_features_match_numpy():
     x = cl.features(lbm, torch.from_numpy(cells.astype(np.int32)).cuda(), 30.0, 1e3)
     want = numpy_features(lbm, mask, cells, 30.0, 1e3)
     np.testing.assert_allclose(host(x), O.bf16(want.astype(np.float32)), rtol=0, atol=1e-6)
+
+
+def test_solid_fraction_feature_and_inference():
+    """With a per-cell solid fraction the occupancy feature is that fraction, in the training
+    features and in the fused inference alike."""
+    lbm, mask = small_lattice()
+    rng = np.random.default_rng(7)
+    frac_np = np.where(mask > 0, rng.uniform(0.5, 1.0, mask.shape), rng.uniform(0.0, 0.49, mask.shape))
+    frac_np = frac_np.astype(np.float32)
+    frac = torch.from_numpy(frac_np.reshape(-1)).cuda()
+    cells = np.array([0, 17, 123, 300, 555, 719])
+    x = cl.features(lbm, torch.from_numpy(cells.astype(np.int32)).cuda(), 30.0, 1e3, frac)
+    want = numpy_features(lbm, mask, cells, 30.0, 1e3, frac_np)
+    np.testing.assert_allclose(host(x), O.bf16(want.astype(np.float32)), rtol=0, atol=1e-6)
+    net = cl.ClosureMLP(seed=3)
+    net.pop_scale, net.force_scale, net.out_scale = 30.0, 1e3, 250.0
+    corr = torch.zeros((19, lbm.n_cells), dtype=torch.float32, device="cuda")
+    cl.infer(lbm, net.weights_struct(), corr, cl.rows_buffer(lbm), net.err, frac)
+    net.check()
+    fluid = np.nonzero(mask.reshape(-1) == 0)[0]
+    xf = cl.features(lbm, torch.from_numpy(fluid.astype(np.int32)).cuda(), net.pop_scale, net.force_scale, frac)
+    pad = (-len(fluid)) % 128
+    xp = torch.cat([xf, torch.zeros((pad, 656), dtype=xf.dtype, device="cuda")])
+    y = net.predict(xp)[:len(fluid)] / net.out_scale
+    got = corr[:, torch.from_numpy(fluid).cuda()].t()
+    assert rel_l2(got.cpu().numpy(), y.cpu().numpy()) < 2e-3
 
 
 def test_fused_inference_matches_unfused_passes():
