@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(kBlock)
   a.flags = base.flags + L.off;
   a.accum = base.accum + L.off;
   a.cnt = base.cnt + t.lattice;
-  coupling_forces_body(a, t.first * kBlock + threadIdx.x);
+  coupling_forces_body<false>(a, t.first * kBlock + threadIdx.x);
 }
 
 __global__ void __launch_bounds__(kTileCells)

@@ -19,8 +19,11 @@
 namespace fsi {
 namespace {
 
+constexpr int kGatherAheadMax = 2 * 152 * kBlock;
+
+template <bool kGatherAhead>
 __global__ void __launch_bounds__(kBlock) coupling_forces_kernel(ForceArgs a) {
-  coupling_forces_body(a, blockIdx.x * kBlock + threadIdx.x);
+  coupling_forces_body<kGatherAhead>(a, blockIdx.x * kBlock + threadIdx.x);
 }
 
 __global__ void __launch_bounds__(kBlock) assemble_kernel(AssembleArgs a) {
@@ -133,7 +136,12 @@ extern "C" int fsi_coupling_forces(const fsi_coupling_desc* c, const fsi_mpm_des
   a.valid_out = valid_weight;
   a.mask_out = coupling_mask;
   a.cnt = reinterpret_cast<Cnt*>(counters);
-  coupling_forces_kernel<<<grid_for(a.n, kBlock), kBlock, 0, as_stream(stream)>>>(a);
+  // Few particles (under two CTAs per SM): latency-bound, so the stencil loads go out
+  // together; otherwise the lower register count keeps more warps resident.
+  if (a.n < kGatherAheadMax)
+    coupling_forces_kernel<true><<<grid_for(a.n, kBlock), kBlock, 0, as_stream(stream)>>>(a);
+  else
+    coupling_forces_kernel<false><<<grid_for(a.n, kBlock), kBlock, 0, as_stream(stream)>>>(a);
   return check_launch("coupling_forces_kernel");
 }
 

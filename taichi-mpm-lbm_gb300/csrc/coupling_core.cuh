@@ -56,7 +56,11 @@ struct ForceArgs {
 };
 
 // _compute_coupling_forces_kernel, fsi/coupling.py:332-406, for particle p (this thread);
-// every lane of the warp calls it (warp-aggregated counters).
+// every lane of the warp calls it (warp-aggregated counters). kGatherAhead issues the
+// stencil's loads up front (fewer dependent round trips, more registers: for launches with
+// few particles, where latency and not occupancy bounds the kernel); both orders sum the
+// same values in the same order.
+template <bool kGatherAhead>
 __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) {
   const bool live = p < a.n;
   const long long cap = a.cap;
@@ -76,20 +80,59 @@ __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) 
         for (int i = 0; i < 3; ++i) wv[ax][i] = bspline_w(fx[ax], i);
       float valid = 0.f, uf[3] = {0.f, 0.f, 0.f};
       uint32_t usable = 0;  // bit s: node s of the stencil is in-grid and fluid
+      if (!kGatherAhead) {
 #pragma unroll
-      for (int s = 0; s < 27; ++s) {
-        const int i = s / 9, j = (s / 3) % 3, k = s % 3;
-        const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
-        if (ni < 0 || ni >= a.g.nx || nj < 0 || nj >= a.g.ny || nk < 0 || nk >= a.g.nz) continue;
-        const long long c = ((long long)ni * a.g.ny + nj) * a.g.nz + nk;
-        if (a.flags[c] & kFlagSolid) continue;
-        usable |= 1u << s;
-        const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
-        valid = __fadd_rn(valid, w);
-        const float4 mc = a.macro[c];
-        uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc.x));
-        uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc.y));
-        uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc.z));
+        for (int s = 0; s < 27; ++s) {
+          const int i = s / 9, j = (s / 3) % 3, k = s % 3;
+          const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+          if (ni < 0 || ni >= a.g.nx || nj < 0 || nj >= a.g.ny || nk < 0 || nk >= a.g.nz) continue;
+          const long long c = ((long long)ni * a.g.ny + nj) * a.g.nz + nk;
+          if (a.flags[c] & kFlagSolid) continue;
+          usable |= 1u << s;
+          const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
+          valid = __fadd_rn(valid, w);
+          const float4 mc = a.macro[c];
+          uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc.x));
+          uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc.y));
+          uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc.z));
+        }
+      } else {
+        // All loads go out before the first is needed: the 27 flags together, then the lattice
+        // velocities of the usable nodes in three batches of 9; the sums still run in stencil
+        // order (s = 0..26), so the result is that of the node-by-node loop.
+        uint32_t inside = 0;  // bit s: node s of the stencil lies in the lattice
+        uint32_t fl[27];
+#pragma unroll
+        for (int s = 0; s < 27; ++s) {
+          const int i = s / 9, j = (s / 3) % 3, k = s % 3;
+          const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+          const bool in = ni >= 0 && ni < a.g.nx && nj >= 0 && nj < a.g.ny && nk >= 0 && nk < a.g.nz;
+          inside |= (uint32_t)in << s;
+          fl[s] = in ? a.flags[((long long)ni * a.g.ny + nj) * a.g.nz + nk] : kFlagSolid;
+        }
+#pragma unroll
+        for (int s = 0; s < 27; ++s)
+          if (((inside >> s) & 1u) && !(fl[s] & kFlagSolid)) usable |= 1u << s;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          float4 mc[9];
+#pragma unroll
+          for (int t = 0; t < 9; ++t) {
+            const int s = 9 * b + t, j = t / 3, k = t % 3;
+            if ((usable >> s) & 1u)
+              mc[t] = a.macro[((long long)(base[0] + b) * a.g.ny + (base[1] + j)) * a.g.nz + (base[2] + k)];
+          }
+#pragma unroll
+          for (int t = 0; t < 9; ++t) {
+            const int s = 9 * b + t, j = t / 3, k = t % 3;
+            if (!((usable >> s) & 1u)) continue;
+            const float w = __fmul_rn(__fmul_rn(wv[0][b], wv[1][j]), wv[2][k]);
+            valid = __fadd_rn(valid, w);
+            uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc[t].x));
+            uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc[t].y));
+            uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc[t].z));
+          }
+        }
       }
       a.valid_out[p] = valid;
       if (valid > a.c.min_valid_weight) {
