@@ -151,6 +151,39 @@ def test_fused_inference_matches_unfused_passes():
     assert float(corr[:, torch.from_numpy(solid).cuda()].abs().max()) == 0.0
 
 
+@pytest.mark.parametrize("steps", [6, 7])
+def test_fused_inference_on_a_lattice_of_many_columns(steps):
+    """40x30x70: several inference columns in y and z, partial last blocks on both axes, many
+    segments per CTA; every fluid cell's correction against the unfused feature rows + GEMMs,
+    on both AA parities; solid cells get no correction."""
+    nx, ny, nz = 40, 30, 70
+    cfg = LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=0.04, force=(5e-5, 1e-5, -2e-5), **PERIODIC)
+    mask = channel_mask(nx, ny, nz)
+    rng = np.random.default_rng(11)
+    for _ in range(12):
+        c = rng.integers([2, 3, 3], [nx - 2, ny - 3, nz - 3])
+        mask[c[0] - 1:c[0] + 2, c[1] - 1:c[1] + 2, c[2] - 2:c[2] + 1] = 1
+    lbm = LBMSolver3D(cfg)
+    lbm.initialize(mask)
+    for _ in range(steps):
+        lbm.step()
+    net = cl.ClosureMLP(seed=9)
+    net.pop_scale, net.force_scale, net.out_scale = 30.0, 1e3, 250.0
+    frac = torch.from_numpy(np.where(mask > 0, 0.75, 0.125).astype(np.float32).reshape(-1)).cuda()
+    corr = torch.full((19, lbm.n_cells), 7.0, dtype=torch.float32, device="cuda")
+    cl.infer(lbm, net.weights_struct(), corr, cl.rows_buffer(lbm), net.err, frac)
+    net.check()
+    fluid = np.nonzero(mask.reshape(-1) == 0)[0]
+    x = cl.features(lbm, torch.from_numpy(fluid.astype(np.int32)).cuda(), net.pop_scale, net.force_scale, frac)
+    pad = (-len(fluid)) % 128
+    xp = torch.cat([x, torch.zeros((pad, 656), dtype=x.dtype, device="cuda")])
+    y = net.predict(xp)[:len(fluid)] / net.out_scale
+    got = corr[:, torch.from_numpy(fluid).cuda()].t()
+    assert rel_l2(got.cpu().numpy(), y.cpu().numpy()) < 2e-3
+    solid = np.nonzero(mask.reshape(-1))[0]
+    assert float(corr[:, torch.from_numpy(solid).cuda()].abs().max()) == 0.0
+
+
 def test_in_place_inference_equals_inference_then_apply():
     """fsi_closure_infer_apply gives bit for bit the populations of fsi_closure_infer followed
     by fsi_closure_apply (both parities of the AA layout)."""
