@@ -16,7 +16,7 @@ HEADER = ROOT / "include" / "fsi_gb300.h"
 def declared_functions() -> list[str]:
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|size_t)\s+(fsi_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|size_t)\s+(fsi_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_header_declares_entry_points():
@@ -55,3 +55,22 @@ def test_struct_sizes_match_header_layout():
     assert ctypes.sizeof(_native.MpmDesc) == 4 * 20
     assert ctypes.sizeof(_native.Particles) == 8 * 11
     assert ctypes.sizeof(_native.CouplingDesc) == 4 * 18
+
+
+def test_closure_row_buffer_size():
+    """fsi_closure_rows_bytes (host only): 3 chunks x 16 bytes per row of the lattice padded to
+    whole inference columns (11 lines in y, 32 cells in z) plus one periodic image per side;
+    -1 for lattices the closure rejects."""
+    lib = _native.load()
+    for nx, ny, nz in [(12, 10, 10), (192, 96, 96), (40, 30, 70), (5, 11, 32)]:
+        d = _native.LbmDesc()
+        d.nx, d.ny, d.nz = nx, ny, nz
+        d.storage = _native.STORAGE_F32
+        ny_pad = 11 * -(-ny // 11) + 2
+        nz_pad = 32 * -(-nz // 32) + 2
+        assert lib.fsi_closure_rows_bytes(ctypes.byref(d)) == 3 * nx * ny_pad * nz_pad * 16
+    d = _native.LbmDesc()
+    d.nx, d.ny, d.nz = 4, 10, 10  # too small
+    assert lib.fsi_closure_rows_bytes(ctypes.byref(d)) == -1
+    d.nx, d.ny, d.nz, d.storage = 12, 10, 10, _native.STORAGE_F16  # FP32 populations only
+    assert lib.fsi_closure_rows_bytes(ctypes.byref(d)) == -1
