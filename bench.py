@@ -340,7 +340,8 @@ def time_closure(args, world, stream) -> dict:
     trainer = cl.ClosureTrainer(net)
     for seed in range(100, 116):
         cfg, mask = channel(seed)
-        trainer.add_run(cfg, mask, warmup=30, snapshots=16, every=4)
+        # snapshots over the whole 120-fine-step window the evaluation covers, from rest
+        trainer.add_run(cfg, mask, warmup=0, snapshots=40, every=3)
     rows = trainer.build()
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
