@@ -329,8 +329,10 @@ class ClosureTrainer:
         self.rows_t.clear()
         return int(self.x.shape[0])
 
-    def fit(self, steps: int = 500, batch: int = 16384, lr: float = 2e-3, seed: int = 0) -> list[float]:
-        """Adam on random mini-batches (multiples of 128 rows); returns the loss history."""
+    def fit(self, steps: int = 500, batch: int = 16384, lr: float = 2e-3, seed: int = 0,
+            halvings: float = 3.0) -> list[float]:
+        """Adam on random mini-batches (multiples of 128 rows), the learning rate halving
+        ``halvings`` times over the run; returns the loss history."""
         g = torch.Generator(device="cpu").manual_seed(seed)
         n = self.x.shape[0]
         batch = max(128, min(batch, n) // 128 * 128)
@@ -342,7 +344,7 @@ class ClosureTrainer:
             t = self.t[idx].contiguous()
             y, acts = self.net.forward(x, keep=True)
             hist.append(self.net.backward(x, y, acts, t, xt=xt))
-            self.net.adam_step(lr=lr * (0.5 ** (it / max(steps, 1) * 3)))
+            self.net.adam_step(lr=lr * (0.5 ** (it / max(steps, 1) * halvings)))
         self.net.check()
         return hist
 
