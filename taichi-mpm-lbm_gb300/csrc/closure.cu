@@ -291,11 +291,10 @@ __global__ void __launch_bounds__(128) gemm_kernel(GemmArgs g) {
 // halo (and past line 11) are computed and discarded.
 //
 // Each CTA (one per SM) takes a contiguous range of (column, x) plane steps. Warps 0-15 run
-// the epilogues, as two groups of 8 on alternate tiles (warp w reads TMEM lanes
-// 32 (w % 4) .. + 31); one thread of warp 16 issues layers 2-4 of each tile as its layer-1,
-// -2 and -3 epilogues finish; one thread of warp 17 issues the plane copies and layer 1
-// (42 MMAs) of the tiles ahead, as soon as the tensor-memory half a tile needs is free and
-// its planes are loaded; it refills a slot once its own last MMA reading the slot is done.
+// the epilogues (warp w reads TMEM lanes 32 (w % 4) .. + 31 and columns 16 (w / 4) .. + 15);
+// one thread of warp 16 issues the plane copies and layers 2-4 of each tile as its layer-1,
+// -2 and -3 epilogues finish; one thread of warp 17 issues layer 1 (42 MMAs) of the tiles
+// ahead, as soon as the tensor-memory half and the planes a tile needs are free and loaded.
 // Two tiles are in flight (TMEM halves 0 and 256): the tensor cores run layer 1 of tile
 // t + 1 while the epilogues of tile t run on the CUDA cores, and the small layers of tile t
 // never queue behind a thread that is blocked issuing layer 1. Every hand-over is an
@@ -591,11 +590,16 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
 // waits for (0-2), phases of its hand-over barrier waited and commits to its layer barrier.
 struct Group {
   uint32_t tile, stage = 0, n_h = 0, c_l = 0;
+  Segment seg;
 };
 
 struct ChainCtx {
+  const CUtensorMap* map;
+  uint32_t s_rows;
+  uint64_t* bar_rows;
   uint32_t tmem;
   uint64_t w2, w3, w4;
+  int w1;
   uint32_t ntiles;
 };
 
@@ -612,18 +616,33 @@ __device__ __forceinline__ void fill_segment_start(const CUtensorMap* map, uint3
   }
 }
 
-// If group H has handed over its next epilogue, issues the layer that follows it; returns
-// whether it did.
+// If group H has handed over its next epilogue, issues the layer that follows it (and, after
+// a layer-1 epilogue, the plane copies that tile frees); returns whether it did.
 template <int H>
-__device__ __forceinline__ bool serve(Group& gr, uint64_t& bar_h, uint64_t& bar_l, uint64_t dh, const ChainCtx& cx) {
+__device__ __forceinline__ bool serve(Group& gr, uint64_t& bar_h, uint64_t& bar_l, uint64_t dh, const ChainCtx& cx,
+                                      uint32_t& fills, const LbmGeom& g, const RowGeom& rg) {
   if (gr.tile >= cx.ntiles || !mbar_test(&bar_h, gr.n_h & 1)) return false;
   ++gr.n_h;
   tc::fence_after_sync();
   const uint32_t tb = cx.tmem + ((uint32_t)H << 8);
-  if (gr.stage == 0) {  // layer-1 epilogue done: layer 2
+  if (gr.stage == 0) {  // layer-1 epilogue done: layer 2, plane copies
     issue_layer(tb + 64, dh, cx.w2, kIdesc64);
     tc::mma_commit(&bar_l);
     ++gr.c_l;
+    seek(gr.seg, gr.tile, cx.w1, g, rg);
+    const Segment& s = gr.seg;
+    const int ti = (int)(gr.tile - s.first), q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
+    // Layer 1 of this tile is complete, so is every earlier one: plane step q - 1's oldest
+    // plane gives its slot to plane xs + q + 2; after a segment's last tile, the next
+    // segment's first planes go in.
+    if (m == 0 && q >= 1 && q + 1 < s.nq) {
+      const int sl = (q + 3) & 3;
+      fill_plane(cx.map, cx.s_rows, &cx.bar_rows[sl], sl, wrap(s.xs + q + 2, g.nx), s.y0, s.z0);
+      fills ^= 1u << sl;
+    }
+    if ((uint32_t)ti + 1 == s.ntile && s.p0 + s.nq < cx.w1)
+      fill_segment_start(cx.map, cx.s_rows, cx.bar_rows, fills, segment_at(s.p0 + s.nq, cx.w1, s.first + s.ntile, g, rg),
+                         g.nx);
     gr.stage = 1;
   } else if (gr.stage == 1) {
     issue_layer(tb + 128, dh, cx.w3, kIdesc64);
@@ -698,23 +717,31 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
 
   const uint32_t sRows = tc::smem_addr(smem + kOffRows);
   if (warp == kChainWarp) {
-    // ------------------------------------------------------------ layers 2-4
+    // ------------------------------------------------ plane copies, layers 2-4
     if (lane == 0) {
       const uint64_t dH0 = tc::tile_desc(tc::smem_addr(smem + kOffH), 64, 0);
       const uint64_t dH1 = tc::tile_desc(tc::smem_addr(smem + kOffH + kHBytes), 64, 0);
       const uint64_t dW2 = tc::tile_desc(tc::smem_addr(smem + kOffW2), 64, 0);
       const uint64_t dW3 = tc::tile_desc(tc::smem_addr(smem + kOffW3), 64, 0);
       const uint64_t dW4 = tc::tile_desc(tc::smem_addr(smem + kOffW4), 64, 0);
+      uint32_t fills = 0;  // parity of the copies issued per slot
       bool ok = true;
       Group gr0, gr1;
       gr0.tile = 0;
       gr1.tile = 1;
-      const ChainCtx cx{tmem, dW2, dW3, dW4, ntiles};
+      if (ntiles > 0) {
+        // The first segment's planes: ordinal u is plane xs - 1 + u, in slot u & 3.
+        const Segment s0 = segment_at(w0, w1, 0, g, rg);
+        fill_segment_start(&rows_map, sRows, bar_rows, fills, s0, g.nx);
+        gr0.seg = s0;
+        gr1.seg = s0;
+      }
+      const ChainCtx cx{&rows_map, sRows, bar_rows, tmem, dW2, dW3, dW4, w1, ntiles};
       long long t_idle = clock64();
       // Serve the two epilogue groups in the order their hand-overs arrive.
       while (gr0.tile < ntiles || gr1.tile < ntiles) {
-        const bool p0 = serve<0>(gr0, bar_h[0], bar_l[0], dH0, cx);
-        const bool p1 = serve<1>(gr1, bar_h[1], bar_l[1], dH1, cx);
+        const bool p0 = serve<0>(gr0, bar_h[0], bar_l[0], dH0, cx, fills, g, rg);
+        const bool p1 = serve<1>(gr1, bar_h[1], bar_l[1], dH1, cx, fills, g, rg);
         if (p0 || p1) {
           t_idle = clock64();
         } else if (*abort) {
@@ -730,29 +757,23 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
         }
       }
       if (!ok) {
-        // Let the MMAs this thread issued finish before the CTA exits (bounded).
+        // Let the copies and MMAs this thread issued finish before the CTA exits (bounded).
+        for (int sl = 0; sl < kSlots; ++sl) tc::mbar_wait(&bar_rows[sl], ((fills >> sl) & 1u) ^ 1u, nullptr, 0);
         if (gr0.c_l > 0) tc::mbar_wait(&bar_l[0], (gr0.c_l - 1) & 1, nullptr, 0);
         if (gr1.c_l > 0) tc::mbar_wait(&bar_l[1], (gr1.c_l - 1) & 1, nullptr, 0);
       }
     }
   } else if (warp == kL1Warp) {
-    // ------------------------------------------------------ plane copies, layer 1
+    // ------------------------------------------------------------------ layer 1
     if (lane == 0) {
       const uint64_t dRows = tc::smem_desc(sRows, 0u, 128u);
       const uint64_t dW1 = tc::smem_desc(tc::smem_addr(smem + kOffW1), 128u, 256u);
-      uint32_t tile = 0, rows_phase = 0, fills = 0, issued = 0;  // fills: parity of copies issued per slot
+      uint32_t tile = 0, rows_phase = 0, issued = 0;
       bool ok = true;
 #define FSI_WAIT_ROWS(sl) (ok = tc::mbar_wait_abortable(&bar_rows[(sl)], (rows_phase >> (sl)) & 1u, abort, a.err, 12), rows_phase ^= 1u << (sl), ok)
-// Waits (bounded) for this thread's layer 1 of tile pt to complete, with every earlier MMA.
-#define FSI_WAIT_L1(pt) (ok = tc::mbar_wait_abortable(&bar_l1[(pt) & 1], ((pt) >> 1) & 1u, abort, a.err, 13))
       for (int p0 = w0; p0 < w1 && ok;) {
-        const Segment sg = segment_at(p0, w1, tile, g, rg);
-        const int nq = sg.nq;
+        const int nq = min(g.nx - p0 % g.nx, w1 - p0);
         const int ntile = kPlaneTiles * nq;
-        // The previous segment's layer 1 (the last commit; tiles go in order) has read its
-        // planes: this segment's first planes go in (ordinal u is plane xs - 1 + u, slot u & 3).
-        if (tile > 0 && !FSI_WAIT_L1(tile - 1)) break;
-        fill_segment_start(&rows_map, sRows, bar_rows, fills, sg, g.nx);
         for (int ti = 0; ti < ntile; ++ti, ++tile) {
           const int q = ti / kPlaneTiles, m = ti - q * kPlaneTiles;
           const uint32_t h = tile & 1;
@@ -774,28 +795,15 @@ __global__ void __launch_bounds__(kInferThreads, 1) closure_infer_kernel(InferAr
           issue_l1_chunk<2>(d, dRows, r0, r1, r2, dW1);
           tc::mma_commit(&bar_l1[h]);
           ++issued;
-          // Layer 1 of plane step q - 1 (its last tile, the commit before this one) has read
-          // the oldest plane: its slot takes plane xs + q + 2, two tiles before it is needed.
-          if (m == 0 && q >= 1 && q + 1 < nq) {
-            if (!FSI_WAIT_L1(tile - 1)) break;
-            const int sl = (q + 3) & 3;
-            fill_plane(&rows_map, sRows, &bar_rows[sl], sl, wrap(sg.xs + q + 2, g.nx), sg.y0, sg.z0);
-            fills ^= 1u << sl;
-          }
         }
         p0 += nq;
       }
-      if (!ok) {
-        // Let the copies and MMAs this thread issued finish before the CTA exits (bounded).
-        for (int sl = 0; sl < kSlots; ++sl)
-          if (((fills ^ rows_phase) >> sl) & 1u) tc::mbar_wait(&bar_rows[sl], (rows_phase >> sl) & 1u, nullptr, 0);
-        if (issued > 0) {
-          const uint32_t lt = issued - 1;  // tiles are issued in order
-          tc::mbar_wait(&bar_l1[lt & 1], (lt >> 1) & 1u, nullptr, 0);
-        }
+      if (!ok && issued > 0) {
+        // Let the last layer 1 issued (tile issued - 1; tiles go in order) finish (bounded).
+        const uint32_t lt = issued - 1;
+        tc::mbar_wait(&bar_l1[lt & 1], (lt >> 1) & 1u, nullptr, 0);
       }
 #undef FSI_WAIT_ROWS
-#undef FSI_WAIT_L1
     }
   } else {
     // ------------------------------------------------------------------ epilogues
