@@ -73,6 +73,31 @@ M = mrt_matrix()
 INV = np.linalg.inv(M).astype(np.float32)
 
 
+def forward_plan():
+    """Rows of M as signed terms [(q, coefficient)] in q order (zeros dropped), and for each
+    row b the earlier row a whose first L >= 2 terms are exactly the negatives of b's first L
+    terms: {b: (a, L)}, longest L kept. Round-to-nearest is symmetric, so the partial sum of
+    b after L terms is minus that of a (up to the sign of an exact zero) and b's chain can
+    continue from it: (-p) + X = X - p exactly."""
+    rows = [[(q, int(M[k, q])) for q in range(Q) if M[k, q] != 0] for k in range(Q)]
+    reuse = {}
+    for b in range(Q):
+        best = None
+        for a in range(b):
+            n = 0
+            while (n < min(len(rows[a]), len(rows[b])) and rows[a][n][0] == rows[b][n][0]
+                   and rows[a][n][1] == -rows[b][n][1]):
+                n += 1
+            if n >= 2 and (best is None or n > best[1]):
+                best = (a, n)
+        if best is not None:
+            reuse[b] = best
+    for b, (a, n) in reuse.items():
+        # the prefix of a must be one that a's own chain computes
+        assert a not in reuse or reuse[a][1] <= n
+    return rows, reuse
+
+
 def inverse_plan():
     """Per column k: list of (class_id, base_magnitude); per entry (q,k): (sign, class, shift)."""
     classes = []        # (k, base) per product register
@@ -144,14 +169,29 @@ def gen() -> str:
     need_two = sorted({q for k in range(Q) for q in range(Q) if abs(M[k, q]) == 2})
     for q in need_two:
         w(f"  two[{q}] = vadd(X[{q}], X[{q}]);")
+    rows, reuse = forward_plan()
+    keep = {}  # row a -> prefix lengths that later rows continue from
+    for a, n in reuse.values():
+        keep.setdefault(a, set()).add(n)
     for k in range(Q):
-        terms = []
-        for q in range(Q):
-            c = int(M[k, q])
-            if c == 0:
-                continue
-            terms.append((1 if c > 0 else -1, f"X[{q}]" if abs(c) == 1 else f"two[{q}]"))
-        body = chain(f"m[{k}]", terms)
+        terms = [(1 if c > 0 else -1, f"X[{q}]" if abs(c) == 1 else f"two[{q}]")
+                 for q, c in rows[k]]
+        var = f"m[{k}]"
+        if k in reuse:
+            a, n = reuse[k]
+            pre = f"pre{a}_{n}"
+            if len(terms) == n:
+                body = [f"{var} = vneg({pre});"]
+            else:
+                s, e = terms[n]
+                body = [f"{var} = vsub({e}, {pre});" if s > 0
+                        else f"{var} = vneg(vadd({pre}, {e}));"]
+                for s, e in terms[n + 1:]:
+                    body.append(f"{var} = {'vadd' if s > 0 else 'vsub'}({var}, {e});")
+        else:
+            body = chain(var, terms)
+            for n in sorted(keep.get(k, ()), reverse=True):
+                body.insert(n, f"const V pre{k}_{n} = {var};")
         w("  " + " ".join(body))
     w("}")
     w("")
@@ -318,13 +358,46 @@ def _plan_inverse(m: np.ndarray) -> np.ndarray:
     return out
 
 
+def _plan_forward(x: np.ndarray) -> np.ndarray:
+    """The generated forward transform in numpy: zero terms dropped, 2 X as X + X, rows in
+    ``forward_plan()``'s reuse list continued from the negated prefix of an earlier row."""
+    rows, reuse = forward_plan()
+    out = np.zeros_like(x)
+    prefix = {}
+    for k in range(Q):
+        terms = [(1 if c > 0 else -1, x[:, q] if abs(c) == 1 else (x[:, q] + x[:, q]))
+                 for q, c in rows[k]]
+        if k in reuse:
+            a, used = reuse[k]
+            acc = -prefix[(a, used)]
+        else:
+            s0, t0 = terms[0]
+            acc, used = (t0 if s0 > 0 else -t0), 1
+        for s, t in terms[used:]:
+            acc = (acc + t if s > 0 else acc - t).astype(np.float32)
+            used += 1
+            prefix[(k, used)] = acc
+        out[:, k] = acc
+    return out
+
+
 def self_check(n: int = 200_000, seed: int = 0) -> None:
-    """Planned inverse == literal dense inverse, bit for bit, on near-equilibrium moments."""
+    """Planned forward and inverse == literal dense products, bit for bit, on near-equilibrium
+    populations and moments; the forward also on Guo-like source terms with signed zeros,
+    where only the sign of an exact zero may differ (it is then added to a relaxed moment
+    that is non-zero or +0, which such a zero cannot change)."""
     rng = np.random.default_rng(seed)
     w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
     rho = rng.uniform(0.8, 1.2, n).astype(np.float32)
     F = (w[None, :] * rho[:, None] * (1 + rng.normal(0, 0.05, (n, Q)))).astype(np.float32)
     mom = _seq_dense(M, F)
+    bad = np.count_nonzero(mom.view(np.uint32) != _plan_forward(F).view(np.uint32))
+    if bad:
+        raise AssertionError(f"planned forward differs from the literal sum in {bad} entries")
+    t = (rng.normal(0, 1e-6, (n, Q)) * (rng.uniform(size=(n, Q)) < 0.7)).astype(np.float32)
+    t[rng.uniform(size=(n, Q)) < 0.2] *= np.float32(-1.0)  # +-0 entries
+    if not np.array_equal(_seq_dense(M, t), _plan_forward(t)):
+        raise AssertionError("planned forward differs from the literal sum on source terms")
     mom[:, 3:8] += rng.normal(0, 1e-4, (n, 5)).astype(np.float32)
     full = _seq_dense(INV, mom)
     planned = _plan_inverse(mom)

@@ -30,15 +30,15 @@ __device__ __forceinline__ void mrt_forward(const V (&X)[19], V (&m)[19]) {
   m[6] = vneg(two[3]); m[6] = vadd(m[6], two[4]); m[6] = vadd(m[6], X[7]); m[6] = vsub(m[6], X[8]); m[6] = vsub(m[6], X[9]); m[6] = vadd(m[6], X[10]); m[6] = vadd(m[6], X[15]); m[6] = vsub(m[6], X[16]); m[6] = vadd(m[6], X[17]); m[6] = vsub(m[6], X[18]);
   m[7] = X[5]; m[7] = vsub(m[7], X[6]); m[7] = vadd(m[7], X[11]); m[7] = vsub(m[7], X[12]); m[7] = vsub(m[7], X[13]); m[7] = vadd(m[7], X[14]); m[7] = vadd(m[7], X[15]); m[7] = vsub(m[7], X[16]); m[7] = vsub(m[7], X[17]); m[7] = vadd(m[7], X[18]);
   m[8] = vneg(two[5]); m[8] = vadd(m[8], two[6]); m[8] = vadd(m[8], X[11]); m[8] = vsub(m[8], X[12]); m[8] = vsub(m[8], X[13]); m[8] = vadd(m[8], X[14]); m[8] = vadd(m[8], X[15]); m[8] = vsub(m[8], X[16]); m[8] = vsub(m[8], X[17]); m[8] = vadd(m[8], X[18]);
-  m[9] = two[1]; m[9] = vadd(m[9], two[2]); m[9] = vsub(m[9], X[3]); m[9] = vsub(m[9], X[4]); m[9] = vsub(m[9], X[5]); m[9] = vsub(m[9], X[6]); m[9] = vadd(m[9], X[7]); m[9] = vadd(m[9], X[8]); m[9] = vadd(m[9], X[9]); m[9] = vadd(m[9], X[10]); m[9] = vadd(m[9], X[11]); m[9] = vadd(m[9], X[12]); m[9] = vadd(m[9], X[13]); m[9] = vadd(m[9], X[14]); m[9] = vsub(m[9], two[15]); m[9] = vsub(m[9], two[16]); m[9] = vsub(m[9], two[17]); m[9] = vsub(m[9], two[18]);
-  m[10] = vneg(two[1]); m[10] = vsub(m[10], two[2]); m[10] = vadd(m[10], X[3]); m[10] = vadd(m[10], X[4]); m[10] = vadd(m[10], X[5]); m[10] = vadd(m[10], X[6]); m[10] = vadd(m[10], X[7]); m[10] = vadd(m[10], X[8]); m[10] = vadd(m[10], X[9]); m[10] = vadd(m[10], X[10]); m[10] = vadd(m[10], X[11]); m[10] = vadd(m[10], X[12]); m[10] = vadd(m[10], X[13]); m[10] = vadd(m[10], X[14]); m[10] = vsub(m[10], two[15]); m[10] = vsub(m[10], two[16]); m[10] = vsub(m[10], two[17]); m[10] = vsub(m[10], two[18]);
-  m[11] = X[3]; m[11] = vadd(m[11], X[4]); m[11] = vsub(m[11], X[5]); m[11] = vsub(m[11], X[6]); m[11] = vadd(m[11], X[7]); m[11] = vadd(m[11], X[8]); m[11] = vadd(m[11], X[9]); m[11] = vadd(m[11], X[10]); m[11] = vsub(m[11], X[11]); m[11] = vsub(m[11], X[12]); m[11] = vsub(m[11], X[13]); m[11] = vsub(m[11], X[14]);
-  m[12] = vneg(X[3]); m[12] = vsub(m[12], X[4]); m[12] = vadd(m[12], X[5]); m[12] = vadd(m[12], X[6]); m[12] = vadd(m[12], X[7]); m[12] = vadd(m[12], X[8]); m[12] = vadd(m[12], X[9]); m[12] = vadd(m[12], X[10]); m[12] = vsub(m[12], X[11]); m[12] = vsub(m[12], X[12]); m[12] = vsub(m[12], X[13]); m[12] = vsub(m[12], X[14]);
+  m[9] = two[1]; m[9] = vadd(m[9], two[2]); m[9] = vsub(m[9], X[3]); m[9] = vsub(m[9], X[4]); m[9] = vsub(m[9], X[5]); m[9] = vsub(m[9], X[6]); const V pre9_6 = m[9]; m[9] = vadd(m[9], X[7]); m[9] = vadd(m[9], X[8]); m[9] = vadd(m[9], X[9]); m[9] = vadd(m[9], X[10]); m[9] = vadd(m[9], X[11]); m[9] = vadd(m[9], X[12]); m[9] = vadd(m[9], X[13]); m[9] = vadd(m[9], X[14]); m[9] = vsub(m[9], two[15]); m[9] = vsub(m[9], two[16]); m[9] = vsub(m[9], two[17]); m[9] = vsub(m[9], two[18]);
+  m[10] = vsub(X[7], pre9_6); m[10] = vadd(m[10], X[8]); m[10] = vadd(m[10], X[9]); m[10] = vadd(m[10], X[10]); m[10] = vadd(m[10], X[11]); m[10] = vadd(m[10], X[12]); m[10] = vadd(m[10], X[13]); m[10] = vadd(m[10], X[14]); m[10] = vsub(m[10], two[15]); m[10] = vsub(m[10], two[16]); m[10] = vsub(m[10], two[17]); m[10] = vsub(m[10], two[18]);
+  m[11] = X[3]; m[11] = vadd(m[11], X[4]); m[11] = vsub(m[11], X[5]); m[11] = vsub(m[11], X[6]); const V pre11_4 = m[11]; m[11] = vadd(m[11], X[7]); m[11] = vadd(m[11], X[8]); m[11] = vadd(m[11], X[9]); m[11] = vadd(m[11], X[10]); m[11] = vsub(m[11], X[11]); m[11] = vsub(m[11], X[12]); m[11] = vsub(m[11], X[13]); m[11] = vsub(m[11], X[14]);
+  m[12] = vsub(X[7], pre11_4); m[12] = vadd(m[12], X[8]); m[12] = vadd(m[12], X[9]); m[12] = vadd(m[12], X[10]); m[12] = vsub(m[12], X[11]); m[12] = vsub(m[12], X[12]); m[12] = vsub(m[12], X[13]); m[12] = vsub(m[12], X[14]);
   m[13] = X[7]; m[13] = vadd(m[13], X[8]); m[13] = vsub(m[13], X[9]); m[13] = vsub(m[13], X[10]);
   m[14] = X[15]; m[14] = vadd(m[14], X[16]); m[14] = vsub(m[14], X[17]); m[14] = vsub(m[14], X[18]);
   m[15] = X[11]; m[15] = vadd(m[15], X[12]); m[15] = vsub(m[15], X[13]); m[15] = vsub(m[15], X[14]);
-  m[16] = X[7]; m[16] = vsub(m[16], X[8]); m[16] = vadd(m[16], X[9]); m[16] = vsub(m[16], X[10]); m[16] = vsub(m[16], X[11]); m[16] = vadd(m[16], X[12]); m[16] = vsub(m[16], X[13]); m[16] = vadd(m[16], X[14]);
-  m[17] = vneg(X[7]); m[17] = vadd(m[17], X[8]); m[17] = vadd(m[17], X[9]); m[17] = vsub(m[17], X[10]); m[17] = vadd(m[17], X[15]); m[17] = vsub(m[17], X[16]); m[17] = vadd(m[17], X[17]); m[17] = vsub(m[17], X[18]);
+  m[16] = X[7]; m[16] = vsub(m[16], X[8]); const V pre16_2 = m[16]; m[16] = vadd(m[16], X[9]); m[16] = vsub(m[16], X[10]); m[16] = vsub(m[16], X[11]); m[16] = vadd(m[16], X[12]); m[16] = vsub(m[16], X[13]); m[16] = vadd(m[16], X[14]);
+  m[17] = vsub(X[9], pre16_2); m[17] = vsub(m[17], X[10]); m[17] = vadd(m[17], X[15]); m[17] = vsub(m[17], X[16]); m[17] = vadd(m[17], X[17]); m[17] = vsub(m[17], X[18]);
   m[18] = X[11]; m[18] = vsub(m[18], X[12]); m[18] = vsub(m[18], X[13]); m[18] = vadd(m[18], X[14]); m[18] = vsub(m[18], X[15]); m[18] = vadd(m[18], X[16]); m[18] = vadd(m[18], X[17]); m[18] = vsub(m[18], X[18]);
 }
 
