@@ -310,6 +310,7 @@ extern "C" int fsi_batch_create(const fsi_batch_lattice* lattices, int32_t count
     L.off = off;
     for (int q = 0; q < 19; ++q) {
       L.s[q] = in.s[q];
+      L.sg[q] = 1.0f - 0.5f * in.s[q];
       L.shift[q] = storage == FSI_STORAGE_F32 ? 0.f : weight_of(q) * in.rho0;
     }
     L.rho0 = in.rho0;

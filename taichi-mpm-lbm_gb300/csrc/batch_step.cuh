@@ -15,6 +15,7 @@ struct LatticeView {
   const float* __restrict__ force_prev;
   const uint32_t* __restrict__ flags;
   const float* s;
+  const float* sg;
   const float* shift;
   int write_faces;
 };
@@ -32,6 +33,7 @@ __device__ __forceinline__ LatticeView view_of(const BatchLattice& L, void* pops
   v.force_prev = force_prev ? force_prev + 3 * L.off : nullptr;
   v.flags = flags + L.off;
   v.s = L.s;
+  v.sg = L.sg;
   v.shift = L.shift;
   v.write_faces = 0;
   return v;

@@ -19,6 +19,7 @@ struct BatchLattice {
   LbmGeom g;
   long long off;  // first cell in the concatenated arrays
   float s[19];
+  float sg[19];  // 1 - s_k / 2
   float shift[19];
   float rho0;
   float base[3];

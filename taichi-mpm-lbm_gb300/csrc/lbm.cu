@@ -380,7 +380,10 @@ extern "C" int fsi_lbm_step(const fsi_lbm_desc* d, void* pops, float* macro, con
   a.force = force;
   a.force_prev = force_prev;
   a.flags = flags;
-  for (int k = 0; k < 19; ++k) a.s[k] = d->s[k];
+  for (int k = 0; k < 19; ++k) {
+    a.s[k] = d->s[k];
+    a.sg[k] = 1.0f - 0.5f * d->s[k];
+  }
   fill_shift(d, a.shift);
   a.write_faces = (d->bc_mode_left != 0 || d->bc_mode_right != 0) ? 1 : 0;
   cudaStream_t s = as_stream(stream);

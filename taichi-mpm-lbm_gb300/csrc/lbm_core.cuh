@@ -208,24 +208,30 @@ __device__ __forceinline__ V edot(int q, V vx, V vy, V vz) {
 }
 
 // MRT collision with Guo forcing of one fluid cell (or two, V = float2) in the reference's
-// order (lbm3d.py:276-333).
+// order (lbm3d.py:276-333). SG[k] is the forcing weight 1 - 0.5 S[k] of the reference,
+// evaluated once per launch: 0.5 S[k] is an exact scaling, so 1 - 0.5 S[k] has a single
+// rounding wherever it is computed.
 template <class V>
 __device__ __forceinline__ void collide_cell(const V (&F)[19], V ux, V uy, V uz, V gx, V gy, V gz,
-                                             const float* __restrict__ S, V (&out)[19]) {
+                                             const float* __restrict__ S,
+                                             const float* __restrict__ SG, V (&out)[19]) {
   // Guo source terms t_q = w_q ((e_q - u).G + (e_q.u)(e_q.G)) (lbm3d.py:276-283).
   // (e - u_c) G_c takes three values per axis, for e = -1, 0, +1.
   const V dx[3] = {vmul(vsub(-1.0f, ux), gx), vmul(vneg(ux), gx), vmul(vsub(1.0f, ux), gx)};
   const V dy[3] = {vmul(vsub(-1.0f, uy), gy), vmul(vneg(uy), gy), vmul(vsub(1.0f, uy), gy)};
   const V dz[3] = {vmul(vsub(-1.0f, uz), gz), vmul(vneg(uz), gz), vmul(vsub(1.0f, uz), gz)};
-  V t[19];
+  // (e.u)(e.G) of q and of opp(q) are the same rounded product: both dot products change
+  // sign together and (-x)(-y) = xy. They can differ only in the sign of an exact zero,
+  // which the forcing moments g = M t then carry only into sums that are non-zero or +0.
+  V t[19], b[19];
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
     const V a = vadd(vadd(dx[ex(q) + 1], dy[ey(q) + 1]), dz[ez(q) + 1]);
     if (q == 0) {
       t[q] = vmul(weight_of(q), a);
     } else {
-      const V b = vmul(edot(q, ux, uy, uz), edot(q, gx, gy, gz));
-      t[q] = vmul(weight_of(q), vadd(a, b));
+      b[q] = (q & 1) ? vmul(edot(q, ux, uy, uz), edot(q, gx, gy, gz)) : b[q - 1];
+      t[q] = vmul(weight_of(q), vadd(a, b[q]));
     }
   }
   V g[19], m[19];
@@ -251,7 +257,7 @@ __device__ __forceinline__ void collide_cell(const V (&F)[19], V ux, V uy, V uz,
       const bool has_eq = (k == 1 || k == 9 || k == 11 || k == 13 || k == 14 || k == 15);
       const V d = has_eq ? vsub(m[k], meq[k]) : m[k];
       m[k] = vsub(m[k], vmul(S[k], d));
-      m[k] = vadd(m[k], vmul(__fsub_rn(1.0f, __fmul_rn(0.5f, S[k])), g[k]));
+      m[k] = vadd(m[k], vmul(SG[k], g[k]));  // SG[k] = 1 - S[k]/2, rounded once
     }
   }
   mrt_inverse(m, out);
@@ -265,6 +271,7 @@ struct StepArgs {
   const float* __restrict__ force_prev;
   const uint32_t* __restrict__ flags;
   float s[19];
+  float sg[19];     // 1 - s_k / 2, the weight of the forcing moment g_k (host-rounded once)
   float shift[19];  // w_q rho0, the storage offset of the deviation forms
   int write_faces;
 };
@@ -404,7 +411,7 @@ __device__ __forceinline__ void step_cells(const Args& a,
 
   V out[19];
   if (kFast) mrt_collide_fast(F, rho, ux, uy, uz, gx, gy, gz, a.s, out);
-  else collide_cell(F, ux, uy, uz, gx, gy, gz, a.s, out);
+  else collide_cell(F, ux, uy, uz, gx, gy, gz, a.s, a.sg, out);
 
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
