@@ -205,6 +205,10 @@ def gen() -> str:
         nm = f"p{k}_{ci}"
         names[(k, ci)] = nm
         w(f"  const V {nm} = vmul(m[{k}], {f32hex(b)});")
+    # Each scaled product once; rows that begin with the same terms (same products, signs and
+    # order) continue from one named partial sum, which is the same value in both rows.
+    rows = []
+    scaled = {}
     for q in range(Q):
         terms = []
         for k in range(Q):
@@ -212,9 +216,46 @@ def gen() -> str:
                 continue
             sign, cls, j = entry[(q, k)]
             base = names[cls]
-            expr = base if j == 0 else f"vmul({base}, {f32hex(2.0 ** j)})"
+            if j == 0:
+                expr = base
+            else:
+                if (base, j) not in scaled:
+                    scaled[(base, j)] = f"{base}_s{len(scaled)}"
+                    w(f"  const V {scaled[(base, j)]} = vmul({base}, {f32hex(2.0 ** j)});")
+                expr = scaled[(base, j)]
             terms.append((sign, expr))
-        w("  { V a; " + " ".join(chain("a", terms)) + f" f[{q}] = a; }}")
+        rows.append(terms)
+    shared = {}  # prefix (tuple of terms, length >= 2) -> name, for prefixes a later row reuses
+    for b in range(Q):
+        for a in range(b):
+            n = 0
+            while n < min(len(rows[a]), len(rows[b])) and rows[a][n] == rows[b][n]:
+                n += 1
+            if n >= 2:
+                shared.setdefault(tuple(rows[b][:n]), None)
+    defined = set()
+    for q, terms in enumerate(rows):
+        var = f"f[{q}]"
+        start = 0
+        for n in range(len(terms), 1, -1):
+            if tuple(terms[:n]) in defined:
+                start = n
+                break
+        if start:
+            body = [f"{var} = {shared[tuple(terms[:start])]};"]
+        else:
+            s0, e0 = terms[0]
+            body = [f"{var} = {e0 if s0 > 0 else 'vneg(' + e0 + ')'};"]
+            start = 1
+        for i in range(start, len(terms)):
+            s, e = terms[i]
+            body.append(f"{var} = {'vadd' if s > 0 else 'vsub'}({var}, {e});")
+            key = tuple(terms[:i + 1])
+            if key in shared and key not in defined:
+                shared[key] = f"r{len(defined)}"
+                defined.add(key)
+                body.append(f"const V {shared[key]} = {var};")
+        w("  " + " ".join(body))
     w("}")
     w("")
     out.extend(gen_fast().splitlines())

@@ -68,25 +68,39 @@ __device__ __forceinline__ void mrt_inverse(const V (&m)[19], V (&f)[19]) {
   const V p16_0 = vmul(m[16], 0x1.0000000000000p-3f);
   const V p17_0 = vmul(m[17], 0x1.0000000000000p-3f);
   const V p18_0 = vmul(m[18], 0x1.0000000000000p-3f);
-  { V a; a = p0_0; a = vsub(a, p1_0); a = vadd(a, p2_0); f[0] = a; }
-  { V a; a = p0_1; a = vsub(a, p2_1); a = vadd(a, p3_0); a = vsub(a, p4_0); a = vadd(a, p9_0); a = vsub(a, p10_0); f[1] = a; }
-  { V a; a = p0_1; a = vsub(a, p2_1); a = vsub(a, p3_0); a = vadd(a, p4_0); a = vadd(a, p9_0); a = vsub(a, p10_0); f[2] = a; }
-  { V a; a = p0_1; a = vsub(a, p2_1); a = vadd(a, p5_0); a = vsub(a, p6_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p11_0); a = vsub(a, p12_0); f[3] = a; }
-  { V a; a = p0_1; a = vsub(a, p2_1); a = vsub(a, p5_0); a = vadd(a, p6_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p11_0); a = vsub(a, p12_0); f[4] = a; }
-  { V a; a = p0_1; a = vsub(a, p2_1); a = vadd(a, p7_0); a = vsub(a, p8_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p11_0); a = vadd(a, p12_0); f[5] = a; }
-  { V a; a = p0_1; a = vsub(a, p2_1); a = vsub(a, p7_0); a = vadd(a, p8_0); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p11_0); a = vadd(a, p12_0); f[6] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p13_0); a = vadd(a, p16_0); a = vsub(a, p17_0); f[7] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p13_0); a = vsub(a, p16_0); a = vadd(a, p17_0); f[8] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p13_0); a = vadd(a, p16_0); a = vadd(a, p17_0); f[9] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p13_0); a = vsub(a, p16_0); a = vsub(a, p17_0); f[10] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p15_0); a = vsub(a, p16_0); a = vadd(a, p18_0); f[11] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vadd(a, p15_0); a = vadd(a, p16_0); a = vsub(a, p18_0); f[12] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p15_0); a = vsub(a, p16_0); a = vsub(a, p18_0); f[13] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p3_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p4_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p9_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p10_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p11_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p12_0, 0x1.0000000000000p-1f)); a = vsub(a, p15_0); a = vadd(a, p16_0); a = vadd(a, p18_0); f[14] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p14_0); a = vadd(a, p17_0); a = vsub(a, p18_0); f[15] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vadd(a, p14_0); a = vsub(a, p17_0); a = vadd(a, p18_0); f[16] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p14_0); a = vadd(a, p17_0); a = vadd(a, p18_0); f[17] = a; }
-  { V a; a = vmul(p0_1, 0x1.0000000000000p-1f); a = vadd(a, p1_1); a = vadd(a, vmul(p2_1, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p5_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p6_0, 0x1.0000000000000p-2f)); a = vadd(a, vmul(p7_0, 0x1.0000000000000p-1f)); a = vadd(a, vmul(p8_0, 0x1.0000000000000p-2f)); a = vsub(a, vmul(p9_0, 0x1.0000000000000p-1f)); a = vsub(a, vmul(p10_0, 0x1.0000000000000p-1f)); a = vsub(a, p14_0); a = vsub(a, p17_0); a = vsub(a, p18_0); f[18] = a; }
+  const V p9_0_s0 = vmul(p9_0, 0x1.0000000000000p-1f);
+  const V p10_0_s1 = vmul(p10_0, 0x1.0000000000000p-1f);
+  const V p0_1_s2 = vmul(p0_1, 0x1.0000000000000p-1f);
+  const V p2_1_s3 = vmul(p2_1, 0x1.0000000000000p-2f);
+  const V p3_0_s4 = vmul(p3_0, 0x1.0000000000000p-1f);
+  const V p4_0_s5 = vmul(p4_0, 0x1.0000000000000p-2f);
+  const V p5_0_s6 = vmul(p5_0, 0x1.0000000000000p-1f);
+  const V p6_0_s7 = vmul(p6_0, 0x1.0000000000000p-2f);
+  const V p9_0_s8 = vmul(p9_0, 0x1.0000000000000p-2f);
+  const V p10_0_s9 = vmul(p10_0, 0x1.0000000000000p-2f);
+  const V p11_0_s10 = vmul(p11_0, 0x1.0000000000000p-1f);
+  const V p12_0_s11 = vmul(p12_0, 0x1.0000000000000p-1f);
+  const V p7_0_s12 = vmul(p7_0, 0x1.0000000000000p-1f);
+  const V p8_0_s13 = vmul(p8_0, 0x1.0000000000000p-2f);
+  f[0] = p0_0; f[0] = vsub(f[0], p1_0); f[0] = vadd(f[0], p2_0);
+  f[1] = p0_1; f[1] = vsub(f[1], p2_1); const V r0 = f[1]; f[1] = vadd(f[1], p3_0); f[1] = vsub(f[1], p4_0); f[1] = vadd(f[1], p9_0); f[1] = vsub(f[1], p10_0);
+  f[2] = r0; f[2] = vsub(f[2], p3_0); f[2] = vadd(f[2], p4_0); f[2] = vadd(f[2], p9_0); f[2] = vsub(f[2], p10_0);
+  f[3] = r0; f[3] = vadd(f[3], p5_0); f[3] = vsub(f[3], p6_0); f[3] = vsub(f[3], p9_0_s0); f[3] = vadd(f[3], p10_0_s1); f[3] = vadd(f[3], p11_0); f[3] = vsub(f[3], p12_0);
+  f[4] = r0; f[4] = vsub(f[4], p5_0); f[4] = vadd(f[4], p6_0); f[4] = vsub(f[4], p9_0_s0); f[4] = vadd(f[4], p10_0_s1); f[4] = vadd(f[4], p11_0); f[4] = vsub(f[4], p12_0);
+  f[5] = r0; f[5] = vadd(f[5], p7_0); f[5] = vsub(f[5], p8_0); f[5] = vsub(f[5], p9_0_s0); f[5] = vadd(f[5], p10_0_s1); f[5] = vsub(f[5], p11_0); f[5] = vadd(f[5], p12_0);
+  f[6] = r0; f[6] = vsub(f[6], p7_0); f[6] = vadd(f[6], p8_0); f[6] = vsub(f[6], p9_0_s0); f[6] = vadd(f[6], p10_0_s1); f[6] = vsub(f[6], p11_0); f[6] = vadd(f[6], p12_0);
+  f[7] = p0_1_s2; f[7] = vadd(f[7], p1_1); f[7] = vadd(f[7], p2_1_s3); const V r1 = f[7]; f[7] = vadd(f[7], p3_0_s4); f[7] = vadd(f[7], p4_0_s5); const V r2 = f[7]; f[7] = vadd(f[7], p5_0_s6); f[7] = vadd(f[7], p6_0_s7); f[7] = vadd(f[7], p9_0_s8); f[7] = vadd(f[7], p10_0_s9); f[7] = vadd(f[7], p11_0_s10); f[7] = vadd(f[7], p12_0_s11); f[7] = vadd(f[7], p13_0); f[7] = vadd(f[7], p16_0); f[7] = vsub(f[7], p17_0);
+  f[8] = r1; f[8] = vsub(f[8], p3_0_s4); f[8] = vsub(f[8], p4_0_s5); const V r3 = f[8]; f[8] = vsub(f[8], p5_0_s6); f[8] = vsub(f[8], p6_0_s7); f[8] = vadd(f[8], p9_0_s8); f[8] = vadd(f[8], p10_0_s9); f[8] = vadd(f[8], p11_0_s10); f[8] = vadd(f[8], p12_0_s11); f[8] = vadd(f[8], p13_0); f[8] = vsub(f[8], p16_0); f[8] = vadd(f[8], p17_0);
+  f[9] = r2; f[9] = vsub(f[9], p5_0_s6); f[9] = vsub(f[9], p6_0_s7); f[9] = vadd(f[9], p9_0_s8); f[9] = vadd(f[9], p10_0_s9); f[9] = vadd(f[9], p11_0_s10); f[9] = vadd(f[9], p12_0_s11); f[9] = vsub(f[9], p13_0); f[9] = vadd(f[9], p16_0); f[9] = vadd(f[9], p17_0);
+  f[10] = r3; f[10] = vadd(f[10], p5_0_s6); f[10] = vadd(f[10], p6_0_s7); f[10] = vadd(f[10], p9_0_s8); f[10] = vadd(f[10], p10_0_s9); f[10] = vadd(f[10], p11_0_s10); f[10] = vadd(f[10], p12_0_s11); f[10] = vsub(f[10], p13_0); f[10] = vsub(f[10], p16_0); f[10] = vsub(f[10], p17_0);
+  f[11] = r2; f[11] = vadd(f[11], p7_0_s12); f[11] = vadd(f[11], p8_0_s13); f[11] = vadd(f[11], p9_0_s8); f[11] = vadd(f[11], p10_0_s9); f[11] = vsub(f[11], p11_0_s10); f[11] = vsub(f[11], p12_0_s11); f[11] = vadd(f[11], p15_0); f[11] = vsub(f[11], p16_0); f[11] = vadd(f[11], p18_0);
+  f[12] = r3; f[12] = vsub(f[12], p7_0_s12); f[12] = vsub(f[12], p8_0_s13); f[12] = vadd(f[12], p9_0_s8); f[12] = vadd(f[12], p10_0_s9); f[12] = vsub(f[12], p11_0_s10); f[12] = vsub(f[12], p12_0_s11); f[12] = vadd(f[12], p15_0); f[12] = vadd(f[12], p16_0); f[12] = vsub(f[12], p18_0);
+  f[13] = r2; f[13] = vsub(f[13], p7_0_s12); f[13] = vsub(f[13], p8_0_s13); f[13] = vadd(f[13], p9_0_s8); f[13] = vadd(f[13], p10_0_s9); f[13] = vsub(f[13], p11_0_s10); f[13] = vsub(f[13], p12_0_s11); f[13] = vsub(f[13], p15_0); f[13] = vsub(f[13], p16_0); f[13] = vsub(f[13], p18_0);
+  f[14] = r3; f[14] = vadd(f[14], p7_0_s12); f[14] = vadd(f[14], p8_0_s13); f[14] = vadd(f[14], p9_0_s8); f[14] = vadd(f[14], p10_0_s9); f[14] = vsub(f[14], p11_0_s10); f[14] = vsub(f[14], p12_0_s11); f[14] = vsub(f[14], p15_0); f[14] = vadd(f[14], p16_0); f[14] = vadd(f[14], p18_0);
+  f[15] = r1; f[15] = vadd(f[15], p5_0_s6); f[15] = vadd(f[15], p6_0_s7); const V r4 = f[15]; f[15] = vadd(f[15], p7_0_s12); f[15] = vadd(f[15], p8_0_s13); f[15] = vsub(f[15], p9_0_s0); f[15] = vsub(f[15], p10_0_s1); f[15] = vadd(f[15], p14_0); f[15] = vadd(f[15], p17_0); f[15] = vsub(f[15], p18_0);
+  f[16] = r1; f[16] = vsub(f[16], p5_0_s6); f[16] = vsub(f[16], p6_0_s7); const V r5 = f[16]; f[16] = vsub(f[16], p7_0_s12); f[16] = vsub(f[16], p8_0_s13); f[16] = vsub(f[16], p9_0_s0); f[16] = vsub(f[16], p10_0_s1); f[16] = vadd(f[16], p14_0); f[16] = vsub(f[16], p17_0); f[16] = vadd(f[16], p18_0);
+  f[17] = r4; f[17] = vsub(f[17], p7_0_s12); f[17] = vsub(f[17], p8_0_s13); f[17] = vsub(f[17], p9_0_s0); f[17] = vsub(f[17], p10_0_s1); f[17] = vsub(f[17], p14_0); f[17] = vadd(f[17], p17_0); f[17] = vadd(f[17], p18_0);
+  f[18] = r5; f[18] = vadd(f[18], p7_0_s12); f[18] = vadd(f[18], p8_0_s13); f[18] = vsub(f[18], p9_0_s0); f[18] = vsub(f[18], p10_0_s1); f[18] = vsub(f[18], p14_0); f[18] = vsub(f[18], p17_0); f[18] = vsub(f[18], p18_0);
 }
 
 
