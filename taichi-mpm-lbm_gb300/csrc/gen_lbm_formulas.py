@@ -427,6 +427,14 @@ def self_check(n: int = 200_000, seed: int = 0) -> None:
     populations and moments; the forward also on Guo-like source terms with signed zeros,
     where only the sign of an exact zero may differ (it is then added to a relaxed moment
     that is non-zero or +0, which such a zero cannot change)."""
+    # Rows 0, 3, 5, 7 of the forward transform are update_macro's sums of f, e_x f, e_y f and
+    # e_z f term for term (the step kernel reads rho and j from them).
+    rows, reuse = forward_plan()
+    for k, axis in ((0, None), (3, 0), (5, 1), (7, 2)):
+        want = ([(q, 1) for q in range(Q)] if axis is None
+                else [(q, E[q][axis]) for q in range(Q) if E[q][axis] != 0])
+        if rows[k] != want or k in reuse:
+            raise AssertionError(f"forward row {k} is not the macro sum it stands for")
     rng = np.random.default_rng(seed)
     w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
     rho = rng.uniform(0.8, 1.2, n).astype(np.float32)

@@ -167,6 +167,20 @@ __device__ __forceinline__ void macro_of(const V (&F)[19], V gx, V gy, V gz, V& 
   rho = r; ux = x; uy = y; uz = z;
 }
 
+// The same quantities from the moments m = M F of mrt_forward: its rows 0, 3, 5 and 7 are
+// update_macro's sums of f, e_x f, e_y f and e_z f, term for term in q order (the formula
+// generator's self-check asserts it), so rho and j are the same values.
+template <class V>
+__device__ __forceinline__ void macro_of_moments(const V (&m)[19], V gx, V gy, V gz, V& rho,
+                                                 V& ux, V& uy, V& uz) {
+  const V r = m[0];
+  V x = vdiv(m[3], r), y = vdiv(m[5], r), z = vdiv(m[7], r);
+  x = vadd(x, vdiv(vmul(gx, 0.5f), r));
+  y = vadd(y, vdiv(vmul(gy, 0.5f), r));
+  z = vadd(z, vdiv(vmul(gz, 0.5f), r));
+  rho = r; ux = x; uy = y; uz = z;
+}
+
 // The same quantities with fused operations and one reciprocal (fast forms).
 template <class V>
 __device__ __forceinline__ void macro_fast(const V (&F)[19], V gx, V gy, V gz, V& rho, V& ux,
@@ -208,11 +222,12 @@ __device__ __forceinline__ V edot(int q, V vx, V vy, V vz) {
 }
 
 // MRT collision with Guo forcing of one fluid cell (or two, V = float2) in the reference's
-// order (lbm3d.py:276-333). SG[k] is the forcing weight 1 - 0.5 S[k] of the reference,
+// order (lbm3d.py:276-333), given the moments mF = M F of its populations (mrt_forward, which
+// the caller also reads rho and j from). SG[k] is the forcing weight 1 - 0.5 S[k] of the reference,
 // evaluated once per launch: 0.5 S[k] is an exact scaling, so 1 - 0.5 S[k] has a single
 // rounding wherever it is computed.
 template <class V>
-__device__ __forceinline__ void collide_cell(const V (&F)[19], V ux, V uy, V uz, V gx, V gy, V gz,
+__device__ __forceinline__ void collide_cell(const V (&mF)[19], V ux, V uy, V uz, V gx, V gy, V gz,
                                              const float* __restrict__ S,
                                              const float* __restrict__ SG, V (&out)[19]) {
   // Guo source terms t_q = w_q ((e_q - u).G + (e_q.u)(e_q.G)) (lbm3d.py:276-283).
@@ -236,7 +251,8 @@ __device__ __forceinline__ void collide_cell(const V (&F)[19], V ux, V uy, V uz,
   }
   V g[19], m[19];
   mrt_forward(t, g);
-  mrt_forward(F, m);
+#pragma unroll
+  for (int k = 0; k < 19; ++k) m[k] = mF[k];
   // Relaxation towards meq (lbm3d.py:285-326). S_0 = S_3 = S_5 = S_7 = 0: those
   // moments only receive the forcing term.
   const V uxx = vmul(ux, ux), uyy = vmul(uy, uy), uzz = vmul(uz, uz);
@@ -374,6 +390,9 @@ __device__ __forceinline__ void step_cells(const Args& a,
       F[q] = St::ld(pops, sl[0], a.shift[q]);
     }
   }
+  // Exact form: the moments M F, from which both rho, j and the collision start.
+  V mF[19];
+  if (!kFast) mrt_forward(F, mF);
 
   uint32_t c[L];
 #pragma unroll
@@ -393,7 +412,8 @@ __device__ __forceinline__ void step_cells(const Args& a,
       Ln::set(py, l, a.force_prev[n + c[l]]);
       Ln::set(pz, l, a.force_prev[2 * n + c[l]]);
     }
-    macro_any<kFast>(F, px, py, pz, rho, ux, uy, uz);
+    if (kFast) macro_fast(F, px, py, pz, rho, ux, uy, uz);
+    else macro_of_moments(mF, px, py, pz, rho, ux, uy, uz);
     if (a.write_faces) {
 #pragma unroll
       for (int l = 0; l < L; ++l)
@@ -411,7 +431,7 @@ __device__ __forceinline__ void step_cells(const Args& a,
 
   V out[19];
   if (kFast) mrt_collide_fast(F, rho, ux, uy, uz, gx, gy, gz, a.s, out);
-  else collide_cell(F, ux, uy, uz, gx, gy, gz, a.s, a.sg, out);
+  else collide_cell(mF, ux, uy, uz, gx, gy, gz, a.s, a.sg, out);
 
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
