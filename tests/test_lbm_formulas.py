@@ -115,3 +115,54 @@ def test_fast_collision_is_the_same_operator():
     # The generated coefficients are float32 roundings of 1/3, 1/18, ... (relative 3e-8); an
     # algebra mistake in a moment or forcing term shows up at 1e-5 and above.
     np.testing.assert_allclose(got, want, rtol=1e-7, atol=0)
+
+
+def _exact_as_python(src: str, name: str) -> str:
+    """Body of the generated exact transform `name` as Python statements (arrays as lists)."""
+    import re
+    body = src.split(f"void {name}(", 1)[1].split("{", 1)[1]
+    body = body[: body.index("\n}\n")]
+    body = re.sub(r"(-?0x[0-9a-f.]+p[+-]\d+)f", lambda m: repr(float.fromhex(m.group(1))), body)
+    stmts = []
+    for stmt in filter(None, (s.strip() for s in body.replace("\n", " ").split(";"))):
+        if re.fullmatch(r"V \w+\[\d+\]", stmt):
+            continue  # array declaration
+        stmts.append(re.sub(r"^(const )?V ", "", stmt))
+    return "\n".join(stmts)
+
+
+def _f32_env(**arrays):
+    f32 = np.float32
+    return {"vadd": lambda a, b: (a + b).astype(f32), "vsub": lambda a, b: (a - b).astype(f32),
+            "vmul": lambda a, b: (a * f32(b) if isinstance(b, float) else a * b).astype(f32),
+            "vneg": lambda a: -a, **arrays}
+
+
+def test_generated_exact_transforms_run_bit_exact():
+    """The emitted text of mrt_forward / mrt_inverse (shared and negated prefixes included),
+    run statement by statement in float32, equals the literal sequential sums bit for bit."""
+    gen = load_gen()
+    src = gen.gen()
+    rng = np.random.default_rng(11)
+    n = 20_000
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
+    F = (w * rng.uniform(0.8, 1.2, (n, 1)) * (1 + rng.normal(0, 0.05, (n, 19)))).astype(np.float32)
+
+    def forward(x):
+        env = _f32_env(X=list(x.T), m=[None] * 19, two=[None] * 19)
+        exec(_exact_as_python(src, "mrt_forward"), env)
+        return np.stack(env["m"], axis=1)
+
+    mom = gen._seq_dense(gen.M, F)
+    assert np.array_equal(forward(F).view(np.uint32), mom.view(np.uint32))
+    # Guo-like source terms with exact zeros of both signs: equal as values (the sign of an
+    # exact zero may differ, which the collision cannot carry to an output).
+    t = (rng.normal(0, 1e-6, (n, 19)) * (rng.uniform(size=(n, 19)) < 0.7)).astype(np.float32)
+    t[rng.uniform(size=(n, 19)) < 0.2] *= np.float32(-1.0)
+    assert np.array_equal(forward(t), gen._seq_dense(gen.M, t))
+
+    mom[:, 3:8] += rng.normal(0, 1e-4, (n, 5)).astype(np.float32)
+    env = _f32_env(m=list(mom.T), f=[None] * 19)
+    exec(_exact_as_python(src, "mrt_inverse"), env)
+    got = np.stack(env["f"], axis=1)
+    assert np.array_equal(got.view(np.uint32), gen._seq_dense(gen.INV, mom).view(np.uint32))
