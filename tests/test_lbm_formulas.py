@@ -5,6 +5,7 @@ import importlib.util
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 GEN = ROOT / "taichi-mpm-lbm_gb300" / "csrc" / "gen_lbm_formulas.py"
@@ -166,3 +167,115 @@ def test_generated_exact_transforms_run_bit_exact():
     exec(_exact_as_python(src, "mrt_inverse"), env)
     got = np.stack(env["f"], axis=1)
     assert np.array_equal(got.view(np.uint32), gen._seq_dense(gen.INV, mom).view(np.uint32))
+
+
+def _kernel_exact_collision(gen, src, F, G_prev, G, S):
+    """numpy float32 restatement of the step kernel's exact form for rows of F (cells x 19):
+    rho and u from rows 0, 3, 5, 7 of the emitted M F (macro_of_moments), then collide_cell
+    (Guo terms with (e.u)(e.G) shared by q and opp(q), forcing weights 1 - S/2 rounded once,
+    relaxation, emitted inverse), as csrc/lbm_core.cuh writes them."""
+    f32 = np.float32
+
+    def run(name, **arrays):
+        env = _f32_env(**arrays)
+        exec(_exact_as_python(src, name), env)
+        return env
+
+    mF = run("mrt_forward", X=list(F.T), m=[None] * 19, two=[None] * 19)["m"]
+    r = mF[0]
+    u = [mF[k] / r + (G_prev[:, a] * f32(0.5)) / r for a, k in enumerate((3, 5, 7))]
+    g3 = [G[:, a] for a in range(3)]
+    d = [[(f32(-1.0) - u[a]) * g3[a], (-u[a]) * g3[a], (f32(1.0) - u[a]) * g3[a]]
+         for a in range(3)]
+    E = gen.E
+    w = [f32(1 / 3)] + [f32(1 / 18)] * 6 + [f32(1 / 36)] * 12
+
+    def edot(q, v):
+        s = None
+        for a in range(3):
+            if E[q][a] != 0:
+                term = v[a] if E[q][a] > 0 else -v[a]
+                s = term if s is None else s + term
+        return s
+
+    t, b = [None] * 19, [None] * 19
+    for q in range(19):
+        a = (d[0][E[q][0] + 1] + d[1][E[q][1] + 1]) + d[2][E[q][2] + 1]
+        if q == 0:
+            t[q] = w[q] * a
+        else:
+            b[q] = edot(q, u) * edot(q, g3) if q % 2 else b[q - 1]
+            t[q] = w[q] * (a + b[q])
+    g = run("mrt_forward", X=t, m=[None] * 19, two=[None] * 19)["m"]
+    ux, uy, uz = u
+    uxx, uyy, uzz = ux * ux, uy * uy, uz * uz
+    meq = {1: (uxx + uyy) + uzz, 9: ((f32(2.0) * ux) * ux - uyy) - uzz, 11: uyy - uzz,
+           13: ux * uy, 14: uy * uz, 15: ux * uz}
+    SG = f32(1.0) - f32(0.5) * S
+    m = list(mF)
+    for k in range(19):
+        if k in (0, 3, 5, 7):
+            m[k] = m[k] + g[k]
+        else:
+            dk = m[k] - meq[k] if k in meq else m[k]
+            m[k] = m[k] - S[k] * dk
+            m[k] = m[k] + SG[k] * g[k]
+    f = run("mrt_inverse", m=m, f=[None] * 19)["f"]
+    return r, np.stack(u, axis=1), np.stack(f, axis=1)
+
+
+def _stream_periodic(gen, f_post, solid):
+    """The reference's stream (periodic wrap, half-way bounce-back at solid targets) of
+    post-collision populations (nx, ny, nz, 19); entries of solid cells stay zero."""
+    sol = solid.astype(bool)
+    out = np.zeros_like(f_post)
+    axes = (0, 1, 2)
+    for q in range(19):
+        e = tuple(gen.E[q])
+        moved = np.roll(f_post[..., q], e, axis=axes)          # moved[y] = f*(y - e)
+        from_fluid = (~sol) & np.roll(~sol, e, axis=axes)     # y fluid, y - e fluid
+        out[..., q] = np.where(from_fluid, moved, out[..., q])
+        bounce = (~sol) & np.roll(sol, tuple(-x for x in e), axis=axes)  # x fluid, x + e solid
+        o = gen.OPP[q]
+        out[..., o] = np.where(bounce, f_post[..., q], out[..., o])
+    return out
+
+
+@pytest.mark.parametrize("case", ["rest_unforced", "forced_uniform", "forced_with_solids",
+                                  "moving_with_solids"])
+def test_exact_collision_restatement_matches_the_oracle_bit_for_bit(case):
+    """The kernel's exact-form arithmetic (shared Guo products, rho and j from M F, host-rounded
+    forcing weights) restated in numpy float32 and streamed gives the oracle's next state and
+    its rho, u bit for bit, exact zeros of the unforced rest state included."""
+    from helpers import periodic_lbm
+    from oracle import oracle as O
+
+    gen = load_gen()
+    src = gen.gen()
+    force = (0.0, 0.0, 0.0) if case == "rest_unforced" else (2e-5, -1e-5, 5e-6)
+    u0 = (0.02, -0.01, 0.005) if case in ("forced_uniform", "moving_with_solids") else (0, 0, 0)
+    shape = (6, 5, 7)
+    cfg = periodic_lbm(nx=shape[0], ny=shape[1], nz=shape[2], viscosity=0.05, force=force,
+                       initial_velocity=u0)
+    lbm = O.LBMSolver3D(cfg)
+    solid = np.zeros(shape, np.int32)
+    if case.endswith("with_solids"):
+        solid[2, 1:3, 2:5] = 1
+        solid[4, 3, 1] = 1
+    lbm.initialize(solid)
+    for _ in range(4):
+        lbm.step()
+    fluid = solid.reshape(-1) == 0
+    F = lbm.F.reshape(-1, 19)[fluid].copy()
+    G = lbm.force.reshape(-1, 3)[fluid].copy()
+    rho_want = lbm.rho.reshape(-1)[fluid].copy()
+    u_want = lbm.v.reshape(-1, 3)[fluid].copy()
+    lbm.step()
+    rho, u, f = _kernel_exact_collision(gen, src, F, G, G, lbm.S)
+    assert np.array_equal(rho.view(np.uint32), rho_want.view(np.uint32))
+    assert np.array_equal(u.view(np.uint32), u_want.view(np.uint32))
+    f_post = np.zeros((*shape, 19), np.float32)
+    f_post.reshape(-1, 19)[fluid] = f
+    got = _stream_periodic(gen, f_post, solid).reshape(-1, 19)[fluid]
+    want = lbm.F.reshape(-1, 19)[fluid]
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
