@@ -37,7 +37,7 @@ MPM_BYTES_PER_PARTICLE = 200  # algorithmic bytes per particle-substep (standalo
 MPM_BYTES_PER_NODE = 32       # per touched grid node per substep
 # DRAM bytes per fluid cell and step kernel launch, from the ncu captures of the 192^3 scene
 # (dram__bytes_read.sum + dram__bytes_write.sum, odd/even launch average).
-TRAFFIC_PER_FLUID_CELL = {"f32/exact": 177.7, "f16/fast": 96.1}
+TRAFFIC_PER_FLUID_CELL = {"f32/exact": 177.4, "f16/fast": 96.1}
 METRIC = "MLUPS & particle-steps/s on 1 GB300: plain vs FP16/learned, <=1% drag error"
 
 
