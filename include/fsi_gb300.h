@@ -492,6 +492,14 @@ int fsi_closure_colsum(const void* g, int32_t m, int32_t n, float* out, void* st
 int fsi_closure_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
                      float beta1, float beta2, float eps, int32_t step, void* stream);
 
+/* Self-test of the bounded mbarrier waits of the tensor-core kernels (no reference
+ * counterpart; a failure-detection check that faults nothing). One CTA waits on a barrier that
+ * nothing arrives on: out[0] = 0 when the plain wait gave up after its clock limit (about one
+ * second) and set *err = 7; out[1] = 0 when a second role's abortable wait returned on the
+ * first role's abort flag without setting its own code (8). err (zeroed by the caller) and
+ * out are device int32 arrays of 1 and 2 elements. */
+int fsi_selftest_wait_limit(int32_t* err, int32_t* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1230,3 +1230,45 @@ extern "C" int fsi_closure_adam(float* p, const float* g, float* m, float* v, in
                                                                               beta2, eps, c1, c2);
   return check_launch("closure_adam_kernel");
 }
+
+namespace fsi {
+namespace {
+
+// Self-test of the bounded waits (no reference counterpart): one CTA, two roles, one mbarrier
+// that nothing arrives on. Role A (thread 0) waits with tc::mbar_wait: after tc::kWaitCycles it
+// records kWaitSelfTestCode and raises the abort flag. Role B (thread 32) first sleeps for
+// kWaitSelfTestDelay cycles, so that its own limit falls well after A's, then waits with
+// tc::mbar_wait_abortable and returns on A's abort without recording its code. Both loops
+// end by the clock whatever happens.
+constexpr int kWaitSelfTestCode = 7;
+constexpr long long kWaitSelfTestDelay = 1ll << 29;  // a quarter of the wait limit
+
+__global__ void wait_limit_selftest_kernel(int* __restrict__ err, int* __restrict__ out) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    abort_flag = 0;
+  }
+  __syncthreads();
+  volatile int* abort = &abort_flag;
+  if (threadIdx.x == 0) {
+    const bool ok = tc::mbar_wait(&bar, 0, err, kWaitSelfTestCode);
+    if (!ok) *abort = 1;
+    out[0] = ok ? 1 : 0;
+  } else if (threadIdx.x == 32) {
+    const long long t0 = clock64();
+    while (clock64() - t0 < kWaitSelfTestDelay) __nanosleep(100000);
+    const bool ok = tc::mbar_wait_abortable(&bar, 0, abort, err, kWaitSelfTestCode + 1);
+    out[1] = ok ? 1 : 0;
+  }
+}
+
+}  // namespace
+}  // namespace fsi
+
+extern "C" int fsi_selftest_wait_limit(int32_t* err, int32_t* out, void* stream) {
+  FSI_REQUIRE(err && out, "NULL array");
+  wait_limit_selftest_kernel<<<1, 64, 0, as_stream(stream)>>>(err, out);
+  return check_launch("wait_limit_selftest_kernel");
+}

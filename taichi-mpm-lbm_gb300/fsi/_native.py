@@ -174,6 +174,7 @@ _SIGNATURES = {
     "fsi_closure_infer": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, ctypes.c_int64,
                            ctypes.POINTER(ClosureWeights), _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_closure_apply": ([ctypes.POINTER(LbmDesc), _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "fsi_selftest_wait_limit": ([_VP, _VP, _VP], ctypes.c_int),
     "fsi_closure_restrict": ([ctypes.POINTER(LbmDesc), _VP, _VP, ctypes.c_int64,
                               ctypes.POINTER(LbmDesc), _VP, _VP], ctypes.c_int),
     "fsi_closure_loss": ([_VP, _VP, _VP, ctypes.c_int32, _VP, _VP, ctypes.c_int32, _VP, _VP],

@@ -312,3 +312,23 @@ def test_guard_falls_back_to_the_fine_grid():
     assert sim.fine.steps_done == 4
     u = sim.velocity_numpy()
     assert u.shape == (16, 8, 8, 3) and np.all(np.isfinite(u))
+
+
+def test_bounded_wait_gives_up_reports_and_releases_the_other_role():
+    """A wait on an mbarrier that nothing arrives on ends after its clock limit with error code
+    7 (no fault, no hang); the abortable wait of a second role returns on the first role's abort
+    flag without a code of its own; the context stays usable afterwards."""
+    import time
+
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    out = torch.full((2,), -1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nat.call("fsi_selftest_wait_limit", nat.ptr(err), nat.ptr(out), nat.stream_ptr())
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    assert err.item() == 7
+    assert out.tolist() == [0, 0]
+    assert 0.2 < elapsed < 20.0  # 2^31 SM clock cycles
+    x = torch.arange(8, device="cuda", dtype=torch.float32)
+    assert float((x * 2).sum()) == 56.0
