@@ -218,6 +218,24 @@ int fsi_mpm_substep(const fsi_mpm_desc* desc, const fsi_particles* particles, fl
 #define FSI_NOALLOC_MAX_BLOCKS 32768
 int fsi_mpm_substep_noalloc(const fsi_mpm_desc* desc, const fsi_particles* particles, void* stream);
 
+/* Bytes of the workspace that fsi_mpm_substep_sorted and fsi_coupled_substep need for this
+ * grid and a particle capacity: the per-cell and per-tile counts and starts of the particle
+ * sort, the sorted order and a 128-byte record per particle. The workspace is one device
+ * buffer, 256-byte aligned and zero-filled once before its first use; the substeps leave its
+ * count arrays zero again. No reference counterpart (the reference does not sort). */
+int fsi_mpm_workspace_bytes(const fsi_mpm_desc* desc, int64_t capacity, int64_t* bytes);
+
+/* One MPM substep with a deterministic scatter: the particles are sorted by base cell
+ * trunc(x / dx - 0.5) every substep, each cell's 27 stencil partials are summed over its
+ * particles in ascending index, and each node adds its cells' partials in ascending cell
+ * index; node tiles are owned by one thread block each, so the grid is written with plain
+ * stores and no atomics, and results repeat bit for bit from run to run. `grid` is float[N][4]
+ * (16-byte aligned); it need not be zero on entry and holds the substep's momentum and mass
+ * on the touched nodes on return (other nodes keep stale values). Same physics as
+ * fsi_mpm_substep; replaces MPMSolver3D.clear_grid/p2g/grid_op/g2p (fsi/mpm3d.py:189-318). */
+int fsi_mpm_substep_sorted(const fsi_mpm_desc* desc, const fsi_particles* particles, float* grid,
+                           void* workspace, int64_t workspace_bytes, void* stream);
+
 /* Rotation R of the polar decomposition of n row-major 3x3 matrices (float[n][9]).
  * Replaces the ti.svd call of MPMSolver3D.p2g (fsi/mpm3d.py:245-246). */
 int fsi_mpm_polar(const float* F, float* R, int64_t n, void* stream);
@@ -279,6 +297,18 @@ int fsi_coupling_forces(const fsi_coupling_desc* desc, const fsi_mpm_desc* mpm,
                         const fsi_particles* particles, const float* macro,
                         const uint32_t* flags, float* accum, float* valid_weight,
                         int32_t* coupling_mask, void* counters, void* stream);
+
+/* One coupled MPM substep: fsi_coupling_forces followed by fsi_mpm_substep_sorted, with the
+ * fluid reaction and solid-fraction spread folded into the sorted scatter (same order rule:
+ * per-cell partials over the cell's coupled particles, then ascending cell index per fluid
+ * node, added to `accum`'s current values) and the per-particle coupling force computed in
+ * the same pass as the stress. Zeroes and then fills the unsupported / partial / clipped
+ * counters. Replaces one iteration of the substep loop of LBMMpmCoupler.step
+ * (fsi/coupling.py:146-158): _compute_coupling_forces_kernel and MPMSolver3D.substep. */
+int fsi_coupled_substep(const fsi_coupling_desc* coupling, const fsi_mpm_desc* desc,
+                        const fsi_particles* particles, const float* macro, const uint32_t* flags,
+                        float* accum, float* valid_weight, int32_t* coupling_mask, void* counters,
+                        float* grid, void* workspace, int64_t workspace_bytes, void* stream);
 
 /* Rebuilds the LBM force field float[3][N] for the next lattice step:
  *   FSI_ASSEMBLE_CLAMP_FRACTION  accum.w = min(accum.w, 1)   (coupling.py:408-411)

@@ -450,19 +450,28 @@ struct MpmParams {
   int material;    // 0: fixed-corotated (reference), 1: Neo-Hookean extension
 };
 
+// Per-particle quantities of one P2G evaluation: the particle's stencil and the terms of
+// its grid contributions (mpm3d.py:236-256).
 template <class T>
-inline void p2g_particle(int p, const Particles<T>& P, Grid<T>& G, const MpmParams<T>& mp,
-                         bool atomic) {
-  if (P.active[p] == 0) return;
-  T x[3] = {P.x[3 * p], P.x[3 * p + 1], P.x[3 * p + 2]};
+struct P2GPrep {
   int base[3];
   T fx[3];
-  base_fx(x, mp.inv_dx, base, fx);
-  T w[3][3];
+  T w[3][3];  // w[i][axis]
+  T affine[9];
+  T mv[3], dtf[3];
+  T m;
+};
+
+// The part of p2g (mpm3d.py:236-256) that runs once per particle: F <- (I + dt C) F,
+// the stress and the affine term. F is written back.
+template <class T>
+inline void p2g_prepare(int p, const Particles<T>& P, const MpmParams<T>& mp, P2GPrep<T>& r) {
+  T x[3] = {P.x[3 * p], P.x[3 * p + 1], P.x[3 * p + 2]};
+  base_fx(x, mp.inv_dx, r.base, r.fx);
   for (int a = 0; a < 3; ++a) {
     T ww[3];
-    bspline(fx[a], ww);
-    for (int i = 0; i < 3; ++i) w[i][a] = ww[i];
+    bspline(r.fx[a], ww);
+    for (int i = 0; i < 3; ++i) r.w[i][a] = ww[i];
   }
   const T dt = mp.dt;
   T* Cp = P.C + 9 * p;
@@ -512,42 +521,153 @@ inline void p2g_particle(int p, const Particles<T>& P, Grid<T>& G, const MpmPara
   }
   T coef = (((-dt) * P.vol[p]) * (T)4.0) * mp.inv_dx;
   coef = coef * mp.inv_dx;
-  T affine[9];
-  const T m = P.mass[p];
-  for (int i = 0; i < 9; ++i) affine[i] = coef * stress[i] + m * Cp[i];
-  T mv[3], dtf[3];
+  r.m = P.mass[p];
+  for (int i = 0; i < 9; ++i) r.affine[i] = coef * stress[i] + r.m * Cp[i];
   for (int a = 0; a < 3; ++a) {
-    mv[a] = m * P.v[3 * p + a];
-    dtf[a] = dt * P.fp[3 * p + a];
+    r.mv[a] = r.m * P.v[3 * p + a];
+    r.dtf[a] = dt * P.fp[3 * p + a];
   }
+}
+
+// Contribution of a prepared particle to stencil node (i, j, k) (mpm3d.py:253-266):
+// add[0..2] to grid_v, add[3] to grid_m.
+template <class T>
+inline void p2g_contrib(const P2GPrep<T>& r, int i, int j, int k, T dx, T add[4]) {
+  T dpos[3] = {((T)i - r.fx[0]) * dx, ((T)j - r.fx[1]) * dx, ((T)k - r.fx[2]) * dx};
+  T weight = (r.w[i][0] * r.w[j][1]) * r.w[k][2];
+  for (int a = 0; a < 3; ++a) {
+    T ad = r.affine[3 * a] * dpos[0];
+    ad = ad + r.affine[3 * a + 1] * dpos[1];
+    ad = ad + r.affine[3 * a + 2] * dpos[2];
+    T mom = (r.mv[a] + ad) + r.dtf[a];
+    add[a] = weight * mom;
+  }
+  add[3] = weight * r.m;
+}
+
+template <class T>
+inline void p2g_particle(int p, const Particles<T>& P, Grid<T>& G, const MpmParams<T>& mp,
+                         bool atomic) {
+  if (P.active[p] == 0) return;
+  P2GPrep<T> r;
+  p2g_prepare(p, P, mp, r);
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j)
       for (int k = 0; k < 3; ++k) {
-        int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+        int ni = r.base[0] + i, nj = r.base[1] + j, nk = r.base[2] + k;
         if (!G.inside(ni, nj, nk)) continue;
-        T dpos[3] = {((T)i - fx[0]) * mp.dx, ((T)j - fx[1]) * mp.dx, ((T)k - fx[2]) * mp.dx};
-        T weight = (w[i][0] * w[j][1]) * w[k][2];
         long c = G.cell(ni, nj, nk);
+        T add[4];
+        p2g_contrib(r, i, j, k, mp.dx, add);
         for (int a = 0; a < 3; ++a) {
-          T ad = affine[3 * a] * dpos[0];
-          ad = ad + affine[3 * a + 1] * dpos[1];
-          ad = ad + affine[3 * a + 2] * dpos[2];
-          T mom = (mv[a] + ad) + dtf[a];
-          T add = weight * mom;
           if (atomic) {
 #pragma omp atomic
-            G.gv[3 * c + a] += add;
+            G.gv[3 * c + a] += add[a];
           } else {
-            G.gv[3 * c + a] = G.gv[3 * c + a] + add;
+            G.gv[3 * c + a] = G.gv[3 * c + a] + add[a];
           }
         }
-        T addm = weight * m;
         if (atomic) {
 #pragma omp atomic
-          G.gm[c] += addm;
+          G.gm[c] += add[3];
         } else {
-          G.gm[c] = G.gm[c] + addm;
+          G.gm[c] = G.gm[c] + add[3];
         }
+      }
+}
+
+// ------------------------------------------------------- cell-ordered sums -
+// The summation order of the GPU's sorted, atomic-free scatter. Particles are grouped by
+// their base cell b = trunc(x / dx - 0.5); a cell takes part when b lies in [-2, n - 1] on
+// every axis (otherwise none of its stencil nodes is in the grid). For each cell and each
+// of the 27 stencil offsets o the contributions of its particles are summed sequentially
+// in ascending particle index, starting from zero: the cell partial S_b(o). A node's value
+// is then its value before the scatter plus the partials S_b(node - b) of its non-empty
+// cells b added one at a time in ascending linear cell index, which is descending
+// lexicographic o = (2,2,2), (2,2,1), ..., (0,0,0). Each contribution itself is the
+// reference's expression, so only the order of the additions differs from a serial loop.
+struct CellGroups {
+  int ex, ey, ez;                 // extended cell grid [-2, n-1] per axis
+  std::vector<int> first, count;  // per group: range in `members`
+  std::vector<int> members;       // particle indices, grouped, ascending within a group
+  std::vector<int> group_of;      // extended cell -> group id or -1
+  long ext(int i, int j, int k) const { return ((long)(i + 2) * ey + (j + 2)) * ez + (k + 2); }
+};
+
+// Groups the particles p with include[p] by base cell.
+inline void build_cell_groups(int nx, int ny, int nz, int n, const int* base3,
+                              const std::vector<char>& include, CellGroups& g) {
+  g.ex = nx + 2; g.ey = ny + 2; g.ez = nz + 2;
+  const long ncell = (long)g.ex * g.ey * g.ez;
+  g.group_of.assign(ncell, -1);
+  std::vector<int> cnt;
+  for (int p = 0; p < n; ++p) {
+    if (!include[p]) continue;
+    const int* b = base3 + 3 * p;
+    long c = g.ext(b[0], b[1], b[2]);
+    if (g.group_of[c] < 0) { g.group_of[c] = (int)cnt.size(); cnt.push_back(0); }
+    ++cnt[g.group_of[c]];
+  }
+  const int ng = (int)cnt.size();
+  g.first.assign(ng, 0);
+  g.count.assign(ng, 0);
+  int run = 0;
+  for (int i = 0; i < ng; ++i) { g.first[i] = run; run += cnt[i]; }
+  g.members.assign(run, 0);
+  for (int p = 0; p < n; ++p) {  // ascending p keeps each group in index order
+    if (!include[p]) continue;
+    const int* b = base3 + 3 * p;
+    int gid = g.group_of[g.ext(b[0], b[1], b[2])];
+    g.members[g.first[gid] + g.count[gid]++] = p;
+  }
+}
+
+inline bool base_in_cell_range(const int b[3], int nx, int ny, int nz) {
+  return b[0] >= -2 && b[0] < nx && b[1] >= -2 && b[1] < ny && b[2] >= -2 && b[2] < nz;
+}
+
+// p2g in the cell order (all active particles are prepared: F is updated for each).
+template <class T>
+void p2g_cell_order(const Particles<T>& P, Grid<T>& G, const MpmParams<T>& mp) {
+  const int n = P.n;
+  std::vector<P2GPrep<T>> prep(n);
+  std::vector<int> base3(3 * (size_t)n, 0);
+  std::vector<char> include(n, 0);
+  for (int p = 0; p < n; ++p) {
+    if (P.active[p] == 0) continue;
+    p2g_prepare(p, P, mp, prep[p]);
+    for (int a = 0; a < 3; ++a) base3[3 * p + a] = prep[p].base[a];
+    include[p] = base_in_cell_range(prep[p].base, G.nx, G.ny, G.nz);
+  }
+  CellGroups g;
+  build_cell_groups(G.nx, G.ny, G.nz, n, base3.data(), include, g);
+  const int ng = (int)g.first.size();
+  std::vector<T> S((size_t)ng * 27 * 4, (T)0);
+  for (int gi = 0; gi < ng; ++gi) {
+    for (int o = 0; o < 27; ++o) {
+      const int i = o / 9, j = (o / 3) % 3, k = o % 3;
+      T acc[4] = {0, 0, 0, 0};
+      for (int m = 0; m < g.count[gi]; ++m) {
+        T add[4];
+        p2g_contrib(prep[g.members[g.first[gi] + m]], i, j, k, mp.dx, add);
+        for (int a = 0; a < 4; ++a) acc[a] = acc[a] + add[a];
+      }
+      for (int a = 0; a < 4; ++a) S[((size_t)gi * 27 + o) * 4 + a] = acc[a];
+    }
+  }
+  for (int ni = 0; ni < G.nx; ++ni)
+    for (int nj = 0; nj < G.ny; ++nj)
+      for (int nk = 0; nk < G.nz; ++nk) {
+        const long c = G.cell(ni, nj, nk);
+        T acc[4] = {G.gv[3 * c], G.gv[3 * c + 1], G.gv[3 * c + 2], G.gm[c]};
+        for (int o = 26; o >= 0; --o) {
+          const int i = o / 9, j = (o / 3) % 3, k = o % 3;
+          const int gi = g.group_of[g.ext(ni - i, nj - j, nk - k)];
+          if (gi < 0) continue;
+          for (int a = 0; a < 4; ++a) acc[a] = acc[a] + S[((size_t)gi * 27 + o) * 4 + a];
+        }
+        G.gv[3 * c] = acc[0]; G.gv[3 * c + 1] = acc[1]; G.gv[3 * c + 2] = acc[2];
+        G.gm[c] = acc[3];
       }
 }
 
@@ -688,8 +808,8 @@ FSI_ORACLE_EXPORT void oracle_lbm_init_f64(int nx, int ny, int nz, double* f, do
 }
 
 // MPMSolver3D.substep, fsi/mpm3d.py:189-203: clear_grid -> p2g -> grid_op -> g2p.
-// `deterministic` != 0 runs P2G serially in particle order; otherwise P2G runs
-// on `nthreads` threads with atomic adds, like a parallel Taichi CPU loop.
+// `deterministic` 1 runs P2G serially in particle order, 2 in the cell order above;
+// 0 runs it on `nthreads` threads with atomic adds, like a parallel Taichi CPU loop.
 template <class T>
 static void mpm_substep_impl(int nx, int ny, int nz, int n, T* x, T* v, T* C, T* Fd, const T* mass,
                              const T* vol, const int32_t* active, T* fp, T* gv, T* gm, T dt, T dx,
@@ -703,7 +823,9 @@ static void mpm_substep_impl(int nx, int ny, int nz, int n, T* x, T* v, T* C, T*
   const long N = (long)nx * ny * nz;
   std::memset(gv, 0, sizeof(T) * 3 * N);
   std::memset(gm, 0, sizeof(T) * N);
-  if (deterministic) {
+  if (deterministic == 2) {
+    p2g_cell_order(P, G, mp);
+  } else if (deterministic) {
     for (int p = 0; p < n; ++p) p2g_particle(p, P, G, mp, false);
   } else {
 #pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads))
@@ -752,7 +874,10 @@ FSI_ORACLE_EXPORT void oracle_polar_rotation_f64(int n, const double* F, double*
   for (int i = 0; i < n; ++i) polar_rotation_f64(F + 9 * i, R + 9 * i);
 }
 
-// _compute_coupling_forces_kernel, fsi/coupling.py:332-406 (serial particle order).
+// _compute_coupling_forces_kernel, fsi/coupling.py:332-406. With cell_order == 0 the
+// reaction and solid fraction are spread in serial particle order; with cell_order != 0 in
+// the cell order of p2g_cell_order (per-cell partials over the coupled particles of the
+// cell in ascending index, then each fluid node's partials in ascending cell index).
 // counters[0..2] += unsupported, partial, clipped.
 template <class T>
 static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv, const T* mass,
@@ -760,31 +885,46 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
                           const int32_t* solid, T* cforce, T* phi, T* valid_out, int32_t* mask_out,
                           int32_t* counters, T inv_dx, T gamma_eff, T dt_ratio, T cell_volume,
                           int build_fraction, T min_valid_weight, int use_rel, T rel_limit,
-                          int use_force_limit, T force_limit) {
+                          int use_force_limit, T force_limit, int cell_order) {
   Grid<T> G{nx, ny, nz, nullptr, nullptr};
   const T support_tolerance = (T)1.0e-5;
+  struct Spread {
+    int base[3];
+    T w[3][3];
+    T valid, pf[3], vol;
+  };
+  std::vector<Spread> sp(cell_order ? n : 0);
+  std::vector<int> base3(cell_order ? 3 * (size_t)n : 0, 0);
+  std::vector<char> include(cell_order ? n : 0, 0);
+  // The spread of one coupled particle into stencil node (i, j, k): reaction xyz and, when
+  // building it, the solid fraction (coupling.py:389-400).
+  auto spread_terms = [&](const Spread& r, int i, int j, int k, T out[4]) {
+    T weight = (r.w[i][0] * r.w[j][1]) * r.w[k][2];
+    T nw = weight / r.valid;
+    for (int a = 0; a < 3; ++a) out[a] = (((-nw) * r.pf[a]) * dt_ratio) / cell_volume;
+    out[3] = (nw * r.vol) / cell_volume;
+  };
   for (int p = 0; p < n; ++p) {
     if (active[p] == 0) continue;
     T xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
-    int base[3];
+    Spread r;
     T fx[3];
-    base_fx(xp, inv_dx, base, fx);
-    T w[3][3];
+    base_fx(xp, inv_dx, r.base, fx);
     for (int a = 0; a < 3; ++a) {
       T ww[3];
       bspline(fx[a], ww);
-      for (int i = 0; i < 3; ++i) w[i][a] = ww[i];
+      for (int i = 0; i < 3; ++i) r.w[i][a] = ww[i];
     }
     T valid = 0;
     T uf[3] = {0, 0, 0};
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j)
         for (int k = 0; k < 3; ++k) {
-          int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+          int ni = r.base[0] + i, nj = r.base[1] + j, nk = r.base[2] + k;
           if (!G.inside(ni, nj, nk)) continue;
           long c = G.cell(ni, nj, nk);
           if (solid[c] != 0) continue;
-          T weight = (w[i][0] * w[j][1]) * w[k][2];
+          T weight = (r.w[i][0] * r.w[j][1]) * r.w[k][2];
           valid = valid + weight;
           for (int a = 0; a < 3; ++a) uf[a] = uf[a] + weight * lbm_v[3 * c + a];
         }
@@ -816,20 +956,26 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
       for (int a = 0; a < 3; ++a) fp[3 * p + a] = pf[a];
       mask_out[p] = 1;
       if (clipped) counters[2] += 1;
+      r.valid = valid;
+      for (int a = 0; a < 3; ++a) r.pf[a] = pf[a];
+      r.vol = vol[p];
+      if (cell_order) {
+        sp[p] = r;
+        for (int a = 0; a < 3; ++a) base3[3 * p + a] = r.base[a];
+        include[p] = base_in_cell_range(r.base, nx, ny, nz);
+        continue;
+      }
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
           for (int k = 0; k < 3; ++k) {
-            int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+            int ni = r.base[0] + i, nj = r.base[1] + j, nk = r.base[2] + k;
             if (!G.inside(ni, nj, nk)) continue;
             long c = G.cell(ni, nj, nk);
             if (solid[c] != 0) continue;
-            T weight = (w[i][0] * w[j][1]) * w[k][2];
-            T nw = weight / valid;
-            for (int a = 0; a < 3; ++a) {
-              T add = (((-nw) * pf[a]) * dt_ratio) / cell_volume;
-              cforce[3 * c + a] = cforce[3 * c + a] + add;
-            }
-            if (build_fraction) phi[c] = phi[c] + (nw * vol[p]) / cell_volume;
+            T add[4];
+            spread_terms(r, i, j, k, add);
+            for (int a = 0; a < 3; ++a) cforce[3 * c + a] = cforce[3 * c + a] + add[a];
+            if (build_fraction) phi[c] = phi[c] + add[3];
           }
     } else {
       fp[3 * p] = fp[3 * p + 1] = fp[3 * p + 2] = 0;
@@ -837,6 +983,36 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
       counters[0] += 1;
     }
   }
+  if (!cell_order) return;
+  CellGroups g;
+  build_cell_groups(nx, ny, nz, n, base3.data(), include, g);
+  const int ng = (int)g.first.size();
+  std::vector<T> S((size_t)ng * 27 * 4, (T)0);
+  for (int gi = 0; gi < ng; ++gi)
+    for (int o = 0; o < 27; ++o) {
+      const int i = o / 9, j = (o / 3) % 3, k = o % 3;
+      T acc[4] = {0, 0, 0, 0};
+      for (int m = 0; m < g.count[gi]; ++m) {
+        T add[4];
+        spread_terms(sp[g.members[g.first[gi] + m]], i, j, k, add);
+        for (int a = 0; a < 4; ++a) acc[a] = acc[a] + add[a];
+      }
+      for (int a = 0; a < 4; ++a) S[((size_t)gi * 27 + o) * 4 + a] = acc[a];
+    }
+  for (int ni = 0; ni < nx; ++ni)
+    for (int nj = 0; nj < ny; ++nj)
+      for (int nk = 0; nk < nz; ++nk) {
+        const long c = G.cell(ni, nj, nk);
+        if (solid[c] != 0) continue;
+        for (int o = 26; o >= 0; --o) {
+          const int i = o / 9, j = (o / 3) % 3, k = o % 3;
+          const int gi = g.group_of[g.ext(ni - i, nj - j, nk - k)];
+          if (gi < 0) continue;
+          const T* s4 = &S[((size_t)gi * 27 + o) * 4];
+          for (int a = 0; a < 3; ++a) cforce[3 * c + a] = cforce[3 * c + a] + s4[a];
+          if (build_fraction) phi[c] = phi[c] + s4[3];
+        }
+      }
 }
 
 FSI_ORACLE_EXPORT void oracle_coupling_f32(int nx, int ny, int nz, int n, const float* x,
@@ -847,11 +1023,12 @@ FSI_ORACLE_EXPORT void oracle_coupling_f32(int nx, int ny, int nz, int n, const 
                                            float inv_dx, float gamma_eff, float dt_ratio,
                                            float cell_volume, int build_fraction,
                                            float min_valid_weight, int use_rel, float rel_limit,
-                                           int use_force_limit, float force_limit) {
+                                           int use_force_limit, float force_limit,
+                                           int cell_order) {
   coupling_impl<float>(nx, ny, nz, n, x, pv, mass, vol, active, fp, lbm_v, solid, cforce, phi,
                        valid_out, mask_out, counters, inv_dx, gamma_eff, dt_ratio, cell_volume,
                        build_fraction, min_valid_weight, use_rel, rel_limit, use_force_limit,
-                       force_limit);
+                       force_limit, cell_order);
 }
 
 FSI_ORACLE_EXPORT void oracle_coupling_f64(int nx, int ny, int nz, int n, const double* x,
@@ -862,11 +1039,12 @@ FSI_ORACLE_EXPORT void oracle_coupling_f64(int nx, int ny, int nz, int n, const 
                                            double inv_dx, double gamma_eff, double dt_ratio,
                                            double cell_volume, int build_fraction,
                                            double min_valid_weight, int use_rel, double rel_limit,
-                                           int use_force_limit, double force_limit) {
+                                           int use_force_limit, double force_limit,
+                                           int cell_order) {
   coupling_impl<double>(nx, ny, nz, n, x, pv, mass, vol, active, fp, lbm_v, solid, cforce, phi,
                         valid_out, mask_out, counters, inv_dx, gamma_eff, dt_ratio, cell_volume,
                         build_fraction, min_valid_weight, use_rel, rel_limit, use_force_limit,
-                        force_limit);
+                        force_limit, cell_order);
 }
 
 // _compute_immersed_boundary_force_kernel, fsi/coupling.py:421-452 (serial cell order).

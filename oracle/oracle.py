@@ -250,11 +250,15 @@ class MPMSolver3D:
     """Oracle of fsi/mpm3d.py:9-368 over numpy arrays."""
 
     def __init__(self, config, dtype=np.float32, nthreads: int = 1, deterministic: bool = True,
-                 polar: str = "exact"):
+                 polar: str = "exact", cell_order: bool = False):
+        """``cell_order`` sums the P2G scatter (and the coupler's spread) in the cell order of
+        the GPU's sorted scatter (oracle/fsi_oracle.cpp, p2g_cell_order); otherwise
+        ``deterministic`` selects a serial particle-order loop or threads with atomics."""
         config.validate()
         if polar not in ("exact", "device"):
             raise ValueError("polar must be 'exact' or 'device'")
         self.polar = polar
+        self.cell_order = bool(cell_order)
         self.config = config
         self.dtype = np.dtype(dtype)
         self.nthreads = nthreads
@@ -371,7 +375,8 @@ class MPMSolver3D:
             _p(self.grid_v), _p(self.grid_m), cast(dt_value), cast(self.dx), cast(self.inv_dx),
             cast(self.mu), cast(self.lam), _p(grav), self.boundary_width,
             cast(self.boundary_damping), int(self.apic), cast(0.5 * self.dx), _p(upper),
-            self.nthreads, int(self.deterministic), 1 if self.polar == "device" else 0,
+            self.nthreads, 2 if self.cell_order else int(self.deterministic),
+            1 if self.polar == "device" else 0,
             _p(self.mu_p) if self.mu_p is not None else None,
             _p(self.lam_p) if self.lam_p is not None else None,
             1 if getattr(self.config, "constitutive_model", "fixed_corotated") == "neo_hookean" else 0)
@@ -504,7 +509,7 @@ class LBMMpmCoupler:
             int(build_fraction), self._real(c.min_valid_weight),
             int(c.relative_velocity_limit is not None),
             self._real(c.relative_velocity_limit or 0.0), int(c.force_limit is not None),
-            self._real(c.force_limit or 0.0))
+            self._real(c.force_limit or 0.0), int(getattr(self.mpm, "cell_order", False)))
 
     def _clamp_fraction(self):
         np.minimum(self.solid_volume_fraction, self.dtype.type(1.0), out=self.solid_volume_fraction)
@@ -644,12 +649,12 @@ class FSISimulation:
     """Oracle of fsi/simulation.py:12-153 (no snapshot writer)."""
 
     def __init__(self, config, dtype=np.float32, nthreads: int = 1, polar: str = "exact",
-                 deterministic: bool = True):
+                 deterministic: bool = True, cell_order: bool = False):
         config.validate()
         self.config = config
         self.lbm = LBMSolver3D(config.lbm, dtype=dtype, nthreads=nthreads)
         self.mpm = MPMSolver3D(config.mpm, dtype=dtype, nthreads=nthreads, polar=polar,
-                               deterministic=deterministic)
+                               deterministic=deterministic, cell_order=cell_order)
         self.coupler = LBMMpmCoupler(config.coupling, self.lbm, self.mpm)
         self.step_index = 0
         self.time = 0.0

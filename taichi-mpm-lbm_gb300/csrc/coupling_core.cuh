@@ -55,11 +55,145 @@ struct ForceArgs {
   Cnt* __restrict__ cnt;
 };
 
-// _compute_coupling_forces_kernel, fsi/coupling.py:332-406, for particle p (this thread);
-// every lane of the warp calls it (warp-aggregated counters). kGatherAhead issues the
+// The per-particle part of _compute_coupling_forces_kernel (fsi/coupling.py:336-387) for
+// active particle p: interpolates the fluid velocity over the in-grid fluid nodes of its
+// stencil, and if the valid weight exceeds min_valid_weight computes the penalty force with
+// its clipping. Writes the particle force, valid weight and coupling mask; returns true for
+// a coupled particle, whose force, valid weight, stencil weights and usable-node mask (bit s:
+// node s = 9i + 3j + k is in-grid and fluid) the spread needs. kGatherAhead issues the
 // stencil's loads up front (fewer dependent round trips, more registers: for launches with
 // few particles, where latency and not occupancy bounds the kernel); both orders sum the
 // same values in the same order.
+template <bool kGatherAhead>
+__device__ __forceinline__ bool coupling_particle(const ForceArgs& a, int p, int base[3],
+                                                  float wv[3][3], uint32_t& usable, float& valid,
+                                                  float pf[3], bool& partial, bool& clipped,
+                                                  bool& unsupported) {
+  const long long cap = a.cap;
+  const float x[3] = {a.x[p], a.x[cap + p], a.x[2 * cap + p]};
+  float fx[3];
+  stencil_base(a.c.inv_dx, x, base, fx);
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) wv[ax][i] = bspline_w(fx[ax], i);
+  valid = 0.f;
+  float uf[3] = {0.f, 0.f, 0.f};
+  usable = 0;
+  if (!kGatherAhead) {
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int i = s / 9, j = (s / 3) % 3, k = s % 3;
+      const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+      if (ni < 0 || ni >= a.g.nx || nj < 0 || nj >= a.g.ny || nk < 0 || nk >= a.g.nz) continue;
+      const long long c = ((long long)ni * a.g.ny + nj) * a.g.nz + nk;
+      if (a.flags[c] & kFlagSolid) continue;
+      usable |= 1u << s;
+      const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
+      valid = __fadd_rn(valid, w);
+      const float4 mc = a.macro[c];
+      uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc.x));
+      uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc.y));
+      uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc.z));
+    }
+  } else {
+    // All loads go out before the first is needed: the 27 flags together, then the lattice
+    // velocities of the usable nodes in three batches of 9; the sums still run in stencil
+    // order (s = 0..26), so the result is that of the node-by-node loop.
+    uint32_t inside = 0;  // bit s: node s of the stencil lies in the lattice
+    uint32_t fl[27];
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int i = s / 9, j = (s / 3) % 3, k = s % 3;
+      const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
+      const bool in = ni >= 0 && ni < a.g.nx && nj >= 0 && nj < a.g.ny && nk >= 0 && nk < a.g.nz;
+      inside |= (uint32_t)in << s;
+      fl[s] = in ? a.flags[((long long)ni * a.g.ny + nj) * a.g.nz + nk] : kFlagSolid;
+    }
+#pragma unroll
+    for (int s = 0; s < 27; ++s)
+      if (((inside >> s) & 1u) && !(fl[s] & kFlagSolid)) usable |= 1u << s;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      float4 mc[9];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const int s = 9 * b + t, j = t / 3, k = t % 3;
+        if ((usable >> s) & 1u)
+          mc[t] = a.macro[((long long)(base[0] + b) * a.g.ny + (base[1] + j)) * a.g.nz + (base[2] + k)];
+      }
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const int s = 9 * b + t, j = t / 3, k = t % 3;
+        if (!((usable >> s) & 1u)) continue;
+        const float w = __fmul_rn(__fmul_rn(wv[0][b], wv[1][j]), wv[2][k]);
+        valid = __fadd_rn(valid, w);
+        uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc[t].x));
+        uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc[t].y));
+        uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc[t].z));
+      }
+    }
+  }
+  a.valid_out[p] = valid;
+  if (!(valid > a.c.min_valid_weight)) {
+    a.fp[p] = 0.f; a.fp[cap + p] = 0.f; a.fp[2 * cap + p] = 0.f;
+    a.mask_out[p] = 0;
+    unsupported = true;
+    return false;
+  }
+  partial = valid < __fsub_rn(1.0f, 1.0e-5f);
+  float dv[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    uf[ax] = __fdiv_rn(uf[ax], valid);
+    dv[ax] = __fsub_rn(uf[ax], a.v[ax * cap + p]);
+  }
+  if (a.c.use_rel_limit) {
+    const float nrm = norm3(dv[0], dv[1], dv[2]);
+    if (nrm > a.c.rel_limit && nrm > 0.f) {
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) dv[ax] = __fmul_rn(__fdiv_rn(dv[ax], nrm), a.c.rel_limit);
+      clipped = true;
+    }
+  }
+  const float gm = __fmul_rn(a.c.gamma_eff, a.mass[p]);
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) pf[ax] = __fmul_rn(gm, dv[ax]);
+  if (a.c.use_force_limit) {
+    const float nrm = norm3(pf[0], pf[1], pf[2]);
+    if (nrm > a.c.force_limit && nrm > 0.f) {
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) pf[ax] = __fmul_rn(__fdiv_rn(pf[ax], nrm), a.c.force_limit);
+      clipped = true;
+    }
+  }
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) a.fp[ax * cap + p] = pf[ax];
+  a.mask_out[p] = 1;
+  return true;
+}
+
+// Reaction force xyz and solid-fraction term (w) that a coupled particle with stencil weight
+// w, valid weight `valid` and force pf spreads into one fluid node (coupling.py:389-400).
+__device__ __forceinline__ float4 coupling_spread_terms(const fsi_coupling_desc& c, float w,
+                                                        float valid, const float pf[3], float vp) {
+  // x / 1 is exactly x: the divisions by the cell volume are skipped for unit cells (dx = 1).
+  const bool unit_cell = c.cell_volume == 1.0f;
+  const float nw = __fdiv_rn(w, valid);
+  float add[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    add[ax] = __fmul_rn(__fmul_rn(-nw, pf[ax]), c.dt_ratio);
+    if (!unit_cell) add[ax] = __fdiv_rn(add[ax], c.cell_volume);
+  }
+  float ph = __fmul_rn(nw, vp);
+  if (!unit_cell) ph = __fdiv_rn(ph, c.cell_volume);
+  return make_float4(add[0], add[1], add[2], ph);
+}
+
+// _compute_coupling_forces_kernel, fsi/coupling.py:332-406, for particle p (this thread);
+// every lane of the warp calls it (warp-aggregated counters). The reaction and solid
+// fraction are spread with vector atomics (order of arrival).
 template <bool kGatherAhead>
 __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) {
   const bool live = p < a.n;
@@ -69,103 +203,12 @@ __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) 
     if (a.active[p] == 0) {
       a.fp[p] = 0.f; a.fp[cap + p] = 0.f; a.fp[2 * cap + p] = 0.f;
     } else {
-      const float x[3] = {a.x[p], a.x[cap + p], a.x[2 * cap + p]};
       int base[3];
-      float fx[3];
-      stencil_base(a.c.inv_dx, x, base, fx);
-      float wv[3][3];
-#pragma unroll
-      for (int ax = 0; ax < 3; ++ax)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) wv[ax][i] = bspline_w(fx[ax], i);
-      float valid = 0.f, uf[3] = {0.f, 0.f, 0.f};
-      uint32_t usable = 0;  // bit s: node s of the stencil is in-grid and fluid
-      if (!kGatherAhead) {
-#pragma unroll
-        for (int s = 0; s < 27; ++s) {
-          const int i = s / 9, j = (s / 3) % 3, k = s % 3;
-          const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
-          if (ni < 0 || ni >= a.g.nx || nj < 0 || nj >= a.g.ny || nk < 0 || nk >= a.g.nz) continue;
-          const long long c = ((long long)ni * a.g.ny + nj) * a.g.nz + nk;
-          if (a.flags[c] & kFlagSolid) continue;
-          usable |= 1u << s;
-          const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
-          valid = __fadd_rn(valid, w);
-          const float4 mc = a.macro[c];
-          uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc.x));
-          uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc.y));
-          uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc.z));
-        }
-      } else {
-        // All loads go out before the first is needed: the 27 flags together, then the lattice
-        // velocities of the usable nodes in three batches of 9; the sums still run in stencil
-        // order (s = 0..26), so the result is that of the node-by-node loop.
-        uint32_t inside = 0;  // bit s: node s of the stencil lies in the lattice
-        uint32_t fl[27];
-#pragma unroll
-        for (int s = 0; s < 27; ++s) {
-          const int i = s / 9, j = (s / 3) % 3, k = s % 3;
-          const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
-          const bool in = ni >= 0 && ni < a.g.nx && nj >= 0 && nj < a.g.ny && nk >= 0 && nk < a.g.nz;
-          inside |= (uint32_t)in << s;
-          fl[s] = in ? a.flags[((long long)ni * a.g.ny + nj) * a.g.nz + nk] : kFlagSolid;
-        }
-#pragma unroll
-        for (int s = 0; s < 27; ++s)
-          if (((inside >> s) & 1u) && !(fl[s] & kFlagSolid)) usable |= 1u << s;
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          float4 mc[9];
-#pragma unroll
-          for (int t = 0; t < 9; ++t) {
-            const int s = 9 * b + t, j = t / 3, k = t % 3;
-            if ((usable >> s) & 1u)
-              mc[t] = a.macro[((long long)(base[0] + b) * a.g.ny + (base[1] + j)) * a.g.nz + (base[2] + k)];
-          }
-#pragma unroll
-          for (int t = 0; t < 9; ++t) {
-            const int s = 9 * b + t, j = t / 3, k = t % 3;
-            if (!((usable >> s) & 1u)) continue;
-            const float w = __fmul_rn(__fmul_rn(wv[0][b], wv[1][j]), wv[2][k]);
-            valid = __fadd_rn(valid, w);
-            uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc[t].x));
-            uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc[t].y));
-            uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc[t].z));
-          }
-        }
-      }
-      a.valid_out[p] = valid;
-      if (valid > a.c.min_valid_weight) {
-        partial = valid < __fsub_rn(1.0f, 1.0e-5f);
-        float dv[3];
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-          uf[ax] = __fdiv_rn(uf[ax], valid);
-          dv[ax] = __fsub_rn(uf[ax], a.v[ax * cap + p]);
-        }
-        if (a.c.use_rel_limit) {
-          const float nrm = norm3(dv[0], dv[1], dv[2]);
-          if (nrm > a.c.rel_limit && nrm > 0.f) {
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) dv[ax] = __fmul_rn(__fdiv_rn(dv[ax], nrm), a.c.rel_limit);
-            clipped = true;
-          }
-        }
-        const float gm = __fmul_rn(a.c.gamma_eff, a.mass[p]);
-        float pf[3] = {__fmul_rn(gm, dv[0]), __fmul_rn(gm, dv[1]), __fmul_rn(gm, dv[2])};
-        if (a.c.use_force_limit) {
-          const float nrm = norm3(pf[0], pf[1], pf[2]);
-          if (nrm > a.c.force_limit && nrm > 0.f) {
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) pf[ax] = __fmul_rn(__fdiv_rn(pf[ax], nrm), a.c.force_limit);
-            clipped = true;
-          }
-        }
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) a.fp[ax * cap + p] = pf[ax];
-        a.mask_out[p] = 1;
+      float wv[3][3], valid, pf[3];
+      uint32_t usable;
+      if (coupling_particle<kGatherAhead>(a, p, base, wv, usable, valid, pf, partial, clipped,
+                                          unsupported)) {
         const float vp = a.vol[p];
-        const bool unit_cell = a.c.cell_volume == 1.0f;
 #pragma unroll
         for (int s = 0; s < 27; ++s) {
           if (!(usable & (1u << s))) continue;
@@ -173,25 +216,10 @@ __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) 
           const long long c =
               ((long long)(base[0] + i) * a.g.ny + (base[1] + j)) * a.g.nz + (base[2] + k);
           const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
-          const float nw = __fdiv_rn(w, valid);
-          float add[3];
-#pragma unroll
-          for (int ax = 0; ax < 3; ++ax) {
-            add[ax] = __fmul_rn(__fmul_rn(-nw, pf[ax]), a.c.dt_ratio);
-            // x / 1 is exactly x: skip the division for unit cells (dx = 1).
-            if (!unit_cell) add[ax] = __fdiv_rn(add[ax], a.c.cell_volume);
-          }
-          float ph = 0.f;
-          if (a.c.build_fraction) {
-            ph = __fmul_rn(nw, vp);
-            if (!unit_cell) ph = __fdiv_rn(ph, a.c.cell_volume);
-          }
-          red_add_v4(a.accum + c, add[0], add[1], add[2], ph);
+          float4 t = coupling_spread_terms(a.c, w, valid, pf, vp);
+          if (!a.c.build_fraction) t.w = 0.f;
+          red_add_v4(a.accum + c, t.x, t.y, t.z, t.w);
         }
-      } else {
-        a.fp[p] = 0.f; a.fp[cap + p] = 0.f; a.fp[2 * cap + p] = 0.f;
-        a.mask_out[p] = 0;
-        unsupported = true;
       }
     }
   }

@@ -220,6 +220,56 @@ __device__ __forceinline__ void load_particle_x(const PView& P, long long cap, i
   x[0] = P.x[p]; x[1] = P.x[cap + p]; x[2] = P.x[2 * cap + p];
 }
 
+// The once-per-particle part of P2G for active particle p (mpm3d.py:242-252):
+// F <- (I + dt C) F (written back), the stress, and affine = stress term + m C.
+__device__ __forceinline__ void p2g_stress_affine(const Mpm& m, const PView& P, int p,
+                                                  float affine[9], float& mass) {
+  const long long cap = m.cap;
+  float Cp[9], Fp[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) { Cp[i] = P.C[i * cap + p]; Fp[i] = P.F[i * cap + p]; }
+  // F <- (I + dt C) F (mpm3d.py:243)
+  float A[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) A[i] = __fadd_rn((i % 4 == 0) ? 1.f : 0.f, __fmul_rn(m.dt, Cp[i]));
+  float Fn[9];
+  matmul3(A, Fp, Fn);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) P.F[i * cap + p] = Fn[i];
+  const float J = det3(Fn);
+  const float mu = P.mu ? P.mu[p] : m.mu;
+  const float lam = P.lam ? P.lam[p] : m.lam;
+  float Ft[9], S[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) Ft[3 * a + b] = Fn[3 * b + a];
+  if (m.material == FSI_MATERIAL_NEO_HOOKEAN) {
+    // Kirchhoff stress of compressible Neo-Hookean: mu (F F^T - I) + lam ln(J) I.
+    matmul3(Fn, Ft, S);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) S[i] = __fmul_rn(mu, __fsub_rn(S[i], (i % 4 == 0) ? 1.f : 0.f));
+    const float ll = __fmul_rn(lam, logf(J));
+    S[0] = __fadd_rn(S[0], ll); S[4] = __fadd_rn(S[4], ll); S[8] = __fadd_rn(S[8], ll);
+  } else {
+    // Fixed-corotated: 2 mu (F - R) F^T + lam J (J - 1) I (mpm3d.py:247-251)
+    float R[9];
+    polar_rotation(Fn, R);
+    const float twomu = __fmul_rn(2.f, mu);
+    float Pm[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Pm[i] = __fmul_rn(twomu, __fsub_rn(Fn[i], R[i]));
+    matmul3(Pm, Ft, S);
+    const float lj = __fmul_rn(__fmul_rn(lam, J), __fsub_rn(J, 1.f));
+    S[0] = __fadd_rn(S[0], lj); S[4] = __fadd_rn(S[4], lj); S[8] = __fadd_rn(S[8], lj);
+  }
+  float coef = __fmul_rn(__fmul_rn(__fmul_rn(-m.dt, P.vol[p]), 4.f), m.inv_dx);
+  coef = __fmul_rn(coef, m.inv_dx);
+  mass = P.mass[p];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) affine[i] = __fadd_rn(__fmul_rn(coef, S[i]), __fmul_rn(mass, Cp[i]));
+}
+
 // P2G of particle p (this thread) within its CTA; every thread of the CTA calls it.
 __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* __restrict__ grid,
                                          uint8_t* __restrict__ dirty, int p) {
@@ -235,49 +285,7 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
     float x[3];
     load_particle_x(P, cap, p, x);
     base_fx(m, x, base, fx);
-    float Cp[9], Fp[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) { Cp[i] = P.C[i * cap + p]; Fp[i] = P.F[i * cap + p]; }
-    // F <- (I + dt C) F (mpm3d.py:243)
-    float A[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A[i] = __fadd_rn((i % 4 == 0) ? 1.f : 0.f, __fmul_rn(m.dt, Cp[i]));
-    float Fn[9];
-    matmul3(A, Fp, Fn);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) P.F[i * cap + p] = Fn[i];
-    const float J = det3(Fn);
-    const float mu = P.mu ? P.mu[p] : m.mu;
-    const float lam = P.lam ? P.lam[p] : m.lam;
-    float Ft[9], S[9];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) Ft[3 * a + b] = Fn[3 * b + a];
-    if (m.material == FSI_MATERIAL_NEO_HOOKEAN) {
-      // Kirchhoff stress of compressible Neo-Hookean: mu (F F^T - I) + lam ln(J) I.
-      matmul3(Fn, Ft, S);
-#pragma unroll
-      for (int i = 0; i < 9; ++i) S[i] = __fmul_rn(mu, __fsub_rn(S[i], (i % 4 == 0) ? 1.f : 0.f));
-      const float ll = __fmul_rn(lam, logf(J));
-      S[0] = __fadd_rn(S[0], ll); S[4] = __fadd_rn(S[4], ll); S[8] = __fadd_rn(S[8], ll);
-    } else {
-      // Fixed-corotated: 2 mu (F - R) F^T + lam J (J - 1) I (mpm3d.py:247-251)
-      float R[9];
-      polar_rotation(Fn, R);
-      const float twomu = __fmul_rn(2.f, mu);
-      float Pm[9];
-#pragma unroll
-      for (int i = 0; i < 9; ++i) Pm[i] = __fmul_rn(twomu, __fsub_rn(Fn[i], R[i]));
-      matmul3(Pm, Ft, S);
-      const float lj = __fmul_rn(__fmul_rn(lam, J), __fsub_rn(J, 1.f));
-      S[0] = __fadd_rn(S[0], lj); S[4] = __fadd_rn(S[4], lj); S[8] = __fadd_rn(S[8], lj);
-    }
-    float coef = __fmul_rn(__fmul_rn(__fmul_rn(-m.dt, P.vol[p]), 4.f), m.inv_dx);
-    coef = __fmul_rn(coef, m.inv_dx);
-    mass = P.mass[p];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) affine[i] = __fadd_rn(__fmul_rn(coef, S[i]), __fmul_rn(mass, Cp[i]));
+    p2g_stress_affine(m, P, p, affine, mass);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       mv[a] = __fmul_rn(mass, P.v[a * cap + p]);

@@ -147,6 +147,13 @@ _SIGNATURES = {
     "fsi_lbm_macro_diagnostics": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, ctypes.c_int64, _VP, _VP, _VP], ctypes.c_int),
     "fsi_mpm_substep": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),
     "fsi_mpm_substep_noalloc": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP], ctypes.c_int),
+    "fsi_mpm_workspace_bytes": ([ctypes.POINTER(MpmDesc), ctypes.c_int64,
+                                 ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "fsi_mpm_substep_sorted": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP,
+                                ctypes.c_int64, _VP], ctypes.c_int),
+    "fsi_coupled_substep": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc),
+                             ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                             ctypes.c_int64, _VP], ctypes.c_int),
     "fsi_mpm_polar": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "fsi_mpm_base_cells": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP], ctypes.c_int),
     "fsi_mpm_reduce": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),

@@ -147,6 +147,10 @@ class MPMConfig:
     # Extension (no reference counterpart): the elastic model. The reference's solver is
     # fixed-corotated (mpm3d.py:247-251); "neo_hookean" selects mu (F F^T - I) + lam ln(J) I.
     constitutive_model: Literal["fixed_corotated", "neo_hookean"] = "fixed_corotated"
+    # Extension (no reference counterpart): how P2G sums the grid. "sorted" sorts the
+    # particles by cell each substep and adds every node's contributions in a fixed order
+    # (deterministic, atomic-free); "atomic" scatters in arrival order with atomics.
+    p2g_mode: Literal["sorted", "atomic"] = "sorted"
 
     def validate(self) -> None:
         _check_grid("MPM", self.nx, self.ny, self.nz)
@@ -173,6 +177,8 @@ class MPMConfig:
             raise ValueError("boundary_damping must be in [0, 1].")
         if self.constitutive_model not in _CONSTITUTIVE_MODELS:
             raise ValueError(f"Unsupported constitutive model: {self.constitutive_model}.")
+        if self.p2g_mode not in ("sorted", "atomic"):
+            raise ValueError(f"Unsupported p2g_mode: {self.p2g_mode}.")
 
 
 _CONSTITUTIVE_MODELS = frozenset({"fixed_corotated", "neo_hookean"})

@@ -118,6 +118,19 @@ class LBMMpmCoupler:
                  nat.ptr(self._valid), nat.ptr(self._mask), nat.ptr(self._counters),
                  nat.stream_ptr())
 
+    def _coupled_substep(self, mpm_dt: float, dt_ratio: float, build_fraction: bool) -> None:
+        """Coupling force + MPM substep in one sorted pass (the spread folded into P2G)."""
+        self._desc.gamma_eff = self._gamma_for_kernel()
+        self._desc.dt_ratio = float(np.float32(dt_ratio))
+        self._desc.build_fraction = int(build_fraction)
+        mpm = self.mpm
+        mpm.desc.dt = float(np.float32(mpm_dt))
+        nat.call("fsi_coupled_substep", self._desc, mpm.desc, mpm.particles,
+                 nat.ptr(self.lbm.macro), nat.ptr(self.lbm.flags), nat.ptr(self._accum),
+                 nat.ptr(self._valid), nat.ptr(self._mask), nat.ptr(self._counters),
+                 nat.ptr(mpm._grid), nat.ptr(mpm.workspace), mpm.workspace.numel(),
+                 nat.stream_ptr())
+
     def _contact_kernel(self) -> None:
         nat.call("fsi_contact", self._desc, self.mpm.desc, self.mpm.particles,
                  nat.ptr(self._accum), nat.ptr(self.lbm.flags), nat.ptr(self._contact_mask),
@@ -144,6 +157,15 @@ class LBMMpmCoupler:
         mpm_dt = lbm_dt_value / float(self.substeps)
         dt_ratio = mpm_dt / lbm_dt_value
         for substep in range(self.substeps):
+            if self.enabled and self.mpm.sorted:
+                # Coupling force, spread and MPM substep in one sorted pass; it zeroes the
+                # per-substep counters itself (clear_particle_diagnostics of coupling.py:147
+                # for the counters; weights and masks are rewritten for every active particle).
+                self._coupled_substep(mpm_dt, dt_ratio,
+                                      substep == 0 and self.build_solid_volume_fraction)
+                if self.contact_enabled:
+                    self._contact_kernel()
+                continue
             if self.enabled:
                 # clear_particle_diagnostics() of coupling.py:147: the coupling kernel rewrites
                 # the weight and mask of every active particle, and inactive particles keep

@@ -2,9 +2,12 @@
 
 Particles are stored as structure-of-arrays torch CUDA tensors (x, v, force
 ``[3, capacity]``; C, F ``[9, capacity]``; mass, volume, active ``[capacity]``)
-and advanced by the library's sm_103a substep (shared-memory tiled P2G, grid
-update fused into G2P). The grid is a float4 (momentum, mass) array kept
+and advanced by the library's sm_103a substep. The default ("sorted" p2g_mode)
+sorts the particles by cell every substep and sums each grid node's
+contributions in a fixed order with plain stores (deterministic); "atomic"
+scatters through shared-memory tiles with atomics and keeps the float4 grid
 all-zero between substeps by clearing only the node blocks that were touched.
+The grid update is fused into G2P in both.
 
 Public methods, accessors and exceptions follow fsi/mpm3d.py:9-368.
 """
@@ -92,6 +95,10 @@ class MPMSolver3D:
         self._grid = torch.zeros((n_nodes, 4), dtype=f32, device=dev)
         nblocks = ((self.nx + 3) // 4) * ((self.ny + 3) // 4) * ((self.nz + 3) // 4)
         self._dirty = torch.zeros(nblocks, dtype=torch.uint8, device=dev)
+        self.sorted = config.p2g_mode == "sorted"
+        self._work = None
+        if self.sorted:
+            self._work = torch.zeros(self._workspace_bytes(), dtype=torch.uint8, device=dev)
         self._diag = torch.zeros(8, dtype=torch.float64, device=dev)
         self._diag_host = torch.zeros(8, dtype=torch.float64).pin_memory()
         self._num_particles = 0
@@ -103,6 +110,17 @@ class MPMSolver3D:
     # ----------------------------------------------------------------- setup
     def _make_desc(self) -> nat.MpmDesc:
         return mpm_descriptor(self.config)
+
+    def _workspace_bytes(self) -> int:
+        out = nat.ctypes.c_int64(0)
+        nat.call("fsi_mpm_workspace_bytes", mpm_descriptor(self.config), self.max_particles,
+                 nat.ctypes.byref(out))
+        return int(out.value)
+
+    @property
+    def workspace(self) -> torch.Tensor | None:
+        """The sort workspace of the "sorted" P2G (None in "atomic" mode)."""
+        return self._work
 
     @staticmethod
     def lame_parameters(youngs_modulus, poisson_ratio):
@@ -238,8 +256,12 @@ class MPMSolver3D:
         if dt_value <= 0.0:
             raise ValueError("dt must be positive.")
         self._desc.dt = float(np.float32(dt_value))
-        nat.call("fsi_mpm_substep", self._desc, self._parts, nat.ptr(self._grid),
-                 nat.ptr(self._dirty), nat.stream_ptr())
+        if self.sorted:
+            nat.call("fsi_mpm_substep_sorted", self._desc, self._parts, nat.ptr(self._grid),
+                     nat.ptr(self._work), self._work.numel(), nat.stream_ptr())
+        else:
+            nat.call("fsi_mpm_substep", self._desc, self._parts, nat.ptr(self._grid),
+                     nat.ptr(self._dirty), nat.stream_ptr())
 
     def clear_particle_force(self) -> None:
         self._force[:, : self._num_particles].zero_()
