@@ -4,25 +4,28 @@
 // Every substep re-sorts the particles by base cell b = trunc(x / dx - 0.5) and then sums
 // each grid node's contributions in one fixed order, so the result does not depend on
 // thread scheduling:
-//   1. count:   per particle, its base cell's slot (atomic) and its 8^3 cell tile's count.
-//   2. tiles:   one block scans the tile counts (tile starts), lists the non-empty cell tiles
-//               and the node tiles they touch, and resets the counters for the next substep.
-//   3. cells:   per non-empty tile, a block scans its 512 cell counts (cell starts).
-//   4. scatter: per particle, its index into its cell's range (arrival order).
-//   5. prepare: per particle, its rank in the cell (ascending particle index) gives its
-//               sorted position; the coupling force (interpolated fluid velocity, penalty,
-//               clipping), F <- (I + dt C) F, the stress and the affine term are computed
-//               and the particle's terms (weights, affine, momentum, force, valid weight)
-//               are written to the payload at the sorted position.
-//   6. tile:    one block per 8^3 node tile streams the 10 x-planes of its 10^3-cell region
-//               (the tile's cells and two layers below it). For each non-empty cell a warp
-//               forms the 27 cell partials S_b(o), lane o summing the cell's particles in
-//               ascending index; then each tile node adds its partials in ascending cell
-//               index into a ring of three node planes in shared memory. A completed node
-//               plane is stored with plain stores: momentum/mass to the grid and the
-//               reaction force / solid fraction to the lattice accumulator. No atomics, and
-//               no grid clear: the tiles write every node any stencil touches.
-//   7. g2p:     grid update and G2P per particle in sorted order (compact CTA boxes).
+//   1. count:    per particle, its base cell's slot (atomic), its 8^3 cell tile's count and a
+//                mark on the node tiles its stencil touches.
+//   2. tiles:    a two-pass scan of the tile counts (tile starts); the non-empty cell tiles and
+//                the marked node tiles are listed, and counts and marks reset for the next
+//                substep.
+//   3. cells:    per non-empty tile, a block scans its 512 cell counts (cell starts).
+//   4. scatter:  per particle, its index into its cell's range (arrival order).
+//   5. prepare:  per particle, its rank in the cell (ascending particle index) gives its
+//                sorted position; the coupling force (interpolated fluid velocity, penalty,
+//                clipping), F <- (I + dt C) F, the stress and the affine term are computed
+//                and the particle's terms (weights, affine, momentum, force, valid weight)
+//                are written to the payload at the sorted position.
+//   6. partials: per non-empty cell b and stencil offset o, the sum of the cell's particles'
+//                contributions to node b + o in ascending particle index (and, coupled, the
+//                reaction / solid-fraction sum of its coupled particles): one block per
+//                non-empty cell tile, a warp per z-run of three cells, particles staged in
+//                shared memory by asynchronous copies one chunk ahead of the arithmetic.
+//   7. nodes:    each node of a touched 8^3 node tile adds its cells' partials in ascending
+//                cell index: momentum/mass into the grid from zero, the coupling partials onto
+//                the lattice accumulator. Plain stores, no atomics, and no grid clear: the
+//                node tiles cover every node a stencil touches.
+//   8. g2p:      grid update and G2P per particle (storage order, coalesced).
 // The contributions are the reference's expressions term for term; only the order of the
 // additions is fixed, and the oracle restates it (oracle/fsi_oracle.cpp, p2g_cell_order).
 #include <cuda_runtime.h>
@@ -38,9 +41,6 @@ namespace {
 
 constexpr int kT = 8;                  // tile edge (cells and nodes)
 constexpr int kTC = kT * kT * kT;      // cells per cell tile
-constexpr int kRE = kT + 2;            // region edge of a node tile, in cells
-constexpr int kRP = kRE * kRE;         // region cells per x-plane
-constexpr int kTN = kT * kT;           // nodes per x-plane of a node tile
 constexpr int kPay = 8;                // payload float4 per particle
 constexpr int kTileThreads = 256;
 constexpr int kScanThreads = 1024;
@@ -53,18 +53,22 @@ struct SortGeo {
 };
 
 struct Work {
-  int32_t* cell_count;  // [ntiles * 512], zero between substeps
-  int32_t* cell_start;  // [ntiles * 512]
-  int32_t* tile_count;  // [ntiles], zero between substeps
-  int32_t* tile_start;  // [ntiles + 1]
-  int32_t* cell_tiles;  // [ntiles] non-empty cell tiles
-  int32_t* node_tiles;  // [nntiles] node tiles touched by some stencil
-  int32_t* header;      // [0] cell tiles, [1] node tiles, [2] particles outside, [3] tile cursor
-  int32_t* key;         // [cap] tile * 512 + local cell, or -1
-  int32_t* slot;        // [cap]
-  int32_t* unsorted;    // [cap]
-  int32_t* sorted;      // [cap]
-  float4* payload;      // [cap * kPay]
+  int32_t* cell_count;    // [ntiles * 512], zero between substeps
+  int32_t* cell_start;    // [ntiles * 512]
+  int32_t* cell_row;      // [ntiles * 512] first sorted position of a non-empty cell, else -1
+  int32_t* tile_count;    // [ntiles], zero between substeps
+  int32_t* tile_start;    // [ntiles + 1]
+  int32_t* chunk_sum;     // [ntiles / 1024 + 1] tile counts per scan chunk
+  int32_t* cell_tiles;    // [ntiles] non-empty cell tiles
+  int32_t* node_tiles;    // [nntiles] node tiles touched by some stencil
+  uint8_t* node_flag;     // [nntiles] touched this substep, zero between substeps
+  int32_t* header;        // [0] cell tiles, [1] node tiles, [4] partials work cursor
+  int32_t* key;           // [cap] tile * 512 + local cell, or -1
+  int32_t* slot;          // [cap]
+  int32_t* unsorted;      // [cap]
+  float4* payload;        // [cap * kPay]
+  float4* partial;        // [cap * 27 * 2] cell partials at the cell's first sorted position
+  uint8_t* cell_coupled;  // [cap] the cell (at its first sorted position) has coupled particles
 };
 
 SortGeo sort_geo(int nx, int ny, int nz) {
@@ -92,16 +96,20 @@ size_t carve(const SortGeo& g, long long cap, char* base, Work& w) {
   };
   w.cell_count = reinterpret_cast<int32_t*>(take((size_t)g.ntiles * kTC * 4));
   w.cell_start = reinterpret_cast<int32_t*>(take((size_t)g.ntiles * kTC * 4));
+  w.cell_row = reinterpret_cast<int32_t*>(take((size_t)g.ntiles * kTC * 4));
   w.tile_count = reinterpret_cast<int32_t*>(take((size_t)g.ntiles * 4));
   w.tile_start = reinterpret_cast<int32_t*>(take((size_t)(g.ntiles + 1) * 4));
+  w.chunk_sum = reinterpret_cast<int32_t*>(take((size_t)(g.ntiles / kScanThreads + 1) * 4));
   w.cell_tiles = reinterpret_cast<int32_t*>(take((size_t)g.ntiles * 4));
   w.node_tiles = reinterpret_cast<int32_t*>(take((size_t)g.nntiles * 4));
+  w.node_flag = reinterpret_cast<uint8_t*>(take((size_t)g.nntiles));
   w.header = reinterpret_cast<int32_t*>(take(64));
   w.key = reinterpret_cast<int32_t*>(take((size_t)cap * 4));
   w.slot = reinterpret_cast<int32_t*>(take((size_t)cap * 4));
   w.unsorted = reinterpret_cast<int32_t*>(take((size_t)cap * 4));
-  w.sorted = reinterpret_cast<int32_t*>(take((size_t)cap * 4));
   w.payload = reinterpret_cast<float4*>(take((size_t)cap * kPay * sizeof(float4)));
+  w.partial = reinterpret_cast<float4*>(take((size_t)cap * 27 * 2 * sizeof(float4)));
+  w.cell_coupled = reinterpret_cast<uint8_t*>(take((size_t)cap));
   return off;
 }
 
@@ -134,12 +142,14 @@ __device__ int block_excl_scan(int v, int* ws, int* total) {
   return excl;
 }
 
-// 1. Base cell slot and tile count of every active particle; zeroes the step counters.
+// 1. Base cell slot and tile count of every active particle, and the marks on the node tiles
+// of its stencil; zeroes the step counters and the list lengths.
 __global__ void __launch_bounds__(kBlock) sort_count_kernel(Mpm m, PView P, SortGeo g, Work w,
                                                             Cnt* cnt) {
   const int p = blockIdx.x * kBlock + threadIdx.x;
   if (p == 0) {
-    w.header[2] = 0;
+    w.header[0] = 0;
+    w.header[1] = 0;
     if (cnt) { cnt->unsupported = 0; cnt->partial = 0; cnt->clipped = 0; }
   }
   int key = -1, tile = -1, slot = 0;
@@ -155,6 +165,17 @@ __global__ void __launch_bounds__(kBlock) sort_count_kernel(Mpm m, PView P, Sort
       tile = ((s0 >> 3) * g.cty + (s1 >> 3)) * g.ctz + (s2 >> 3);
       key = tile * kTC + (((s0 & 7) << 6) | ((s1 & 7) << 3) | (s2 & 7));
       slot = atomicAdd(&w.cell_count[key], 1);
+      // The node tiles of the stencil's in-grid nodes [max(b, 0), min(b + 2, n - 1)].
+      const int n3[3] = {m.nx, m.ny, m.nz};
+      int lo[3], hi[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = max(base[a], 0) >> 3;
+        hi[a] = min(base[a] + 2, n3[a] - 1) >> 3;
+      }
+      for (int ta = lo[0]; ta <= hi[0]; ++ta)
+        for (int tb = lo[1]; tb <= hi[1]; ++tb)
+          for (int tc = lo[2]; tc <= hi[2]; ++tc) w.node_flag[(ta * g.nty + tb) * g.ntz + tc] = 1;
     }
   }
   const unsigned peers = __match_any_sync(0xffffffffu, tile);
@@ -165,64 +186,50 @@ __global__ void __launch_bounds__(kBlock) sort_count_kernel(Mpm m, PView P, Sort
   }
 }
 
-// 2. Tile starts, the lists of non-empty cell tiles and touched node tiles (ascending), and
-// the reset of the tile counts and the tile cursor. One block.
-__global__ void __launch_bounds__(kScanThreads) sort_tile_scan_kernel(SortGeo g, Work w) {
+// 2a. Per chunk of 1024 cell tiles: the exclusive prefix of the tile counts within the chunk
+// (into tile_start) and the chunk's total (into chunk_sum).
+__global__ void __launch_bounds__(kScanThreads) sort_tile_scan_local_kernel(SortGeo g, Work w) {
   __shared__ int ws[32];
-  __shared__ int carry[2];
-  const int t = threadIdx.x;
-  if (t == 0) { carry[0] = 0; carry[1] = 0; }
-  __syncthreads();
-  // Cell tiles, in chunks of one entry per thread.
-  for (int base = 0; base < g.ntiles; base += kScanThreads) {
-    const int i = base + t;
-    const int c = i < g.ntiles ? w.tile_count[i] : 0;
-    int tot, tot_a;
-    const int ex = block_excl_scan(c, ws, &tot);
-    const int ea = block_excl_scan(c > 0 ? 1 : 0, ws, &tot_a);
-    if (i < g.ntiles) {
-      w.tile_start[i] = carry[0] + ex;
-      if (c > 0) w.cell_tiles[carry[1] + ea] = i;
-      w.tile_count[i] = 0;
-    }
-    __syncthreads();
-    if (t == 0) { carry[0] += tot; carry[1] += tot_a; }
-    __syncthreads();
-  }
-  if (t == 0) {
-    w.tile_start[g.ntiles] = carry[0];
-    w.header[0] = carry[1];
-    w.header[3] = 0;
-    carry[1] = 0;
-  }
-  __syncthreads();
-  // Node tile (a, b, c) receives from cell tiles (a..a+1, b..b+1, c..c+1).
-  for (int base = 0; base < g.nntiles; base += kScanThreads) {
-    const int i = base + t;
-    int act = 0;
-    if (i < g.nntiles) {
-      const int a = i / (g.nty * g.ntz), b = (i / g.ntz) % g.nty, c = i % g.ntz;
-      for (int da = 0; da < 2; ++da)
-        for (int db = 0; db < 2; ++db)
-          for (int dc = 0; dc < 2; ++dc) {
-            const int ta = a + da, tb = b + db, tc = c + dc;
-            if (ta >= g.ctx || tb >= g.cty || tc >= g.ctz) continue;
-            const int ti = (ta * g.cty + tb) * g.ctz + tc;
-            act |= w.tile_start[ti + 1] > w.tile_start[ti];
-          }
-    }
-    int tot;
-    const int ex = block_excl_scan(act, ws, &tot);
-    if (act) w.node_tiles[carry[1] + ex] = i;
-    __syncthreads();
-    if (t == 0) carry[1] += tot;
-    __syncthreads();
-  }
-  if (t == 0) w.header[1] = carry[1];
+  const int i = blockIdx.x * kScanThreads + threadIdx.x;
+  const int c = i < g.ntiles ? w.tile_count[i] : 0;
+  int tot;
+  const int ex = block_excl_scan(c, ws, &tot);
+  if (i < g.ntiles) w.tile_start[i] = ex;
+  if (threadIdx.x == 0) w.chunk_sum[blockIdx.x] = tot;
 }
 
-// 3. Cell starts of each non-empty cell tile (one block of 512 threads per tile); the cell
-// counts are reset for the next substep.
+// 2b. Tile starts = chunk offset + local prefix (the last block also writes the total); the
+// non-empty cell tiles are listed in arrival order (the list only schedules work) and the
+// tile counts reset.
+__global__ void __launch_bounds__(kScanThreads) sort_tile_scan_global_kernel(SortGeo g, Work w) {
+  __shared__ int off;
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int b = 0; b < (int)blockIdx.x; ++b) o += w.chunk_sum[b];
+    off = o;
+    if (blockIdx.x == gridDim.x - 1) w.tile_start[g.ntiles] = o + w.chunk_sum[blockIdx.x];
+  }
+  __syncthreads();
+  const int i = blockIdx.x * kScanThreads + threadIdx.x;
+  if (i >= g.ntiles) return;
+  const int c = w.tile_count[i];
+  w.tile_start[i] += off;
+  if (c > 0) w.cell_tiles[atomicAdd(&w.header[0], 1)] = i;
+  w.tile_count[i] = 0;
+}
+
+// 2c. The node tiles some stencil touched are listed (arrival order) and their marks reset;
+// the partials kernel's work cursor is reset.
+__global__ void __launch_bounds__(kBlock) sort_node_tiles_kernel(SortGeo g, Work w) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i == 0) w.header[4] = 0;
+  if (i >= g.nntiles || w.node_flag[i] == 0) return;
+  w.node_flag[i] = 0;
+  w.node_tiles[atomicAdd(&w.header[1], 1)] = i;
+}
+
+// 3. Cell starts (and the first sorted position of each non-empty cell) of each non-empty
+// cell tile, one block of 512 threads per tile; the cell counts are reset.
 __global__ void __launch_bounds__(kTC) sort_cell_scan_kernel(Work w) {
   __shared__ int ws[32];
   const int n = w.header[0];
@@ -232,7 +239,9 @@ __global__ void __launch_bounds__(kTC) sort_cell_scan_kernel(Work w) {
     const int c = w.cell_count[idx];
     int tot;
     const int ex = block_excl_scan(c, ws, &tot);
-    w.cell_start[idx] = w.tile_start[t] + ex;
+    const int start = w.tile_start[t] + ex;
+    w.cell_start[idx] = start;
+    w.cell_row[idx] = c > 0 ? start : -1;
     w.cell_count[idx] = 0;
   }
 }
@@ -253,7 +262,7 @@ __device__ __forceinline__ int cell_end(const Work& w, int key) {
 // Payload (float4 x 8): (wx0 wx1 wx2 wy0) (wy1 wy2 wz0 wz1) (wz2 fx0 fx1 fx2) (A0..A3)
 // (A4..A7) (A8 mv0 mv1 mv2) (f0 f1 f2 m) (valid vol coupled 0).
 template <bool kCoupled, bool kGatherAhead>
-__global__ void __launch_bounds__(kBlock) sorted_prepare_kernel(Mpm m, PView P, SortGeo g, Work w,
+__global__ void __launch_bounds__(kBlock) sorted_prepare_kernel(Mpm m, PView P, Work w,
                                                                 ForceArgs fa) {
   const int p = blockIdx.x * kBlock + threadIdx.x;
   const long long cap = m.cap;
@@ -263,16 +272,13 @@ __global__ void __launch_bounds__(kBlock) sorted_prepare_kernel(Mpm m, PView P, 
       if (kCoupled) { P.fp[p] = 0.f; P.fp[cap + p] = 0.f; P.fp[2 * cap + p] = 0.f; }
     } else {
       const int key = w.key[p];
-      int pos;
+      int pos = -1;
       if (key >= 0) {
         const int start = w.cell_start[key], end = cell_end(w, key);
         int rank = 0;
         for (int s = start; s < end; ++s) rank += w.unsorted[s] < p;
         pos = start + rank;
-      } else {
-        pos = w.tile_start[g.ntiles] + atomicAdd(&w.header[2], 1);
       }
-      w.sorted[pos] = p;
       float pf[3], valid = 0.f;
       bool coupled = false;
       if (kCoupled) {
@@ -321,182 +327,294 @@ __global__ void __launch_bounds__(kBlock) sorted_prepare_kernel(Mpm m, PView P, 
   }
 }
 
-template <bool kCoupled>
-struct TileSmem {
-  static constexpr int kNC = kCoupled ? 2 : 1;  // float4 per partial: grid (+ coupling)
-  static constexpr size_t kBytes =
-      (size_t)(kRP * 27 + 3 * kTN) * kNC * sizeof(float4) + (3 * kRP + 4) * sizeof(int);
-};
-
 __device__ __forceinline__ float sel3(int i, float a, float b, float c) {
   return i == 0 ? a : (i == 1 ? b : c);
 }
 
-// 6. The scatter of one 8^3 node tile per loop iteration (tiles taken from a cursor).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Particles per cell and chunk staged in shared memory by the partials kernel, and the
+// float4 slots per staged particle (the payload's 8 plus one, which with the extra slot per
+// cell area puts the three cells of a warp on different shared-memory banks).
+constexpr int kChunk = 8;
+constexpr int kSlot = kPay + 1;
+constexpr int kGroupF4 = kChunk * kSlot + 1;  // one cell's staging area, in float4
+constexpr int kWarpBufF4 = 3 * kGroupF4;      // three cells
+constexpr int kPartialWarps = kTileThreads / 32;
+constexpr size_t kPartialSmem =
+    (size_t)2 * kPartialWarps * kWarpBufF4 * sizeof(float4) + kTC * sizeof(int2);
+
+// One triple of cells of a cell tile: a z-run (cells lz = 3 r, 3 r + 1, 3 r + 2 of row
+// (lx, ly)); the lanes 9 g .. 9 g + 8 of a warp serve cell g of the triple.
+struct Triple {
+  int start, count;  // this lane's cell (count 0: no cell or empty)
+  int maxcount;      // warp-wide
+};
+
+// cells: the tile's (start, count) per local cell, staged in shared memory.
+__device__ __forceinline__ Triple load_triple(const int2* cells, int tr, int grp) {
+  Triple t;
+  t.start = 0;
+  t.count = 0;
+  const int row = tr / 3, lz = 3 * (tr % 3) + grp;
+  if (grp < 3 && lz < kT) {
+    const int2 c = cells[row * kT + lz];
+    t.start = c.x;
+    t.count = c.y;
+  }
+  t.maxcount = __reduce_max_sync(0xffffffffu, t.count);
+  return t;
+}
+
+// Stages particles [chunk * kChunk, ...) of the warp's three cells into buf (all lanes copy).
+__device__ __forceinline__ void stage_chunk(const Work& w, float4* buf, int lane, int start,
+                                            int count, int chunk) {
+  const int lo = chunk * kChunk;
+  const int n_own = max(0, min(count - lo, kChunk));
+  int n[3], st[3];
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {
+    n[g] = __shfl_sync(0xffffffffu, n_own, 9 * g);
+    st[g] = __shfl_sync(0xffffffffu, start, 9 * g) + lo;
+  }
+  const int total = (n[0] + n[1] + n[2]) * kPay;
+  for (int i = lane; i < total; i += 32) {
+    int g = 0, r = i;
+    if (r >= n[0] * kPay) {
+      r -= n[0] * kPay;
+      g = 1;
+      if (r >= n[1] * kPay) { r -= n[1] * kPay; g = 2; }
+    }
+    const int part = r / kPay, comp = r - part * kPay;
+    cp_async16(buf + g * kGroupF4 + part * kSlot + comp,
+               w.payload + (long long)(st[g] + part) * kPay + comp);
+  }
+  cp_async_commit();
+}
+
+// 6. Cell partials: for every non-empty cell b and stencil offset o, the sum over the cell's
+// particles (ascending index, from zero) of their contribution to node b + o, written to
+// partial[cell_row(b) * 27 + o]; the coupling partial (reaction, solid fraction) sums the
+// cell's coupled particles. A block takes non-empty cell tiles from a cursor; a warp handles
+// z-runs of three cells, their particles staged in shared memory with asynchronous copies one
+// chunk ahead of the arithmetic. Lane (g, ox, oy) forms the partials of offsets (ox, oy, 0..2)
+// of cell g, which share the x and y factors of the weight and the first two terms of the
+// affine product.
 template <bool kCoupled>
-__global__ void __launch_bounds__(kTileThreads, 2) sorted_tile_kernel(Mpm m, SortGeo g, Work w,
-                                                                      float4* __restrict__ grid,
-                                                                      fsi_coupling_desc cd,
-                                                                      const uint32_t* __restrict__ flags,
-                                                                      float4* __restrict__ accum) {
-  constexpr int NC = TileSmem<kCoupled>::kNC;
+__global__ void __launch_bounds__(kTileThreads, kCoupled ? 2 : 3)
+    sorted_partials_kernel(Mpm m, Work w, fsi_coupling_desc cd) {
+  constexpr int NC = kCoupled ? 2 : 1;
   extern __shared__ float4 smem[];
-  float4* S = smem;                                            // [kRP * 27][NC]
-  float4* ring = S + kRP * 27 * NC;                            // [3 * kTN][NC]
-  int* cstart = reinterpret_cast<int*>(ring + 3 * kTN * NC);   // [kRP]
-  int* ccount = cstart + kRP;                                  // [kRP]
-  int* cflag = ccount + kRP;                                   // [kRP]
-  int* cursor = cflag + kRP;                                   // [1]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  __shared__ int next_tile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float4* bufs = smem + (size_t)warp * 2 * kWarpBufF4;
+  int2* cells = reinterpret_cast<int2*>(smem + (size_t)2 * kPartialWarps * kWarpBufF4);
+  const int grp = lane / 9, r9 = lane - 9 * grp;
+  const int ox = r9 / 3, oy = r9 - 3 * ox;
+  const int gsel = grp < 3 ? grp : 0;
+  const int ntiles = w.header[0];
+  constexpr int kTriples = kT * kT * 3;  // (lx, ly) rows x three z-runs
   for (;;) {
-    if (tid == 0) cursor[0] = atomicAdd(&w.header[3], 1);
+    __syncthreads();  // the previous tile's cell table and cursor are no longer read
+    if (threadIdx.x == 0) next_tile = atomicAdd(&w.header[4], 1);
     __syncthreads();
-    const int it = cursor[0];
-    if (it >= w.header[1]) break;
-    const int t = w.node_tiles[it];
-    const int n0x = (t / (g.nty * g.ntz)) * kT, n0y = ((t / g.ntz) % g.nty) * kT,
-              n0z = (t % g.ntz) * kT;
-    // This thread's node column (Phase B / init / flush): yz = tid % 64.
-    const int yz = tid & (kTN - 1);
-    const int nj = n0y + (yz >> 3), nk = n0z + (yz & 7);
-    const bool col_in = nj < m.ny && nk < m.nz;
-    for (int ci = n0x - 2; ci <= n0x + kT - 1; ++ci) {
-      // Node plane ci + 2 receives its first partials from cell plane ci.
-      if (tid < kTN) {
-        const int ni = ci + 2;
-        if (ni >= n0x && ni < n0x + kT && ni < m.nx && col_in) {
-          float4* r = ring + ((ni % 3) * kTN + yz) * NC;
-          r[0] = zero4;
-          if (kCoupled) r[1] = accum[node_index(m, ni, nj, nk)];
-        }
-      }
-      // Particle ranges of the region's cells in this plane.
-      if (tid < kRP) {
-        const int cj = n0y - 2 + tid / kRE, ck = n0z - 2 + tid % kRE;
-        int start = 0, count = 0;
-        const int s0 = ci + 2, s1 = cj + 2, s2 = ck + 2;
-        if (s0 < m.nx + 2 && s1 < m.ny + 2 && s2 < m.nz + 2) {
-          const int tile = ((s0 >> 3) * g.cty + (s1 >> 3)) * g.ctz + (s2 >> 3);
-          if (w.tile_start[tile + 1] > w.tile_start[tile]) {
-            const int key = tile * kTC + (((s0 & 7) << 6) | ((s1 & 7) << 3) | (s2 & 7));
-            start = w.cell_start[key];
-            count = cell_end(w, key) - start;
-          }
-        }
-        cstart[tid] = start;
-        ccount[tid] = count;
-        cflag[tid] = 0;
-      }
-      __syncthreads();
-      // Phase A: cell partials, one warp per cell, lane o = 9 ox + 3 oy + oz.
-      {
-        const int ox = lane / 9, oy = (lane / 3) % 3, oz = lane % 3;
-        const int ni = ci + ox;
-        const bool ni_in = lane < 27 && ni >= n0x && ni < n0x + kT && ni < m.nx;
-        for (int q = warp; q < kRP; q += kTileThreads / 32) {
-          const int cnt = ccount[q];
-          if (cnt == 0) continue;
-          const int cj = n0y - 2 + q / kRE, ck = n0z - 2 + q % kRE;
-          const int nnj = cj + oy, nnk = ck + oz;
-          const bool in_tile = ni_in && nnj >= n0y && nnj < n0y + kT && nnj < m.ny &&
-                               nnk >= n0z && nnk < n0z + kT && nnk < m.nz;
-          bool fluid = false;
-          if (kCoupled && in_tile) fluid = !(flags[node_index(m, ni, nnj, nnk)] & kFlagSolid);
-          float am[4] = {0.f, 0.f, 0.f, 0.f}, ac[4] = {0.f, 0.f, 0.f, 0.f};
-          bool any_coupled = false;
-          const float4* pl = w.payload + (long long)cstart[q] * kPay;
-          for (int s = 0; s < cnt; ++s, pl += kPay) {
-            float4 r[kPay];
-#pragma unroll
-            for (int c = 0; c < kPay; ++c) r[c] = pl[c];
-            const bool coupled = kCoupled && r[7].z != 0.f;
-            any_coupled |= coupled;
-            if (!in_tile) continue;
-            const float wx = sel3(ox, r[0].x, r[0].y, r[0].z);
-            const float wy = sel3(oy, r[0].w, r[1].x, r[1].y);
-            const float wz = sel3(oz, r[1].z, r[1].w, r[2].x);
-            const float wgt = __fmul_rn(__fmul_rn(wx, wy), wz);
-            const float d0 = __fmul_rn(__fsub_rn((float)ox, r[2].y), m.dx);
-            const float d1 = __fmul_rn(__fsub_rn((float)oy, r[2].z), m.dx);
-            const float d2 = __fmul_rn(__fsub_rn((float)oz, r[2].w), m.dx);
-            const float A[9] = {r[3].x, r[3].y, r[3].z, r[3].w, r[4].x, r[4].y, r[4].z, r[4].w, r[5].x};
-            const float mv[3] = {r[5].y, r[5].z, r[5].w};
-            const float pf[3] = {r[6].x, r[6].y, r[6].z};
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-              const float ad = dot3r(A[3 * a], A[3 * a + 1], A[3 * a + 2], d0, d1, d2);
-              const float dtf = __fmul_rn(m.dt, pf[a]);
-              am[a] = __fadd_rn(am[a], __fmul_rn(wgt, __fadd_rn(__fadd_rn(mv[a], ad), dtf)));
-            }
-            am[3] = __fadd_rn(am[3], __fmul_rn(wgt, r[6].w));
-            if (kCoupled && coupled && fluid) {
-              const float4 tc = coupling_spread_terms(cd, wgt, r[7].x, pf, r[7].y);
-              ac[0] = __fadd_rn(ac[0], tc.x);
-              ac[1] = __fadd_rn(ac[1], tc.y);
-              ac[2] = __fadd_rn(ac[2], tc.z);
-              if (cd.build_fraction) ac[3] = __fadd_rn(ac[3], tc.w);
-            }
-          }
-          if (in_tile) {
-            S[(q * 27 + lane) * NC] = make_float4(am[0], am[1], am[2], am[3]);
-            if (kCoupled) S[(q * 27 + lane) * NC + 1] = make_float4(ac[0], ac[1], ac[2], ac[3]);
-          }
-          if (lane == 0 && any_coupled) cflag[q] = 1;
-        }
-      }
-      __syncthreads();
-      // Phase B: node (ci + ox, nj, nk) adds the partials of its 9 cells in plane ci in
-      // ascending cell index, i.e. (oy, oz) from (2, 2) down to (0, 0).
-      if (tid < 3 * kTN) {
-        const int ox = tid / kTN, ni = ci + ox;
-        if (ni >= n0x && ni < n0x + kT && ni < m.nx && col_in) {
-          float4* r = ring + ((ni % 3) * kTN + yz) * NC;
-          float4 rm = r[0], rc = kCoupled ? r[1] : zero4;
-          const bool nfluid = kCoupled && !(flags[node_index(m, ni, nj, nk)] & kFlagSolid);
-          for (int oy = 2; oy >= 0; --oy)
-            for (int oz = 2; oz >= 0; --oz) {
-              const int q = ((yz >> 3) + 2 - oy) * kRE + ((yz & 7) + 2 - oz);
-              const int o = ox * 9 + oy * 3 + oz;
-              if (ccount[q] > 0) {
-                const float4 sm = S[(q * 27 + o) * NC];
-                rm.x = __fadd_rn(rm.x, sm.x);
-                rm.y = __fadd_rn(rm.y, sm.y);
-                rm.z = __fadd_rn(rm.z, sm.z);
-                rm.w = __fadd_rn(rm.w, sm.w);
-              }
-              if (kCoupled && nfluid && cflag[q] != 0) {
-                const float4 sc = S[(q * 27 + o) * NC + 1];
-                rc.x = __fadd_rn(rc.x, sc.x);
-                rc.y = __fadd_rn(rc.y, sc.y);
-                rc.z = __fadd_rn(rc.z, sc.z);
-                if (cd.build_fraction) rc.w = __fadd_rn(rc.w, sc.w);
-              }
-            }
-          r[0] = rm;
-          if (kCoupled) r[1] = rc;
-        }
-      }
-      __syncthreads();
-      // Node plane ci is complete: store it.
-      if (tid < kTN && ci >= n0x && ci < m.nx && col_in) {
-        const float4* r = ring + ((ci % 3) * kTN + yz) * NC;
-        const long long node = node_index(m, ci, nj, nk);
-        grid[node] = r[0];
-        if (kCoupled) accum[node] = r[1];
-      }
+    const int ti = next_tile;
+    if (ti >= ntiles) break;
+    const int tile = w.cell_tiles[ti];
+    for (int c = threadIdx.x; c < kTC; c += kTileThreads) {
+      const int key = tile * kTC + c;
+      const int st = w.cell_start[key];
+      cells[c] = make_int2(st, cell_end(w, key) - st);
     }
     __syncthreads();
+    // Job sequence of this warp: (triple, chunk) pairs of its non-empty triples, in order.
+    int tr = warp;
+    Triple cur;
+    for (; tr < kTriples; tr += kPartialWarps) {
+      cur = load_triple(cells, tr, grp);
+      if (cur.maxcount > 0) break;
+    }
+    if (tr >= kTriples) continue;
+    int chunk = 0, slot = 0;
+    stage_chunk(w, bufs, lane, cur.start, cur.count, 0);
+    float am[3][4], ac[3][4];
+#pragma unroll
+    for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+      for (int a = 0; a < 4; ++a) { am[oz][a] = 0.f; ac[oz][a] = 0.f; }
+    bool any_coupled = false;
+    for (;;) {
+      // The next job, whose copies go out before this job's arithmetic.
+      int ntr = tr, nchunk = chunk + 1;
+      Triple nxt = cur;
+      if (nchunk * kChunk >= cur.maxcount) {
+        nchunk = 0;
+        for (ntr = tr + kPartialWarps; ntr < kTriples; ntr += kPartialWarps) {
+          nxt = load_triple(cells, ntr, grp);
+          if (nxt.maxcount > 0) break;
+        }
+      }
+      const bool more = ntr < kTriples;
+      if (more) stage_chunk(w, bufs + (slot ^ 1) * kWarpBufF4, lane, nxt.start, nxt.count, nchunk);
+      if (more) cp_async_wait<1>(); else cp_async_wait<0>();
+      __syncwarp();
+      const float4* gb = bufs + slot * kWarpBufF4 + gsel * kGroupF4;
+      const int n_own = grp < 3 ? max(0, min(cur.count - chunk * kChunk, kChunk)) : 0;
+      for (int s = 0; s < n_own; ++s) {
+        const float4* r = gb + s * kSlot;
+        const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4], r5 = r[5], r6 = r[6];
+        const float4 r7 = kCoupled ? r[7] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool coupled = kCoupled && r7.z != 0.f;
+        any_coupled |= coupled;
+        const float wxy = __fmul_rn(sel3(ox, r0.x, r0.y, r0.z), sel3(oy, r0.w, r1.x, r1.y));
+        const float wz[3] = {r1.z, r1.w, r2.x};
+        const float d0 = __fmul_rn(__fsub_rn((float)ox, r2.y), m.dx);
+        const float d1 = __fmul_rn(__fsub_rn((float)oy, r2.z), m.dx);
+        const float A[9] = {r3.x, r3.y, r3.z, r3.w, r4.x, r4.y, r4.z, r4.w, r5.x};
+        const float mv[3] = {r5.y, r5.z, r5.w};
+        const float pf[3] = {r6.x, r6.y, r6.z};
+        float pa[3], dtf[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          // dot3r's ((A0 d0 + A1 d1) + A2 d2): the first two terms are shared by the 3 oz.
+          pa[a] = __fadd_rn(__fmul_rn(A[3 * a], d0), __fmul_rn(A[3 * a + 1], d1));
+          dtf[a] = __fmul_rn(m.dt, pf[a]);
+        }
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz) {
+          const float wgt = __fmul_rn(wxy, wz[oz]);
+          const float d2 = __fmul_rn(__fsub_rn((float)oz, r2.w), m.dx);
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float ad = __fadd_rn(pa[a], __fmul_rn(A[3 * a + 2], d2));
+            am[oz][a] = __fadd_rn(am[oz][a], __fmul_rn(wgt, __fadd_rn(__fadd_rn(mv[a], ad), dtf[a])));
+          }
+          am[oz][3] = __fadd_rn(am[oz][3], __fmul_rn(wgt, r6.w));
+          if (kCoupled && coupled) {
+            const float4 tc = coupling_spread_terms(cd, wgt, r7.x, pf, r7.y);
+            ac[oz][0] = __fadd_rn(ac[oz][0], tc.x);
+            ac[oz][1] = __fadd_rn(ac[oz][1], tc.y);
+            ac[oz][2] = __fadd_rn(ac[oz][2], tc.z);
+            ac[oz][3] = __fadd_rn(ac[oz][3], tc.w);
+          }
+        }
+      }
+      __syncwarp();  // the slot is restaged two jobs from now
+      if (nchunk == 0) {
+        // Last chunk of this triple: store the partials of this lane's cell.
+        if (grp < 3 && cur.count > 0) {
+          float4* out = w.partial + ((long long)cur.start * 27 + 9 * ox + 3 * oy) * NC;
+#pragma unroll
+          for (int oz = 0; oz < 3; ++oz) {
+            out[oz * NC] = make_float4(am[oz][0], am[oz][1], am[oz][2], am[oz][3]);
+            if (kCoupled) out[oz * NC + 1] = make_float4(ac[oz][0], ac[oz][1], ac[oz][2], ac[oz][3]);
+          }
+          if (kCoupled && r9 == 0) w.cell_coupled[cur.start] = any_coupled ? 1 : 0;
+        }
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+          for (int a = 0; a < 4; ++a) { am[oz][a] = 0.f; ac[oz][a] = 0.f; }
+        any_coupled = false;
+      }
+      if (!more) break;
+      tr = ntr;
+      chunk = nchunk;
+      cur = nxt;
+      slot ^= 1;
+    }
   }
 }
 
-// 7. Grid update + G2P of the particles in sorted order.
-__global__ void __launch_bounds__(kBlock) sorted_g2p_kernel(Mpm m, PView P, SortGeo g, Work w,
+// 7. Node sums: every node of a touched 8^3 node tile (one thread each) adds the partials of
+// its non-empty cells b = node - o in ascending cell index (o from (2,2,2) down to (0,0,0)):
+// momentum and mass from zero into the grid, and on fluid nodes the coupling partials of
+// cells with coupled particles onto the accumulator's current value (the solid fraction
+// only when it is being built). Plain stores: each node belongs to one block.
+template <bool kCoupled>
+__global__ void __launch_bounds__(kTC, 2) sorted_nodes_kernel(Mpm m, SortGeo g, Work w,
+                                                              float4* __restrict__ grid,
+                                                              fsi_coupling_desc cd,
+                                                              const uint32_t* __restrict__ flags,
+                                                              float4* __restrict__ accum) {
+  constexpr int NC = kCoupled ? 2 : 1;
+  constexpr int kRE = kT + 2;  // the region of a node tile: (kT + 2)^3 cells
+  __shared__ int region[kRE * kRE * kRE];  // partial row of each region cell, or -1
+  const int ntiles = w.header[1];
+  for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
+    const int t = w.node_tiles[it];
+    const int a0 = (t / (g.nty * g.ntz)) * kT, b0 = ((t / g.ntz) % g.nty) * kT, c0 = (t % g.ntz) * kT;
+    __syncthreads();  // the previous tile's region is no longer read
+    // Region cell (x, y, z) has shifted coordinates (a0 + x, b0 + y, c0 + z): base cell
+    // (a0 - 2 + x, ...).
+    for (int r = threadIdx.x; r < kRE * kRE * kRE; r += kTC) {
+      const int s0 = a0 + r / (kRE * kRE), s1 = b0 + (r / kRE) % kRE, s2 = c0 + r % kRE;
+      int row = -1;
+      if (s0 < m.nx + 2 && s1 < m.ny + 2 && s2 < m.nz + 2) {
+        const int tile = ((s0 >> 3) * g.cty + (s1 >> 3)) * g.ctz + (s2 >> 3);
+        if (w.tile_start[tile + 1] > w.tile_start[tile])
+          row = w.cell_row[tile * kTC + (((s0 & 7) << 6) | ((s1 & 7) << 3) | (s2 & 7))];
+      }
+      region[r] = row;
+    }
+    __syncthreads();
+    const int x = threadIdx.x >> 6, y = (threadIdx.x >> 3) & 7, z = threadIdx.x & 7;
+    const int ni = a0 + x, nj = b0 + y, nk = c0 + z;
+    if (ni >= m.nx || nj >= m.ny || nk >= m.nz) continue;
+    const long long node = node_index(m, ni, nj, nk);
+    float4 am = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 ac = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool fluid = false;
+    if (kCoupled) {
+      ac = accum[node];
+      fluid = !(flags[node] & kFlagSolid);
+    }
+    // Cell node - o sits at region (x + 2 - i, y + 2 - j, z + 2 - k). The partials of a z-run
+    // of three cells are loaded together, then added in order.
+#pragma unroll
+    for (int ij = 8; ij >= 0; --ij) {
+      const int i = ij / 3, j = ij % 3;
+      const int* rr = region + ((x + 2 - i) * kRE + (y + 2 - j)) * kRE + z;
+      const int rows[3] = {rr[0], rr[1], rr[2]};  // k = 2, 1, 0
+      float4 pm[3];
+#pragma unroll
+      for (int t3 = 0; t3 < 3; ++t3)
+        pm[t3] = rows[t3] >= 0 ? w.partial[((long long)rows[t3] * 27 + 3 * ij + 2 - t3) * NC]
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int t3 = 0; t3 < 3; ++t3) {
+        if (rows[t3] < 0) continue;
+        am.x = __fadd_rn(am.x, pm[t3].x);
+        am.y = __fadd_rn(am.y, pm[t3].y);
+        am.z = __fadd_rn(am.z, pm[t3].z);
+        am.w = __fadd_rn(am.w, pm[t3].w);
+        if (kCoupled && fluid && w.cell_coupled[rows[t3]]) {
+          const float4 sc = w.partial[((long long)rows[t3] * 27 + 3 * ij + 2 - t3) * NC + 1];
+          ac.x = __fadd_rn(ac.x, sc.x);
+          ac.y = __fadd_rn(ac.y, sc.y);
+          ac.z = __fadd_rn(ac.z, sc.z);
+          if (cd.build_fraction) ac.w = __fadd_rn(ac.w, sc.w);
+        }
+      }
+    }
+    grid[node] = am;
+    if (kCoupled) accum[node] = ac;
+  }
+}
+
+// 8. Grid update + G2P per particle, in storage order (coalesced particle reads and writes;
+// the CTA's stencil box is staged in shared memory when it fits).
+__global__ void __launch_bounds__(kBlock) sorted_g2p_kernel(Mpm m, PView P,
                                                             const float4* __restrict__ grid) {
-  const int s = blockIdx.x * kBlock + threadIdx.x;
-  const int total = w.tile_start[g.ntiles] + w.header[2];
-  const int p = s < total ? w.sorted[s] : m.n;  // m.n: no particle
-  g2p_body(m, P, grid, p);
+  g2p_body(m, P, grid, blockIdx.x * kBlock + threadIdx.x);
 }
 
 int num_sms() {
@@ -512,16 +630,17 @@ int num_sms() {
   return sms;
 }
 
-// Opts the tile kernel into its dynamic shared memory, once per device.
+// Opts the partials kernel into its dynamic shared memory, once per device.
 template <bool kCoupled>
-int tile_smem_attr() {
+int partials_smem_attr() {
   static bool done[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("cudaGetDevice");
   if (dev < 0 || dev >= 64 || !done[dev]) {
-    if (cudaFuncSetAttribute(sorted_tile_kernel<kCoupled>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)TileSmem<kCoupled>::kBytes) != cudaSuccess)
-      return check_launch("cudaFuncSetAttribute(sorted_tile_kernel)");
+    if (cudaFuncSetAttribute(sorted_partials_kernel<kCoupled>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPartialSmem) !=
+        cudaSuccess)
+      return check_launch("cudaFuncSetAttribute(sorted_partials_kernel)");
     if (dev >= 0 && dev < 64) done[dev] = true;
   }
   return FSI_OK;
@@ -539,17 +658,22 @@ int check_workspace(const Mpm& m, void* work, int64_t work_bytes, SortGeo& g, Wo
   return FSI_OK;
 }
 
-// The seven launches of a sorted substep (kCoupled: with the coupling folded in).
+// The ten launches of a sorted substep (kCoupled: with the coupling folded in).
 template <bool kCoupled>
 int sorted_substep(const Mpm& m, const PView& P, const SortGeo& g, const Work& w, float4* grid,
                    const ForceArgs& fa, cudaStream_t s) {
-  if (int e = tile_smem_attr<kCoupled>()) return e;
+  if (int e = partials_smem_attr<kCoupled>()) return e;
   const unsigned pg = grid_for(m.n, kBlock);
+  const int sms = num_sms();
   sort_count_kernel<<<pg, kBlock, 0, s>>>(m, P, g, w, kCoupled ? fa.cnt : nullptr);
   if (int e = check_launch("sort_count_kernel")) return e;
-  sort_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(g, w);
-  if (int e = check_launch("sort_tile_scan_kernel")) return e;
-  const int sms = num_sms();
+  const unsigned chunks = (unsigned)((g.ntiles + kScanThreads - 1) / kScanThreads);
+  sort_tile_scan_local_kernel<<<chunks, kScanThreads, 0, s>>>(g, w);
+  if (int e = check_launch("sort_tile_scan_local_kernel")) return e;
+  sort_tile_scan_global_kernel<<<chunks, kScanThreads, 0, s>>>(g, w);
+  if (int e = check_launch("sort_tile_scan_global_kernel")) return e;
+  sort_node_tiles_kernel<<<grid_for(g.nntiles, kBlock), kBlock, 0, s>>>(g, w);
+  if (int e = check_launch("sort_node_tiles_kernel")) return e;
   sort_cell_scan_kernel<<<g.ntiles < 4 * sms ? g.ntiles : 4 * sms, kTC, 0, s>>>(w);
   if (int e = check_launch("sort_cell_scan_kernel")) return e;
   sort_scatter_kernel<<<pg, kBlock, 0, s>>>(m.n, w);
@@ -557,15 +681,17 @@ int sorted_substep(const Mpm& m, const PView& P, const SortGeo& g, const Work& w
   // Few particles (under two CTAs per SM): latency-bound, so the coupling's stencil loads go
   // out together.
   if (m.n < 2 * sms * kBlock)
-    sorted_prepare_kernel<kCoupled, true><<<pg, kBlock, 0, s>>>(m, P, g, w, fa);
+    sorted_prepare_kernel<kCoupled, true><<<pg, kBlock, 0, s>>>(m, P, w, fa);
   else
-    sorted_prepare_kernel<kCoupled, false><<<pg, kBlock, 0, s>>>(m, P, g, w, fa);
+    sorted_prepare_kernel<kCoupled, false><<<pg, kBlock, 0, s>>>(m, P, w, fa);
   if (int e = check_launch("sorted_prepare_kernel")) return e;
-  const int tb = g.nntiles < 2 * sms ? g.nntiles : 2 * sms;
-  sorted_tile_kernel<kCoupled><<<tb, kTileThreads, TileSmem<kCoupled>::kBytes, s>>>(
-      m, g, w, grid, fa.c, fa.flags, fa.accum);
-  if (int e = check_launch("sorted_tile_kernel")) return e;
-  sorted_g2p_kernel<<<pg, kBlock, 0, s>>>(m, P, g, w, grid);
+  const int pb = g.ntiles < 3 * sms ? g.ntiles : 3 * sms;
+  sorted_partials_kernel<kCoupled><<<pb, kTileThreads, kPartialSmem, s>>>(m, w, fa.c);
+  if (int e = check_launch("sorted_partials_kernel")) return e;
+  const int nb = g.nntiles < 4 * sms ? g.nntiles : 4 * sms;
+  sorted_nodes_kernel<kCoupled><<<nb, kTC, 0, s>>>(m, g, w, grid, fa.c, fa.flags, fa.accum);
+  if (int e = check_launch("sorted_nodes_kernel")) return e;
+  sorted_g2p_kernel<<<pg, kBlock, 0, s>>>(m, P, grid);
   return check_launch("sorted_g2p_kernel");
 }
 
