@@ -147,10 +147,12 @@ class MPMConfig:
     # Extension (no reference counterpart): the elastic model. The reference's solver is
     # fixed-corotated (mpm3d.py:247-251); "neo_hookean" selects mu (F F^T - I) + lam ln(J) I.
     constitutive_model: Literal["fixed_corotated", "neo_hookean"] = "fixed_corotated"
-    # Extension (no reference counterpart): how P2G sums the grid. "sorted" sorts the
-    # particles by cell each substep and adds every node's contributions in a fixed order
-    # (deterministic, atomic-free); "atomic" scatters in arrival order with atomics.
-    p2g_mode: Literal["sorted", "atomic"] = "sorted"
+    # Extension (no reference counterpart): how P2G sums the grid. "atomic" (default, the
+    # faster on coupled steps) scatters through shared-memory tiles with atomics, so sums
+    # arrive in scheduling order like the reference's parallel loop; "sorted" sorts the
+    # particles by cell each substep and adds every node's contributions in one fixed order
+    # (atomic-free, bit-reproducible from run to run).
+    p2g_mode: Literal["sorted", "atomic"] = "atomic"
 
     def validate(self) -> None:
         _check_grid("MPM", self.nx, self.ny, self.nz)

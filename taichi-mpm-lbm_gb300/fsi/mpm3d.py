@@ -2,12 +2,12 @@
 
 Particles are stored as structure-of-arrays torch CUDA tensors (x, v, force
 ``[3, capacity]``; C, F ``[9, capacity]``; mass, volume, active ``[capacity]``)
-and advanced by the library's sm_103a substep. The default ("sorted" p2g_mode)
-sorts the particles by cell every substep and sums each grid node's
-contributions in a fixed order with plain stores (deterministic); "atomic"
+and advanced by the library's sm_103a substep. The default ("atomic" p2g_mode)
 scatters through shared-memory tiles with atomics and keeps the float4 grid
-all-zero between substeps by clearing only the node blocks that were touched.
-The grid update is fused into G2P in both.
+all-zero between substeps by clearing only the node blocks that were touched;
+"sorted" sorts the particles by cell every substep and sums each grid node's
+contributions in one fixed order with plain stores (bit-reproducible). The grid
+update is fused into G2P in both.
 
 Public methods, accessors and exceptions follow fsi/mpm3d.py:9-368.
 """

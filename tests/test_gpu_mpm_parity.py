@@ -2,7 +2,7 @@
 
 Bit-exact: particle-to-cell indices (trunc(x/dx - 0.5), negative positions
 included), a full substep while no rotation is involved, and every substep of the
-sorted (default) scatter against the oracle summing in the same cell order with the
+sorted scatter (p2g_mode="sorted") against the oracle summing in the same cell order with the
 device's float32 polar rotation. Tolerance: the polar rotation (float32 Newton
 iteration vs a float64 SVD) and the atomic scatter, whose grid sums arrive in a
 different order on the GPU.
@@ -189,10 +189,10 @@ def _assert_state_equal(g, o, what=""):
 
 @pytest.mark.parametrize("case", ["box", "walls", "outside", "two_bodies", "neo_hookean"])
 def test_sorted_scatter_bit_exact_against_cell_order(case):
-    """The sorted scatter (default p2g_mode) sums each node in the oracle's cell order
+    """The sorted scatter (p2g_mode="sorted") sums each node in the oracle's cell order
     (per-cell partials in ascending particle index, then ascending cell index), so with the
     device's float32 polar rotation every substep is bit-identical to the oracle."""
-    kw = dict(gravity=(0.0, -1.0e-3, 0.0), dt=1.0e-2, youngs_modulus=1000.0)
+    kw = dict(gravity=(0.0, -1.0e-3, 0.0), dt=1.0e-2, youngs_modulus=1000.0, p2g_mode="sorted")
     rng = np.random.default_rng({"box": 4, "walls": 5, "outside": 6, "two_bodies": 7,
                                  "neo_hookean": 8}[case])
     if case == "walls":
@@ -237,7 +237,8 @@ def test_sorted_scatter_bit_exact_against_cell_order(case):
 def test_sorted_scatter_repeats_bit_for_bit():
     """Two runs of the sorted scatter from the same state agree bit for bit, inactive
     particles included (the atomic scatter's sums depend on arrival order)."""
-    cfg = mpm_cfg(gravity=(0.0, -1.0e-3, 0.0), dt=1.0e-2, youngs_modulus=1000.0)
+    cfg = mpm_cfg(gravity=(0.0, -1.0e-3, 0.0), dt=1.0e-2, youngs_modulus=1000.0,
+                  p2g_mode="sorted")
     rng = np.random.default_rng(9)
     pos = rng.uniform(4.0, 12.0, (6000, 3)).astype(np.float32)
     vel = rng.normal(0, 1e-2, pos.shape).astype(np.float32)
