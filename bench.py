@@ -1,12 +1,14 @@
-"""Benchmark of the GB300 coupled LBM-MPM kernels on the standalone-at-scale workload.
+"""Benchmark of the GB300 coupled LBM-MPM timestep (LBMMpmCoupler.step / FSISimulation.step).
 
-Workload (seeded, synthetic):
-  lattice: 256^3 D3Q19 MRT channel, tau 0.6, g_x = 1e-6, walls in y and z (mask planes),
-           ~10% volume of non-overlapping static spheres with radii U[4, 12] (seed 1);
-  solid:   64 elastic cubes of 16^3 cells at 8 particles per cell = 2,097,152 particles at
-           random positions (seed 2) in a 256^3 grid, gravity -1e-4, dt 0.1.
-A timed "step" is one lattice step (value: MLUPS over all cells); the solid is timed the same
-way per MPM substep (particle-steps/s) and reported beside it.
+Headline workload (seeded, synthetic; the coupled configuration at scale):
+  384x192x192 D3Q19 MRT channel, tau 0.55, velocity inlet 0.05 at x = 0, pressure outlet at
+  x = nx-1, walls in y and z (mask planes); 48 elastic bodies (24 cubes of edge 12, 24 balls of
+  radius 6) at 8 particles per cell, 502,304 particles, Young's modulus U[0.02, 0.1] per body
+  (seed 3); 10 MPM substeps per lattice step, penalty coupling gamma 0.1.
+A timed "step" is one coupled lattice step (10 coupling + MPM substeps, force assembly, lattice
+step): value = coupled MLUPS (all lattice cells per second), with particle-steps/s beside it.
+The standalone kernels at scale (256^3 lattice, 2,097,152-particle MPM), the coupled smoke
+workload, the precision forms, the batched scenes and the learned closure are timed as extras.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -31,14 +33,54 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "taichi-mpm-lbm_gb300"))
 
-LBM_BYTES_PER_CELL = 181     # algorithmic bytes per FP32 cell update (pops 152, mask 1, force 12, rho+u 16)
+LBM_BYTES_PER_CELL = 181     # algorithmic bytes per FP32 fluid cell update (pops 152, mask 1, force 12, rho+u 16)
+SOLID_CELL_BYTES = 4         # a solid cell costs the step its flag word only
 KERNEL_BYTES_PER_CELL = 168  # what the fused step moves: pops 152, flag word 4, force 12
 MPM_BYTES_PER_PARTICLE = 200  # algorithmic bytes per particle-substep (standalone)
+COUPLED_BYTES_PER_PARTICLE = 224  # per particle-substep with the coupling force written and read
 MPM_BYTES_PER_NODE = 32       # per touched grid node per substep
+# Kernel launches per call of each entry point the timed regions use.
+LAUNCHES = {"fsi_coupling_forces": 1, "fsi_mpm_substep": 3, "fsi_mpm_substep_sorted": 10,
+            "fsi_coupled_substep": 10, "fsi_coupling_assemble": 1, "fsi_contact": 1,
+            "fsi_lbm_update_macro": 1, "fsi_lbm_macro_diagnostics": 1, "fsi_lbm_reduce": 1,
+            "fsi_coupled_diagnostics": 1, "fsi_lbm_force_op": 1, "fsi_mpm_reduce": 1,
+            "fsi_coupling_reduce": 1}
 # DRAM bytes per fluid cell and step kernel launch, from the ncu captures of the 192^3 scene
 # (dram__bytes_read.sum + dram__bytes_write.sum, odd/even launch average).
 TRAFFIC_PER_FLUID_CELL = {"f32/exact": 177.4, "f16/fast": 96.1}
 METRIC = "MLUPS & particle-steps/s on 1 GB300: plain vs FP16/learned, <=1% drag error"
+
+
+def lattice_bytes(fluid_cells: int, solid_cells: int, per_fluid: int = LBM_BYTES_PER_CELL) -> int:
+    """Algorithmic bytes of one lattice step: the per-cell figure for each fluid cell and the
+    flag word for each solid cell (whose populations the step does not touch)."""
+    return per_fluid * fluid_cells + SOLID_CELL_BYTES * solid_cells
+
+
+def touched_nodes(base: np.ndarray, dims) -> int:
+    """Grid nodes in the union of the particles' 27-node stencils (inside the grid)."""
+    nx, ny, nz = dims
+    b = base.astype(np.int64)
+    cells = np.unique(b[np.all((b >= -2) & (b < np.array(dims)), axis=1)], axis=0)
+    out = []
+    for di in range(3):
+        for dj in range(3):
+            for dk in range(3):
+                n = cells + np.array([di, dj, dk])
+                n = n[np.all((n >= 0) & (n < np.array(dims)), axis=1)]
+                out.append((n[:, 0] * ny + n[:, 1]) * nz + n[:, 2])
+    return int(np.unique(np.concatenate(out)).size) if out else 0
+
+
+def launches_since(before, lbm_step_launches: int = 1) -> int:
+    """Kernel launches of the library entry points called since the snapshot `before`
+    (fsi_lbm_step launches its face kernel too when the lattice has x faces)."""
+    from fsi import _native as nat
+    table = dict(LAUNCHES, fsi_lbm_step=lbm_step_launches)
+    total = 0
+    for name, count in nat.CALLS.items():
+        total += (count - before.get(name, 0)) * table.get(name, 1)
+    return total
 
 
 def load_peaks() -> tuple[float, str]:
@@ -186,66 +228,121 @@ def time_lbm_forms(lcfg, mask, args, world, stream) -> dict:
     return out
 
 
-def time_coupled(args, world, stream) -> dict:
-    """Coupled LBM-MPM steps (LBMMpmCoupler.step) on the coupled smoke workload (48x32x32,
-    4096 particles) and the coupled workload at scale (384x192x192, 48 bodies), FP32 exact."""
+def time_coupled_extras(args, world, stream, at_scale: bool) -> dict:
+    """The coupled smoke workload (48x32x32, one 8^3-cell cube of 4096 particles, 10
+    substeps; eager and CUDA-graph steps) and, on the headline scene, the graph-replayed
+    steps and the sorted (deterministic) scatter."""
+    import dataclasses
+
     import torch
     from fsi import scenes
     from fsi.simulation import FSISimulation
 
     out = {}
-    cases = [("smoke_48x32x32", 100)]
-    if not args.no_coupled_scale:
-        cases.append(("bodies_384x192x192", 20))
-    for name, steps in cases:
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, steps):
+        barrier(world)
+        a.record(stream)
+        fn(steps)
+        b.record(stream)
+        barrier(world)
+        return max_over_ranks(a.elapsed_time(b), world) / steps
+
+    cases = [("smoke_48x32x32", "atomic"), ("smoke_48x32x32", "sorted")]
+    if at_scale:
+        cases += [("bodies_384x192x192", "atomic"), ("bodies_384x192x192", "sorted")]
+    for name, mode in cases:
         if name.startswith("smoke"):
-            cfg, solid, pos = scenes.coupled_smoke(steps)
-            young = None
+            cfg, solid, pos = scenes.coupled_smoke(100)
+            young, steps = None, 100
         else:
             cfg, solid, pos, young = scenes.coupled_bodies()
+            steps = args.steps
+        cfg = dataclasses.replace(cfg, mpm=dataclasses.replace(cfg.mpm, p2g_mode=mode))
         sim = FSISimulation(cfg)
         sim.initialize_lbm(solid)
         sim.initialize_mpm_from_numpy(pos, youngs_modulus=young,
                                       poisson_ratio=None if young is None else 0.3)
         for _ in range(3):
             sim.coupler.step(cfg.lbm_dt)
-        barrier(world)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(steps):
-            sim.coupler.step(cfg.lbm_dt)
-        b.record(stream)
-        barrier(world)
-        eager_ms = max_over_ranks(a.elapsed_time(b), world) / steps
-        # the same steps replayed from a captured CUDA graph (capture outside the timed region)
+        eager_ms = timed(lambda k: [sim.coupler.step(cfg.lbm_dt) for _ in range(k)], steps)
         sim.coupler.step_many(cfg.lbm_dt, 4)
-        barrier(world)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        a.record(stream)
-        sim.coupler.step_many(cfg.lbm_dt, steps)
-        b.record(stream)
-        barrier(world)
-        torch.cuda.synchronize()
-        graph_wall_ms = (time.perf_counter() - t0) * 1e3 / steps
-        ms = max_over_ranks(a.elapsed_time(b), world) / steps
+        graph_ms = timed(lambda k: sim.coupler.step_many(cfg.lbm_dt, k), steps)
         sub = cfg.coupling.mpm_substeps_per_lbm_step
         cells = cfg.lbm.nx * cfg.lbm.ny * cfg.lbm.nz
-        out[name] = {
-            "coupled_steps_per_s": round(1e3 / ms * world, 2), "ms_per_step": round(ms, 4),
-            "eager_ms_per_step": round(eager_ms, 4),
-            "graph_wall_ms_per_step": round(graph_wall_ms, 4),
-            "mode": "step_many (CUDA graph of two coupled steps, capture included)",
-            "mlups": round(cells / (ms * 1e-3) / 1e6 * world, 2),
-            "particle_steps_per_s": round(len(pos) * sub / (ms * 1e-3) * world, 1),
-            "cells": cells, "particles": int(len(pos)), "substeps": sub, "timed_steps": steps,
-            # per substep: coupling forces + P2G + G2P + block clear; per step: force assembly,
-            # lattice step and, with x-face conditions, the face kernel
-            "gpu_launches": 2 * steps * (4 * sub + 2 + (1 if sim.lbm.bc_x_left_mode
-                                                        or sim.lbm.bc_x_right_mode else 0)),
+        out[f"{name}_{mode}"] = {
+            "p2g_mode": mode, "cells": cells, "particles": int(len(pos)), "substeps": sub,
+            "eager_ms_per_step": round(eager_ms, 4), "graph_ms_per_step": round(graph_ms, 4),
+            "coupled_steps_per_s": round(1e3 / min(eager_ms, graph_ms) * world, 2),
+            "mlups": round(cells / (min(eager_ms, graph_ms) * 1e-3) / 1e6 * world, 2),
+            "particle_steps_per_s": round(len(pos) * sub / (min(eager_ms, graph_ms) * 1e-3) * world, 1),
+            "graph": "step_many: replays of a captured CUDA graph of two coupled steps "
+                     "(capture included)",
         }
         del sim
         torch.cuda.empty_cache()
+    return out
+
+
+def time_headline(args, world, stream) -> dict:
+    """The coupled configuration at scale: device-timed coupled steps (state resident), the
+    lattice phase alone on the same lattice, and FSISimulation.step end to end."""
+    import torch
+    from fsi import _native as nat
+    from fsi import scenes
+    from fsi.simulation import FSISimulation
+
+    cfg, solid, pos, young = scenes.coupled_bodies()
+    sim = FSISimulation(cfg)
+    sim.initialize_lbm(solid)
+    sim.initialize_mpm_from_numpy(pos, youngs_modulus=young, poisson_ratio=0.3)
+    faces = 2 if (sim.lbm.bc_x_left_mode or sim.lbm.bc_x_right_mode) else 1
+    for _ in range(args.warmup):
+        sim.coupler.step(cfg.lbm_dt)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    before = dict(nat.CALLS)
+    a.record(stream)
+    for _ in range(args.steps):
+        sim.coupler.step(cfg.lbm_dt)
+    b.record(stream)
+    barrier(world)
+    launches = launches_since(before, faces)
+    step_ms = max_over_ranks(a.elapsed_time(b), world) / args.steps
+    base = sim.mpm.base_cells_numpy()
+    touched = touched_nodes(base, (cfg.lbm.nx, cfg.lbm.ny, cfg.lbm.nz))
+    # the lattice phase alone (same lattice, force and parity cycle)
+    barrier(world)
+    a.record(stream)
+    for _ in range(args.steps):
+        sim.lbm.step()
+    b.record(stream)
+    barrier(world)
+    lattice_ms = max_over_ranks(a.elapsed_time(b), world) / args.steps
+    # end to end: FSISimulation.step with this step's driving force from pinned host memory
+    # and its 18 diagnostics back on the host
+    g_host = torch.tensor(cfg.lbm.force, dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        sim.step(body_force=g_host.numpy())
+    barrier(world)
+    t0 = time.perf_counter()
+    diag = None
+    for _ in range(args.steps):
+        diag = sim.step(body_force=g_host.numpy())
+    barrier(world)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    n_particles = sim.mpm.particle_count()
+    out = {
+        "step_ms": step_ms, "lattice_ms": lattice_ms, "e2e_s": e2e_s, "launches": launches,
+        "cells": sim.lbm.n_cells, "fluid_cells": int((solid == 0).sum()),
+        "solid_cells": int((solid != 0).sum()), "particles": n_particles, "touched": touched,
+        "substeps": cfg.coupling.mpm_substeps_per_lbm_step,
+        "last_diagnostics": {k: (v.tolist() if hasattr(v, "tolist") else v)
+                             for k, v in (diag or {}).items()},
+    }
+    del sim
+    torch.cuda.empty_cache()
     return out
 
 
@@ -420,142 +517,151 @@ def run_gpu(args) -> dict:
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-
-    import dataclasses
-    lcfg, mask = scenes.channel_spheres_lbm(n=args.n)
-    storage, arithmetic = args.lbm_form.split("/")
-    head_cfg = dataclasses.replace(lcfg, population_storage=storage, collision_arithmetic=arithmetic)
-    alg_bytes, moved_bytes = FORM_BYTES[(storage, arithmetic)]
-    lbm = LBMSolver3D(head_cfg)
-    lbm.initialize(mask)
-    cells = lbm.n_cells
-    fluid_cells = int((mask == 0).sum())
-
-    mcfg, pos = scenes.cubes_mpm(n=args.n)
-    mpm = MPMSolver3D(mcfg)
-    mpm.initialize_particles_from_numpy(pos)
-    particles = mpm.particle_count()
-
     stream = torch.cuda.current_stream()
-    # --- lattice, device-resident -------------------------------------------------
-    for _ in range(args.warmup):
-        lbm.step()
-    barrier(world)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, peak_kind = load_peaks()
+
     clocks = ClockSampler(local)
     with clocks:
         time.sleep(0.3)  # let the sampler start before the timed region
+        # --- headline: coupled steps at scale --------------------------------------
+        head = time_headline(args, world, stream)
+        # --- standalone kernels at scale: 256^3 lattice, 2M-particle solid ----------
+        import dataclasses
+        lcfg, mask = scenes.channel_spheres_lbm(n=args.n)
+        storage, arithmetic = args.lbm_form.split("/")
+        alg_bytes, moved_bytes = FORM_BYTES[(storage, arithmetic)]
+        lbm = LBMSolver3D(dataclasses.replace(lcfg, population_storage=storage,
+                                              collision_arithmetic=arithmetic))
+        lbm.initialize(mask)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(args.warmup):
+            lbm.step()
+        barrier(world)
         e0.record(stream)
         for _ in range(args.steps):
             lbm.step()
         e1.record(stream)
         barrier(world)
-        # --- solid, device-resident -----------------------------------------------
-        for _ in range(args.warmup):
-            mpm.substep()
-        barrier(world)
-        m0.record(stream)
-        for _ in range(args.steps):
-            mpm.substep()
-        m1.record(stream)
-        barrier(world)
+        lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+        cells = lbm.n_cells
+        fluid_cells = int((mask == 0).sum())
+        del lbm
+        torch.cuda.empty_cache()
+        mpm_out = {}
+        mcfg, pos = scenes.cubes_mpm(n=args.n)
+        for mode in ("atomic", "sorted"):
+            mpm = MPMSolver3D(dataclasses.replace(mcfg, p2g_mode=mode))
+            mpm.initialize_particles_from_numpy(pos)
+            for _ in range(args.warmup):
+                mpm.substep()
+            barrier(world)
+            e0.record(stream)
+            for _ in range(args.steps):
+                mpm.substep()
+            e1.record(stream)
+            barrier(world)
+            mpm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+            touched = touched_nodes(mpm.base_cells_numpy(), (args.n,) * 3)
+            alg = MPM_BYTES_PER_PARTICLE * len(pos) + MPM_BYTES_PER_NODE * touched
+            mpm_out[mode] = {"value": round(len(pos) / (mpm_ms * 1e-3) * world, 1),
+                             "ms_per_substep": round(mpm_ms, 5),
+                             "algorithmic_gbs": round(alg / (mpm_ms * 1e-3) / 1e9, 1),
+                             "frac": round(alg / (mpm_ms * 1e-3) / 1e9 / peak, 4)}
+            del mpm
+            torch.cuda.empty_cache()
         # --- the lattice in the other storage / arithmetic forms ----------------
         forms = time_lbm_forms(lcfg, mask, args, world, stream) if not args.no_forms else {}
-        # --- coupled steps -------------------------------------------------------
-        coupled = time_coupled(args, world, stream) if not args.no_coupled else {}
+        # --- coupled smoke workload, graph replays, sorted scatter ------------------
+        coupled = (time_coupled_extras(args, world, stream, not args.no_coupled_scale)
+                   if not args.no_coupled else {})
         # --- many scenes at once ------------------------------------------------
         batched = time_batched(args, world, stream) if args.batch_scenes > 0 else {}
         # --- learned coarse-grid closure ------------------------------------------
         learned = time_closure(args, world, stream) if not args.no_closure else {}
-    lbm_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
-    lbm_launches = args.steps
-    mpm_ms = max_over_ranks(m0.elapsed_time(m1), world) / args.steps
-    base = mpm.base_cells_numpy().astype(np.int64)
-    # grid nodes touched per substep: the union of the particles' 27-node stencils
-    occupied = np.unique((base[:, 0] * args.n + base[:, 1]) * args.n + base[:, 2])
-    oi, oj, ok = occupied // (args.n * args.n), (occupied // args.n) % args.n, occupied % args.n
-    stencil = np.unique(np.concatenate([((oi + di) * args.n + oj + dj) * args.n + ok + dk
-                                        for di in range(3) for dj in range(3) for dk in range(3)]))
-    touched = int(len(stencil))
 
-    # --- end to end through the public API (host input, host result each step) ----
-    g_host = np.array(lcfg.force, dtype=np.float32)
-    for _ in range(2):
-        lbm.set_uniform_force(g_host)
-        lbm.step()
-        lbm.total_mass()
-    barrier(world)
-    t0 = time.perf_counter()
-    diag = None
-    for _ in range(args.steps):
-        lbm.set_uniform_force(g_host)   # 12 B of step input from the host
-        lbm.step()
-        diag = (lbm.total_mass(), lbm.max_velocity_norm())  # 16 B of step result to the host
-    barrier(world)
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-
-    peak, peak_kind = load_peaks()
-    achieved = alg_bytes * cells / (lbm_ms * 1e-3) / 1e9
-    mlups = cells / (lbm_ms * 1e-3) / 1e6
+    h = head
+    step_ms = h["step_ms"]
+    lat_bytes = lattice_bytes(h["fluid_cells"], h["solid_cells"])
+    mpm_bytes = h["substeps"] * (COUPLED_BYTES_PER_PARTICLE * h["particles"]
+                                 + MPM_BYTES_PER_NODE * h["touched"])
+    step_bytes = lat_bytes + mpm_bytes
+    achieved = step_bytes / (step_ms * 1e-3) / 1e9
+    sub_ms = step_ms - h["lattice_ms"]
+    lat_alone = lattice_bytes(fluid_cells, cells - fluid_cells, alg_bytes)
     result = {
         "metric": METRIC,
-        "value": round(mlups * world, 3),
+        "value": round(h["cells"] / (step_ms * 1e-3) / 1e6 * world, 3),
         "unit": "MLUPS",
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": round(lbm_ms, 5),
+        "ms_per_step": round(step_ms, 5),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32" if storage == "f32" else f"{storage} storage, f32 arithmetic",
+        "dtype": "f32",
         "data": "synthetic (seeded scene generators; no dataset)",
         "config": {
-            "workload": "standalone lattice 256^3 channel + 64 elastic cubes (2,097,152 particles)",
-            "lbm_form": args.lbm_form,
-            "lattice": [args.n] * 3, "tau": 0.6, "g_x": 1e-6,
-            "solid_fraction": round(float(mask.mean()), 4),
-            "fluid_cells": fluid_cells,
-            "particles": particles, "mpm_dt": 0.1, "gravity_y": -1e-4,
-            "l2": "inputs larger than L2 (populations 1.27 GB, particles 0.25 GB)",
+            "workload": "coupled at scale: 384x192x192 channel, 48 elastic bodies "
+                        f"({h['particles']} particles), 10 MPM substeps per lattice step",
+            "step": "LBMMpmCoupler.step: 10 x (coupling + MPM substep), force assembly, "
+                    "lattice step (FP32 exact, velocity inlet / pressure outlet faces)",
+            "p2g_mode": "atomic",
+            "lattice": [384, 192, 192], "tau": 0.55, "inflow": 0.05,
+            "fluid_cells": h["fluid_cells"], "particles": h["particles"], "substeps": h["substeps"],
+            "l2": "inputs larger than L2 (populations 1.08 GB, particles 60 MB, grid 0.23 GB)",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         },
-        "fluid_mlups": round(fluid_cells / (lbm_ms * 1e-3) / 1e6 * world, 3),
-        "mpm": {
-            "metric": "particle-steps/s",
-            "value": round(particles / (mpm_ms * 1e-3) * world, 1),
-            "ms_per_substep": round(mpm_ms, 5),
-            "algorithmic_gbs": round((MPM_BYTES_PER_PARTICLE * particles
-                                      + MPM_BYTES_PER_NODE * touched) / (mpm_ms * 1e-3) / 1e9, 1),
-        },
+        "particle_steps_per_s": round(h["particles"] * h["substeps"] / (step_ms * 1e-3) * world, 1),
+        "coupled_steps_per_s": round(1e3 / step_ms * world, 2),
+        "phases_ms": {"lattice_step": round(h["lattice_ms"], 4),
+                      "substeps_and_assembly": round(sub_ms, 4)},
         "roofline": {
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4),
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "kernel": "coupled step (all launches of LBMMpmCoupler.step)",
+            "peak_source": peak_kind,
+            "algorithmic_bytes_per_step": step_bytes,
+            "bytes_basis": ("lattice: 181 B per fluid cell + 4 B per solid cell; per substep: "
+                            "224 B per particle + 32 B per touched grid node"),
+            "lattice_step": {
+                "achieved": round(lat_bytes / (h["lattice_ms"] * 1e-3) / 1e9, 1),
+                "frac": round(lat_bytes / (h["lattice_ms"] * 1e-3) / 1e9 / peak, 4)},
+            "substeps": {
+                "achieved": round(mpm_bytes / (sub_ms * 1e-3) / 1e9, 1),
+                "frac": round(mpm_bytes / (sub_ms * 1e-3) / 1e9 / peak, 4)},
+        },
+        "e2e": {
+            "value": round(h["cells"] * args.steps / h["e2e_s"] / 1e6 * world, 3), "unit": "MLUPS",
+            "h2d_bytes_per_step": 12, "d2h_bytes_per_step": 240,
+            "api": "FSISimulation.step(body_force=g): the step's driving force from pinned host "
+                   "memory in, the 18 diagnostics (one 240-byte device record) out",
+            "last_diagnostics": h["last_diagnostics"],
+        },
+        "lattice": {
+            "workload": "standalone 256^3 channel, ~10 % static spheres (seed 1), g_x 1e-6",
+            "form": args.lbm_form,
+            "value": round(cells / (lbm_ms * 1e-3) / 1e6 * world, 3), "unit": "MLUPS",
+            "fluid_mlups": round(fluid_cells / (lbm_ms * 1e-3) / 1e6 * world, 3),
+            "ms_per_step": round(lbm_ms, 5),
+            "achieved_gbs": round(lat_alone / (lbm_ms * 1e-3) / 1e9, 1),
+            "frac": round(lat_alone / (lbm_ms * 1e-3) / 1e9 / peak, 4),
+            "bytes_basis": f"{alg_bytes} B per fluid cell + 4 B per solid cell",
             "traffic": (round(TRAFFIC_PER_FLUID_CELL[args.lbm_form] * fluid_cells)
                         if args.lbm_form in TRAFFIC_PER_FLUID_CELL else None),
             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of the "
                                "192^3 capture (odd/even average per fluid cell), scaled to this "
                                "lattice's fluid cells"),
-            "kernel": "lbm_step_kernel", "peak_source": peak_kind,
-            "algorithmic_bytes_per_cell": alg_bytes,
-            "kernel_bytes_per_cell": moved_bytes,
         },
-        "e2e": {
-            "value": round(cells * args.steps / e2e_s / 1e6 * world, 3), "unit": "MLUPS",
-            "h2d_bytes_per_step": 12, "d2h_bytes_per_step": 16,
-            "api": "LBMSolver3D.set_uniform_force + step + total_mass + max_velocity_norm",
-            "last_diagnostics": [float(diag[0]), float(diag[1])] if diag else None,
-        },
+        "mpm": {"metric": "particle-steps/s",
+                "workload": "64 elastic cubes of 16^3 cells (2,097,152 particles), 256^3 grid",
+                **mpm_out},
         "lbm_forms": forms,
         "coupled": coupled,
         "batched": batched,
         "learned_closure": learned,
-        # lattice steps + 3 MPM launches per substep + 3 launches per end-to-end step
-        # (force op, step, fused macro + diagnostics) + one step per form per step + coupled
-        "gpu_launches": (lbm_launches + 3 * args.steps + 3 * args.steps + len(forms) * args.steps
-                         + sum(c["gpu_launches"] for c in coupled.values())
-                         + batched.get("gpu_launches", 0) + learned.get("gpu_launches", 0)),
+        "gpu_launches": h["launches"],
+        "gpu_launches_basis": "kernel launches of the timed coupled steps (the headline)",
         "clocks": clocks.summary(),
     }
     if world > 1:
@@ -566,49 +672,42 @@ def run_gpu(args) -> dict:
 
 # --------------------------------------------------------------- CPU leg
 
-def cpu_sample(steps: int, warmup: int, nthreads: int, n: int = 256, slab: int = 32,
-               cubes: int = 8) -> dict:
-    """The oracle (C++ OpenMP restatement of the reference) on a bounded sample of the same
-    workload: a slab of `slab` x n x n cells of the lattice and `cubes` of the 64 cubes."""
+# The reference arm times full coupled steps of the headline scene while the whole run stays
+# within a few minutes (about 2.5 s per step on 16 Arm cores); longer runs time a bounded sample.
+FULL_REFERENCE_STEPS = 40
+SAMPLE_SCENE = dict(nx=96, bodies=12)  # the first quarter of the channel, a quarter of the bodies
+
+
+def cpu_coupled_sample(steps: int, warmup: int, nthreads: int, **scene_kw) -> dict:
+    """The oracle (C++ OpenMP restatement of the reference kernels; P2G and the coupling as
+    parallel loops with atomic adds, like the reference's parallel Taichi loops) timed on
+    coupled steps of the headline scene (scene_kw selects a smaller sample of it)."""
     from fsi import scenes
     from oracle import oracle as O
 
-    lcfg, mask = scenes.channel_spheres_lbm(n=n)
-    sub = mask[:slab].copy()
-    from dataclasses import replace
-    scfg = replace(lcfg, nx=slab)
-    lbm = O.LBMSolver3D(scfg, nthreads=nthreads)
-    lbm.initialize(sub)
+    cfg, solid, pos, young = scenes.coupled_bodies(**scene_kw)
+    sim = O.FSISimulation(cfg, nthreads=nthreads, polar="device", deterministic=False)
+    sim.initialize_lbm(solid)
+    sim.initialize_mpm_from_numpy(pos)
     for _ in range(warmup):
-        lbm.step()
+        sim.coupler.step(cfg.lbm_dt)
     t0 = time.perf_counter()
     for _ in range(steps):
-        lbm.step()
-    lbm_s = time.perf_counter() - t0
-    mcfg, pos = scenes.cubes_mpm(n=n)
-    per_cube = len(pos) // 64
-    pos = pos[: cubes * per_cube]
-    mpm = O.MPMSolver3D(replace(mcfg, max_particles=len(pos)), nthreads=nthreads,
-                        deterministic=False)
-    mpm.initialize_particles_from_numpy(pos)
-    for _ in range(max(1, warmup // 2)):
-        mpm.substep()
-    t1 = time.perf_counter()
-    for _ in range(steps):
-        mpm.substep()
-    mpm_s = time.perf_counter() - t1
-    cells = slab * n * n
-    return {"mlups": cells * steps / lbm_s / 1e6, "lbm_s_per_step": lbm_s / steps,
-            "particle_steps_per_s": len(pos) * steps / mpm_s, "mpm_s_per_substep": mpm_s / steps,
-            "cells": cells, "particles": len(pos), "cores": nthreads}
+        sim.coupler.step(cfg.lbm_dt)
+    dt = (time.perf_counter() - t0) / max(steps, 1)
+    cells = cfg.lbm.nx * cfg.lbm.ny * cfg.lbm.nz
+    sub = cfg.coupling.mpm_substeps_per_lbm_step
+    return {"mlups": cells / dt / 1e6, "s_per_step": dt, "cells": cells,
+            "particles": int(len(pos)), "particle_steps_per_s": len(pos) * sub / dt,
+            "cores": nthreads, "lattice": [cfg.lbm.nx, cfg.lbm.ny, cfg.lbm.nz]}
 
 
 def cpu_baseline_entry(nthreads: int) -> dict:
-    s = cpu_sample(steps=3, warmup=1, nthreads=nthreads)
+    s = cpu_coupled_sample(steps=2, warmup=1, nthreads=nthreads)
     return {"value": round(s["mlups"], 3), "unit": "MLUPS", "cores": s["cores"], "kind": "port",
-            "sample": (f"oracle (C++ OpenMP float32 restatement; Taichi is not installable) on a "
-                       f"32x256x256 slab of the lattice ({s['cells']} cells, 3 steps) and 8 of the "
-                       f"64 cubes ({s['particles']} particles, 3 substeps)"),
+            "sample": (f"oracle (C++ OpenMP float32 restatement; Taichi is not installable) on 2 "
+                       f"coupled steps of the headline scene ({s['cells']} cells, "
+                       f"{s['particles']} particles, 10 substeps each) after 1 warm-up step"),
             "particle_steps_per_s": round(s["particle_steps_per_s"], 1)}
 
 
@@ -618,21 +717,27 @@ def run_reference(args) -> dict | None:
         return None
     from oracle import oracle as O
     nthreads = O.max_threads()
-    s = cpu_sample(steps=args.steps, warmup=args.warmup, nthreads=nthreads)
+    full = args.steps + args.warmup <= FULL_REFERENCE_STEPS
+    s = cpu_coupled_sample(args.steps, args.warmup, nthreads, **({} if full else SAMPLE_SCENE))
+    sample = ("full coupled steps of the headline scene" if full else
+              f"coupled steps of a {s['lattice'][0]}x192x192 slab of the headline channel with "
+              f"{s['particles']} particles (a bounded sample for long runs)")
     return {
         "impl": "reference",
         "metric": METRIC, "value": round(s["mlups"], 3), "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(s["lbm_s_per_step"] * 1e3, 3), "higher_is_better": True,
+        "ms_per_step": round(s["s_per_step"] * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene generators; no dataset)",
-        "config": {"workload": "standalone lattice 256^3 channel + 64 elastic cubes (2,097,152 particles)",
-                   "sample": "32x256x256 lattice slab per step; 8 of 64 cubes per substep"},
-        "mpm": {"metric": "particle-steps/s", "value": round(s["particle_steps_per_s"], 1)},
+        "config": {"workload": "coupled at scale: 384x192x192 channel, 48 elastic bodies, "
+                               "10 MPM substeps per lattice step",
+                   "sample": sample},
+        "particle_steps_per_s": round(s["particle_steps_per_s"], 1),
         "cpu_baseline": {"value": round(s["mlups"], 3), "unit": "MLUPS", "cores": nthreads,
                          "kind": "port",
-                         "sample": "reference's Taichi CPU path unavailable (taichi not installable); "
-                                   "the oracle restatement of it, all host threads"},
+                         "sample": "reference's Taichi CPU path unavailable (taichi not "
+                                   "installable); the oracle restatement of it, all host "
+                                   "threads, " + sample},
         "e2e": {"value": round(s["mlups"], 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -641,7 +746,7 @@ def run_reference(args) -> dict | None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (default 256)")
@@ -649,12 +754,12 @@ def main() -> None:
     ap.add_argument("--lbm-form", default="f32/exact",
                     choices=["f32/exact", "f32/fast", "f16/fast", "bf16/fast"],
                     help="population storage / collision arithmetic of the headline lattice")
-    ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-step timings")
+    ap.add_argument("--no-coupled", action="store_true", help="skip the extra coupled-step timings")
     ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure section")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched workload (0 skips it)")
     ap.add_argument("--no-coupled-scale", action="store_true",
-                    help="time only the small coupled workload")
+                    help="skip the extra timings of the headline scene (graph, sorted scatter)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip timing the FP32-fast / FP16 / BF16 lattice forms")
     args = ap.parse_args()

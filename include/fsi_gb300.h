@@ -338,6 +338,17 @@ int fsi_contact(const fsi_coupling_desc* desc, const fsi_mpm_desc* mpm,
 int fsi_coupling_reduce(const fsi_lbm_desc* lbm, const float* accum, const uint32_t* flags,
                         double* out, void* stream);
 
+/* The coupled runner's per-step diagnostics in one launch, into device double out[22]
+ * (zeroed here): [0] sum of particle mass, [1..3] sum of m x, [4] max |v|, [5..7] sum of the
+ * particle coupling force (as fsi_mpm_reduce); [8..10] sum of the fluid reaction over fluid
+ * cells (as fsi_coupling_reduce; 0 when accum is NULL); [11..18] the eight int32 counters of
+ * fsi_coupling_counters and [19..21] its IB force totals (0 when counters is NULL). Replaces
+ * the host reductions behind FSISimulation.diagnostics (simulation.py:117-147), which the
+ * caller reads back with one copy. */
+int fsi_coupled_diagnostics(const fsi_mpm_desc* mpm, const fsi_particles* particles,
+                            const fsi_lbm_desc* lbm, const float* accum, const uint32_t* flags,
+                            const void* counters, double* out, void* stream);
+
 /* ------------------------------------------------------------- batches of scenes
  * Many independent lattices advanced together: one launch per phase covers every lattice
  * of the batch. No reference counterpart (the reference runs one scene per FSISimulation).

@@ -885,8 +885,11 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
                           const int32_t* solid, T* cforce, T* phi, T* valid_out, int32_t* mask_out,
                           int32_t* counters, T inv_dx, T gamma_eff, T dt_ratio, T cell_volume,
                           int build_fraction, T min_valid_weight, int use_rel, T rel_limit,
-                          int use_force_limit, T force_limit, int cell_order) {
+                          int use_force_limit, T force_limit, int cell_order, int nthreads) {
   Grid<T> G{nx, ny, nz, nullptr, nullptr};
+  // Serial particle order unless nthreads > 1 (then a parallel loop with atomic adds, like
+  // the reference's parallel Taichi loop; used for timing) or the cell order is asked for.
+  const bool parallel = !cell_order && nthreads > 1;
   const T support_tolerance = (T)1.0e-5;
   struct Spread {
     int base[3];
@@ -904,6 +907,7 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
     for (int a = 0; a < 3; ++a) out[a] = (((-nw) * r.pf[a]) * dt_ratio) / cell_volume;
     out[3] = (nw * r.vol) / cell_volume;
   };
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_default(nthreads)) if (parallel)
   for (int p = 0; p < n; ++p) {
     if (active[p] == 0) continue;
     T xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
@@ -930,7 +934,10 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
         }
     valid_out[p] = valid;
     if (valid > min_valid_weight) {
-      if (valid < (T)1.0 - support_tolerance) counters[1] += 1;
+      if (valid < (T)1.0 - support_tolerance) {
+#pragma omp atomic
+        counters[1] += 1;
+      }
       T dv[3];
       for (int a = 0; a < 3; ++a) {
         uf[a] = uf[a] / valid;
@@ -955,7 +962,10 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
       }
       for (int a = 0; a < 3; ++a) fp[3 * p + a] = pf[a];
       mask_out[p] = 1;
-      if (clipped) counters[2] += 1;
+      if (clipped) {
+#pragma omp atomic
+        counters[2] += 1;
+      }
       r.valid = valid;
       for (int a = 0; a < 3; ++a) r.pf[a] = pf[a];
       r.vol = vol[p];
@@ -974,12 +984,24 @@ static void coupling_impl(int nx, int ny, int nz, int n, const T* x, const T* pv
             if (solid[c] != 0) continue;
             T add[4];
             spread_terms(r, i, j, k, add);
-            for (int a = 0; a < 3; ++a) cforce[3 * c + a] = cforce[3 * c + a] + add[a];
-            if (build_fraction) phi[c] = phi[c] + add[3];
+            if (parallel) {
+              for (int a = 0; a < 3; ++a) {
+#pragma omp atomic
+                cforce[3 * c + a] += add[a];
+              }
+              if (build_fraction) {
+#pragma omp atomic
+                phi[c] += add[3];
+              }
+            } else {
+              for (int a = 0; a < 3; ++a) cforce[3 * c + a] = cforce[3 * c + a] + add[a];
+              if (build_fraction) phi[c] = phi[c] + add[3];
+            }
           }
     } else {
       fp[3 * p] = fp[3 * p + 1] = fp[3 * p + 2] = 0;
       mask_out[p] = 0;
+#pragma omp atomic
       counters[0] += 1;
     }
   }
@@ -1024,11 +1046,11 @@ FSI_ORACLE_EXPORT void oracle_coupling_f32(int nx, int ny, int nz, int n, const 
                                            float cell_volume, int build_fraction,
                                            float min_valid_weight, int use_rel, float rel_limit,
                                            int use_force_limit, float force_limit,
-                                           int cell_order) {
+                                           int cell_order, int nthreads) {
   coupling_impl<float>(nx, ny, nz, n, x, pv, mass, vol, active, fp, lbm_v, solid, cforce, phi,
                        valid_out, mask_out, counters, inv_dx, gamma_eff, dt_ratio, cell_volume,
                        build_fraction, min_valid_weight, use_rel, rel_limit, use_force_limit,
-                       force_limit, cell_order);
+                       force_limit, cell_order, nthreads);
 }
 
 FSI_ORACLE_EXPORT void oracle_coupling_f64(int nx, int ny, int nz, int n, const double* x,
@@ -1040,11 +1062,11 @@ FSI_ORACLE_EXPORT void oracle_coupling_f64(int nx, int ny, int nz, int n, const 
                                            double cell_volume, int build_fraction,
                                            double min_valid_weight, int use_rel, double rel_limit,
                                            int use_force_limit, double force_limit,
-                                           int cell_order) {
+                                           int cell_order, int nthreads) {
   coupling_impl<double>(nx, ny, nz, n, x, pv, mass, vol, active, fp, lbm_v, solid, cforce, phi,
                         valid_out, mask_out, counters, inv_dx, gamma_eff, dt_ratio, cell_volume,
                         build_fraction, min_valid_weight, use_rel, rel_limit, use_force_limit,
-                        force_limit, cell_order);
+                        force_limit, cell_order, nthreads);
 }
 
 // _compute_immersed_boundary_force_kernel, fsi/coupling.py:421-452 (serial cell order).

@@ -509,7 +509,8 @@ class LBMMpmCoupler:
             int(build_fraction), self._real(c.min_valid_weight),
             int(c.relative_velocity_limit is not None),
             self._real(c.relative_velocity_limit or 0.0), int(c.force_limit is not None),
-            self._real(c.force_limit or 0.0), int(getattr(self.mpm, "cell_order", False)))
+            self._real(c.force_limit or 0.0), int(getattr(self.mpm, "cell_order", False)),
+            self.mpm.nthreads if not self.mpm.deterministic else 1)
 
     def _clamp_fraction(self):
         np.minimum(self.solid_volume_fraction, self.dtype.type(1.0), out=self.solid_volume_fraction)

@@ -106,6 +106,87 @@ __global__ void __launch_bounds__(kBlock) accum_reduce_kernel(Geo g, const float
   }
 }
 
+// The per-step diagnostics of the coupled runner in one pass (FSISimulation.diagnostics,
+// simulation.py:117-147): blocks [0, pblocks) reduce the particles, the rest the lattice
+// accumulator over fluid cells; block 0 also copies the counters. out (zeroed by the caller):
+// [0] sum m, [1..3] sum m x, [4] max |v|, [5..7] sum particle force, [8..10] sum of the fluid
+// reaction over fluid cells, [11..18] the eight counters, [19..21] the IB force totals.
+struct RunnerDiagArgs {
+  int n;
+  long long cap;
+  const float* __restrict__ x;
+  const float* __restrict__ v;
+  const float* __restrict__ mass;
+  const float* __restrict__ fp;
+  Geo g;
+  const float4* __restrict__ accum;
+  const uint32_t* __restrict__ flags;
+  const Cnt* __restrict__ cnt;
+  int pblocks;
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kBlock / 32; ++w) t += sh[w];
+  return t;
+}
+
+__global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, double* __restrict__ out) {
+  __shared__ double sh[kBlock / 32];
+  if (blockIdx.x == 0 && threadIdx.x < 12) {
+    if (a.cnt) {
+      if (threadIdx.x < 8) {
+        const int32_t* c = &a.cnt->unsupported;
+        out[11 + threadIdx.x] = (double)c[threadIdx.x];
+      } else if (threadIdx.x < 11) {
+        out[19 + threadIdx.x - 8] = (double)a.cnt->ib_total[threadIdx.x - 8];
+      }
+    }
+  }
+  if ((int)blockIdx.x < a.pblocks) {
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    float vmax = 0.f;
+    for (int p = blockIdx.x * kBlock + threadIdx.x; p < a.n; p += a.pblocks * kBlock) {
+      const double ms = a.mass[p];
+      acc[0] += ms;
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) acc[1 + ax] += ms * (double)a.x[ax * a.cap + p];
+      const float vx = a.v[p], vy = a.v[a.cap + p], vz = a.v[2 * a.cap + p];
+      vmax = fmaxf(vmax, norm3(vx, vy, vz));
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) acc[4 + ax] += (double)a.fp[ax * a.cap + p];
+    }
+    for (int i = 0; i < 7; ++i) {
+      const double t = block_sum(acc[i], sh);
+      if (threadIdx.x == 0) atomicAdd(out + (i < 4 ? i : i + 1), t);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+    if ((threadIdx.x & 31) == 0)
+      atomicMax(reinterpret_cast<unsigned long long*>(out + 4),
+                (unsigned long long)__double_as_longlong((double)vmax));
+  } else if (a.accum) {
+    double s3[3] = {0, 0, 0};
+    const int nb = gridDim.x - a.pblocks;
+    for (long long c = (long long)(blockIdx.x - a.pblocks) * kBlock + threadIdx.x; c < a.g.n;
+         c += (long long)nb * kBlock) {
+      if (a.flags[c] & kFlagSolid) continue;
+      const float4 v = a.accum[c];
+      s3[0] += v.x; s3[1] += v.y; s3[2] += v.z;
+    }
+    for (int i = 0; i < 3; ++i) {
+      const double t = block_sum(s3[i], sh);
+      if (threadIdx.x == 0) atomicAdd(out + 8 + i, t);
+    }
+  }
+}
+
 Geo geo_of(const fsi_lbm_desc* d) { return Geo{d->nx, d->ny, d->nz, (long long)d->nx * d->ny * d->nz}; }
 Geo geo_of(const fsi_mpm_desc* d) { return Geo{d->nx, d->ny, d->nz, (long long)d->nx * d->ny * d->nz}; }
 
@@ -201,4 +282,31 @@ extern "C" int fsi_coupling_reduce(const fsi_lbm_desc* l, const float* accum,
   if (blocks > 152 * 4) blocks = 152 * 4;
   accum_reduce_kernel<<<blocks, kBlock, 0, s>>>(g, reinterpret_cast<const float4*>(accum), flags, out);
   return check_launch("accum_reduce_kernel");
+}
+
+extern "C" int fsi_coupled_diagnostics(const fsi_mpm_desc* m, const fsi_particles* p,
+                                       const fsi_lbm_desc* l, const float* accum,
+                                       const uint32_t* flags, const void* counters, double* out,
+                                       void* stream) {
+  FSI_REQUIRE(m && p && l && out, "NULL argument");
+  FSI_REQUIRE(!accum || flags, "accum needs flags");
+  FSI_REQUIRE(m->num_particles >= 0 && m->num_particles <= p->capacity, "bad particle count");
+  FSI_REQUIRE(m->nx == l->nx && m->ny == l->ny && m->nz == l->nz, "grids differ");
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(out, 0, 22 * sizeof(double), s) != cudaSuccess) return check_launch("memset");
+  RunnerDiagArgs a;
+  a.n = m->num_particles;
+  a.cap = p->capacity;
+  a.x = p->x; a.v = p->v; a.mass = p->mass; a.fp = p->force;
+  a.g = geo_of(l);
+  a.accum = reinterpret_cast<const float4*>(accum);
+  a.flags = flags;
+  a.cnt = reinterpret_cast<const Cnt*>(counters);
+  int pb = (int)grid_for(a.n, kBlock);
+  if (pb > 152 * 2) pb = 152 * 2;
+  int cb = accum ? (int)grid_for(a.g.n, kBlock) : 0;
+  if (cb > 152 * 2) cb = 152 * 2;
+  a.pblocks = pb;
+  runner_diag_kernel<<<pb + cb, kBlock, 0, s>>>(a, out);
+  return check_launch("runner_diag_kernel");
 }

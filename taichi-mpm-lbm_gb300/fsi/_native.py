@@ -6,6 +6,7 @@ device raises ``RuntimeError``.
 """
 from __future__ import annotations
 
+import collections
 import ctypes
 import os
 from pathlib import Path
@@ -161,6 +162,8 @@ _SIGNATURES = {
     "fsi_coupling_assemble": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(LbmDesc), _VP, ctypes.POINTER(ctypes.c_float), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_contact": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_coupling_reduce": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_coupled_diagnostics": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles),
+                                 ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_batch_create": ([ctypes.POINTER(BatchLattice), ctypes.c_int32, ctypes.c_int32,
                           ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "fsi_batch_destroy": ([_BATCH], ctypes.c_int),
@@ -243,10 +246,15 @@ def last_error() -> str:
     return buf.value.decode(errors="replace")
 
 
+# Number of successful calls per entry point (read by the benchmark to count launches).
+CALLS: collections.Counter = collections.Counter()
+
+
 def call(name: str, *args) -> None:
     """Invoke an entry point and translate its status into a Python exception."""
     lib = load()
     status = getattr(lib, name)(*args)
+    CALLS[name] += 1
     if status != FSI_OK:
         msg = f"{name} failed ({status}): {last_error()}"
         if status == FSI_ERR_INVALID_ARG:

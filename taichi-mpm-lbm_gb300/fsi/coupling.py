@@ -136,8 +136,11 @@ class LBMMpmCoupler:
                  nat.ptr(self._accum), nat.ptr(self.lbm.flags), nat.ptr(self._contact_mask),
                  nat.ptr(self._counters), nat.stream_ptr())
 
-    def _assemble(self, mode: int, force: torch.Tensor | None) -> None:
-        base = np.asarray(self.lbm.config.force, dtype=np.float32)
+    def _assemble(self, mode: int, force: torch.Tensor | None, body_force=None) -> None:
+        base = np.asarray(self.lbm.config.force if body_force is None else body_force,
+                          dtype=np.float32)
+        if base.shape != (3,):
+            raise ValueError("body_force must have 3 components.")
         base_p = base.ctypes.data_as(nat.ctypes.POINTER(nat.ctypes.c_float))
         if mode & nat.ASSEMBLE_IB:
             self._counters[5:7].zero_()
@@ -147,11 +150,17 @@ class LBMMpmCoupler:
                  base_p, mode, nat.ptr(self._accum), nat.ptr(macro), nat.ptr(force),
                  nat.ptr(self._ib), nat.ptr(self._counters), nat.stream_ptr())
 
-    def step(self, lbm_dt: float) -> None:
-        """One explicit coupled lattice step with the configured MPM substeps (coupling.py:135-173)."""
+    def step(self, lbm_dt: float, body_force=None) -> None:
+        """One explicit coupled lattice step with the configured MPM substeps (coupling.py:135-173).
+
+        ``body_force`` (extension): the lattice's uniform driving force for this step in
+        place of ``LBMConfig.force`` (reset_force's base, lbm3d.py:504-510), e.g. a forcing
+        schedule supplied by the host step by step."""
         lbm_dt_value = float(lbm_dt)
         if lbm_dt_value <= 0.0:
             raise ValueError("lbm_dt must be positive.")
+        if body_force is not None and np.asarray(body_force).shape != (3,):
+            raise ValueError("body_force must have 3 components.")
         self._validate_initialized()
         self.clear_coupling_fields()
         mpm_dt = lbm_dt_value / float(self.substeps)
@@ -185,7 +194,7 @@ class LBMMpmCoupler:
             mode |= nat.ASSEMBLE_COUPLING
         if self.immersed_boundary_enabled:
             mode |= nat.ASSEMBLE_IB
-        self._assemble(mode, self.lbm._writable_force())
+        self._assemble(mode, self.lbm._writable_force(), body_force)
         self.lbm.step()
         if self.enabled:
             self._coupled_step += 1

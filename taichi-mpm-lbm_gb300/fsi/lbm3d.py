@@ -277,6 +277,26 @@ class LBMSolver3D:
         self._mass_speed_cache = (key, val)
         return val
 
+    def _enqueue_mass_speed(self, out: torch.Tensor) -> tuple | None:
+        """Enqueue (total mass, max |u|) of the current state into device double out[0:2]
+        (out has at least 8 elements) without synchronising; refreshes rho and u when stale.
+        Returns the cached pair when this state's values are already known."""
+        key = (self._steps_done, self._initialized)
+        if self._mass_speed_cache is not None and self._mass_speed_cache[0] == key:
+            return self._mass_speed_cache[1]
+        if self._macro_fresh:
+            self._call("fsi_lbm_reduce", nat.ptr(self._macro), nat.ptr(self._force_buf[self._fcur]),
+                       nat.ptr(self._flags), nat.ptr(out), nat.stream_ptr())
+        else:
+            self._call("fsi_lbm_macro_diagnostics", nat.ptr(self._pops),
+                       nat.ptr(self._force_buf[self._fprev]), nat.ptr(self._flags),
+                       self._steps_done, nat.ptr(self._macro), nat.ptr(out), nat.stream_ptr())
+            self._macro_fresh = True
+        return None
+
+    def _remember_mass_speed(self, mass: float, speed: float) -> None:
+        self._mass_speed_cache = ((self._steps_done, self._initialized), (mass, speed))
+
     def total_mass(self) -> float:
         return self._mass_and_speed()[0]
 

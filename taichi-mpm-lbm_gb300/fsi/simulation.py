@@ -24,6 +24,8 @@ class FSISimulation:
         self.time = 0.0
         self._lbm_initialized = False
         self._mpm_initialized = False
+        self._dbuf = None
+        self._dhost = None
 
     def initialize_lbm(self, solid_np: np.ndarray | None = None) -> None:
         self.lbm.initialize(solid_np=solid_np)
@@ -57,9 +59,11 @@ class FSISimulation:
                                        spacing=mpm_box_spacing,
                                        initial_velocity=mpm_initial_velocity)
 
-    def step(self) -> dict[str, object]:
+    def step(self, body_force=None) -> dict[str, object]:
+        """One coupled step and its diagnostics (simulation.py:84-89). ``body_force`` is the
+        extension of LBMMpmCoupler.step: this step's lattice driving force (3 components)."""
         self._validate_initialized()
-        self.coupler.step(self.config.lbm_dt)
+        self.coupler.step(self.config.lbm_dt, body_force=body_force)
         self.step_index += 1
         self.time += self.config.lbm_dt
         return self.diagnostics()
@@ -97,28 +101,60 @@ class FSISimulation:
         return self.output_writer.write_snapshot(self)
 
     def diagnostics(self) -> dict[str, object]:
-        """Per-step diagnostics with the reference's keys (simulation.py:117-147)."""
+        """Per-step diagnostics with the reference's keys (simulation.py:117-147).
+
+        All reductions run on the device (float64 sums of the float32 fields): the lattice's
+        fused macro refresh + mass / max |u| pass and one launch for the particles, the fluid
+        reaction and the counters, followed by a single 240-byte copy to pinned host memory
+        and one synchronisation. The reference copies every field to the host instead; its
+        centre of mass is a float32 numpy sum, here the float64 quotient rounded to float32
+        (MPMSolver3D.center_of_mass() keeps the float32 host arithmetic)."""
         self._validate_initialized()
-        cd = self.coupler.coupling_diagnostics()
+        import torch
+
+        from . import _native as nat
+
+        if self._dbuf is None:
+            dev = self.lbm.macro.device
+            self._dbuf = torch.zeros(30, dtype=torch.float64, device=dev)
+            self._dhost = torch.zeros(30, dtype=torch.float64).pin_memory()
+        cached = self.lbm._enqueue_mass_speed(self._dbuf[0:8])
+        c = self.coupler
+        nat.call("fsi_coupled_diagnostics", self.mpm.desc, self.mpm.particles, self.lbm._desc,
+                 nat.ptr(c._accum), nat.ptr(self.lbm.flags), nat.ptr(c._counters),
+                 nat.ptr(self._dbuf[8:]), nat.stream_ptr())
+        self._dhost.copy_(self._dbuf, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        r = self._dhost.numpy().copy()
+        if cached is None:
+            mass, speed = float(r[0]), float(r[1])
+            self.lbm._remember_mass_speed(mass, speed)
+        else:
+            mass, speed = cached
+        d = r[8:]
+        n = self.mpm.particle_count()
+        com = (d[1:4] / d[0]).astype(np.float32) if n and d[0] > 0.0 else np.zeros(3, np.float32)
+        counts = d[11:19].astype(np.int64)
+        ib_total = d[19:22].astype(np.float32).astype(np.float64)
         return {
             "step": self.step_index,
             "time": self.time,
-            "lbm_total_mass": self.lbm.total_mass(),
-            "lbm_max_velocity_norm": self.lbm.max_velocity_norm(),
-            "mpm_particle_count": self.mpm.particle_count(),
-            "mpm_center_of_mass": self.mpm.center_of_mass(),
-            "mpm_max_velocity_norm": self.mpm.max_velocity_norm(),
-            "total_particle_coupling_force": self.coupler.total_particle_coupling_force(),
-            "total_fluid_coupling_force": self.coupler.total_fluid_coupling_force(),
-            "coupling_unsupported_particle_count": cd["unsupported_particle_count"],
-            "coupling_partial_support_particle_count": cd["partial_support_particle_count"],
-            "coupling_clipped_particle_count": cd["clipped_particle_count"],
-            "coupling_effective_gamma": cd["effective_gamma"],
-            "coupling_ib_active_cell_count": cd["ib_active_cell_count"],
-            "coupling_ib_clipped_cell_count": cd["ib_clipped_cell_count"],
-            "coupling_ib_total_force_norm": cd["ib_total_force_norm"],
-            "coupling_contact_candidate_count": cd["contact_candidate_count"],
-            "coupling_contact_damped_particle_count": cd["contact_damped_particle_count"],
+            "lbm_total_mass": mass,
+            "lbm_max_velocity_norm": speed,
+            "mpm_particle_count": n,
+            "mpm_center_of_mass": com,
+            "mpm_max_velocity_norm": float(d[4]) if n else 0.0,
+            "total_particle_coupling_force": d[5:8].astype(np.float32),
+            "total_fluid_coupling_force": d[8:11].astype(np.float32),
+            "coupling_unsupported_particle_count": int(counts[0]),
+            "coupling_partial_support_particle_count": int(counts[1]),
+            "coupling_clipped_particle_count": int(counts[2]),
+            "coupling_effective_gamma": c.effective_gamma(),
+            "coupling_ib_active_cell_count": int(counts[5]),
+            "coupling_ib_clipped_cell_count": int(counts[6]),
+            "coupling_ib_total_force_norm": float(np.linalg.norm(ib_total)),
+            "coupling_contact_candidate_count": int(counts[3]),
+            "coupling_contact_damped_particle_count": int(counts[4]),
         }
 
     # ------------------------------------------------------- checkpointing

@@ -7,6 +7,7 @@ import json
 from pathlib import Path
 from types import SimpleNamespace
 
+import numpy as np
 import pytest
 
 import bench
@@ -46,13 +47,13 @@ def test_roofline_peak_is_the_measured_copy_bandwidth():
 
 @pytest.fixture
 def small_sample(monkeypatch):
-    """cpu_sample on a 64^3 scene: a 6-cell slab of the lattice and 2 of 64 small cubes."""
+    """cpu_coupled_sample on a small channel of the headline kind: 64x24x24, two bodies."""
     for var in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
         monkeypatch.delenv(var, raising=False)
-    monkeypatch.setattr(scenes, "cubes_mpm", functools.partial(scenes.cubes_mpm, edge=4))
-    real = bench.cpu_sample
-    monkeypatch.setattr(bench, "cpu_sample", lambda steps, warmup, nthreads:
-                        real(steps, warmup, nthreads, n=64, slab=6, cubes=2))
+    real = bench.cpu_coupled_sample
+    monkeypatch.setattr(bench, "cpu_coupled_sample", lambda steps, warmup, nthreads, **kw:
+                        real(steps, warmup, nthreads, nx=64, ny=24, nz=24, bodies=2,
+                             cube_edge=4, sphere_radius=2.0))
 
 
 def test_reference_arm_prints_the_contract_line(small_sample):
@@ -61,13 +62,27 @@ def test_reference_arm_prints_the_contract_line(small_sample):
     assert out["unit"] == "MLUPS" and out["value"] > 0 and out["higher_is_better"] is True
     assert out["n_gpus"] == 1 and (out["steps"], out["warmup"]) == (2, 1)
     assert out["ms_per_step"] > 0 and out["vs_baseline"] is None and out["scaling"] == "weak"
-    assert out["config"]["workload"].startswith("standalone lattice 256^3")
+    assert out["config"]["workload"].startswith("coupled at scale")
     cb = out["cpu_baseline"]
     assert cb["kind"] == "port" and cb["value"] == out["value"] and cb["cores"] >= 1
     assert out["e2e"] == {"value": out["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
                           "d2h_bytes_per_step": 0}
-    assert out["mpm"]["value"] > 0
+    assert out["particle_steps_per_s"] > 0
     json.dumps(out)  # one JSON line
+
+
+def test_bounded_sample_for_long_reference_runs(small_sample):
+    out = bench.run_reference(SimpleNamespace(steps=bench.FULL_REFERENCE_STEPS, warmup=1))
+    assert "bounded sample" in out["config"]["sample"]
+
+
+def test_roofline_bytes_basis():
+    assert bench.lattice_bytes(10, 3) == 10 * 181 + 3 * 4
+    base = np.array([[0, 0, 0], [0, 0, 0], [5, 5, 5], [-3, 0, 0]])
+    # one cell at the corner: its 27 stencil nodes; one interior cell: 27 more; the last
+    # particle's stencil lies outside the grid
+    assert bench.touched_nodes(base, (16, 16, 16)) == 54
+    assert bench.touched_nodes(np.array([[14, 14, 14]]), (16, 16, 16)) == 8
 
 
 def test_reference_arm_runs_on_rank_zero_only(small_sample, monkeypatch):

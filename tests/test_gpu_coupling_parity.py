@@ -270,3 +270,82 @@ def test_simulation_runner_bookkeeping(tmp_path):
         sim.run(steps=0)
     fr = sim.coupler.solid_volume_fraction_numpy()
     assert fr.min() >= 0.0 and fr.max() <= 1.0
+
+
+def test_runner_diagnostics_are_device_resident():
+    """FSISimulation.step() returns the reference's 18 diagnostics from device reductions
+    with a single host synchronisation and no tensor copied to the host by .cpu()/.item();
+    the values agree with the per-accessor host path (float64 sums vs float32 numpy)."""
+    import torch
+
+    cfg, solid, pos = coupled_smoke_config(steps=5)
+    cfg = dataclasses.replace(cfg, coupling=dataclasses.replace(
+        cfg.coupling, immersed_boundary_enabled=True, immersed_boundary_drag=0.1,
+        immersed_boundary_fraction_threshold=0.05, contact_enabled=True,
+        contact_fraction_threshold=0.5, contact_velocity_damping=0.01))
+    sim = FSISimulation(cfg)
+    sim.initialize_lbm(solid)
+    sim.initialize_mpm_from_numpy(pos)
+    for _ in range(2):
+        sim.step()
+    counts = {"sync": 0, "cpu": 0, "item": 0}
+    real_sync, real_cpu, real_item = torch.cuda.Stream.synchronize, torch.Tensor.cpu, torch.Tensor.item
+
+    def sync(self, *a, **k):
+        counts["sync"] += 1
+        return real_sync(self, *a, **k)
+
+    def cpu(self, *a, **k):
+        counts["cpu"] += 1
+        return real_cpu(self, *a, **k)
+
+    def item(self, *a, **k):
+        counts["item"] += 1
+        return real_item(self, *a, **k)
+
+    torch.cuda.Stream.synchronize, torch.Tensor.cpu, torch.Tensor.item = sync, cpu, item
+    try:
+        d = sim.step(body_force=(2.0e-5, 0.0, 0.0))
+    finally:
+        torch.cuda.Stream.synchronize, torch.Tensor.cpu, torch.Tensor.item = real_sync, real_cpu, real_item
+    assert counts == {"sync": 1, "cpu": 0, "item": 0}, counts
+    assert list(d) == [k for k in (
+        "step", "time", "lbm_total_mass", "lbm_max_velocity_norm", "mpm_particle_count",
+        "mpm_center_of_mass", "mpm_max_velocity_norm", "total_particle_coupling_force",
+        "total_fluid_coupling_force", "coupling_unsupported_particle_count",
+        "coupling_partial_support_particle_count", "coupling_clipped_particle_count",
+        "coupling_effective_gamma", "coupling_ib_active_cell_count",
+        "coupling_ib_clipped_cell_count", "coupling_ib_total_force_norm",
+        "coupling_contact_candidate_count", "coupling_contact_damped_particle_count")]
+    cd = sim.coupler.coupling_diagnostics()
+    assert d["lbm_total_mass"] == pytest.approx(sim.lbm.total_mass(), rel=1e-12)
+    assert d["lbm_max_velocity_norm"] == pytest.approx(sim.lbm.max_velocity_norm(), rel=1e-12)
+    np.testing.assert_allclose(d["mpm_center_of_mass"], sim.mpm.center_of_mass(), rtol=1e-6)
+    assert d["mpm_max_velocity_norm"] == pytest.approx(sim.mpm.max_velocity_norm(), rel=1e-6)
+    np.testing.assert_allclose(d["total_particle_coupling_force"],
+                               sim.coupler.total_particle_coupling_force(), rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(d["total_fluid_coupling_force"],
+                               sim.coupler.total_fluid_coupling_force(), rtol=1e-5, atol=1e-12)
+    for key in ("unsupported_particle_count", "partial_support_particle_count",
+                "clipped_particle_count", "ib_active_cell_count", "ib_clipped_cell_count",
+                "contact_candidate_count", "contact_damped_particle_count"):
+        assert d["coupling_" + key] == cd[key], key
+    assert d["coupling_ib_total_force_norm"] == pytest.approx(cd["ib_total_force_norm"], rel=1e-6)
+    assert d["coupling_ib_active_cell_count"] > 0 and d["coupling_contact_candidate_count"] > 0
+
+
+def test_body_force_per_step_matches_config_force():
+    """step(body_force=g) with g equal to LBMConfig.force repeats the plain step bit for bit."""
+    cfg, solid, pos = coupled_smoke_config(steps=3)
+    sims = []
+    for bf in (None, cfg.lbm.force):
+        sim = FSISimulation(cfg)
+        sim.initialize_lbm(solid)
+        sim.initialize_mpm_from_numpy(pos)
+        for _ in range(3):
+            sim.step(body_force=bf)
+        sims.append(sim)
+    np.testing.assert_array_equal(sims[0].lbm.distribution_numpy(), sims[1].lbm.distribution_numpy())
+    np.testing.assert_array_equal(sims[0].mpm.positions_numpy(), sims[1].mpm.positions_numpy())
+    with pytest.raises(ValueError):
+        sims[0].step(body_force=(1.0, 2.0))
