@@ -304,33 +304,64 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
   }
 
   if (act) {
-    const int lane = threadIdx.x & 31;
-    for (int it = 0; it < 27; ++it) {
-      const int s = (it + lane) % 27;
-      const int i = s / 9, j = (s / 3) % 3, k = s % 3;
-      const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
-      if (!inside(m, ni, nj, nk)) continue;
-      const float wx = bspline_w(fx[0], i), wy = bspline_w(fx[1], j), wz = bspline_w(fx[2], k);
-      const float w = __fmul_rn(__fmul_rn(wx, wy), wz);
-      const float d0 = __fmul_rn(__fsub_rn((float)i, fx[0]), m.dx);
-      const float d1 = __fmul_rn(__fsub_rn((float)j, fx[1]), m.dx);
-      const float d2 = __fmul_rn(__fsub_rn((float)k, fx[2]), m.dx);
-      float add[3];
+    // Per-axis stencil terms, once per particle: weights, offsets (i - fx) dx, in-grid tests
+    // and the node's place in the tile (or grid). Odd lanes walk the stencil backwards (their
+    // axis terms are stored reversed), so the two particles of a sub-cell pair, which share a
+    // base cell, add into different nodes at each step.
+    const bool rev = (threadIdx.x & 1) != 0;
+    float wa[3][3], da[3][3];
+    bool ina[3][3];
+    int oa[3][3];  // axis offset of stencil step s: the node index is base + oa
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float ad = dot3r(affine[3 * a], affine[3 * a + 1], affine[3 * a + 2], d0, d1, d2);
-        add[a] = __fmul_rn(w, __fadd_rn(__fadd_rn(mv[a], ad), dtf[a]));
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int s3 = 0; s3 < 3; ++s3) {
+        const int o = rev ? 2 - s3 : s3;
+        oa[a][s3] = o;
+        wa[a][s3] = bspline_w(fx[a], o);
+        da[a][s3] = __fmul_rn(__fsub_rn((float)o, fx[a]), m.dx);
+        const int n = base[a] + o;
+        ina[a][s3] = n >= 0 && n < (a == 0 ? m.nx : (a == 1 ? m.ny : m.nz));
       }
-      const float addm = __fmul_rn(w, mass);
-      if (use_tile) {
-        const int t = ((ni - box.lo[0]) * box.ext[1] + (nj - box.lo[1])) * box.ext[2] + (nk - box.lo[2]);
-        atomicAdd(&tile[0][t], add[0]);
-        atomicAdd(&tile[1][t], add[1]);
-        atomicAdd(&tile[2][t], add[2]);
-        atomicAdd(&tile[3][t], addm);
-      } else {
-        red_add_v4(grid + node_index(m, ni, nj, nk), add[0], add[1], add[2], addm);
-        mark_block(m, dirty, ni, nj, nk);
+    const int st1 = use_tile ? box.ext[2] : m.nz;
+    const long long st0 = use_tile ? (long long)box.ext[1] * box.ext[2] : (long long)m.ny * m.nz;
+    const long long t0 = use_tile
+        ? ((long long)(base[0] - box.lo[0]) * box.ext[1] + (base[1] - box.lo[1])) * box.ext[2] + (base[2] - box.lo[2])
+        : ((long long)base[0] * m.ny + base[1]) * m.nz + base[2];
+#pragma unroll
+    for (int si = 0; si < 3; ++si) {
+      if (!ina[0][si]) continue;
+#pragma unroll
+      for (int sj = 0; sj < 3; ++sj) {
+        if (!ina[1][sj]) continue;
+        const float wxy = __fmul_rn(wa[0][si], wa[1][sj]);
+        // dot3r's ((A0 d0 + A1 d1) + A2 d2): the first two terms are shared by the 3 k.
+        float pa[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          pa[a] = __fadd_rn(__fmul_rn(affine[3 * a], da[0][si]), __fmul_rn(affine[3 * a + 1], da[1][sj]));
+#pragma unroll
+        for (int sk = 0; sk < 3; ++sk) {
+          if (!ina[2][sk]) continue;
+          const float w = __fmul_rn(wxy, wa[2][sk]);
+          float add[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float ad = __fadd_rn(pa[a], __fmul_rn(affine[3 * a + 2], da[2][sk]));
+            add[a] = __fmul_rn(w, __fadd_rn(__fadd_rn(mv[a], ad), dtf[a]));
+          }
+          const float addm = __fmul_rn(w, mass);
+          const long long t = t0 + oa[0][si] * st0 + oa[1][sj] * st1 + oa[2][sk];
+          if (use_tile) {
+            atomicAdd(&tile[0][t], add[0]);
+            atomicAdd(&tile[1][t], add[1]);
+            atomicAdd(&tile[2][t], add[2]);
+            atomicAdd(&tile[3][t], addm);
+          } else {
+            red_add_v4(grid + t, add[0], add[1], add[2], addm);
+            mark_block(m, dirty, base[0] + oa[0][si], base[1] + oa[1][sj], base[2] + oa[2][sk]);
+          }
+        }
       }
     }
   }
@@ -407,26 +438,42 @@ __device__ __forceinline__ void g2p_body(const Mpm& m, const PView& P,
   float nv[3] = {0.f, 0.f, 0.f};
   float nc[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   const float four_inv_dx = __fmul_rn(4.f, m.inv_dx);
+  // Per-axis stencil terms, once per particle; the sums run in the reference's node order.
+  float wa[3][3], dp[3][3];
+  bool ina[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {
+      wa[a][o] = bspline_w(fx[a], o);
+      dp[a][o] = __fsub_rn((float)o, fx[a]);
+      const int n = base[a] + o;
+      ina[a][o] = n >= 0 && n < (a == 0 ? m.nx : (a == 1 ? m.ny : m.nz));
+    }
+  const int st1 = use_tile ? box.ext[2] : m.nz;
+  const long long st0 = use_tile ? (long long)box.ext[1] * box.ext[2] : (long long)m.ny * m.nz;
+  const long long t0 = use_tile
+      ? ((long long)(base[0] - box.lo[0]) * box.ext[1] + (base[1] - box.lo[1])) * box.ext[2] + (base[2] - box.lo[2])
+      : ((long long)base[0] * m.ny + base[1]) * m.nz + base[2];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const float wx = bspline_w(fx[0], i);
+    if (!ina[0][i]) continue;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const float wy = bspline_w(fx[1], j);
+      if (!ina[1][j]) continue;
+      const float wxy = __fmul_rn(wa[0][i], wa[1][j]);
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const int ni = base[0] + i, nj = base[1] + j, nk = base[2] + k;
-        if (!inside(m, ni, nj, nk)) continue;
-        const float w = __fmul_rn(__fmul_rn(wx, wy), bspline_w(fx[2], k));
-        const float dpos[3] = {__fsub_rn((float)i, fx[0]), __fsub_rn((float)j, fx[1]),
-                               __fsub_rn((float)k, fx[2])};
+        if (!ina[2][k]) continue;
+        const float w = __fmul_rn(wxy, wa[2][k]);
+        const long long t = t0 + i * st0 + j * st1 + k;
         float gv[3];
         if (use_tile) {
-          const int t = ((ni - box.lo[0]) * box.ext[1] + (nj - box.lo[1])) * box.ext[2] + (nk - box.lo[2]);
           gv[0] = tile[0][t]; gv[1] = tile[1][t]; gv[2] = tile[2][t];
         } else {
-          grid_op(m, grid[node_index(m, ni, nj, nk)], ni, nj, nk, gv);
+          grid_op(m, grid[t], base[0] + i, base[1] + j, base[2] + k, gv);
         }
+        const float dpos[3] = {dp[0][i], dp[1][j], dp[2][k]};
 #pragma unroll
         for (int a = 0; a < 3; ++a) nv[a] = __fadd_rn(nv[a], __fmul_rn(w, gv[a]));
         const float s = __fmul_rn(four_inv_dx, w);
