@@ -41,7 +41,8 @@ COUPLED_BYTES_PER_PARTICLE = 224  # per particle-substep with the coupling force
 MPM_BYTES_PER_NODE = 32       # per touched grid node per substep
 # Kernel launches per call of each entry point the timed regions use.
 LAUNCHES = {"fsi_coupling_forces": 1, "fsi_mpm_substep": 3, "fsi_mpm_substep_sorted": 10,
-            "fsi_coupled_substep": 10, "fsi_coupling_assemble": 1, "fsi_contact": 1,
+            "fsi_coupled_substep": 10, "fsi_coupled_substep_tiled": 4,
+            "fsi_coupling_assemble": 1, "fsi_contact": 1,
             "fsi_lbm_update_macro": 1, "fsi_lbm_macro_diagnostics": 1, "fsi_lbm_reduce": 1,
             "fsi_coupled_diagnostics": 1, "fsi_lbm_force_op": 1, "fsi_mpm_reduce": 1,
             "fsi_coupling_reduce": 1}

@@ -310,6 +310,20 @@ int fsi_coupled_substep(const fsi_coupling_desc* coupling, const fsi_mpm_desc* d
                         float* accum, float* valid_weight, int32_t* coupling_mask, void* counters,
                         float* grid, void* workspace, int64_t workspace_bytes, void* stream);
 
+/* One coupled MPM substep on the tiled scatter of fsi_mpm_substep: fsi_coupling_forces and
+ * P2G, then grid update + G2P and the block clear. Under 2 x 152 x 256 particles the coupling
+ * is folded into P2G (each particle's coupling force formed first, then the stress and the
+ * 27-node scatter, the fluid reaction and solid fraction reduced into `accum` beside it);
+ * above it the coupling runs as its own lighter kernel before P2G. Zeroes and then fills the unsupported /
+ * partial / clipped counters. `grid` and `dirty` as for fsi_mpm_substep. Replaces one
+ * iteration of the substep loop of LBMMpmCoupler.step (fsi/coupling.py:146-158):
+ * _compute_coupling_forces_kernel and MPMSolver3D.substep. */
+int fsi_coupled_substep_tiled(const fsi_coupling_desc* coupling, const fsi_mpm_desc* desc,
+                              const fsi_particles* particles, const float* macro,
+                              const uint32_t* flags, float* accum, float* valid_weight,
+                              int32_t* coupling_mask, void* counters, float* grid,
+                              uint8_t* dirty, void* stream);
+
 /* Rebuilds the LBM force field float[3][N] for the next lattice step:
  *   FSI_ASSEMBLE_CLAMP_FRACTION  accum.w = min(accum.w, 1)   (coupling.py:408-411)
  *   (always)                     force = fluid ? base : 0     (lbm3d.py:504-510)

@@ -1,9 +1,11 @@
 // MLS-MPM building blocks shared by the single-solver kernels (mpm.cu) and the batched
 // kernels (batch.cu): solver parameters, particle views, B-spline weights, the polar
-// rotation, and the per-CTA bodies of P2G, grid update + G2P and the block clear.
+// rotation, and the per-CTA bodies of P2G (optionally with the penalty coupling folded in),
+// grid update + G2P and the block clear.
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include "coupling_core.cuh"
 #include "fsi_common.cuh"
 
 namespace fsi {
@@ -271,8 +273,13 @@ __device__ __forceinline__ void p2g_stress_affine(const Mpm& m, const PView& P, 
 }
 
 // P2G of particle p (this thread) within its CTA; every thread of the CTA calls it.
+// kCoupled folds _compute_coupling_forces_kernel (fsi/coupling.py:332-406) in front of the
+// scatter: the particle's coupling force is formed first (it is P2G's dt f term) and the
+// fluid reaction and solid fraction are spread into fa.accum beside the grid scatter.
+template <bool kCoupled = false>
 __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* __restrict__ grid,
-                                         uint8_t* __restrict__ dirty, int p) {
+                                         uint8_t* __restrict__ dirty, int p,
+                                         const ForceArgs* fa = nullptr) {
   __shared__ float tile[4][kTileCap];
   __shared__ int sh[8];
   const long long cap = m.cap;
@@ -281,6 +288,27 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
   int base[3] = {0, 0, 0};
   float fx[3] = {0.f, 0.f, 0.f};
   float affine[9], mv[3], dtf[3], mass = 0.f;
+  // coupling: in-grid fluid stencil nodes (bit 9i + 3j + k), valid weight, force, volume
+  uint32_t usable = 0;
+  float valid = 0.f, pf[3] = {0.f, 0.f, 0.f}, vp = 0.f;
+  if (kCoupled) {
+    bool partial = false, clipped = false, unsupported = false;
+    if (act) {
+      int cb[3];
+      float cw[3][3];
+      if (!coupling_particle<false>(*fa, p, cb, cw, usable, valid, pf, partial, clipped,
+                                    unsupported)) {
+        usable = 0;
+        pf[0] = pf[1] = pf[2] = 0.f;
+      }
+      vp = P.vol[p];
+    } else if (p < m.n) {
+      P.fp[p] = 0.f; P.fp[cap + p] = 0.f; P.fp[2 * cap + p] = 0.f;
+    }
+    warp_count(&fa->cnt->unsupported, unsupported);
+    warp_count(&fa->cnt->partial, partial);
+    warp_count(&fa->cnt->clipped, clipped);
+  }
   if (act) {
     float x[3];
     load_particle_x(P, cap, p, x);
@@ -289,7 +317,7 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       mv[a] = __fmul_rn(mass, P.v[a * cap + p]);
-      dtf[a] = __fmul_rn(m.dt, P.fp[a * cap + p]);
+      dtf[a] = __fmul_rn(m.dt, kCoupled ? pf[a] : P.fp[a * cap + p]);
     }
   }
 
@@ -328,6 +356,8 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
     const long long t0 = use_tile
         ? ((long long)(base[0] - box.lo[0]) * box.ext[1] + (base[1] - box.lo[1])) * box.ext[2] + (base[2] - box.lo[2])
         : ((long long)base[0] * m.ny + base[1]) * m.nz + base[2];
+    const long long g0 = ((long long)base[0] * m.ny + base[1]) * m.nz + base[2];  // lattice node
+    const long long gs0 = (long long)m.ny * m.nz;
 #pragma unroll
     for (int si = 0; si < 3; ++si) {
       if (!ina[0][si]) continue;
@@ -352,6 +382,12 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
           }
           const float addm = __fmul_rn(w, mass);
           const long long t = t0 + oa[0][si] * st0 + oa[1][sj] * st1 + oa[2][sk];
+          if (kCoupled && ((usable >> (9 * oa[0][si] + 3 * oa[1][sj] + oa[2][sk])) & 1u)) {
+            float4 c = coupling_spread_terms(fa->c, w, valid, pf, vp);
+            if (!fa->c.build_fraction) c.w = 0.f;
+            red_add_v4(fa->accum + g0 + oa[0][si] * gs0 + oa[1][sj] * m.nz + oa[2][sk],
+                       c.x, c.y, c.z, c.w);
+          }
           if (use_tile) {
             atomicAdd(&tile[0][t], add[0]);
             atomicAdd(&tile[1][t], add[1]);

@@ -155,6 +155,9 @@ _SIGNATURES = {
     "fsi_coupled_substep": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc),
                              ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                              ctypes.c_int64, _VP], ctypes.c_int),
+    "fsi_coupled_substep_tiled": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc),
+                                   ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                   _VP, _VP], ctypes.c_int),
     "fsi_mpm_polar": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "fsi_mpm_base_cells": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP], ctypes.c_int),
     "fsi_mpm_reduce": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),

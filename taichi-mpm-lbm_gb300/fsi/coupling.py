@@ -119,17 +119,21 @@ class LBMMpmCoupler:
                  nat.stream_ptr())
 
     def _coupled_substep(self, mpm_dt: float, dt_ratio: float, build_fraction: bool) -> None:
-        """Coupling force + MPM substep in one sorted pass (the spread folded into P2G)."""
+        """Coupling force + MPM substep with the coupling folded into P2G (the sorted or the
+        tiled scatter, after the solver's p2g_mode)."""
         self._desc.gamma_eff = self._gamma_for_kernel()
         self._desc.dt_ratio = float(np.float32(dt_ratio))
         self._desc.build_fraction = int(build_fraction)
         mpm = self.mpm
         mpm.desc.dt = float(np.float32(mpm_dt))
-        nat.call("fsi_coupled_substep", self._desc, mpm.desc, mpm.particles,
-                 nat.ptr(self.lbm.macro), nat.ptr(self.lbm.flags), nat.ptr(self._accum),
-                 nat.ptr(self._valid), nat.ptr(self._mask), nat.ptr(self._counters),
-                 nat.ptr(mpm._grid), nat.ptr(mpm.workspace), mpm.workspace.numel(),
-                 nat.stream_ptr())
+        common = (self._desc, mpm.desc, mpm.particles, nat.ptr(self.lbm.macro),
+                  nat.ptr(self.lbm.flags), nat.ptr(self._accum), nat.ptr(self._valid),
+                  nat.ptr(self._mask), nat.ptr(self._counters), nat.ptr(mpm._grid))
+        if mpm.sorted:
+            nat.call("fsi_coupled_substep", *common, nat.ptr(mpm.workspace),
+                     mpm.workspace.numel(), nat.stream_ptr())
+        else:
+            nat.call("fsi_coupled_substep_tiled", *common, nat.ptr(mpm._dirty), nat.stream_ptr())
 
     def _contact_kernel(self) -> None:
         nat.call("fsi_contact", self._desc, self.mpm.desc, self.mpm.particles,
@@ -166,25 +170,16 @@ class LBMMpmCoupler:
         mpm_dt = lbm_dt_value / float(self.substeps)
         dt_ratio = mpm_dt / lbm_dt_value
         for substep in range(self.substeps):
-            if self.enabled and self.mpm.sorted:
-                # Coupling force, spread and MPM substep in one sorted pass; it zeroes the
-                # per-substep counters itself (clear_particle_diagnostics of coupling.py:147
-                # for the counters; weights and masks are rewritten for every active particle).
+            if self.enabled:
+                # Coupling force, spread and MPM substep in one pass. clear_particle_diagnostics
+                # of coupling.py:147: the pass zeroes the per-substep counters itself, rewrites
+                # the weight and mask of every active particle, and inactive particles keep the
+                # zeros written by clear_coupling_fields() above.
                 self._coupled_substep(mpm_dt, dt_ratio,
                                       substep == 0 and self.build_solid_volume_fraction)
-                if self.contact_enabled:
-                    self._contact_kernel()
-                continue
-            if self.enabled:
-                # clear_particle_diagnostics() of coupling.py:147: the coupling kernel rewrites
-                # the weight and mask of every active particle, and inactive particles keep
-                # the zeros written by clear_coupling_fields() above, so only the per-substep
-                # counters need clearing here.
-                self._counters[0:5].zero_()
-                self._coupling_kernel(dt_ratio, substep == 0 and self.build_solid_volume_fraction)
             else:
                 self.mpm.clear_particle_force()
-            self.mpm.substep(dt=mpm_dt)
+                self.mpm.substep(dt=mpm_dt)
             if self.contact_enabled:
                 self._contact_kernel()
         mode = 0
