@@ -672,8 +672,9 @@ class FSISimulation:
         return n
 
     def initialize_mpm_from_numpy(self, positions, velocities=None, particle_mass=None,
-                                  particle_volume=None):
-        n = self.mpm.initialize_particles_from_numpy(positions, velocities, particle_mass, particle_volume)
+                                  particle_volume=None, youngs_modulus=None, poisson_ratio=None):
+        n = self.mpm.initialize_particles_from_numpy(positions, velocities, particle_mass,
+                                                     particle_volume, youngs_modulus, poisson_ratio)
         self._mpm_initialized = True
         return n
 

@@ -349,3 +349,35 @@ def test_body_force_per_step_matches_config_force():
     np.testing.assert_array_equal(sims[0].mpm.positions_numpy(), sims[1].mpm.positions_numpy())
     with pytest.raises(ValueError):
         sims[0].step(body_force=(1.0, 2.0))
+
+
+def test_coupled_large_launch_matches_oracle():
+    """A coupled step with enough particles (85,184) for the coupling's own shared-memory
+    kernel on the tiled scatter: lattice and particle fields within relative L2 1e-5 of the
+    oracle after two steps, coupling masks and counters exact, the coupling force within the
+    atomic scatter's float32 noise."""
+    from fsi import scenes
+
+    nx, ny, nz = 48, 40, 40
+    lbm = periodic_lbm(nx=nx, ny=ny, nz=nz, viscosity=(0.6 - 0.5) / 3.0, force=(1e-5, 0.0, 0.0))
+    mpm = small_mpm(nx=nx, ny=ny, nz=nz, max_particles=90_000, dt=0.25, density=1.5,
+                    youngs_modulus=0.05, poisson_ratio=0.3, boundary_width=3)
+    cfg = SimulationConfig(num_steps=2, lbm_dt=1.0, lbm=lbm, mpm=mpm,
+                           coupling=CouplingConfig(gamma=0.1, mpm_substeps_per_lbm_step=4))
+    solid = scenes.wall_mask(nx, ny, nz)
+    pos = scenes.cube_particles(np.array([10.0, 9.0, 9.0]), 22, 2, np.random.default_rng(5))
+    assert len(pos) == 85_184
+    sim = FSISimulation(cfg)
+    ref = O.FSISimulation(cfg, nthreads=NTHREADS, polar="device")
+    for s in (sim, ref):
+        s.initialize_lbm(solid)
+        s.initialize_mpm_from_numpy(pos)
+    for _ in range(2):
+        sim.coupler.step(cfg.lbm_dt)
+        ref.coupler.step(cfg.lbm_dt)
+    assert rel_l2(sim.lbm.density_numpy(), ref.lbm.rho) <= 1e-5
+    assert rel_l2(sim.lbm.velocity_numpy(), ref.lbm.v) <= 1e-5
+    assert rel_l2(sim.mpm.positions_numpy(), ref.mpm.positions_numpy()) <= 1e-5
+    assert rel_l2(sim.mpm.particle_forces_numpy(), ref.mpm.particle_forces_numpy()) <= 1e-4
+    assert rel_l2(sim.coupler.coupling_force_numpy(), ref.coupler.coupling_force_numpy()) <= 1e-4
+    _assert_masks_and_counters(sim, ref)
