@@ -209,9 +209,9 @@ int fsi_mpm_substep(const fsi_mpm_desc* desc, const fsi_particles* particles, fl
  * particles; the grid and dirty-block map live in one static device array of this library
  * (FSI_NOALLOC_MAX_NODES float4 nodes + FSI_NOALLOC_MAX_BLOCKS bytes, about 4 MB held on every
  * GPU that loads the library until exit). Grids above either limit are rejected with
- * FSI_ERR_INVALID_ARG. The first call on a device looks up the array's device address with
- * cudaGetSymbolAddress (that device current) and caches it; make that first call before any
- * stream capture. All calls share the array: each call clears the part it uses, and calls
+ * FSI_ERR_INVALID_ARG. The first call in a CUDA context (per device and per context, e.g.
+ * again after cudaDeviceReset) looks up the array's device address with cudaGetSymbolAddress
+ * and caches it under the context's ID; make that first call before any stream capture. All calls share the array: each call clears the part it uses, and calls
  * whose work overlaps on the GPU (other streams, other threads) race on it. Nothing is
  * allocated or freed. */
 #define FSI_NOALLOC_MAX_NODES (64 * 64 * 64)

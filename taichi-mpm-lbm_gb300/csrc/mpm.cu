@@ -229,13 +229,45 @@ constexpr long long kNoAllocBytes = kNoAllocGridBytes + FSI_NOALLOC_MAX_BLOCKS;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kMaxDevices] = {};
+// Cache of the array's device address per CUDA context (identified by its driver-assigned
+// context ID, which is never reused: a context re-created after cudaDeviceReset, or another
+// context of the same device made current by a driver-API host, gets its own lookup).
+unsigned long long g_noalloc_ctx[kMaxContexts] = {};
+void* g_noalloc_ptr[kMaxContexts] = {};
+int g_noalloc_used = 0;
 
-// Device address of the static array on the current device. Host code cannot
-// use the symbol itself (it names a host-side stand-in), so the address is
-// looked up once per device, with that device current, and cached.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+// The driver's cuCtxGetCurrent / cuCtxGetId, reached through the runtime (the library does
+// not link the driver library); NULL when unavailable.
+template <class Fn>
+Fn driver_fn(const char* name) {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<Fn>(fn);
+}
+
+// ID of the current context (0 when it cannot be read or no context is current yet).
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+  static CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId");
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || ctx == nullptr) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != 0) return 0;
+  return id + 1;  // 0 stays "unknown"
+}
+
+// Device address of the static array in the current context. Host code cannot use the
+// symbol itself (it names a host-side stand-in), so the address is looked up with
+// cudaGetSymbolAddress, once per context, and cached under that context's ID.
 int noalloc_scratch(void** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -243,18 +275,26 @@ int noalloc_scratch(void** out) {
     set_error("cudaGetDevice: %s", cudaGetErrorString(e));
     return FSI_ERR_CUDA;
   }
-  FSI_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal %d out of range", dev);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_ptr[dev] == nullptr) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      set_error("cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
-      return FSI_ERR_CUDA;
+  unsigned long long id = current_context_id();
+  for (int i = 0; id != 0 && i < g_noalloc_used; ++i)
+    if (g_noalloc_ctx[i] == id) {
+      *out = g_noalloc_ptr[i];
+      return FSI_OK;
     }
-    g_noalloc_ptr[dev] = p;
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the primary context current if none is
+  if (e != cudaSuccess || p == nullptr) {
+    set_error("cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+    return FSI_ERR_CUDA;
   }
-  *out = g_noalloc_ptr[dev];
+  if (id == 0) id = current_context_id();
+  if (id != 0 && g_noalloc_used < kMaxContexts) {
+    g_noalloc_ctx[g_noalloc_used] = id;
+    g_noalloc_ptr[g_noalloc_used] = p;
+    ++g_noalloc_used;
+  }
+  *out = p;
   return FSI_OK;
 }
 

@@ -83,9 +83,9 @@ def run_lbm_mass_conservation_case() -> ValidationReport:
         case_name="lbm_periodic_mass_conservation",
         metrics=(
             bounded_metric("relative_mass_error", relative_error(mass1, mass0), upper=1.0e-5,
-                           description="Relative total fluid mass drift on a periodic grid."),
+                           description="Periodic lattice: change of total mass relative to the start."),
             finite_metric("max_velocity_norm", solver.max_velocity_norm(), upper=1.0e-4,
-                          description="Maximum velocity norm remains finite and near zero."),
+                          description="Largest fluid speed stays finite and close to zero."),
         ),
         metadata={"steps": steps, "grid": [solver.nx, solver.ny, solver.nz]},
     )
@@ -103,9 +103,9 @@ def run_lbm_force_response_case() -> ValidationReport:
         case_name="lbm_force_response",
         metrics=(
             bounded_metric("mean_ux_growth", ux1 - ux0, lower=1.0e-12,
-                           description="Mean x velocity grows under positive x force."),
+                           description="A positive x body force raises the mean x velocity."),
             finite_metric("max_velocity_norm", solver.max_velocity_norm(), upper=1.0e-2,
-                          description="Forced velocity remains bounded in the smoke case."),
+                          description="The forced flow speed stays bounded."),
         ),
         metadata={"steps": steps, "grid": [solver.nx, solver.ny, solver.nz]},
     )
@@ -124,9 +124,9 @@ def run_mpm_zero_gravity_com_case() -> ValidationReport:
         metrics=(
             bounded_metric("center_of_mass_drift_norm", float(np.linalg.norm(com1 - com0)),
                            upper=1.0e-3, units="grid",
-                           description="COM drift stays small without gravity or initial velocity."),
+                           description="Centre of mass barely moves with no gravity and no initial velocity."),
             finite_metric("max_velocity_norm", solver.max_velocity_norm(), upper=1.0e-3,
-                          description="MPM velocities remain bounded without gravity."),
+                          description="Particle speeds stay bounded with gravity off."),
         ),
         metadata={"steps": steps, "particle_count": solver.particle_count()},
     )
@@ -147,13 +147,13 @@ def run_mpm_gravity_response_case() -> ValidationReport:
         metrics=(
             bounded_metric("center_of_mass_y_delta", float(com1[1] - com0[1]), upper=-1.0e-12,
                            units="grid",
-                           description="COM moves downward under weak negative y gravity."),
+                           description="A weak -y gravity lowers the centre of mass."),
             bounded_metric("positions_finite", 1.0 if np.isfinite(positions).all() else 0.0,
                            lower=1.0, upper=1.0,
-                           description="All particle positions remain finite."),
+                           description="No particle position becomes NaN or infinite."),
             bounded_metric("velocities_finite", 1.0 if np.isfinite(velocities).all() else 0.0,
                            lower=1.0, upper=1.0,
-                           description="All particle velocities remain finite."),
+                           description="No particle velocity becomes NaN or infinite."),
         ),
         metadata={"steps": steps, "particle_count": solver.particle_count()},
     )
@@ -172,12 +172,12 @@ def run_coupled_drift_case() -> ValidationReport:
         case_name="coupled_enabled_vs_disabled_drift",
         metrics=(
             bounded_metric("enabled_dx", enabled_dx, lower=1.0e-7, units="grid",
-                           description="Enabled coupling advects the particle in +x."),
+                           description="With coupling on, the +x flow carries the particle in +x."),
             bounded_metric("disabled_dx_abs", abs(disabled_dx), upper=1.0e-6, units="grid",
-                           description="Disabled coupling leaves the particle nearly fixed."),
+                           description="With coupling off, the particle stays put."),
             bounded_metric("enabled_minus_disabled_dx", enabled_dx - disabled_dx, lower=1.0e-7,
                            units="grid",
-                           description="Enabled drift exceeds the disabled baseline."),
+                           description="Coupling on moves the particle farther than coupling off."),
         ),
         metadata={"steps": 2, "gamma": 5.0, "initial_lbm_ux": 1.0e-3},
     )
@@ -192,11 +192,11 @@ def run_coupling_force_balance_case() -> ValidationReport:
         case_name="coupling_force_balance",
         metrics=(
             bounded_metric("particle_force_x", float(particle_force[0]), lower=1.0e-12,
-                           description="Particle receives positive x force from uniform flow."),
+                           description="A uniform +x flow pushes the particle in +x."),
             bounded_metric("fluid_force_x", float(fluid_force[0]), upper=-1.0e-12,
-                           description="Fluid receives opposite x reaction force."),
+                           description="The fluid takes the equal and opposite x reaction."),
             bounded_metric("force_balance_norm", _force_balance_norm(sim.coupler), upper=1.0e-6,
-                           description="Particle force plus integrated fluid reaction is balanced."),
+                           description="Particle force and summed fluid reaction cancel."),
         ),
         metadata={"dt_ratio": 1.0, "cell_volume": sim.coupler.cell_volume},
     )
@@ -220,12 +220,12 @@ def run_coupling_force_limit_case() -> ValidationReport:
         metrics=(
             bounded_metric("particle_force_norm", float(np.linalg.norm(particle_force)),
                            upper=0.05 + 1.0e-7,
-                           description="High-gamma particle coupling force is clipped."),
+                           description="A large penalty gamma triggers the force clip."),
             bounded_metric("clipped_particle_count", float(diagnostics["clipped_particle_count"]),
                            lower=1.0,
-                           description="At least one particle records force or velocity clipping."),
+                           description="The clip counter records at least one particle."),
             bounded_metric("force_balance_norm", _force_balance_norm(sim.coupler), upper=1.0e-6,
-                           description="Clipped particle force still balances fluid reaction."),
+                           description="After clipping, particle force and fluid reaction still cancel."),
         ),
         metadata={"gamma": 100.0, "force_limit": 0.05},
     )
@@ -245,16 +245,16 @@ def run_coupling_boundary_support_case() -> ValidationReport:
         metrics=(
             bounded_metric("partial_support_particle_count",
                            float(diagnostics["partial_support_particle_count"]), lower=1.0,
-                           description="Near-boundary particle records partial support."),
+                           description="A particle by the grid edge is counted as partially supported."),
             bounded_metric("min_particle_valid_weight",
                            float(diagnostics["min_particle_valid_weight"]), lower=1.0e-6,
                            upper=1.0 - 1.0e-5,
-                           description="Valid support is finite and below full support."),
+                           description="Its valid weight is positive and below one."),
             bounded_metric("force_balance_norm", _force_balance_norm(sim.coupler), upper=1.0e-6,
-                           description="Partial-support coupling still balances fluid reaction."),
+                           description="With partial support, particle force and fluid reaction still cancel."),
             bounded_metric("particle_force_finite",
                            1.0 if np.isfinite(particle_force).all() else 0.0, lower=1.0,
-                           upper=1.0, description="Boundary particle force remains finite."),
+                           upper=1.0, description="The edge particle's force stays finite."),
         ),
         metadata={"particle_position": [-0.75, 4.0, 4.0], "min_valid_weight": 1.0e-6},
     )
@@ -283,18 +283,18 @@ def run_immersed_boundary_drag_case() -> ValidationReport:
         metrics=(
             bounded_metric("ib_active_cell_count", float(diagnostics["ib_active_cell_count"]),
                            lower=1.0,
-                           description="At least one dynamic occupied fluid cell receives IB drag."),
+                           description="Some fluid cell covered by the body gets immersed-boundary drag."),
             bounded_metric("ib_total_force_x", float(diagnostics["ib_total_force_x"]),
                            upper=-1.0e-12,
-                           description="IB drag opposes positive x fluid velocity."),
+                           description="The immersed-boundary drag points against the +x flow."),
             bounded_metric("ib_total_force_norm", float(diagnostics["ib_total_force_norm"]),
-                           lower=1.0e-12, description="IB drag total force is nonzero."),
+                           lower=1.0e-12, description="The summed immersed-boundary drag is not zero."),
             bounded_metric("max_velocity_not_increased",
                            float(sim.lbm.max_velocity_norm() - initial_speed), upper=1.0e-8,
-                           description="The IB smoke case does not increase max fluid speed."),
+                           description="Immersed-boundary drag does not speed up the fluid."),
             bounded_metric("velocity_finite", 1.0 if np.isfinite(velocity).all() else 0.0,
                            lower=1.0, upper=1.0,
-                           description="LBM velocity remains finite with IB drag enabled."),
+                           description="Fluid velocity stays finite with immersed-boundary drag on."),
         ),
         metadata={"drag": 0.1, "particle_volume": 4.0},
     )
@@ -319,14 +319,14 @@ def run_contact_diagnostics_case() -> ValidationReport:
         metrics=(
             bounded_metric("contact_candidate_count",
                            float(diagnostics["contact_candidate_count"]), lower=1.0,
-                           description="Static solid support marks at least one contact candidate."),
+                           description="Support from static solid flags at least one contact candidate."),
             bounded_metric("contact_damped_particle_count",
                            float(diagnostics["contact_damped_particle_count"]), lower=1.0,
-                           description="Contact damping is applied to at least one particle."),
+                           description="At least one particle is damped on contact."),
             bounded_metric("particle_contact_mask_sum", contact_mask_sum, lower=1.0,
-                           description="The active particle contact mask is set."),
+                           description="The contact mask of the particle is set."),
             bounded_metric("particle_speed_delta", float(final_speed - initial_speed),
-                           upper=-1.0e-6, description="Contact damping reduces particle speed."),
+                           upper=-1.0e-6, description="Contact damping slows the particle."),
         ),
         metadata={"damping": 0.25, "initial_speed": initial_speed},
     )

@@ -1,16 +1,14 @@
 """Regenerate the committed golden fixtures.
 
-1. The reference's own golden datasets (``data/reference/*.json`` of
-   lizhuoh9/taichi-mpm-lbm, schema v1 with per-metric tolerances) are copied
-   byte-for-byte into ``taichi-mpm-lbm_gb300/data/reference/``, where
-   ``fsi.reference_cases.default_reference_data_dir()`` finds them. They are
-   data (metric values and tolerances produced by the reference's Taichi
-   path), not source.
-2. ``oracle_fields_*.npz``: field-level vectors of the CPU oracle on small
-   seeded cases, used by tests that must run without the oracle library.
+The reference's own golden datasets (``data/reference/*.json`` of
+lizhuoh9/taichi-mpm-lbm, schema v1 with per-metric tolerances) are copied
+byte-for-byte into ``taichi-mpm-lbm_gb300/data/reference/``, where
+``fsi.reference_cases.default_reference_data_dir()`` finds them. They are data
+(metric values and tolerances produced by the reference's Taichi path), not
+source.
 
-Run from the repository root with the reference checkout available:
-    python tests/golden/make_golden.py [/path/to/reference]
+Run from the repository root, naming a checkout of the reference:
+    python tests/golden/make_golden.py /path/to/reference/checkout
 """
 from __future__ import annotations
 
@@ -34,6 +32,7 @@ def copy_reference_goldens(reference_root: Path) -> list[Path]:
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-    for p in copy_reference_goldens(ref):
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/reference/checkout")
+    for p in copy_reference_goldens(Path(sys.argv[1])):
         print("wrote", p.relative_to(ROOT))
