@@ -49,6 +49,9 @@ LAUNCHES = {"fsi_coupling_forces": 1, "fsi_mpm_substep": 3, "fsi_mpm_substep_sor
 # DRAM bytes per fluid cell and step kernel launch, from the ncu captures of the 192^3 scene
 # (dram__bytes_read.sum + dram__bytes_write.sum, odd/even launch average).
 TRAFFIC_PER_FLUID_CELL = {"f32/exact": 177.4, "f16/fast": 96.1}
+# DRAM bytes of one coupled step of the headline scene (dram__bytes_read.sum +
+# dram__bytes_write.sum summed over the step's launches, ncu capture of the third coupled step).
+TRAFFIC_PER_COUPLED_STEP = 5_665_800_000
 METRIC = "MLUPS & particle-steps/s on 1 GB300: plain vs FP16/learned, <=1% drag error"
 
 
@@ -619,7 +622,9 @@ def run_gpu(args) -> dict:
                       "substeps_and_assembly": round(sub_ms, 4)},
         "roofline": {
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None,
+            "frac": round(achieved / peak, 4), "traffic": TRAFFIC_PER_COUPLED_STEP,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the "
+                               "launches of one coupled step (the third) of this scene"),
             "kernel": "coupled step (all launches of LBMMpmCoupler.step)",
             "peak_source": peak_kind,
             "algorithmic_bytes_per_step": step_bytes,

@@ -250,7 +250,8 @@ __device__ __forceinline__ void assemble_body(const AssembleArgs& a, long long c
   if (c < a.g.n) {
     const bool fluid = !(a.flags[c] & kFlagSolid);
     float4 acc = a.accum[c];
-    if (a.mode & FSI_ASSEMBLE_CLAMP_FRACTION) {
+    if ((a.mode & FSI_ASSEMBLE_CLAMP_FRACTION) && !(acc.w <= 1.0f)) {
+      // min(phi, 1): only cells above one (or NaN) change, so only they are written back
       acc.w = fminf(acc.w, 1.0f);
       a.accum[c].w = acc.w;
     }

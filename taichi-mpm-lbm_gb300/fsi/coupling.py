@@ -86,6 +86,7 @@ class LBMMpmCoupler:
         self._counters = torch.zeros(12, dtype=torch.int32, device=dev)  # fsi_coupling_counters
         self._diag = torch.zeros(4, dtype=torch.float64, device=dev)
         self._coupled_step = 0
+        self._ib_written = False
         self._desc = nat.CouplingDesc()
         self._fill_desc()
 
@@ -149,6 +150,7 @@ class LBMMpmCoupler:
         if mode & nat.ASSEMBLE_IB:
             self._counters[5:7].zero_()
             self._counters[8:12].zero_()
+            self._ib_written = True
         macro = self.lbm.macro if mode & nat.ASSEMBLE_IB else None
         nat.call("fsi_coupling_assemble", self._desc, self.lbm._desc, nat.ptr(self.lbm.flags),
                  base_p, mode, nat.ptr(self._accum), nat.ptr(macro), nat.ptr(force),
@@ -272,7 +274,9 @@ class LBMMpmCoupler:
 
     def clear_coupling_fields(self) -> None:
         self._accum.zero_()
-        self._ib.zero_()
+        if self._ib_written:  # the IB force field stays zero while nothing writes it
+            self._ib.zero_()
+            self._ib_written = self.immersed_boundary_enabled
         self._counters.zero_()
         self.clear_particle_diagnostics()
 
@@ -376,6 +380,7 @@ class LBMMpmCoupler:
             raise ValueError("not a coupler checkpoint")
         for name in ("accum", "ib", "valid", "mask", "contact_mask", "counters"):
             getattr(self, "_" + name).copy_(state[name])
+        self._ib_written = True
         self._coupled_step = int(state["coupled_step"])
 
     def _validate_initialized(self) -> None:
