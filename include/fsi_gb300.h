@@ -4,8 +4,9 @@
  * Each entry point replaces one or more Taichi kernels of the reference
  * lizhuoh9/taichi-mpm-lbm (cited as file:line). Conventions:
  *   - all array arguments are device pointers owned by the caller (the Python
- *     package allocates them as torch CUDA tensors); the library never
- *     allocates or frees device memory;
+ *     package allocates them as torch CUDA tensors); the library allocates
+ *     device memory only for the scratch of a context or batch, in their
+ *     create / set-up calls, and frees it in their destroy calls;
  *   - descriptor structs and small `const float*` parameter vectors marked
  *     "host" are read on the host during the call;
  *   - work is enqueued on `stream` (a cudaStream_t passed as void*, NULL = the
@@ -362,6 +363,80 @@ int fsi_coupling_reduce(const fsi_lbm_desc* lbm, const float* accum, const uint3
 int fsi_coupled_diagnostics(const fsi_mpm_desc* mpm, const fsi_particles* particles,
                             const fsi_lbm_desc* lbm, const float* accum, const uint32_t* flags,
                             const void* counters, double* out, void* stream);
+
+/* ------------------------------------------------------------- one coupled scene
+ * The coupled timestep in one call, for hosts that do not run the Python package (C, C++,
+ * FFI). A context binds the caller's device buffers of one scene and owns only scratch (the
+ * MPM grid and block map or the sorted-scatter workspace); fsi_coupled_step then performs
+ * LBMMpmCoupler.step (fsi/coupling.py:135-173) with the lattice bookkeeping of
+ * LBMSolver3D.step (fsi/lbm3d.py:427-433): the same launches, in the same order and with the
+ * same arguments as the Python package, so both give the same results. */
+typedef struct fsi_ctx fsi_ctx;
+
+/* Scatter order of the MPM substep (MPMConfig.p2g_mode). */
+#define FSI_P2G_ATOMIC 0 /* fsi_mpm_substep / fsi_coupled_substep_tiled */
+#define FSI_P2G_SORTED 1 /* fsi_mpm_substep_sorted / fsi_coupled_substep */
+
+typedef struct fsi_scene_desc {
+  fsi_lbm_desc lbm;
+  fsi_mpm_desc mpm;           /* dt is set per substep to float32(lbm_dt / substeps) */
+  fsi_coupling_desc coupling; /* gamma_eff, dt_ratio, build_fraction: set per step / substep */
+  float base_force[3];        /* LBMConfig.force, the lattice's uniform body force */
+  float gamma;                /* CouplingConfig.gamma, ramped over gamma_ramp_steps */
+  int32_t gamma_ramp_steps;
+  int32_t coupling_enabled;          /* CouplingConfig.enabled */
+  int32_t build_solid_fraction;      /* CouplingConfig.build_solid_volume_fraction */
+  int32_t contact_enabled;           /* CouplingConfig.contact_enabled */
+  int32_t immersed_boundary_enabled; /* CouplingConfig.immersed_boundary_enabled */
+  int32_t p2g_mode;                  /* FSI_P2G_* */
+} fsi_scene_desc;
+
+/* Device buffers of the scene, owned by the caller; they must outlive the context. */
+typedef struct fsi_scene_buffers {
+  void* pops;           /* populations [19][N] in lbm.storage (fsi_lbm_init_fields) */
+  float* macro;         /* float[N][4] */
+  float* force[2];      /* two float[3][N] force buffers; force[0] holds the current force */
+  uint32_t* flags;      /* fsi_lbm_build_flags */
+  fsi_particles particles;
+  float* accum;         /* float[N][4]: the coupling fields of the last step */
+  float* ib_force;      /* float[3][N], or NULL without the immersed boundary */
+  float* valid_weight;  /* float[capacity] */
+  int32_t* coupling_mask; /* int32[capacity] */
+  int32_t* contact_mask;  /* int32[capacity], or NULL without contact */
+  void* counters;       /* fsi_coupling_counters */
+} fsi_scene_buffers;
+
+/* Validates the description and buffers and allocates the context's scratch (device memory,
+ * zero-filled; synchronous: call outside stream capture). The lattice starts as
+ * fsi_lbm_init_fields leaves it: no step taken, macro current, force[0] current; the
+ * coupled-step counter (the gamma ramp's) starts at 0. */
+int fsi_ctx_create(const fsi_scene_desc* desc, const fsi_scene_buffers* buffers, fsi_ctx** ctx);
+int fsi_ctx_destroy(fsi_ctx* ctx);
+
+/* Host bookkeeping of the context: lattice steps taken (their parity selects the AA access
+ * pattern), whether `macro` is current, the force buffers of the next and of the last
+ * lattice step (-1: none), and coupled steps taken. set_state adopts the state of a lattice
+ * stepped elsewhere (e.g. by the Python package on the same buffers). */
+int fsi_ctx_get_state(const fsi_ctx* ctx, int64_t* lattice_steps, int32_t* macro_current,
+                      int32_t* force_next, int32_t* force_last, int64_t* coupled_steps);
+int fsi_ctx_set_state(fsi_ctx* ctx, int64_t lattice_steps, int32_t macro_current,
+                      int32_t force_next, int32_t force_last, int64_t coupled_steps);
+
+/* `steps` coupled steps of lbm_dt with n_substeps MPM substeps each: per step, the coupling
+ * fields are cleared, each substep runs the coupling force, its spread and the MPM substep
+ * (fsi_coupled_substep_tiled or fsi_coupled_substep), then contact when enabled; the force
+ * for the next lattice step is assembled (base force `body_force`, host float[3], or
+ * desc.base_force when NULL) and the lattice steps. Asynchronous on `stream`, no allocation
+ * and no synchronisation: capturable in a CUDA graph (a graph of an even number of lattice
+ * steps returns the buffers to the same parity; the host state advances at capture). */
+int fsi_coupled_step(fsi_ctx* ctx, double lbm_dt, const float* body_force, int32_t n_substeps,
+                     int32_t steps, void* stream);
+
+/* The reductions behind FSISimulation.diagnostics (simulation.py:117-147) into device double
+ * out[30]: [0] sum of rho over fluid cells and [1] max |u| of the current state
+ * (fsi_lbm_macro_diagnostics, which also makes `macro` current, or fsi_lbm_reduce when it is;
+ * [2..7] scratch), [8..29] fsi_coupled_diagnostics. */
+int fsi_ctx_diagnostics(fsi_ctx* ctx, double* out, void* stream);
 
 /* ------------------------------------------------------------- batches of scenes
  * Many independent lattices advanced together: one launch per phase covers every lattice

@@ -24,7 +24,7 @@ LIB_DIR = PKG / "fsi" / "_lib"
 OBJ_DIR = LIB_DIR / "obj"
 LIB = LIB_DIR / "libfsi_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "lbm.cu", "mpm.cu", "mpm_sorted.cu", "coupling.cu", "batch.cu", "batch_step_f32.cu",
+SOURCES = ["capi.cu", "lbm.cu", "mpm.cu", "mpm_sorted.cu", "coupling.cu", "context.cu", "batch.cu", "batch_step_f32.cu",
            "batch_step_f16.cu", "batch_step_bf16.cu", "closure.cu"]
 
 

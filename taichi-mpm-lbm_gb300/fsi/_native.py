@@ -93,6 +93,31 @@ class CouplingDesc(ctypes.Structure):
     ]
 
 
+P2G_ATOMIC, P2G_SORTED = 0, 1
+
+
+class SceneDesc(ctypes.Structure):
+    _fields_ = [
+        ("lbm", LbmDesc), ("mpm", MpmDesc), ("coupling", CouplingDesc),
+        ("base_force", c_float3),
+        ("gamma", ctypes.c_float), ("gamma_ramp_steps", ctypes.c_int32),
+        ("coupling_enabled", ctypes.c_int32), ("build_solid_fraction", ctypes.c_int32),
+        ("contact_enabled", ctypes.c_int32), ("immersed_boundary_enabled", ctypes.c_int32),
+        ("p2g_mode", ctypes.c_int32),
+    ]
+
+
+class SceneBuffers(ctypes.Structure):
+    _fields_ = [
+        ("pops", ctypes.c_void_p), ("macro", ctypes.c_void_p),
+        ("force", ctypes.c_void_p * 2), ("flags", ctypes.c_void_p),
+        ("particles", Particles),
+        ("accum", ctypes.c_void_p), ("ib_force", ctypes.c_void_p),
+        ("valid_weight", ctypes.c_void_p), ("coupling_mask", ctypes.c_void_p),
+        ("contact_mask", ctypes.c_void_p), ("counters", ctypes.c_void_p),
+    ]
+
+
 class BatchLattice(ctypes.Structure):
     _fields_ = [
         ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
@@ -167,6 +192,17 @@ _SIGNATURES = {
     "fsi_coupling_reduce": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_coupled_diagnostics": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles),
                                  ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_ctx_create": ([ctypes.POINTER(SceneDesc), ctypes.POINTER(SceneBuffers),
+                        ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "fsi_ctx_destroy": ([_VP], ctypes.c_int),
+    "fsi_ctx_get_state": ([_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32),
+                           ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                           ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "fsi_ctx_set_state": ([_VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                           ctypes.c_int64], ctypes.c_int),
+    "fsi_coupled_step": ([_VP, ctypes.c_double, ctypes.POINTER(ctypes.c_float), ctypes.c_int32,
+                          ctypes.c_int32, _VP], ctypes.c_int),
+    "fsi_ctx_diagnostics": ([_VP, _VP, _VP], ctypes.c_int),
     "fsi_batch_create": ([ctypes.POINTER(BatchLattice), ctypes.c_int32, ctypes.c_int32,
                           ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "fsi_batch_destroy": ([_BATCH], ctypes.c_int),

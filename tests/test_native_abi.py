@@ -74,3 +74,22 @@ def test_closure_row_buffer_size():
     assert lib.fsi_closure_rows_bytes(ctypes.byref(d)) == -1
     d.nx, d.ny, d.nz, d.storage = 12, 10, 10, _native.STORAGE_F16  # FP32 populations only
     assert lib.fsi_closure_rows_bytes(ctypes.byref(d)) == -1
+
+
+def test_scene_context_layout_and_argument_checks():
+    """fsi_scene_desc / fsi_scene_buffers layouts, and fsi_ctx_create / fsi_coupled_step
+    rejecting bad arguments before any device work."""
+    assert ctypes.sizeof(_native.SceneDesc) == 4 * (35 + 20 + 18) + 4 * (3 + 2 + 5)
+    assert ctypes.sizeof(_native.SceneBuffers) == 8 * 5 + 8 * 11 + 8 * 6
+    d, b = _native.SceneDesc(), _native.SceneBuffers()
+    d.lbm.nx = d.lbm.ny = d.lbm.nz = 8
+    d.mpm.nx, d.mpm.ny, d.mpm.nz = 8, 8, 4  # grid differs from the lattice
+    handle = ctypes.c_void_p()
+    with pytest.raises(ValueError, match="coincide"):
+        _native.call("fsi_ctx_create", ctypes.byref(d), ctypes.byref(b), ctypes.byref(handle))
+    d.mpm.nz = 8
+    with pytest.raises(ValueError, match="NULL lattice buffer"):
+        _native.call("fsi_ctx_create", ctypes.byref(d), ctypes.byref(b), ctypes.byref(handle))
+    assert not handle.value
+    with pytest.raises(ValueError, match="NULL context"):
+        _native.call("fsi_coupled_step", None, 1.0, None, 10, 1, None)
