@@ -87,6 +87,42 @@ def prolongate(coarse_f: torch.Tensor, shape) -> torch.Tensor:
     return f.reshape(-1, OUT).contiguous()
 
 
+# D3Q19 velocities in the reference's order (fsi/lbm3d.py:221-239) and opposite directions.
+_EX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+_EY = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1])
+_EZ = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1])
+_OPP = np.array([0] + [q + 1 if q % 2 else q - 1 for q in range(1, 19)])
+
+
+def _near(body: np.ndarray) -> np.ndarray:
+    """Cells with a cell of ``body`` in their periodic 3^3 neighbourhood (bool)."""
+    b = np.asarray(body) > 0
+    out = np.zeros_like(b)
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                out |= np.roll(b, (dx, dy, dz), axis=(0, 1, 2))
+    return out
+
+
+def momentum_exchange(lbm: LBMSolver3D, body_mask: np.ndarray) -> np.ndarray:
+    """Hydrodynamic force on the bodies of ``body_mask`` (bool/0-1 (nx, ny, nz)), in the
+    lattice's units, by momentum exchange over the half-way bounce-back links: every
+    population that left a fluid cell x towards a body cell x + c_q came back reversed, so the
+    body received 2 c_q f_q*(x); after the step that population is the post-stream f_opp(q)(x).
+    Float64 sums of the float32 populations."""
+    f = lbm.distribution_numpy()
+    body = np.asarray(body_mask) > 0
+    fluid = lbm.solid_numpy() == 0
+    out = np.zeros(3)
+    for q in range(1, 19):
+        c = (int(_EX[q]), int(_EY[q]), int(_EZ[q]))
+        links = fluid & np.roll(body, shift=(-c[0], -c[1], -c[2]), axis=(0, 1, 2))
+        total = float(f[..., _OPP[q]][links].astype(np.float64).sum())
+        out += 2.0 * total * np.array(c, np.float64)
+    return out
+
+
 # ------------------------------------------------------------------- net
 def _gemm(a, b, lda, ldb, m, n, k, mode, err, c=None, ldc=0, bias=None, h=None, ht=None,
           ldht=0, zout=None, zin=None, k_chunk=None):
@@ -287,6 +323,36 @@ def training_pairs(fine_cfg: LBMConfig, fine_mask: np.ndarray, warmup: int, snap
             fine.step()
 
 
+def rollout_pairs(fine_cfg: LBMConfig, fine_mask: np.ndarray, net: "ClosureMLP",
+                  coarse_steps: int, every: int = 2):
+    """Training pairs along the closure's own trajectory (solver in the loop): the coarse run
+    with ``net``'s corrections and the plain fine run advance together from rest; every
+    ``every`` coarse steps, the coarse state s is stepped once without correction and the
+    target is the restricted fine state of the same time minus that step, R(f(t + 2 dt_f)) -
+    C(s). One-step pairs from restricted fine states alone teach no recovery from the
+    network's own drift, which in rollouts can grow step by step.
+    Yields (coarse solver after its uncorrected step, fluid cells, target [m][19])."""
+    fine = LBMSolver3D(fine_cfg)
+    fine.initialize(fine_mask)
+    sim = ClosureSimulation(fine_cfg, fine_mask, net, check_every=0)
+    probe = LBMSolver3D(sim.coarse.config)
+    cmask = coarse_mask(fine_mask)
+    probe.initialize(cmask)
+    fluid = torch.nonzero(torch.from_numpy(cmask.reshape(-1) == 0)).reshape(-1).to(
+        torch.int32).to(fine._device)
+    for k in range(coarse_steps):
+        if k % every == 0:
+            probe.load_state_dict(sim.coarse.state_dict())
+            probe.step()
+        fine.step()
+        fine.step()
+        if k % every == 0:
+            r1 = restrict(fine, probe)
+            cstate = torch.from_numpy(probe.distribution_numpy().reshape(-1, OUT)).to(fine._device)
+            yield probe, fluid, (r1 - cstate)[fluid.long()]
+        sim.step()
+
+
 class ClosureTrainer:
     """Collects training rows from restricted fine runs and fits a ClosureMLP."""
 
@@ -297,10 +363,42 @@ class ClosureTrainer:
         self._pending = []  # (coarse state copy, cells, raw target) before scales are known
 
     def add_run(self, fine_cfg: LBMConfig, fine_mask: np.ndarray, warmup: int = 40,
-                snapshots: int = 10, every: int = 4) -> None:
+                snapshots: int = 10, every: int = 4, cell_fraction: float = 1.0,
+                seed: int = 0) -> None:
+        """Pairs of one restricted fine run; ``cell_fraction`` < 1 keeps a seeded random share
+        of each snapshot's fluid cells (bounding the rows of large data sets)."""
         frac = solid_fraction(fine_mask, self.net.device) if self.net.use_fraction else None
+        g = torch.Generator(device="cpu").manual_seed(seed)
         for coarse, cells, target in training_pairs(fine_cfg, fine_mask, warmup, snapshots, every):
+            if cell_fraction < 1.0:
+                keep = torch.rand(cells.numel(), generator=g) < cell_fraction
+                keep = keep.to(cells.device)
+                cells, target = cells[keep], target[keep]
             self._pending.append((coarse.state_dict(), coarse.config, cells, target.clone(), frac))
+
+    def add_rollout_run(self, fine_cfg: LBMConfig, fine_mask: np.ndarray, coarse_steps: int,
+                        every: int = 2, cell_fraction: float = 1.0, seed: int = 0) -> None:
+        """Pairs along the current network's own closure trajectory (``rollout_pairs``), built
+        with the scales already fitted; call after a first ``build`` / ``fit``."""
+        frac = solid_fraction(fine_mask, self.net.device) if self.net.use_fraction else None
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        for probe, cells, target in rollout_pairs(fine_cfg, fine_mask, self.net, coarse_steps,
+                                                   every):
+            if cell_fraction < 1.0:
+                keep = (torch.rand(cells.numel(), generator=g) < cell_fraction).to(cells.device)
+                cells, target = cells[keep], target[keep]
+            self.rows_x.append(features(probe, cells, self.net.pop_scale, self.net.force_scale,
+                                        frac))
+            self.rows_t.append((target * self.net.out_scale).float())
+
+    def merge(self) -> int:
+        """Append the rows of add_rollout_run to the data set; returns the row count."""
+        if self.rows_x:
+            self.x = torch.cat([self.x, *self.rows_x])
+            self.t = torch.cat([self.t, *self.rows_t]).contiguous()
+            self.rows_x.clear()
+            self.rows_t.clear()
+        return int(self.x.shape[0])
 
     def _fit_scales(self) -> None:
         devs, forces, targets = [], [], []
@@ -418,20 +516,44 @@ class ClosureSimulation:
         self.fallback_step = self.coarse_steps
         self.fallback_reason = reason
 
-    def step(self) -> None:
-        """One coarse step (= two fine steps of time), or two fine steps after a fallback."""
+    def step(self, drag_mask: np.ndarray | None = None) -> np.ndarray | None:
+        """One coarse step (= two fine steps of time), or two fine steps after a fallback.
+        With ``drag_mask`` (the fine-grid body mask) returns the momentum-exchange force on
+        those bodies in fine-lattice units: on the coarse grid it is taken after the coarse
+        step and before the learned correction (the populations the bounce-back links
+        produced; the correction is a volume term and no link exchange), times 4 for the
+        coarse lattice's units under acoustic scaling."""
         if self.fine is not None:
             self.fine.step()
             self.fine.step()
-            return
+            return None if drag_mask is None else momentum_exchange(self.fine, drag_mask)
         c = self.coarse
         c.step()
-        infer_apply(c, self._weights, self._rows, self.net.err, self._frac)
+        if drag_mask is None:
+            drag = None
+            infer_apply(c, self._weights, self._rows, self.net.err, self._frac)
+        else:
+            cbody = coarse_mask(drag_mask)
+            drag = 4.0 * momentum_exchange(c, cbody)
+            # The correction is the closure's sub-grid force: the momentum it removes from the
+            # cells next to the bodies (those with a body cell in their 3^3 neighbourhood) is
+            # drag on the bodies that no bounce-back link carries.
+            corr = torch.zeros((OUT, c.n_cells), dtype=torch.float32, device=c._device)
+            infer(c, self._weights, corr, self._rows, self.net.err, self._frac)
+            near = torch.from_numpy(_near(cbody).reshape(-1)).to(c._device)
+            e = torch.tensor(np.stack([_EX, _EY, _EZ]), dtype=torch.float64, device=c._device)
+            q = (e @ corr[:, near].double()).sum(dim=1).cpu().numpy()
+            self.last_correction_momentum = 4.0 * q
+            drag = drag - 4.0 * q
+            nat.call("fsi_closure_apply", c._desc, nat.ptr(c._pops), nat.ptr(c.flags),
+                     c.steps_done, nat.ptr(corr), nat.stream_ptr())
+            c._mass_speed_cache = None
         self.coarse_steps += 1
         if self.check_every and self.coarse_steps % self.check_every == 0:
             reason = self._guard()
             if reason:
                 self._fall_back(reason)
+        return drag
 
     def velocity_numpy(self) -> np.ndarray:
         """Velocity on the coarse grid (restricting the fine field after a fallback)."""
@@ -443,23 +565,40 @@ class ClosureSimulation:
 
 
 def evaluate(fine_cfg: LBMConfig, fine_mask: np.ndarray, net: ClosureMLP, coarse_steps: int,
-             flow_axis: int = 0) -> dict:
+             flow_axis: int = 0, body_mask: np.ndarray | None = None,
+             check_every: int = 10) -> dict:
     """Error of the coarse runs against the restricted plain fine run after ``coarse_steps``
     coarse steps (2 * coarse_steps fine steps): rel-L2 velocity of the plain coarse run and
-    of the closure run, and the relative error of the mean flow along ``flow_axis`` (the
-    channel's flow rate, the body-drag balance of a force-driven channel)."""
+    of the closure run, the relative error of the mean flow along ``flow_axis`` (the
+    channel's flow rate), and with ``body_mask`` the relative error of the drag on the bodies
+    along ``flow_axis``: momentum exchange on each run's own body mask (a coarse lattice force
+    is 4x the fine-lattice force of the same physical force under acoustic scaling), for the
+    closure run taken before its last correction and less the momentum that correction adds
+    next to the bodies (ClosureSimulation.step). The closure run keeps its guards
+    (``check_every``); ``fallback`` names the tripped guard."""
     fine = LBMSolver3D(fine_cfg)
     fine.initialize(fine_mask)
     ccfg = coarse_config(fine_cfg)
     cmask = coarse_mask(fine_mask)
     plain = LBMSolver3D(ccfg)
     plain.initialize(cmask)
-    sim = ClosureSimulation(fine_cfg, fine_mask, net)
-    for _ in range(coarse_steps):
+    sim = ClosureSimulation(fine_cfg, fine_mask, net, check_every=check_every)
+    d_sim = None
+    for k in range(coarse_steps):
         fine.step()
         fine.step()
         plain.step()
-        sim.step()
+        d_sim = sim.step(body_mask if k == coarse_steps - 1 else None)
+    drag = {}
+    if body_mask is not None:
+        d_ref = momentum_exchange(fine, body_mask)[flow_axis]
+        d_plain = 4.0 * momentum_exchange(plain, coarse_mask(body_mask))[flow_axis]
+        d_cl = float(d_sim[flow_axis])
+        q = 0.0 if sim.fine is not None else float(sim.last_correction_momentum[flow_axis])
+        drag = {"drag_fine": d_ref, "drag_plain": d_plain, "drag_closure": d_cl,
+                "drag_closure_links_only": d_cl + q,
+                "drag_error_plain": abs(d_plain - d_ref) / abs(d_ref),
+                "drag_error_closure": abs(d_cl - d_ref) / abs(d_ref)}
     ref = LBMSolver3D(ccfg)
     ref.initialize(cmask)
     ref.load_populations(restrict(fine, plain))
@@ -477,4 +616,4 @@ def evaluate(fine_cfg: LBMConfig, fine_mask: np.ndarray, net: ClosureMLP, coarse
             "velocity_l2_closure": l2(u_cl),
             "flow_rate_error_plain": abs(flow(u_plain) - q_ref) / abs(q_ref),
             "flow_rate_error_closure": abs(flow(u_cl) - q_ref) / abs(q_ref),
-            "fallback": sim.fallback_reason or None}
+            "fallback": sim.fallback_reason or None, **drag}

@@ -126,6 +126,20 @@ def channel_spheres_lbm(n: int = 256, tau: float = 0.6, gx: float = 1.0e-6, seed
     return cfg, mask
 
 
+def closure_channel(seed: int, nx: int = 96, ny: int = 48, nz: int = 48, tau: float = 0.6,
+                    gx: float = 1.0e-5, fraction: float = 0.10, rmin: float = 3.0,
+                    rmax: float = 6.0) -> tuple[LBMConfig, np.ndarray, np.ndarray]:
+    """A scene of the learned closure's data set: the standalone lattice's geometry (channel
+    with walls in y and z, g_x drive, non-overlapping static spheres filling ``fraction`` of
+    the volume) at a reduced size, with radii scaled to the lattice (U[3, 6] cells at 96x48x48).
+    Returns (config, solid mask incl. walls, body mask: the spheres alone)."""
+    bodies, _, _ = sphere_packing((nx, ny, nz), fraction, rmin, rmax, seed, margin=2)
+    mask = np.maximum(bodies, wall_mask(nx, ny, nz))
+    cfg = LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=viscosity_for_tau(tau), force=(gx, 0.0, 0.0),
+                    **PERIODIC_FACES)
+    return cfg, mask, bodies
+
+
 def cubes_mpm(n: int = 256, cubes: int = 64, edge: int = 16, seed: int = 2,
               gravity: float = -1.0e-4, dt: float = 0.1) -> tuple[MPMConfig, np.ndarray]:
     """The standalone solid at scale: ``cubes`` elastic cubes of ``edge``^3 cells at 8

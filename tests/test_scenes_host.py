@@ -86,3 +86,20 @@ def test_batch_scenes_are_seeded_and_within_bounds():
         assert ma.shape == (n, n, n) and len(pa) == len(ya) == ca.mpm.max_particles
         assert np.all((pa >= 0) & (pa < n))
         assert 1 <= len(np.unique(ya)) <= 4
+
+
+def test_closure_channel_scenes():
+    """The learned closure's data-set scenes: seeded, bodies filling ~10 % inside the walls,
+    walls and bodies together in the solid mask, different geometry per seed."""
+    from fsi import scenes
+
+    cfg, mask, body = scenes.closure_channel(100)
+    cfg2, mask2, body2 = scenes.closure_channel(100)
+    assert (mask == mask2).all() and (body == body2).all()
+    assert mask.shape == body.shape == (96, 48, 48) == (cfg.nx, cfg.ny, cfg.nz)
+    assert 0.10 <= body.mean() < 0.12
+    assert ((mask >= body) & (mask >= scenes.wall_mask(96, 48, 48))).all()
+    assert not body[:, 0, :].any() and not body[:, :, -1].any()
+    _, _, other = scenes.closure_channel(300)
+    assert (other != body).any()
+    assert cfg.force == (1e-5, 0.0, 0.0)
