@@ -20,7 +20,10 @@
  *   macro   float[N][4]   (ux, uy, uz, rho) per cell
  *   force   float[3][N]   body force density, structure of arrays
  *   flags   uint32[N]     bit 0 solid; bit q (1..18) neighbour x+e_q solid;
- *                         bit 20/21 x=0 / x=nx-1 face cell
+ *                         bit 20/21 x=0 / x=nx-1 face cell; bit 22+4a+2b+c corner
+ *                         neighbour x+(2a-1,2b-1,2c-1) solid (neighbours wrap
+ *                         periodically); built by fsi_lbm_build_flags, which the
+ *                         coupling entry points rely on
  *   solid   int32[N]      0/1 solid mask as the reference stores it
  */
 #ifndef FSI_GB300_H

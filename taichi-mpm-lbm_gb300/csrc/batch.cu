@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(kTileCells)
 #pragma unroll
   for (int q = 1; q < 19; ++q)
     if (solid[d.nb(q, +1)] != 0) f |= 1u << q;
+  f |= corner_flag_bits(solid, d);
   if (i == 0) f |= kFlagFaceLeft;
   if (i == L.g.nx - 1) f |= kFlagFaceRight;
   flags_all[L.off + c] = f;

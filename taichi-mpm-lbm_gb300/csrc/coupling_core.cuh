@@ -55,15 +55,30 @@ struct ForceArgs {
   Cnt* __restrict__ cnt;
 };
 
+// Flag bit that records whether node s = 9i + 3j + k of a stencil is solid, in the flag word
+// of the stencil's centre node (offset (i-1, j-1, k-1) from it): bit 0 for the centre, bit q
+// for the neighbour e_q, a corner bit for the 8 corners.
+__host__ __device__ constexpr int stencil_flag_bit(int s) {
+  const int di = s / 9 - 1, dj = (s / 3) % 3 - 1, dk = s % 3 - 1;
+  if (di == 0 && dj == 0 && dk == 0) return 0;
+  if (di != 0 && dj != 0 && dk != 0)
+    return kFlagCornerShift + 4 * (di > 0) + 2 * (dj > 0) + (dk > 0);
+  for (int q = 1; q < 19; ++q)
+    if (ex(q) == di && ey(q) == dj && ez(q) == dk) return q;
+  return -1;
+}
+
 // The per-particle part of _compute_coupling_forces_kernel (fsi/coupling.py:336-387) for
 // active particle p: interpolates the fluid velocity over the in-grid fluid nodes of its
 // stencil, and if the valid weight exceeds min_valid_weight computes the penalty force with
 // its clipping. Writes the particle force, valid weight and coupling mask; returns true for
 // a coupled particle, whose force, valid weight, stencil weights and usable-node mask (bit s:
-// node s = 9i + 3j + k is in-grid and fluid) the spread needs. kGatherAhead issues the
-// stencil's loads up front (fewer dependent round trips, more registers: for launches with
-// few particles, where latency and not occupancy bounds the kernel); both orders sum the
-// same values in the same order.
+// node s = 9i + 3j + k is in-grid and fluid) the spread needs. A stencil inside the lattice
+// takes the fluid state of its 27 nodes from the centre node's flag word; one that reaches
+// past the lattice's faces tests node by node, where kGatherAhead issues the stencil's loads
+// up front (fewer dependent round trips, more registers: for launches with few particles,
+// where latency and not occupancy bounds the kernel). Every path sums the same values in the
+// same order.
 template <bool kGatherAhead>
 __device__ __forceinline__ bool coupling_particle(const ForceArgs& a, int p, int base[3],
                                                   float wv[3][3], uint32_t& usable, float& valid,
@@ -80,7 +95,39 @@ __device__ __forceinline__ bool coupling_particle(const ForceArgs& a, int p, int
   valid = 0.f;
   float uf[3] = {0.f, 0.f, 0.f};
   usable = 0;
-  if (!kGatherAhead) {
+  const bool interior = base[0] >= 0 && base[0] + 2 < a.g.nx && base[1] >= 0 &&
+                        base[1] + 2 < a.g.ny && base[2] >= 0 && base[2] + 2 < a.g.nz;
+  if (interior) {
+    // The whole stencil lies in the lattice: the flag word of its centre node says which of
+    // the 27 nodes are fluid, so the lattice-velocity loads go out together (an x-plane of 9
+    // nodes at a time) after one dependent load; the sums run in stencil order.
+    const long long sx = (long long)a.g.ny * a.g.nz, sy = a.g.nz;
+    const long long c1 = (base[0] + 1) * sx + (base[1] + 1) * sy + (base[2] + 1);
+    const uint32_t fl = a.flags[c1];
+#pragma unroll
+    for (int s = 0; s < 27; ++s) usable |= ((~fl >> stencil_flag_bit(s)) & 1u) << s;
+    constexpr int kB = 9;
+    const float4* __restrict__ m0 = a.macro + (c1 - sx - sy - 1);
+#pragma unroll
+    for (int b = 0; b < 27 / kB; ++b) {
+      float4 mc[kB];
+#pragma unroll
+      for (int t = 0; t < kB; ++t) {
+        const int s = kB * b + t, i = s / 9, j = (s / 3) % 3, k = s % 3;
+        if ((usable >> s) & 1u) mc[t] = m0[i * sx + j * sy + k];
+      }
+#pragma unroll
+      for (int t = 0; t < kB; ++t) {
+        const int s = kB * b + t, i = s / 9, j = (s / 3) % 3, k = s % 3;
+        if (!((usable >> s) & 1u)) continue;
+        const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
+        valid = __fadd_rn(valid, w);
+        uf[0] = __fadd_rn(uf[0], __fmul_rn(w, mc[t].x));
+        uf[1] = __fadd_rn(uf[1], __fmul_rn(w, mc[t].y));
+        uf[2] = __fadd_rn(uf[2], __fmul_rn(w, mc[t].z));
+      }
+    }
+  } else if (!kGatherAhead) {
 #pragma unroll
     for (int s = 0; s < 27; ++s) {
       const int i = s / 9, j = (s / 3) % 3, k = s % 3;

@@ -64,9 +64,13 @@ __host__ __device__ constexpr float weight_of(int q) { return q == 0 ? kW0 : (q 
 //   bit 0       this cell is solid
 //   bit q 1..18 neighbour x + e_q (periodic wrap) is solid
 //   bit 20/21   cell lies on the x = 0 / x = nx-1 face
+//   bit 22 + 4a + 2b + c   corner neighbour x + (2a-1, 2b-1, 2c-1) (periodic wrap) is solid
+// With the cell's own bit and the 18 neighbour bits, the corner bits give the solid state of
+// the whole 3^3 block around the cell from one word (the coupling's stencil).
 constexpr uint32_t kFlagSolid = 1u;
 constexpr uint32_t kFlagFaceLeft = 1u << 20;
 constexpr uint32_t kFlagFaceRight = 1u << 21;
+constexpr int kFlagCornerShift = 22;
 
 // ------------------------------------------------------------ atomics ------
 // Vector reduction into global memory (no return value), 16-byte aligned address.

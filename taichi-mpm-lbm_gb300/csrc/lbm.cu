@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(kBlock) lbm_flags_kernel(LbmGeom g,
 #pragma unroll
   for (int q = 1; q < 19; ++q)
     if (solid[d.nb(q, +1)] != 0) f |= 1u << q;
+  f |= corner_flag_bits(solid, d);
   if (i == 0) f |= kFlagFaceLeft;
   if (i == g.nx - 1) f |= kFlagFaceRight;
   flags[d.c] = f;
