@@ -126,14 +126,19 @@ def channel_spheres_lbm(n: int = 256, tau: float = 0.6, gx: float = 1.0e-6, seed
     return cfg, mask
 
 
-def closure_channel(seed: int, nx: int = 96, ny: int = 48, nz: int = 48, tau: float = 0.6,
-                    gx: float = 1.0e-5, fraction: float = 0.10, rmin: float = 3.0,
-                    rmax: float = 6.0) -> tuple[LBMConfig, np.ndarray, np.ndarray]:
+def closure_channel(seed: int, nx: int = 48, ny: int = 24, nz: int = 24, tau: float = 0.6,
+                    gx: float = 2.0e-5, balls: int = 4, rmin: float = 2.5,
+                    rmax: float = 4.5) -> tuple[LBMConfig, np.ndarray, np.ndarray]:
     """A scene of the learned closure's data set: the standalone lattice's geometry (channel
-    with walls in y and z, g_x drive, non-overlapping static spheres filling ``fraction`` of
-    the volume) at a reduced size, with radii scaled to the lattice (U[3, 6] cells at 96x48x48).
-    Returns (config, solid mask incl. walls, body mask: the spheres alone)."""
-    bodies, _, _ = sphere_packing((nx, ny, nz), fraction, rmin, rmax, seed, margin=2)
+    with walls in y and z, periodic in x, driven by g_x, static balls) at a reduced size:
+    ``balls`` balls with centres uniform in the interior (x in [5, nx-5], y, z 6 cells off
+    the walls) and radii U[rmin, rmax], drawn from ``seed`` (balls may overlap).
+    Returns (config, solid mask incl. walls, body mask: the balls alone)."""
+    rng = np.random.default_rng(seed)
+    bodies = np.zeros((nx, ny, nz), np.int32)
+    for _ in range(balls):
+        c = [rng.uniform(5, nx - 5), rng.uniform(6, ny - 6), rng.uniform(6, nz - 6)]
+        add_sphere(bodies, c, rng.uniform(rmin, rmax))
     mask = np.maximum(bodies, wall_mask(nx, ny, nz))
     cfg = LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=viscosity_for_tau(tau), force=(gx, 0.0, 0.0),
                     **PERIODIC_FACES)
@@ -184,15 +189,20 @@ def sphere_particles(center, radius: float, ppc_axis: int, rng=None) -> np.ndarr
 
 def coupled_bodies(nx: int = 384, ny: int = 192, nz: int = 192, bodies: int = 48,
                    cube_edge: int = 12, sphere_radius: float = 6.0, tau: float = 0.55,
-                   inflow: float = 0.05, seed: int = 3, substeps: int = 10):
+                   inflow: float = 0.05, seed: int = 3, substeps: int = 10,
+                   start_moving: bool = True):
     """The coupled workload at scale: an nx*ny*nz channel (walls in y and z as mask planes)
     with a velocity inlet of ``inflow`` in x at x = 0 and a pressure outlet (rho 1) at
     x = nx-1; ``bodies`` elastic bodies, half cubes of edge ``cube_edge`` cells and half
     balls of radius ``sphere_radius``, at non-overlapping positions from ``seed``, 8
-    particles per cell, Young's modulus U[0.02, 0.1] per body, nu 0.3, rho_s 1.2.
+    particles per cell, Young's modulus U[0.02, 0.1] per body, nu 0.3, rho_s 1.2. With
+    ``start_moving`` the fluid starts at the inflow velocity everywhere (so the bodies are
+    driven, deform and move from the first step), else at rest (the inlet's flow then takes
+    ~x/0.6 steps to reach a body at x).
     Returns (config, solid mask, positions, per-particle Young's modulus)."""
     rng = np.random.default_rng(seed)
     lbm = LBMConfig(nx=nx, ny=ny, nz=nz, viscosity=viscosity_for_tau(tau), rho0=1.0,
+                    initial_velocity=(inflow, 0.0, 0.0) if start_moving else (0.0, 0.0, 0.0),
                     x_left=BoundaryConfig("velocity", velocity=(inflow, 0.0, 0.0)),
                     x_right=BoundaryConfig("pressure", rho=1.0),
                     y_left=BoundaryConfig("periodic"), y_right=BoundaryConfig("periodic"),

@@ -74,6 +74,7 @@ def test_coupled_workloads():
     assert cfg.lbm.x_left.boundary_type == "velocity" and cfg.lbm.x_right.boundary_type == "pressure"
     assert np.all((pos >= 0) & (pos < [112, 48, 48]))
     assert 1 <= len(np.unique(young)) <= 4 and np.all((young >= 0.02) & (young <= 0.1))
+    assert cfg.lbm.initial_velocity == (0.05, 0.0, 0.0)  # the channel starts at its inflow
 
 
 def test_batch_scenes_are_seeded_and_within_bounds():
@@ -89,17 +90,17 @@ def test_batch_scenes_are_seeded_and_within_bounds():
 
 
 def test_closure_channel_scenes():
-    """The learned closure's data-set scenes: seeded, bodies filling ~10 % inside the walls,
-    walls and bodies together in the solid mask, different geometry per seed."""
+    """The learned closure's data-set scenes: seeded, four balls inside the walls, walls and
+    balls together in the solid mask, different geometry per seed."""
     from fsi import scenes
 
     cfg, mask, body = scenes.closure_channel(100)
     cfg2, mask2, body2 = scenes.closure_channel(100)
     assert (mask == mask2).all() and (body == body2).all()
-    assert mask.shape == body.shape == (96, 48, 48) == (cfg.nx, cfg.ny, cfg.nz)
-    assert 0.10 <= body.mean() < 0.12
-    assert ((mask >= body) & (mask >= scenes.wall_mask(96, 48, 48))).all()
+    assert mask.shape == body.shape == (48, 24, 24) == (cfg.nx, cfg.ny, cfg.nz)
+    assert 0.005 < body.mean() < 0.1
+    assert ((mask >= body) & (mask >= scenes.wall_mask(48, 24, 24))).all()
     assert not body[:, 0, :].any() and not body[:, :, -1].any()
     _, _, other = scenes.closure_channel(300)
     assert (other != body).any()
-    assert cfg.force == (1e-5, 0.0, 0.0)
+    assert cfg.force == (2e-5, 0.0, 0.0)
