@@ -353,8 +353,9 @@ def time_headline(args, world, stream) -> dict:
 def time_batched(args, world, stream) -> dict:
     """The batched workload: 256 independent coupled scenes (lattice edges 32-96, 1-4 bodies,
     seed 4) in FP16 deviation storage, advanced together by SceneBatch.run (one launch per
-    phase over all scenes, CUDA graph), after autotuning; beside it the same per-scene work
-    done one scene at a time (FSISimulation, eager) on the first 8 scenes."""
+    phase over all scenes, CUDA graph) after autotuning, and by SceneBatch.run_persistent (all
+    steps in one persistent cooperative launch); beside it the same per-scene work done one
+    scene at a time (FSISimulation, eager) on the first 8 scenes."""
     import torch
     from fsi import scenes
     from fsi.batch import SceneBatch
@@ -376,6 +377,14 @@ def time_batched(args, world, stream) -> dict:
     b.record(stream)
     barrier(world)
     ms = max_over_ranks(a.elapsed_time(b), world) / steps
+    # the same steps as one persistent cooperative launch (grid-wide barriers between phases)
+    batch.run_persistent(2)
+    barrier(world)
+    a.record(stream)
+    batch.run_persistent(steps)
+    b.record(stream)
+    barrier(world)
+    persist_ms = max_over_ranks(a.elapsed_time(b), world) / steps
     cells = batch.lattice.cells
     particles = sum(batch.particle_counts)
     sub = batch.substeps
@@ -409,6 +418,10 @@ def time_batched(args, world, stream) -> dict:
                           "mode": "FSISimulation coupler.step, eager, one scene after another"},
         "speedup_vs_one_at_a_time": round(cells / (ms * 1e-3) / 1e6 / single_mlups, 2),
         "gpu_launches": steps * (4 * sub + 3),
+        "persistent": {"ms_per_coupled_step": round(persist_ms, 4),
+                       "mlups": round(cells / (persist_ms * 1e-3) / 1e6 * world, 1),
+                       "launches": 1, "steps_per_launch": steps,
+                       "mode": "SceneBatch.run_persistent: one cooperative launch of all steps"},
     }
     del batch
     torch.cuda.empty_cache()

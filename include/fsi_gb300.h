@@ -527,6 +527,41 @@ int fsi_batch_coupling_assemble(const fsi_batch* batch, const uint32_t* flags, i
                                 float* accum, const float* macro, float* force, float* ib_force,
                                 void* counters, void* stream);
 
+/* Device arrays of a scene batch's coupled state, for fsi_batch_run_persistent. */
+typedef struct fsi_batch_state {
+  void* pops;             /* populations, the batch's storage form */
+  float* macro;           /* float[cells][4] */
+  float* force[2];        /* the two force buffers, float[3][cells] scene blocks each */
+  const uint32_t* flags;  /* from fsi_batch_lbm_flags */
+  float* accum;           /* float[cells][4] coupling accumulator */
+  float* ib_force;        /* float[3][cells] scene blocks, or NULL */
+  float* valid_weight;    /* float[capacity] */
+  int32_t* coupling_mask; /* int32[capacity] */
+  void* counters;         /* fsi_coupling_counters[count] */
+  float* grid;            /* float4[cells], all-zero between substeps */
+  uint8_t* dirty;         /* dirty map of fsi_batch_set_solids */
+  uint32_t* sync;         /* one device word for the grid barrier (zeroed by each call) */
+  int32_t* error;         /* one device word: left 0, or set to FSI_ERR_TIMEOUT when a
+                             barrier wait gave up (the caller clears it) */
+} fsi_batch_state;
+
+/* `steps` coupled steps of every scene in one persistent cooperative launch (as many
+ * 256-thread blocks as are resident at once, grid-wide barriers between phases): per step
+ * the rho / u refresh and accumulator zeroing, `substeps` x (fsi_batch_coupling_forces with
+ * build_fraction on the first substep, fsi_batch_mpm_substep), fsi_batch_coupling_assemble
+ * with assemble_mode into force[1 - prev], and the lattice step (parity of steps_done) with
+ * that force; then prev flips. prev_force is the buffer of the step before the first;
+ * macro_fresh says whether rho / u of the current state are already in macro. Every
+ * barrier wait is bounded by wait_cycles SM clock cycles (0: 2^31, about a second): a launch
+ * that gives up sets *error and ends, its state then undefined.
+ * Each scene's result is that of the per-phase calls. No reference counterpart: the
+ * reference runs one scene per simulation (fsi/simulation.py:12-153). */
+int fsi_batch_run_persistent(const fsi_batch* batch, const fsi_particles* particles,
+                             const fsi_batch_state* state, int64_t steps_done, int32_t steps,
+                             int32_t substeps, float dt_ratio, int32_t build_fraction,
+                             int32_t assemble_mode, int32_t prev_force, int32_t macro_fresh,
+                             int64_t wait_cycles, void* stream);
+
 /* ------------------------------------------------------------ learned closure
  * A per-cell MLP (656 -> 64 -> 64 -> 64 -> 19, GELU, BF16 weights, FP32 accumulation) that
  * corrects the post-stream populations of a lattice run on a grid 2x coarser than the one it

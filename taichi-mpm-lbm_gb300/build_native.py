@@ -25,7 +25,8 @@ OBJ_DIR = LIB_DIR / "obj"
 LIB = LIB_DIR / "libfsi_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["capi.cu", "lbm.cu", "mpm.cu", "mpm_sorted.cu", "coupling.cu", "context.cu", "batch.cu", "batch_step_f32.cu",
-           "batch_step_f16.cu", "batch_step_bf16.cu", "closure.cu"]
+           "batch_step_f16.cu", "batch_step_bf16.cu", "batch_persist_f32.cu", "batch_persist_f16.cu",
+           "batch_persist_bf16.cu", "closure.cu"]
 
 
 def nvcc() -> str:

@@ -58,28 +58,9 @@ __global__ void __launch_bounds__(kTileCells)
   const BatchLattice& L = lat[t.lattice];
   const int c = t.first + threadIdx.x;
   float mass = 0.f, vmax = 0.f;
-  if (c < L.g.n) {
-    int i, j, k;
-    cell_ijk(L.g, c, i, j, k);
-    const Deltas d(L.g, i, j, k);
-    const uint32_t fl = flags_all[L.off + c];
-    float4* macro = reinterpret_cast<float4*>(macro_all) + L.off;
-    if (fl & kFlagSolid) {
-      macro[c] = make_float4(0.f, 0.f, 0.f, L.rho0);
-    } else {
-      const uint32_t n = (uint32_t)L.g.n;
-      const auto* pops = reinterpret_cast<const typename Store<kStore>::T*>(pops_v) + 19 * L.off;
-      const float* force = force_all + 3 * L.off;
-      float F[19];
-#pragma unroll
-      for (int q = 0; q < 19; ++q) F[q] = gather32<kStore>(pops, n, d, fl, q, parity, L.shift[q]);
-      float rho, ux, uy, uz;
-      macro_any<kFast>(F, force[c], force[n + c], force[2 * n + c], rho, ux, uy, uz);
-      macro[c] = make_float4(ux, uy, uz, rho);
-      mass = rho;
-      vmax = norm3_ref(ux, uy, uz);
-    }
-  }
+  if (c < L.g.n)
+    batch_macro_cell<kStore, kFast>(L, c, pops_v, force_all, flags_all, parity, macro_all, mass,
+                                    vmax);
   if (diag) {
     const float s[1] = {mass};
     block_accumulate<1>(diag + 2 * t.lattice, s, diag + 2 * t.lattice + 1, vmax);
@@ -237,18 +218,8 @@ __global__ void __launch_bounds__(kBlock)
                                  const BatchSolid* __restrict__ sol, const Tile* __restrict__ ptiles,
                                  ForceArgs base, float dt_ratio, int build_fraction) {
   const Tile t = ptiles[blockIdx.x];
-  const BatchLattice& L = lat[t.lattice];
-  const BatchSolid& S = sol[t.lattice];
-  ForceArgs a = base;
-  a.c = S.c;
-  a.c.dt_ratio = dt_ratio;
-  a.c.build_fraction = build_fraction;
-  a.g = Geo{L.g.nx, L.g.ny, L.g.nz, L.g.n};
-  a.n = S.m.n;
-  a.macro = base.macro + L.off;
-  a.flags = base.flags + L.off;
-  a.accum = base.accum + L.off;
-  a.cnt = base.cnt + t.lattice;
+  const ForceArgs a = scene_force_args(base, lat[t.lattice], sol[t.lattice], t.lattice, dt_ratio,
+                                       build_fraction);
   coupling_forces_body<false>(a, t.first * kBlock + threadIdx.x);
 }
 
@@ -256,18 +227,7 @@ __global__ void __launch_bounds__(kTileCells)
     batch_assemble_kernel(const BatchLattice* __restrict__ lat, const BatchSolid* __restrict__ sol,
                           const Tile* __restrict__ tiles, AssembleArgs base) {
   const Tile t = tiles[blockIdx.x];
-  const BatchLattice& L = lat[t.lattice];
-  AssembleArgs a = base;
-  a.c = sol[t.lattice].c;
-  a.g = Geo{L.g.nx, L.g.ny, L.g.nz, L.g.n};
-  a.flags = base.flags + L.off;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) a.base[i] = L.base[i];
-  a.accum = base.accum + L.off;
-  a.macro = base.macro ? base.macro + L.off : nullptr;
-  a.force = base.force ? base.force + 3 * L.off : nullptr;
-  a.ib = base.ib ? base.ib + 3 * L.off : nullptr;
-  a.cnt = base.cnt + t.lattice;
+  const AssembleArgs a = scene_assemble_args(base, lat[t.lattice], sol[t.lattice], t.lattice);
   assemble_body(a, (long long)t.first + threadIdx.x);
 }
 
@@ -612,4 +572,83 @@ extern "C" int fsi_batch_coupling_assemble(const fsi_batch* b, const uint32_t* f
   a.cnt = reinterpret_cast<Cnt*>(counters);
   batch_assemble_kernel<<<b->ntiles, kTileCells, 0, as_stream(stream)>>>(b->lat, b->sol, b->tiles, a);
   return check_launch("batch_assemble_kernel");
+}
+
+extern "C" int fsi_batch_run_persistent(const fsi_batch* b, const fsi_particles* particles,
+                                        const fsi_batch_state* st, int64_t steps_done,
+                                        int32_t steps, int32_t substeps, float dt_ratio,
+                                        int32_t build_fraction, int32_t assemble_mode,
+                                        int32_t prev_force, int32_t macro_fresh,
+                                        int64_t wait_cycles, void* stream) {
+  if (int e = check_solids(b)) return e;
+  FSI_REQUIRE(st != nullptr, "NULL state");
+  FSI_REQUIRE(st->pops && st->macro && st->force[0] && st->force[1] && st->flags && st->accum &&
+                  st->valid_weight && st->coupling_mask && st->counters && st->grid &&
+                  st->dirty && st->sync && st->error,
+              "NULL array in the batch state");
+  FSI_REQUIRE(((uintptr_t)st->grid & 15) == 0 && ((uintptr_t)st->accum & 15) == 0 &&
+                  ((uintptr_t)st->macro & 15) == 0,
+              "grid, accum and macro must be 16-byte aligned");
+  FSI_REQUIRE(steps_done >= 0 && steps >= 0 && substeps > 0, "bad step counts");
+  FSI_REQUIRE(prev_force == 0 || prev_force == 1, "prev_force must be 0 or 1");
+  FSI_REQUIRE(!(assemble_mode & FSI_ASSEMBLE_IB) || st->ib_force, "IB needs ib_force");
+  PView P;
+  if (int e = particle_view(b, particles, P)) return e;
+  if (steps == 0) return FSI_OK;
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(st->sync, 0, sizeof(uint32_t), s) != cudaSuccess) return check_launch("memset");
+  PersistArgs a{};
+  a.lat = b->lat;
+  a.sol = b->sol;
+  a.cell_tiles = b->tiles;
+  a.ncell_tiles = b->ntiles;
+  a.step_tiles = b->step_tiles;
+  a.nstep_tiles = b->nstep_tiles;
+  a.step_tile_cells = b->step_tile_cells;
+  a.ptiles = b->ptiles;
+  a.nptiles = b->nptiles;
+  a.ctiles = b->ctiles;
+  a.nctiles = b->nctiles;
+  a.count = b->count;
+  a.P = P;
+  a.fa.cap = b->capacity;
+  a.fa.x = P.x; a.fa.v = P.v; a.fa.mass = P.mass; a.fa.vol = P.vol; a.fa.active = P.active;
+  a.fa.fp = P.fp;
+  a.fa.macro = reinterpret_cast<const float4*>(st->macro);
+  a.fa.flags = st->flags;
+  a.fa.accum = reinterpret_cast<float4*>(st->accum);
+  a.fa.valid_out = st->valid_weight;
+  a.fa.mask_out = st->coupling_mask;
+  a.fa.cnt = reinterpret_cast<Cnt*>(st->counters);
+  a.aa.flags = st->flags;
+  a.aa.mode = assemble_mode;
+  a.aa.accum = reinterpret_cast<float4*>(st->accum);
+  a.aa.macro = reinterpret_cast<const float4*>(st->macro);
+  a.aa.force = nullptr;  // the step's buffer, set in the kernel
+  a.aa.ib = st->ib_force;
+  a.aa.cnt = reinterpret_cast<Cnt*>(st->counters);
+  a.pops = st->pops;
+  a.macro = st->macro;
+  a.force[0] = st->force[0];
+  a.force[1] = st->force[1];
+  a.flags = st->flags;
+  a.grid = reinterpret_cast<float4*>(st->grid);
+  a.dirty = st->dirty;
+  a.sync = st->sync;
+  a.err = st->error;
+  a.steps_done = steps_done;
+  a.steps = steps;
+  a.substeps = substeps;
+  a.dt_ratio = dt_ratio;
+  a.build_fraction = build_fraction;
+  a.prev = prev_force;
+  a.macro_fresh = macro_fresh;
+  FSI_REQUIRE(wait_cycles >= 0, "wait_cycles must be non-negative");
+  a.wait_cycles = wait_cycles > 0 ? wait_cycles : (1ll << 31);  // about a second
+  const bool fast = b->arithmetic == FSI_ARITH_FAST;
+  switch (b->storage) {
+    case FSI_STORAGE_F16: return batch_persist_launch_f16(&a, fast, s);
+    case FSI_STORAGE_BF16: return batch_persist_launch_bf16(&a, fast, s);
+    default: return batch_persist_launch_f32(&a, fast, s);
+  }
 }

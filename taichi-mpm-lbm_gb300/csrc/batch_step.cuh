@@ -6,39 +6,6 @@
 namespace fsi {
 namespace {
 
-// The lattice of a tile as the argument type of step_cells.
-struct LatticeView {
-  LbmGeom g;
-  void* __restrict__ pops;
-  float4* __restrict__ macro;
-  const float* __restrict__ force;
-  const float* __restrict__ force_prev;
-  const uint32_t* __restrict__ flags;
-  const float* s;
-  const float* sg;
-  const float* shift;
-  int write_faces;
-};
-
-template <int kStore>
-__device__ __forceinline__ LatticeView view_of(const BatchLattice& L, void* pops, float* macro,
-                                               const float* force, const float* force_prev,
-                                               const uint32_t* flags) {
-  using T = typename Store<kStore>::T;
-  LatticeView v;
-  v.g = L.g;
-  v.pops = reinterpret_cast<T*>(pops) + 19 * L.off;
-  v.macro = reinterpret_cast<float4*>(macro) + L.off;
-  v.force = force + 3 * L.off;
-  v.force_prev = force_prev ? force_prev + 3 * L.off : nullptr;
-  v.flags = flags + L.off;
-  v.s = L.s;
-  v.sg = L.sg;
-  v.shift = L.shift;
-  v.write_faces = 0;
-  return v;
-}
-
 struct BatchStepArgs {
   const BatchLattice* lat;
   const Tile* tiles;

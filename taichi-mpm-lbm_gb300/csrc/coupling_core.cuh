@@ -41,13 +41,13 @@ struct ForceArgs {
   Geo g;
   int n;
   long long cap;
-  const float* __restrict__ x;
-  const float* __restrict__ v;
+  const float* FSI_LAUNCH_RO x;
+  const float* FSI_LAUNCH_RO v;
   const float* __restrict__ mass;
   const float* __restrict__ vol;
   const int32_t* __restrict__ active;
   float* __restrict__ fp;
-  const float4* __restrict__ macro;
+  const float4* FSI_LAUNCH_RO macro;
   const uint32_t* __restrict__ flags;
   float4* __restrict__ accum;
   float* __restrict__ valid_out;
@@ -107,7 +107,7 @@ __device__ __forceinline__ bool coupling_particle(const ForceArgs& a, int p, int
 #pragma unroll
     for (int s = 0; s < 27; ++s) usable |= ((~fl >> stencil_flag_bit(s)) & 1u) << s;
     constexpr int kB = 9;
-    const float4* __restrict__ m0 = a.macro + (c1 - sx - sy - 1);
+    const float4* FSI_LAUNCH_RO m0 = a.macro + (c1 - sx - sy - 1);
 #pragma unroll
     for (int b = 0; b < 27 / kB; ++b) {
       float4 mc[kB];
@@ -282,7 +282,7 @@ struct AssembleArgs {
   float base[3];
   int mode;
   float4* __restrict__ accum;
-  const float4* __restrict__ macro;
+  const float4* FSI_LAUNCH_RO macro;
   float* __restrict__ force;
   float* __restrict__ ib;
   Cnt* __restrict__ cnt;

@@ -7,6 +7,16 @@
 
 #include "../../include/fsi_gb300.h"
 
+// Qualifier of device pointers that a kernel only reads but that another phase of the same
+// launch may write (particle positions, rho / u, the force field, the grid, populations).
+// __restrict__ (the default) lets the compiler serve such reads from the read-only data
+// path, which is only valid when the data does not change during the launch; the translation
+// units of the persistent batch kernel, whose phases write what later phases read, define it
+// empty.
+#ifndef FSI_LAUNCH_RO
+#define FSI_LAUNCH_RO __restrict__
+#endif
+
 namespace fsi {
 
 // ------------------------------------------------------------ errors -------

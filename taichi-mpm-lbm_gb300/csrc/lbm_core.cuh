@@ -81,14 +81,6 @@ __device__ __forceinline__ uint32_t corner_flag_bits(const int32_t* __restrict__
   return f;
 }
 
-// Where the two cells of a packed (fast-form) thread lie: (i, j, k) and (i, j + 1, k)
-// (FSI_LBM_PAIR_K 0), or (i, j, k) and (i, j, k + 1) with k even (1): then a warp covers 64
-// consecutive cells of a row and the two cells' slots of one population are adjacent, so
-// aligned pairs move as one vector access.
-#ifndef FSI_LBM_PAIR_K
-#define FSI_LBM_PAIR_K 0
-#endif
-
 // ------------------------------------------------------------- storage forms
 // ld(p, i, s) returns population i as float given its rest-equilibrium shift s = w_q rho0;
 // st(p, i, v, s) stores population value v.
@@ -101,14 +93,9 @@ struct Store<FSI_STORAGE_F32> {
   static __device__ __forceinline__ float ld(const T* p, uint32_t i, float) { return p[i]; }
   static __device__ __forceinline__ void st(T* p, uint32_t i, float v, float) { p[i] = v; }
   static __device__ __forceinline__ float2 ld2(const T* p, uint32_t i0, uint32_t i1, float) {
-    if (FSI_LBM_PAIR_K && i1 == i0 + 1 && (i0 & 1u) == 0) return *reinterpret_cast<const float2*>(p + i0);
     return make_float2(p[i0], p[i1]);
   }
   static __device__ __forceinline__ void st2(T* p, uint32_t i0, uint32_t i1, float2 v, float) {
-    if (FSI_LBM_PAIR_K && i1 == i0 + 1 && (i0 & 1u) == 0) {
-      *reinterpret_cast<float2*>(p + i0) = v;
-      return;
-    }
     p[i0] = v.x;
     p[i1] = v.y;
   }
@@ -127,18 +114,11 @@ struct Store<FSI_STORAGE_F16> {
   }
   // Two values at once: one packed conversion and one packed fma / sub+mul per pair.
   static __device__ __forceinline__ float2 ld2(const T* p, uint32_t i0, uint32_t i1, float s) {
-    const __half2 raw = (FSI_LBM_PAIR_K && i1 == i0 + 1 && (i0 & 1u) == 0)
-                            ? *reinterpret_cast<const __half2*>(p + i0)
-                            : __halves2half2(p[i0], p[i1]);
-    const float2 h = __half22float2(raw);
+    const float2 h = __half22float2(__halves2half2(p[i0], p[i1]));
     return vfma(h, make_float2(1.0f / kF16Scale, 1.0f / kF16Scale), make_float2(s, s));
   }
   static __device__ __forceinline__ void st2(T* p, uint32_t i0, uint32_t i1, float2 v, float s) {
     const __half2 h = __float22half2_rn(vmul(vsub(v, s), kF16Scale));
-    if (FSI_LBM_PAIR_K && i1 == i0 + 1 && (i0 & 1u) == 0) {
-      *reinterpret_cast<__half2*>(p + i0) = h;
-      return;
-    }
     p[i0] = __low2half(h);
     p[i1] = __high2half(h);
   }
@@ -154,17 +134,10 @@ struct Store<FSI_STORAGE_BF16> {
     p[i] = __float2bfloat16_rn(v - s);
   }
   static __device__ __forceinline__ float2 ld2(const T* p, uint32_t i0, uint32_t i1, float s) {
-    const __nv_bfloat162 raw = (FSI_LBM_PAIR_K && i1 == i0 + 1 && (i0 & 1u) == 0)
-                                   ? *reinterpret_cast<const __nv_bfloat162*>(p + i0)
-                                   : __halves2bfloat162(p[i0], p[i1]);
-    return vadd(__bfloat1622float2(raw), s);
+    return vadd(__bfloat1622float2(__halves2bfloat162(p[i0], p[i1])), s);
   }
   static __device__ __forceinline__ void st2(T* p, uint32_t i0, uint32_t i1, float2 v, float s) {
     const __nv_bfloat162 h = __float22bfloat162_rn(vsub(v, s));
-    if (FSI_LBM_PAIR_K && i1 == i0 + 1 && (i0 & 1u) == 0) {
-      *reinterpret_cast<__nv_bfloat162*>(p + i0) = h;
-      return;
-    }
     p[i0] = __low2bfloat16(h);
     p[i1] = __high2bfloat16(h);
   }
@@ -172,7 +145,7 @@ struct Store<FSI_STORAGE_BF16> {
 
 // Post-stream F_q(x) of a fluid cell in a state of the given parity.
 template <int kStore>
-__device__ __forceinline__ float gather32(const typename Store<kStore>::T* __restrict__ pops,
+__device__ __forceinline__ float gather32(const typename Store<kStore>::T* FSI_LAUNCH_RO pops,
                                           uint32_t n, const Deltas& d, uint32_t fl, int q,
                                           int parity, float shift) {
   if (parity == 0 || q == 0 || ((fl >> opp(q)) & 1u)) return Store<kStore>::ld(pops, q * n + d.c, shift);
@@ -367,17 +340,14 @@ constexpr int step_min_blocks() {
                : (kOdd ? FSI_LBM_MIN_BLOCKS_EXACT_ODD : FSI_LBM_MIN_BLOCKS_EXACT_EVEN);
 }
 
-// Launch shape of the step kernel: x = z (contiguous), y = rows, z = x planes; the `lanes`
-// cells of a thread lie along y, or along z with FSI_LBM_PAIR_K.
+// Launch shape of the step kernel: x = z (contiguous), y = groups of `lanes` rows, z = x planes.
 CellLaunch step_launch(const LbmGeom& g, int lanes) {
-  const int zl = FSI_LBM_PAIR_K ? lanes : 1, yl = FSI_LBM_PAIR_K ? 1 : lanes;
-  const int zt = (g.nz + zl - 1) / zl;  // threads along z
-  int bz = ((zt + 31) / 32) * 32;
+  int bz = ((g.nz + 31) / 32) * 32;
   if (bz > kStepBlock) bz = kStepBlock;
-  const int rows = (g.ny + yl - 1) / yl;
+  const int rows = (g.ny + lanes - 1) / lanes;
   int by = kStepBlock / bz;
   if (by > rows) by = rows;
-  return CellLaunch{dim3((zt + bz - 1) / bz, (rows + by - 1) / by, g.nx), dim3(bz, by, 1)};
+  return CellLaunch{dim3((g.nz + bz - 1) / bz, (rows + by - 1) / by, g.nx), dim3(bz, by, 1)};
 }
 
 // Storage index that the odd step reads F_q(x) from, and that it writes f*_q(x) to.
@@ -504,19 +474,16 @@ template <int kStore, bool kFast, bool kOdd, bool kRecompute>
 __global__ void __launch_bounds__(kStepBlock, (step_min_blocks<kFast, kOdd>()))
     lbm_step_kernel(StepArgs a) {
   constexpr int L = StepLanes<kFast>::n;
-  constexpr int ZL = FSI_LBM_PAIR_K ? L : 1, YL = FSI_LBM_PAIR_K ? 1 : L;
-  const int k = ZL * (blockIdx.x * blockDim.x + threadIdx.x);
-  const int j = YL * (blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = L * (blockIdx.y * blockDim.y + threadIdx.y);
   const int i = blockIdx.z;
   if (k >= a.g.nz || j >= a.g.ny) return;
   int ci[L], cj[L], ck[L];
   bool has[L];
 #pragma unroll
   for (int l = 0; l < L; ++l) {
-    ci[l] = i;
-    cj[l] = j + (YL > 1 ? l : 0);
-    ck[l] = k + (ZL > 1 ? l : 0);
-    has[l] = cj[l] < a.g.ny && ck[l] < a.g.nz;
+    ci[l] = i; cj[l] = j + l; ck[l] = k;
+    has[l] = j + l < a.g.ny;
   }
   step_cells<kStore, kFast, kOdd, kRecompute, StepArgs>(a, ci, cj, ck, has);
 }

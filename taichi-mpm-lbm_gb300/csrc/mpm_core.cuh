@@ -276,11 +276,15 @@ __device__ __forceinline__ void p2g_stress_affine(const Mpm& m, const PView& P, 
 // kCoupled folds _compute_coupling_forces_kernel (fsi/coupling.py:332-406) in front of the
 // scatter: the particle's coupling force is formed first (it is P2G's dt f term) and the
 // fluid reaction and solid fraction are spread into fa.accum beside the grid scatter.
-template <bool kCoupled = false>
+// kExtTile: the tile is the caller's shared memory `ext` (4 x kTileCap floats) instead of a
+// static array of its own (a kernel that also runs g2p_body then holds one tile, not two).
+template <bool kCoupled = false, bool kExtTile = false>
 __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* __restrict__ grid,
                                          uint8_t* __restrict__ dirty, int p,
-                                         const ForceArgs* fa = nullptr) {
-  __shared__ float tile[4][kTileCap];
+                                         const ForceArgs* fa = nullptr,
+                                         float (*ext)[kTileCap] = nullptr) {
+  __shared__ float own[kExtTile ? 1 : 4][kExtTile ? 1 : kTileCap];
+  float (*tile)[kTileCap] = kExtTile ? ext : reinterpret_cast<float (*)[kTileCap]>(own);
   __shared__ int sh[8];
   const long long cap = m.cap;
   const bool act = p < m.n && P.active[p] != 0;
@@ -444,9 +448,13 @@ __device__ __forceinline__ void grid_op(const Mpm& m, float4 node, int i, int j,
 }
 
 // Grid update + G2P of particle p (this thread) within its CTA; every thread calls it.
+// kExtTile as for p2g_body (3 x kTileCap floats of the caller's shared memory).
+template <bool kExtTile = false>
 __device__ __forceinline__ void g2p_body(const Mpm& m, const PView& P,
-                                         const float4* __restrict__ grid, int p) {
-  __shared__ float tile[3][kTileCap];
+                                         const float4* FSI_LAUNCH_RO grid, int p,
+                                         float (*ext)[kTileCap] = nullptr) {
+  __shared__ float own[kExtTile ? 1 : 3][kExtTile ? 1 : kTileCap];
+  float (*tile)[kTileCap] = kExtTile ? ext : reinterpret_cast<float (*)[kTileCap]>(own);
   __shared__ int sh[8];
   const long long cap = m.cap;
   const bool act = p < m.n && P.active[p] != 0;

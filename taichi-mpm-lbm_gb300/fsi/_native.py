@@ -133,6 +133,16 @@ class BatchSolid(ctypes.Structure):
     _fields_ = [("mpm", MpmDesc), ("coupling", CouplingDesc), ("particle_offset", ctypes.c_int64)]
 
 
+class BatchState(ctypes.Structure):
+    _fields_ = [
+        ("pops", ctypes.c_void_p), ("macro", ctypes.c_void_p), ("force", ctypes.c_void_p * 2),
+        ("flags", ctypes.c_void_p), ("accum", ctypes.c_void_p), ("ib_force", ctypes.c_void_p),
+        ("valid_weight", ctypes.c_void_p), ("coupling_mask", ctypes.c_void_p),
+        ("counters", ctypes.c_void_p), ("grid", ctypes.c_void_p), ("dirty", ctypes.c_void_p),
+        ("sync", ctypes.c_void_p), ("error", ctypes.c_void_p),
+    ]
+
+
 class ClosureGemmDesc(ctypes.Structure):
     _fields_ = [
         ("a", ctypes.c_void_p), ("b", ctypes.c_void_p),
@@ -239,6 +249,10 @@ _SIGNATURES = {
                                    ctypes.c_float, ctypes.c_int32, _VP], ctypes.c_int),
     "fsi_batch_coupling_assemble": ([_BATCH, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP],
                                     ctypes.c_int),
+    "fsi_batch_run_persistent": ([_BATCH, ctypes.POINTER(Particles), ctypes.POINTER(BatchState),
+                                  ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
+                                  ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                  ctypes.c_int64, _VP], ctypes.c_int),
 }
 
 

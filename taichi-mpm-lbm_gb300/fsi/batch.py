@@ -375,6 +375,60 @@ class SceneBatch:
         self._coupled_step += 1
         self.step_index += 1
 
+    def _assemble_mode(self) -> int:
+        build = all(bool(c.coupling.build_solid_volume_fraction) for c in self.configs)
+        mode = nat.ASSEMBLE_COUPLING | (nat.ASSEMBLE_CLAMP_FRACTION if build else 0)
+        if any(c.coupling.immersed_boundary_enabled for c in self.configs):
+            mode |= nat.ASSEMBLE_IB
+        return mode
+
+    def run_persistent(self, steps: int, max_steps_per_launch: int = 1000,
+                       wait_cycles: int = 0) -> None:
+        """``steps`` coupled steps of every scene, each launch of up to
+        ``max_steps_per_launch`` steps one persistent cooperative kernel (grid-wide barriers
+        between the phases of SceneBatch.step, each wait bounded by ``wait_cycles`` SM clock
+        cycles, 0 for about a second). Steps inside the gamma ramp and the first step after
+        initialisation run eagerly. Raises when a launch reports a barrier wait that gave up
+        (the batch's state is then undefined)."""
+        steps = int(steps)
+        if steps < 0:
+            raise ValueError("steps must be non-negative.")
+        L = self.lattice
+        while steps > 0 and (not self._gamma_settled() or L._fcur != L._fprev):
+            self.step()
+            steps -= 1
+        if steps == 0:
+            return
+        self._set_gamma()
+        if not hasattr(self, "_sync"):
+            self._sync = torch.zeros(1, dtype=torch.int32, device=self._device)
+            self._error = torch.zeros(1, dtype=torch.int32, device=self._device)
+        st = nat.BatchState()
+        st.pops, st.macro = L._pops.data_ptr(), L._macro.data_ptr()
+        st.force[0], st.force[1] = L._force_buf[0].data_ptr(), L._force_buf[1].data_ptr()
+        st.flags, st.accum, st.ib_force = L._flags.data_ptr(), self._accum.data_ptr(), self._ib.data_ptr()
+        st.valid_weight, st.coupling_mask = self._valid.data_ptr(), self._mask.data_ptr()
+        st.counters, st.grid, st.dirty = (self._counters.data_ptr(), self._grid.data_ptr(),
+                                          self._dirty.data_ptr())
+        st.sync, st.error = self._sync.data_ptr(), self._error.data_ptr()
+        dt_ratio = float(np.float32((self.lbm_dt / self.substeps) / self.lbm_dt))
+        build = int(all(bool(c.coupling.build_solid_volume_fraction) for c in self.configs))
+        while steps > 0:
+            k = min(steps, int(max_steps_per_launch))
+            nat.call("fsi_batch_run_persistent", self.lattice._handle, self._parts, st,
+                     L._steps_done, k, self.substeps, dt_ratio, build, self._assemble_mode(),
+                     L._fprev, int(L._macro_fresh), int(wait_cycles), nat.stream_ptr())
+            L._steps_done += k
+            L._fprev = L._fcur = L._fprev ^ (k & 1)
+            L._macro_fresh = False
+            self._coupled_step += k
+            self.step_index += k
+            steps -= k
+        err = int(self._error.item())
+        if err:
+            self._error.zero_()
+            raise nat.NativeError(f"persistent batch launch: a grid barrier wait gave up (code {err})")
+
     def autotune(self, steps: int = 4, use_cache: bool = True) -> dict:
         """Tune the batched lattice step (fsi.autotune); the simulation state is unchanged."""
         return self.lattice.autotune(steps=steps, use_cache=use_cache)

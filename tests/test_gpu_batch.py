@@ -182,3 +182,56 @@ def test_batch_scene_generator_runs_in_fp16(tmp_path, monkeypatch):
         assert np.all(np.isfinite(batch.velocity_numpy(s)))
         rho = batch.density_numpy(s)
         assert abs(float(rho.mean()) - 1.0) < 1e-2
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_persistent_run_matches_per_phase_steps(storage):
+    """SceneBatch.run_persistent (one cooperative launch per run, grid-wide barriers between
+    the phases) against the same scenes stepped one launch per phase: the same per-item code
+    in the same phase order, so the states agree to the float32 order noise of the atomic grid
+    and coupling sums; counters and step bookkeeping are equal."""
+    from fsi.batch import SceneBatch
+    cfgs, masks, pos, _ = coupled_scenes()
+    cfgs = [dataclasses.replace(c, lbm=dataclasses.replace(c.lbm, population_storage=storage))
+            for c in cfgs]
+    steps = 9
+    a, b = SceneBatch(cfgs), SceneBatch(cfgs)
+    for x in (a, b):
+        x.initialize(masks, pos)
+    a.run(steps, graph=False)
+    b.run_persistent(steps, max_steps_per_launch=4)
+    assert b.step_index == a.step_index == steps
+    assert b.lattice.steps_done == a.lattice.steps_done
+    np.testing.assert_array_equal(b.counters_numpy()[:, :3], a.counters_numpy()[:, :3])
+    for s in range(len(cfgs)):
+        assert rel_l2(b.density_numpy(s), a.density_numpy(s)) < 1e-5
+        assert rel_l2(b.velocity_numpy(s), a.velocity_numpy(s)) < 1e-3
+        assert rel_l2(b.positions_numpy(s), a.positions_numpy(s)) < 1e-5
+        assert rel_l2(b.velocities_numpy(s), a.velocities_numpy(s)) < 1e-3
+    # both continue in step: a per-phase step after persistent launches, and the reverse
+    a.run_persistent(2)
+    b.run(2, graph=False)
+    for s in range(len(cfgs)):
+        assert rel_l2(b.positions_numpy(s), a.positions_numpy(s)) < 1e-5
+
+
+def test_persistent_run_reports_a_barrier_wait_that_gave_up():
+    """With a wait limit of a few clock cycles the blocks of the persistent launch give up at
+    the first grid barrier: the launch ends with FSI_ERR_TIMEOUT in the error word, which
+    run_persistent turns into an exception; the device stays usable and a fresh batch runs."""
+    from fsi import _native as nat
+    from fsi.batch import SceneBatch
+    cfgs, masks, pos, _ = coupled_scenes()
+    a = SceneBatch(cfgs)
+    a.initialize(masks, pos)
+    a.step()
+    with pytest.raises(nat.NativeError, match="gave up"):
+        a.run_persistent(3, wait_cycles=1)
+    assert int(a._error.item()) == 0  # cleared after the report
+    b, c = SceneBatch(cfgs), SceneBatch(cfgs)
+    for x in (b, c):
+        x.initialize(masks, pos)
+    b.run_persistent(3)
+    c.run(3, graph=False)
+    for s in range(len(cfgs)):
+        assert rel_l2(b.positions_numpy(s), c.positions_numpy(s)) < 1e-5
