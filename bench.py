@@ -76,11 +76,13 @@ def touched_nodes(base: np.ndarray, dims) -> int:
     return int(np.unique(np.concatenate(out)).size) if out else 0
 
 
-def launches_since(before, lbm_step_launches: int = 1) -> int:
+def launches_since(before, lbm_step_launches: int = 1, tiled_substep_launches: int = 4) -> int:
     """Kernel launches of the library entry points called since the snapshot `before`
-    (fsi_lbm_step launches its face kernel too when the lattice has x faces)."""
+    (fsi_lbm_step launches its face kernel too when the lattice has x faces; the tiled coupled
+    substep launches 3 kernels with the coupling inside P2G, 4 with its own kernel)."""
     from fsi import _native as nat
-    table = dict(LAUNCHES, fsi_lbm_step=lbm_step_launches)
+    table = dict(LAUNCHES, fsi_lbm_step=lbm_step_launches,
+                 fsi_coupled_substep_tiled=tiled_substep_launches)
     total = 0
     for name, count in nat.CALLS.items():
         total += (count - before.get(name, 0)) * table.get(name, 1)
@@ -297,11 +299,16 @@ def time_headline(args, world, stream) -> dict:
     from fsi import scenes
     from fsi.simulation import FSISimulation
 
+    from fsi import autotune
+
     cfg, solid, pos, young = scenes.coupled_bodies()
     sim = FSISimulation(cfg)
     sim.initialize_lbm(solid)
     sim.initialize_mpm_from_numpy(pos, youngs_modulus=young, poisson_ratio=0.3)
     faces = 2 if (sim.lbm.bc_x_left_mode or sim.lbm.bc_x_right_mode) else 1
+    sim.coupler.step(cfg.lbm_dt)
+    # substep launch parameters by the project's autotuner (state restored afterwards)
+    tuning = autotune.tune_coupled(sim, steps=2, use_cache=False)
     for _ in range(args.warmup):
         sim.coupler.step(cfg.lbm_dt)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -312,7 +319,8 @@ def time_headline(args, world, stream) -> dict:
         sim.coupler.step(cfg.lbm_dt)
     b.record(stream)
     barrier(world)
-    launches = launches_since(before, faces)
+    fold = tuning["best"][1] == 1
+    launches = launches_since(before, faces, 3 if fold else 4)
     step_ms = max_over_ranks(a.elapsed_time(b), world) / args.steps
     base = sim.mpm.base_cells_numpy()
     touched = touched_nodes(base, (cfg.lbm.nx, cfg.lbm.ny, cfg.lbm.nz))
@@ -339,6 +347,9 @@ def time_headline(args, world, stream) -> dict:
     n_particles = sim.mpm.particle_count()
     out = {
         "step_ms": step_ms, "lattice_ms": lattice_ms, "e2e_s": e2e_s, "launches": launches,
+        "tuning": {"threads_per_block": tuning["best"][0],
+                   "coupling": "in P2G" if tuning["best"][1] == 1 else "own kernel",
+                   "candidates_ms_per_step": {k: round(v, 4) for k, v in tuning["ms"].items()}},
         "cells": sim.lbm.n_cells, "fluid_cells": int((solid == 0).sum()),
         "solid_cells": int((solid != 0).sum()), "particles": n_particles, "touched": touched,
         "substeps": cfg.coupling.mpm_substeps_per_lbm_step,
@@ -645,6 +656,7 @@ def run_gpu(args) -> dict:
             "step": "LBMMpmCoupler.step: 10 x (coupling + MPM substep), force assembly, "
                     "lattice step (FP32 exact, velocity inlet / pressure outlet faces)",
             "p2g_mode": "atomic",
+            "substep_tuning": h["tuning"],
             "lattice": [384, 192, 192], "tau": 0.55, "inflow": 0.05,
             "fluid_cells": h["fluid_cells"], "particles": h["particles"], "substeps": h["substeps"],
             "l2": "inputs larger than L2 (populations 1.08 GB, particles 60 MB, grid 0.23 GB)",

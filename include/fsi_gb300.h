@@ -43,7 +43,7 @@ extern "C" {
 #define FSI_ERR_TIMEOUT 4
 #define FSI_ERR_UNSUPPORTED 5
 
-#define FSI_ABI_VERSION 2
+#define FSI_ABI_VERSION 3
 
 /* Library ABI version (FSI_ABI_VERSION). No reference counterpart. */
 int fsi_abi_version(void);
@@ -170,6 +170,12 @@ typedef struct fsi_mpm_desc {
   float clamp_lower;
   float clamp_upper[3];
   int32_t material; /* FSI_MATERIAL_*; the reference's model is fixed-corotated */
+  /* Launch tuning of the tiled scatter (no reference counterpart; fsi.autotune sets them):
+   * threads per block of P2G and G2P, 128, 256 or 512 (0: 256), which sets the particles whose
+   * stencils share one shared-memory tile; and where a coupled tiled substep forms the
+   * coupling force: 0 by particle count, 1 inside P2G, 2 in a kernel of its own first. */
+  int32_t launch_threads;
+  int32_t coupling_fold;
 } fsi_mpm_desc;
 
 /* Constitutive models. FIXED_COROTATED is the reference's

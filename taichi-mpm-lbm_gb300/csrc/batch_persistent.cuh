@@ -81,7 +81,7 @@ __device__ __forceinline__ void persist_step_tiles(const PersistArgs& a, float* 
 
 // Resident 256-thread blocks per SM the kernel is compiled for (caps its registers).
 #ifndef FSI_PERSIST_MIN_BLOCKS
-#define FSI_PERSIST_MIN_BLOCKS 2
+#define FSI_PERSIST_MIN_BLOCKS 3
 #endif
 
 template <int kStore, bool kFast>

@@ -33,9 +33,12 @@ namespace {
 // natural 75-80): the extra resident warps hide more of the tile-atomic and gather latency
 // (measured: 2,097,152-particle substep 0.475 -> 0.450 ms with P2G capped, 0.454 ms with G2P
 // capped; no spills in P2G, 8 bytes in G2P).
-__global__ void __launch_bounds__(kBlock, 4) p2g_kernel(Mpm m, PView P, float4* __restrict__ grid,
-                                                     uint8_t* __restrict__ dirty) {
-  p2g_body(m, P, grid, dirty, blockIdx.x * kBlock + threadIdx.x);
+// Threads per block kT (m.threads): 128, 256 or 512, each at the same 64-register cap.
+template <int kT>
+__global__ void __launch_bounds__(kT, 1024 / kT) p2g_kernel(Mpm m, PView P,
+                                                            float4* __restrict__ grid,
+                                                            uint8_t* __restrict__ dirty) {
+  p2g_body(m, P, grid, dirty, blockIdx.x * kT + threadIdx.x);
 }
 
 // The penalty coupling alone (one thread per particle), before p2g_kernel on large launches.
@@ -44,16 +47,47 @@ __global__ void __launch_bounds__(kBlock) coupling_only_kernel(ForceArgs fa) {
 }
 
 // P2G with the penalty coupling folded in (one thread per particle).
-__global__ void __launch_bounds__(kBlock) coupled_p2g_kernel(Mpm m, PView P, float4* __restrict__ grid,
-                                                             uint8_t* __restrict__ dirty,
-                                                             ForceArgs fa) {
-  p2g_body<true>(m, P, grid, dirty, blockIdx.x * kBlock + threadIdx.x, &fa);
+template <int kT>
+__global__ void __launch_bounds__(kT) coupled_p2g_kernel(Mpm m, PView P, float4* __restrict__ grid,
+                                                         uint8_t* __restrict__ dirty, ForceArgs fa) {
+  p2g_body<true>(m, P, grid, dirty, blockIdx.x * kT + threadIdx.x, &fa);
 }
 
-__global__ void __launch_bounds__(kBlock, 4) g2p_kernel(Mpm m, PView P,
-                                                     const float4* __restrict__ grid) {
-  g2p_body(m, P, grid, blockIdx.x * kBlock + threadIdx.x);
+template <int kT>
+__global__ void __launch_bounds__(kT, 1024 / kT) g2p_kernel(Mpm m, PView P,
+                                                            const float4* __restrict__ grid) {
+  g2p_body(m, P, grid, blockIdx.x * kT + threadIdx.x);
 }
+
+// Launches K<m.threads> over the particles.
+template <template <int> class K, class... Args>
+int launch_tiled(const Mpm& m, cudaStream_t s, const char* what, Args... args) {
+  switch (m.threads) {
+    case 128: K<128>::run(grid_for(m.n, 128), s, args...); break;
+    case 512: K<512>::run(grid_for(m.n, 512), s, args...); break;
+    default: K<256>::run(grid_for(m.n, 256), s, args...); break;
+  }
+  return check_launch(what);
+}
+template <int kT>
+struct P2G {
+  static void run(unsigned g, cudaStream_t s, Mpm m, PView P, float4* grid, uint8_t* dirty) {
+    p2g_kernel<kT><<<g, kT, 0, s>>>(m, P, grid, dirty);
+  }
+};
+template <int kT>
+struct CoupledP2G {
+  static void run(unsigned g, cudaStream_t s, Mpm m, PView P, float4* grid, uint8_t* dirty,
+                  ForceArgs fa) {
+    coupled_p2g_kernel<kT><<<g, kT, 0, s>>>(m, P, grid, dirty, fa);
+  }
+};
+template <int kT>
+struct G2P {
+  static void run(unsigned g, cudaStream_t s, Mpm m, PView P, const float4* grid) {
+    g2p_kernel<kT><<<g, kT, 0, s>>>(m, P, grid);
+  }
+};
 
 __global__ void __launch_bounds__(kBlock) clear_kernel(Mpm m, float4* __restrict__ grid,
                                                        uint8_t* __restrict__ dirty) {
@@ -168,11 +202,8 @@ extern "C" int fsi_mpm_substep(const fsi_mpm_desc* d, const fsi_particles* parts
   if (m.n == 0) return FSI_OK;
   cudaStream_t s = as_stream(stream);
   float4* g4 = reinterpret_cast<float4*>(grid);
-  const unsigned pg = grid_for(m.n, kBlock);
-  p2g_kernel<<<pg, kBlock, 0, s>>>(m, P, g4, dirty);
-  if (int e = check_launch("p2g_kernel")) return e;
-  g2p_kernel<<<pg, kBlock, 0, s>>>(m, P, g4);
-  if (int e = check_launch("g2p_kernel")) return e;
+  if (int e = launch_tiled<P2G>(m, s, "p2g_kernel", m, P, g4, dirty)) return e;
+  if (int e = launch_tiled<G2P>(m, s, "g2p_kernel", m, P, (const float4*)g4)) return e;
   const long long nblocks = (long long)m.nbx * m.nby * m.nbz;
   clear_dirty_kernel<<<grid_for(nblocks, kBlock), kBlock, 0, s>>>(m, g4, dirty);
   return check_launch("clear_dirty_kernel");
@@ -329,11 +360,8 @@ extern "C" int fsi_mpm_substep_noalloc(const fsi_mpm_desc* d, const fsi_particle
   if (cudaMemsetAsync(g4, 0, (size_t)nodes * sizeof(float4), s) != cudaSuccess ||
       cudaMemsetAsync(dirty, 0, (size_t)nblocks, s) != cudaSuccess)
     return check_launch("no-alloc scratch clear");
-  const unsigned pg = grid_for(m.n, kBlock);
-  p2g_kernel<<<pg, kBlock, 0, s>>>(m, P, g4, dirty);
-  if (int e = check_launch("p2g_kernel (no-alloc)")) return e;
-  g2p_kernel<<<pg, kBlock, 0, s>>>(m, P, g4);
-  if (int e = check_launch("g2p_kernel (no-alloc)")) return e;
+  if (int e = launch_tiled<P2G>(m, s, "p2g_kernel (no-alloc)", m, P, g4, dirty)) return e;
+  if (int e = launch_tiled<G2P>(m, s, "g2p_kernel (no-alloc)", m, P, (const float4*)g4)) return e;
   clear_kernel<<<grid_for(nblocks * 32, kBlock), kBlock, 0, s>>>(m, g4, dirty);
   return check_launch("clear_kernel (no-alloc)");
 }
@@ -369,23 +397,20 @@ extern "C" int fsi_coupled_substep_tiled(const fsi_coupling_desc* c, const fsi_m
   fa.mask_out = coupling_mask;
   fa.cnt = reinterpret_cast<Cnt*>(counters);
   float4* g4 = reinterpret_cast<float4*>(grid);
-  const unsigned pg = grid_for(m.n, kBlock);
   // Few particles (under two CTAs per SM): launch- and latency-bound, so the coupling runs
   // inside P2G (one launch less per substep). Many particles: the coupling's 27 lattice
-  // gathers hide their latency better in a separate lighter kernel (46 registers against 80:
-  // 5 CTAs per SM against 3), so the coupling runs first on its own (measured on the
-  // 384x192x192 coupled step: 3.71 ms separate against 3.93 ms fused).
-  if (m.n < 2 * 152 * kBlock) {
-    coupled_p2g_kernel<<<pg, kBlock, 0, s>>>(m, P, g4, dirty, fa);
-    if (int e = check_launch("coupled_p2g_kernel")) return e;
+  // gathers and reductions run better in a separate lighter kernel than at P2G's occupancy,
+  // so the coupling runs first on its own (measured on the 384x192x192 coupled step: 3.71 ms
+  // separate against 3.93 ms fused). m.fold overrides the choice.
+  const bool fold = m.fold == 1 || (m.fold == 0 && m.n < 2 * 152 * kBlock);
+  if (fold) {
+    if (int e = launch_tiled<CoupledP2G>(m, s, "coupled_p2g_kernel", m, P, g4, dirty, fa)) return e;
   } else {
-    coupling_only_kernel<<<pg, kBlock, 0, s>>>(fa);
+    coupling_only_kernel<<<grid_for(m.n, kBlock), kBlock, 0, s>>>(fa);
     if (int e = check_launch("coupling_only_kernel")) return e;
-    p2g_kernel<<<pg, kBlock, 0, s>>>(m, P, g4, dirty);
-    if (int e = check_launch("p2g_kernel")) return e;
+    if (int e = launch_tiled<P2G>(m, s, "p2g_kernel", m, P, g4, dirty)) return e;
   }
-  g2p_kernel<<<pg, kBlock, 0, s>>>(m, P, g4);
-  if (int e = check_launch("g2p_kernel")) return e;
+  if (int e = launch_tiled<G2P>(m, s, "g2p_kernel", m, P, (const float4*)g4)) return e;
   const long long nblocks = (long long)m.nbx * m.nby * m.nbz;
   clear_dirty_kernel<<<grid_for(nblocks, kBlock), kBlock, 0, s>>>(m, g4, dirty);
   return check_launch("clear_dirty_kernel");

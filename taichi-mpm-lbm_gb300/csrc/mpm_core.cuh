@@ -22,6 +22,8 @@ struct Mpm {
   long long cap;
   int nbx, nby, nbz;  // 4^3 block grid
   int material;       // FSI_MATERIAL_*
+  int threads;        // threads per block of the tiled P2G / G2P (128, 256 or 512)
+  int fold;           // coupled tiled substep: 0 by particle count, 1 in P2G, 2 separate
 };
 
 struct PView {
@@ -329,7 +331,7 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
   if (!cta_box(m, act, base, box, sh)) return;
   const bool use_tile = box.vol <= kTileCap;
   if (use_tile) {
-    for (int t = threadIdx.x; t < box.vol; t += kBlock) {
+    for (int t = threadIdx.x; t < box.vol; t += blockDim.x) {
       tile[0][t] = 0.f; tile[1][t] = 0.f; tile[2][t] = 0.f; tile[3][t] = 0.f;
     }
     __syncthreads();
@@ -410,7 +412,7 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
     __syncthreads();
     if (box.vol == 0) return;  // every stencil node lies outside the grid
     const int e12 = box.ext[1] * box.ext[2];
-    for (int t = threadIdx.x; t < box.vol; t += kBlock) {
+    for (int t = threadIdx.x; t < box.vol; t += blockDim.x) {
       const float a = tile[0][t], b = tile[1][t], c = tile[2][t], d = tile[3][t];
       if (a == 0.f && b == 0.f && c == 0.f && d == 0.f) continue;
       const int ti = t / e12, r = t - ti * e12, tj = r / box.ext[2], tk = r - tj * box.ext[2];
@@ -421,7 +423,7 @@ __device__ __forceinline__ void p2g_body(const Mpm& m, const PView& P, float4* _
     const int b1[3] = {(box.lo[0] + box.ext[0] - 1) >> 2, (box.lo[1] + box.ext[1] - 1) >> 2,
                        (box.lo[2] + box.ext[2] - 1) >> 2};
     const int nbx = b1[0] - b0[0] + 1, nby = b1[1] - b0[1] + 1, nbz = b1[2] - b0[2] + 1;
-    for (int t = threadIdx.x; t < nbx * nby * nbz; t += kBlock) {
+    for (int t = threadIdx.x; t < nbx * nby * nbz; t += blockDim.x) {
       const int bi = b0[0] + t / (nby * nbz), bj = b0[1] + (t / nbz) % nby, bk = b0[2] + t % nbz;
       dirty[((long long)bi * m.nby + bj) * m.nbz + bk] = 1;
     }
@@ -469,7 +471,7 @@ __device__ __forceinline__ void g2p_body(const Mpm& m, const PView& P,
   const bool use_tile = box.vol <= kTileCap;
   if (use_tile) {
     const int e12 = box.ext[1] * box.ext[2];
-    for (int t = threadIdx.x; t < box.vol; t += kBlock) {
+    for (int t = threadIdx.x; t < box.vol; t += blockDim.x) {
       const int ti = t / e12, r = t - ti * e12, tj = r / box.ext[2], tk = r - tj * box.ext[2];
       const int i = box.lo[0] + ti, j = box.lo[1] + tj, k = box.lo[2] + tk;
       float v[3];
@@ -581,6 +583,13 @@ int make_mpm(const fsi_mpm_desc* d, const fsi_particles* p, Mpm& m, PView& v) {
               "unknown material %d", d->material);
   FSI_REQUIRE((p->mu == nullptr) == (p->lam == nullptr), "per-particle mu and lam go together");
   m.material = d->material;
+  FSI_REQUIRE(d->launch_threads == 0 || d->launch_threads == 128 || d->launch_threads == 256 ||
+                  d->launch_threads == 512,
+              "launch_threads %d is not 0, 128, 256 or 512", d->launch_threads);
+  FSI_REQUIRE(d->coupling_fold >= 0 && d->coupling_fold <= 2, "coupling_fold %d outside 0..2",
+              d->coupling_fold);
+  m.threads = d->launch_threads ? d->launch_threads : kBlock;
+  m.fold = d->coupling_fold;
   v.x = p->x; v.v = p->v; v.C = p->C; v.F = p->F; v.mass = p->mass; v.vol = p->volume;
   v.active = p->active; v.fp = p->force; v.mu = p->mu; v.lam = p->lam;
   return FSI_OK;

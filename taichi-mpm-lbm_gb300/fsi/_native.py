@@ -22,7 +22,7 @@ FSI_ERR_CUDA = 2
 FSI_ERR_GUARD = 3
 FSI_ERR_TIMEOUT = 4
 FSI_ERR_UNSUPPORTED = 5
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 STORAGE_F32, STORAGE_F16, STORAGE_BF16 = 0, 1, 2
 ARITH_EXACT, ARITH_FAST = 0, 1
@@ -57,6 +57,7 @@ class MpmDesc(ctypes.Structure):
         ("clamp_lower", ctypes.c_float),
         ("clamp_upper", c_float3),
         ("material", ctypes.c_int32),
+        ("launch_threads", ctypes.c_int32), ("coupling_fold", ctypes.c_int32),
     ]
 
 

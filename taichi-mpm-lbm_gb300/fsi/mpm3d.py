@@ -106,6 +106,7 @@ class MPMSolver3D:
         self._desc = self._make_desc()
         self._parts = self._make_particles()
         self._initialized = False
+        self.tuning = None  # launch parameters chosen by fsi.autotune.tune_coupled
 
     # ----------------------------------------------------------------- setup
     def _make_desc(self) -> nat.MpmDesc:

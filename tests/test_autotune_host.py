@@ -83,3 +83,32 @@ def test_tuning_needs_an_initialized_batch(cache):
     batch._initialized = False
     with pytest.raises(RuntimeError):
         autotune.tune_lattice_batch(batch)
+
+
+def _sim(p2g_mode="atomic", particles=4096, shape=(48, 32, 32)):
+    from fsi import _native as nat
+    lbm = SimpleNamespace(nx=shape[0], ny=shape[1], nz=shape[2], population_storage="f32")
+    cfg = SimpleNamespace(lbm=lbm, mpm=SimpleNamespace(p2g_mode=p2g_mode), lbm_dt=1.0)
+    mpm = SimpleNamespace(desc=nat.MpmDesc(), tuning=None, particle_count=lambda: particles)
+    return SimpleNamespace(config=cfg, mpm=mpm)
+
+
+def test_coupled_candidates_and_signature(cache):
+    assert autotune.coupled_candidates(_sim()) == [(t, f) for t in (128, 256, 512) for f in (1, 2)]
+    assert autotune.coupled_candidates(_sim(p2g_mode="sorted")) == []
+    a = autotune.coupled_signature(_sim(particles=502304))
+    # nearby particle counts share a record, other shapes and modes do not
+    assert autotune.coupled_signature(_sim(particles=502000)) == a
+    assert autotune.coupled_signature(_sim(particles=251000)) != a
+    assert autotune.coupled_signature(_sim(particles=502304, shape=(48, 32, 16))) != a
+    assert autotune.coupled_signature(_sim(particles=502304, p2g_mode="sorted")) != a
+
+
+def test_coupled_tuning_from_the_cache_applies_without_timing(cache):
+    sim = _sim()
+    autotune._store(autotune.coupled_signature(sim), {"best": [512, 2], "ms": {}})
+    rec = autotune.tune_coupled(sim)  # no GPU: only the cached path can run
+    assert rec["best"] == [512, 2]
+    assert (sim.mpm.desc.launch_threads, sim.mpm.desc.coupling_fold) == (512, 2)
+    assert sim.mpm.tuning == {"launch_threads": 512, "coupling_fold": 2}
+    assert autotune.tune_coupled(_sim(p2g_mode="sorted")) == {"best": None, "ms": {}}

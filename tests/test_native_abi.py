@@ -52,7 +52,7 @@ def test_invalid_descriptor_is_rejected_without_touching_the_gpu():
 def test_struct_sizes_match_header_layout():
     assert ctypes.sizeof(_native.LbmDesc) == 4 * (5 + 19 + 3 + 6 + 2)
     assert ctypes.sizeof(_native.BatchLattice) == 4 * 4 + 8 + 4 * (19 + 1 + 3) + 4  # + tail pad
-    assert ctypes.sizeof(_native.MpmDesc) == 4 * 20
+    assert ctypes.sizeof(_native.MpmDesc) == 4 * 22  # + launch_threads, coupling_fold
     assert ctypes.sizeof(_native.Particles) == 8 * 11
     assert ctypes.sizeof(_native.CouplingDesc) == 4 * 18
 
@@ -79,7 +79,7 @@ def test_closure_row_buffer_size():
 def test_scene_context_layout_and_argument_checks():
     """fsi_scene_desc / fsi_scene_buffers layouts, and fsi_ctx_create / fsi_coupled_step
     rejecting bad arguments before any device work."""
-    assert ctypes.sizeof(_native.SceneDesc) == 4 * (35 + 20 + 18) + 4 * (3 + 2 + 5)
+    assert ctypes.sizeof(_native.SceneDesc) == 4 * (35 + 22 + 18) + 4 * (3 + 2 + 5)
     assert ctypes.sizeof(_native.SceneBuffers) == 8 * 5 + 8 * 11 + 8 * 6
     d, b = _native.SceneDesc(), _native.SceneBuffers()
     d.lbm.nx = d.lbm.ny = d.lbm.nz = 8
