@@ -172,13 +172,36 @@ __global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, d
       atomicMax(reinterpret_cast<unsigned long long*>(out + 4),
                 (unsigned long long)__double_as_longlong((double)vmax));
   } else if (a.accum) {
+    // Fluid-cell sums of the reaction field in warp tiles of 32 consecutive cells: float32
+    // warp sums, added in float64 by lane 0 (FP64 adds are scarce on this GPU), four tiles per
+    // pass with their loads issued together (a bandwidth-bound pass).
     double s3[3] = {0, 0, 0};
-    const int nb = gridDim.x - a.pblocks;
-    for (long long c = (long long)(blockIdx.x - a.pblocks) * kBlock + threadIdx.x; c < a.g.n;
-         c += (long long)nb * kBlock) {
-      if (a.flags[c] & kFlagSolid) continue;
-      const float4 v = a.accum[c];
-      s3[0] += v.x; s3[1] += v.y; s3[2] += v.z;
+    const int lane = threadIdx.x & 31;
+    const long long tiles = (a.g.n + 31) / 32;
+    const long long warps = (long long)(gridDim.x - a.pblocks) * (kBlock / 32);
+    for (long long t0 = (long long)(blockIdx.x - a.pblocks) * (kBlock / 32) + (threadIdx.x >> 5);
+         t0 < tiles; t0 += 4 * warps) {
+      uint32_t fl[4];
+      float4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const long long c = (t0 + u * warps) * 32 + lane;
+        const bool in = c < a.g.n;
+        fl[u] = in ? a.flags[c] : kFlagSolid;
+        v[u] = in ? a.accum[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        float w[3] = {0.f, 0.f, 0.f};
+        if (!(fl[u] & kFlagSolid)) { w[0] = v[u].x; w[1] = v[u].y; w[2] = v[u].z; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) w[i] += __shfl_down_sync(0xffffffffu, w[i], o);
+        if (lane == 0)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) s3[i] += (double)w[i];
+      }
     }
     for (int i = 0; i < 3; ++i) {
       const double t = block_sum(s3[i], sh);
@@ -305,7 +328,7 @@ extern "C" int fsi_coupled_diagnostics(const fsi_mpm_desc* m, const fsi_particle
   int pb = (int)grid_for(a.n, kBlock);
   if (pb > 152 * 2) pb = 152 * 2;
   int cb = accum ? (int)grid_for(a.g.n, kBlock) : 0;
-  if (cb > 152 * 2) cb = 152 * 2;
+  if (cb > 152 * 8) cb = 152 * 8;
   a.pblocks = pb;
   runner_diag_kernel<<<pb + cb, kBlock, 0, s>>>(a, out);
   return check_launch("runner_diag_kernel");

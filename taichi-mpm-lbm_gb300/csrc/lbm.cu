@@ -220,28 +220,79 @@ __global__ void __launch_bounds__(kBlock) lbm_force_kernel(LbmGeom g,
 
 // Lattice diagnostics of the current macro and force fields (lbm3d.py:450-483):
 // out[0] += sum rho over fluid, out[1] = max |u| over all cells, out[2..4] += sum force over fluid.
+// Sums over the lattice in warp tiles of 32 consecutive cells of a row (the same tiles as a
+// one-thread-per-cell launch): each tile's fluid rho and force in float32 warp sums, added in
+// float64 per warp over its tiles, then per block, and once per block into out (out[0] sum of
+// rho over fluid, out[1] max |u|, out[2..4] force sums). A bounded grid walks the tiles, so
+// the float64 atomics number a few per block instead of a few per 256 cells.
 __global__ void __launch_bounds__(kBlock) lbm_reduce_kernel(LbmGeom g,
                                                             const float4* __restrict__ macro,
                                                             const float* __restrict__ force,
                                                             const uint32_t* __restrict__ flags,
                                                             double* __restrict__ out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int i = blockIdx.z;
-  float mass = 0.f, vmax = 0.f, f[3] = {0.f, 0.f, 0.f};
-  if (k < g.nz && j < g.ny) {
-    const uint32_t c = (uint32_t)((i * g.ny + j) * g.nz + k);
-    const uint32_t n = (uint32_t)g.n;
-    const float4 m = macro[c];
-    vmax = norm3_ref(m.x, m.y, m.z);
-    if (!(flags[c] & kFlagSolid)) {
-      mass = m.w;
-      if (force) { f[0] = force[c]; f[1] = force[n + c]; f[2] = force[2 * n + c]; }
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long tiles_per_row = (g.nz + 31) / 32;
+  const long long tiles = (long long)g.nx * g.ny * tiles_per_row;
+  const long long warps = (long long)gridDim.x * (kBlock / 32);
+  const uint32_t n = (uint32_t)g.n;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  float vmax = 0.f;
+  // four tiles per pass, their loads issued together
+  for (long long t0 = (long long)blockIdx.x * (kBlock / 32) + wib; t0 < tiles; t0 += 4 * warps) {
+    float4 m[4];
+    uint32_t fl[4];
+    float fv[4][3];
+    bool in[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const long long t = t0 + u * warps;
+      const long long row = t / tiles_per_row;
+      const int k = (int)(t - row * tiles_per_row) * 32 + lane;
+      in[u] = t < tiles && k < g.nz;
+      const uint32_t c = in[u] ? (uint32_t)(row * g.nz + k) : 0u;
+      m[u] = in[u] ? macro[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      fl[u] = in[u] ? flags[c] : kFlagSolid;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) fv[u][a] = (in[u] && force) ? force[a * n + c] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      vmax = fmaxf(vmax, norm3_ref(m[u].x, m[u].y, m[u].z));
+      if (!(fl[u] & kFlagSolid)) {
+        v[0] = m[u].w;
+        v[1] = fv[u][0]; v[2] = fv[u][1]; v[3] = fv[u][2];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+      if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc[i] += (double)v[i];
     }
   }
-  const float s1[1] = {mass};
-  block_accumulate<1>(out, s1, out + 1, vmax);
-  block_accumulate<3>(out + 2, f, nullptr, 0.f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+  __shared__ double sh[4][kBlock / 32];
+  __shared__ float shm[kBlock / 32];
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) sh[i][wib] = acc[i];
+    shm[wib] = vmax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s4[4] = {0.0, 0.0, 0.0, 0.0};
+    float m = 0.f;
+    for (int w = 0; w < kBlock / 32; ++w) {
+      for (int i = 0; i < 4; ++i) s4[i] += sh[i][w];
+      m = fmaxf(m, shm[w]);
+    }
+    atomicAdd(out, s4[0]);
+    atomic_max_nonneg(out + 1, (double)m);
+    for (int i = 0; i < 3; ++i) atomicAdd(out + 2 + i, s4[1 + i]);
+  }
 }
 
 int check_desc(const fsi_lbm_desc* d) {
@@ -456,9 +507,11 @@ extern "C" int fsi_lbm_reduce(const fsi_lbm_desc* d, const float* macro, const f
   LbmGeom g = geom_of(d);
   cudaStream_t s = as_stream(stream);
   if (cudaMemsetAsync(out, 0, 8 * sizeof(double), s) != cudaSuccess) return check_launch("memset");
-  const CellLaunch L = cell_launch(g);
-  lbm_reduce_kernel<<<L.grid, L.block, 0, s>>>(g, reinterpret_cast<const float4*>(macro), force,
-                                               flags, out);
+  const long long tiles = (long long)g.nx * g.ny * ((g.nz + 31) / 32);
+  long long blocks = (tiles + kBlock / 32 - 1) / (kBlock / 32);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  lbm_reduce_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(g, reinterpret_cast<const float4*>(macro),
+                                                        force, flags, out);
   return check_launch("lbm_reduce_kernel");
 }
 
