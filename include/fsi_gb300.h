@@ -340,11 +340,13 @@ int fsi_coupled_substep_tiled(const fsi_coupling_desc* coupling, const fsi_mpm_d
  *   FSI_ASSEMBLE_COUPLING        force += accum.xyz on fluid  (coupling.py:413-419)
  *   FSI_ASSEMBLE_IB              Brinkman drag into ib_force float[3][N], counters
  *                                and totals, force += ib      (coupling.py:421-461)
- * base_force is host float[3]; force may be NULL to update accum/ib_force only.
- * IB counters/totals must be zeroed by the caller. */
+ * base_force is host float[3], or with FSI_ASSEMBLE_BASE_ON_DEVICE a device float[3] that
+ * the kernel reads (a force that changes between replays of a captured CUDA graph); force may
+ * be NULL to update accum/ib_force only. IB counters/totals must be zeroed by the caller. */
 #define FSI_ASSEMBLE_CLAMP_FRACTION 1
 #define FSI_ASSEMBLE_COUPLING 2
 #define FSI_ASSEMBLE_IB 4
+#define FSI_ASSEMBLE_BASE_ON_DEVICE 8
 int fsi_coupling_assemble(const fsi_coupling_desc* desc, const fsi_lbm_desc* lbm,
                           const uint32_t* flags, const float* base_force, int mode, float* accum,
                           const float* macro, float* force, float* ib_force, void* counters,

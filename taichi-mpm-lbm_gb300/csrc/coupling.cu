@@ -173,9 +173,12 @@ __global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, d
                 (unsigned long long)__double_as_longlong((double)vmax));
   } else if (a.accum) {
     // Fluid-cell sums of the reaction field in warp tiles of 32 consecutive cells: float32
-    // warp sums, added in float64 by lane 0 (FP64 adds are scarce on this GPU), four tiles per
-    // pass with their loads issued together (a bandwidth-bound pass).
+    // butterfly warp sums, lane j keeping the warp's j-th tile of each run of 32 and adding it
+    // in float64 once per run (one float64 instruction per 32 tiles: FP64 is this GPU's scarce
+    // pipe), four tiles per pass with their loads issued together.
     double s3[3] = {0, 0, 0};
+    float hold[3] = {0.f, 0.f, 0.f};
+    int slot = 0;
     const int lane = threadIdx.x & 31;
     const long long tiles = (a.g.n + 31) / 32;
     const long long warps = (long long)(gridDim.x - a.pblocks) * (kBlock / 32);
@@ -197,12 +200,19 @@ __global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, d
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-          for (int i = 0; i < 3; ++i) w[i] += __shfl_down_sync(0xffffffffu, w[i], o);
-        if (lane == 0)
+          for (int i = 0; i < 3; ++i) w[i] += __shfl_xor_sync(0xffffffffu, w[i], o);
+        if (lane == slot)
 #pragma unroll
-          for (int i = 0; i < 3; ++i) s3[i] += (double)w[i];
+          for (int i = 0; i < 3; ++i) hold[i] = w[i];
+        if (++slot == 32) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i) { s3[i] += (double)hold[i]; hold[i] = 0.f; }
+          slot = 0;
+        }
       }
     }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s3[i] += (double)hold[i];
     for (int i = 0; i < 3; ++i) {
       const double t = block_sum(s3[i], sh);
       if (threadIdx.x == 0) atomicAdd(out + 8 + i, t);
@@ -260,7 +270,13 @@ extern "C" int fsi_coupling_assemble(const fsi_coupling_desc* c, const fsi_lbm_d
   a.c = *c;
   a.g = geo_of(l);
   a.flags = flags;
-  for (int i = 0; i < 3; ++i) a.base[i] = base_force[i];
+  a.base_dev = nullptr;
+  if (mode & FSI_ASSEMBLE_BASE_ON_DEVICE) {
+    a.base_dev = base_force;
+    for (int i = 0; i < 3; ++i) a.base[i] = 0.f;
+  } else {
+    for (int i = 0; i < 3; ++i) a.base[i] = base_force[i];
+  }
   a.mode = mode;
   a.accum = reinterpret_cast<float4*>(accum);
   a.macro = reinterpret_cast<const float4*>(macro);

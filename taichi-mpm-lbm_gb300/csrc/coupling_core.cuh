@@ -280,6 +280,7 @@ struct AssembleArgs {
   Geo g;
   const uint32_t* __restrict__ flags;
   float base[3];
+  const float* base_dev;  // device float[3] read in place of base, or NULL
   int mode;
   float4* __restrict__ accum;
   const float4* FSI_LAUNCH_RO macro;
@@ -302,7 +303,10 @@ __device__ __forceinline__ void assemble_body(const AssembleArgs& a, long long c
       acc.w = fminf(acc.w, 1.0f);
       a.accum[c].w = acc.w;
     }
-    float f[3] = {fluid ? a.base[0] : 0.f, fluid ? a.base[1] : 0.f, fluid ? a.base[2] : 0.f};
+    const float b0 = a.base_dev ? a.base_dev[0] : a.base[0];
+    const float b1 = a.base_dev ? a.base_dev[1] : a.base[1];
+    const float b2 = a.base_dev ? a.base_dev[2] : a.base[2];
+    float f[3] = {fluid ? b0 : 0.f, fluid ? b1 : 0.f, fluid ? b2 : 0.f};
     if (a.mode & FSI_ASSEMBLE_COUPLING) {
       f[0] = fluid ? __fadd_rn(f[0], acc.x) : 0.f;
       f[1] = fluid ? __fadd_rn(f[1], acc.y) : 0.f;

@@ -221,10 +221,12 @@ __global__ void __launch_bounds__(kBlock) lbm_force_kernel(LbmGeom g,
 // Lattice diagnostics of the current macro and force fields (lbm3d.py:450-483):
 // out[0] += sum rho over fluid, out[1] = max |u| over all cells, out[2..4] += sum force over fluid.
 // Sums over the lattice in warp tiles of 32 consecutive cells of a row (the same tiles as a
-// one-thread-per-cell launch): each tile's fluid rho and force in float32 warp sums, added in
-// float64 per warp over its tiles, then per block, and once per block into out (out[0] sum of
-// rho over fluid, out[1] max |u|, out[2..4] force sums). A bounded grid walks the tiles, so
-// the float64 atomics number a few per block instead of a few per 256 cells.
+// one-thread-per-cell launch): each tile's fluid rho and force in float32 warp sums (a
+// butterfly, so every lane holds the tile's sum), added in float64 per warp over its tiles,
+// then per block, and once per block into out (out[0] sum of rho over fluid, out[1] max |u|,
+// out[2..4] force sums). The float64 adds are this GPU's scarce pipe: lane j keeps the sum of
+// the warp's j-th tile of each run of 32 and converts and adds it once per run, so one float64
+// instruction serves 32 tiles. A bounded grid walks the tiles (a few atomics per block).
 __global__ void __launch_bounds__(kBlock) lbm_reduce_kernel(LbmGeom g,
                                                             const float4* __restrict__ macro,
                                                             const float* __restrict__ force,
@@ -236,24 +238,25 @@ __global__ void __launch_bounds__(kBlock) lbm_reduce_kernel(LbmGeom g,
   const long long warps = (long long)gridDim.x * (kBlock / 32);
   const uint32_t n = (uint32_t)g.n;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  float hold[4] = {0.f, 0.f, 0.f, 0.f};
+  int slot = 0;  // lane that keeps the next tile's sums
   float vmax = 0.f;
   // four tiles per pass, their loads issued together
   for (long long t0 = (long long)blockIdx.x * (kBlock / 32) + wib; t0 < tiles; t0 += 4 * warps) {
     float4 m[4];
     uint32_t fl[4];
     float fv[4][3];
-    bool in[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const long long t = t0 + u * warps;
       const long long row = t / tiles_per_row;
       const int k = (int)(t - row * tiles_per_row) * 32 + lane;
-      in[u] = t < tiles && k < g.nz;
-      const uint32_t c = in[u] ? (uint32_t)(row * g.nz + k) : 0u;
-      m[u] = in[u] ? macro[c] : make_float4(0.f, 0.f, 0.f, 0.f);
-      fl[u] = in[u] ? flags[c] : kFlagSolid;
+      const bool in = t < tiles && k < g.nz;
+      const uint32_t c = in ? (uint32_t)(row * g.nz + k) : 0u;
+      m[u] = in ? macro[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      fl[u] = in ? flags[c] : kFlagSolid;
 #pragma unroll
-      for (int a = 0; a < 3; ++a) fv[u][a] = (in[u] && force) ? force[a * n + c] : 0.f;
+      for (int a = 0; a < 3; ++a) fv[u][a] = (in && force) ? force[a * n + c] : 0.f;
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -266,14 +269,26 @@ __global__ void __launch_bounds__(kBlock) lbm_reduce_kernel(LbmGeom g,
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
-      if (lane == 0)
+        for (int i = 0; i < 4; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+      if (lane == slot)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) acc[i] += (double)v[i];
+        for (int i = 0; i < 4; ++i) hold[i] = v[i];
+      if (++slot == 32) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { acc[i] += (double)hold[i]; hold[i] = 0.f; }
+        slot = 0;
+      }
     }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+  for (int i = 0; i < 4; ++i) acc[i] += (double)hold[i];
+  // float64 warp sums, then block sums
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], o);
+    vmax = fmaxf(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+  }
   __shared__ double sh[4][kBlock / 32];
   __shared__ float shm[kBlock / 32];
   if (lane == 0) {
@@ -284,13 +299,13 @@ __global__ void __launch_bounds__(kBlock) lbm_reduce_kernel(LbmGeom g,
   __syncthreads();
   if (threadIdx.x == 0) {
     double s4[4] = {0.0, 0.0, 0.0, 0.0};
-    float m = 0.f;
+    float mx = 0.f;
     for (int w = 0; w < kBlock / 32; ++w) {
       for (int i = 0; i < 4; ++i) s4[i] += sh[i][w];
-      m = fmaxf(m, shm[w]);
+      mx = fmaxf(mx, shm[w]);
     }
     atomicAdd(out, s4[0]);
-    atomic_max_nonneg(out + 1, (double)m);
+    atomic_max_nonneg(out + 1, (double)mx);
     for (int i = 0; i < 3; ++i) atomicAdd(out + 2 + i, s4[1 + i]);
   }
 }

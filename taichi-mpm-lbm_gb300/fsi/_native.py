@@ -27,7 +27,7 @@ ABI_VERSION = 3
 STORAGE_F32, STORAGE_F16, STORAGE_BF16 = 0, 1, 2
 ARITH_EXACT, ARITH_FAST = 0, 1
 FORCE_CLEAR, FORCE_SET, FORCE_ADD, FORCE_ZERO_SOLID = 0, 1, 2, 3
-ASSEMBLE_CLAMP_FRACTION, ASSEMBLE_COUPLING, ASSEMBLE_IB = 1, 2, 4
+ASSEMBLE_CLAMP_FRACTION, ASSEMBLE_COUPLING, ASSEMBLE_IB, ASSEMBLE_BASE_ON_DEVICE = 1, 2, 4, 8
 
 c_float3 = ctypes.c_float * 3
 

@@ -87,6 +87,7 @@ class LBMMpmCoupler:
         self._diag = torch.zeros(4, dtype=torch.float64, device=dev)
         self._coupled_step = 0
         self._ib_written = False
+        self._device_base = None  # device float32[3] driving force, when its owner sets it
         self._desc = nat.CouplingDesc()
         self._fill_desc()
 
@@ -142,11 +143,18 @@ class LBMMpmCoupler:
                  nat.ptr(self._counters), nat.stream_ptr())
 
     def _assemble(self, mode: int, force: torch.Tensor | None, body_force=None) -> None:
-        base = np.asarray(self.lbm.config.force if body_force is None else body_force,
-                          dtype=np.float32)
-        if base.shape != (3,):
-            raise ValueError("body_force must have 3 components.")
-        base_p = base.ctypes.data_as(nat.ctypes.POINTER(nat.ctypes.c_float))
+        if self._device_base is not None:
+            # the step's driving force is read on the device (a captured step's value changes
+            # between graph replays); its owner fills the buffer before each step
+            mode |= nat.ASSEMBLE_BASE_ON_DEVICE
+            base_p = nat.ctypes.cast(self._device_base.data_ptr(),
+                                     nat.ctypes.POINTER(nat.ctypes.c_float))
+        else:
+            base = np.asarray(self.lbm.config.force if body_force is None else body_force,
+                              dtype=np.float32)
+            if base.shape != (3,):
+                raise ValueError("body_force must have 3 components.")
+            base_p = base.ctypes.data_as(nat.ctypes.POINTER(nat.ctypes.c_float))
         if mode & nat.ASSEMBLE_IB:
             self._counters[5:7].zero_()
             self._counters[8:12].zero_()

@@ -26,6 +26,10 @@ class FSISimulation:
         self._mpm_initialized = False
         self._dbuf = None
         self._dhost = None
+        # step() replays a captured CUDA graph of (coupled step + diagnostics) once the state
+        # repeats with period two (no reference counterpart; set False for eager steps)
+        self.graph_steps = True
+        self._graphs = {}
 
     def initialize_lbm(self, solid_np: np.ndarray | None = None) -> None:
         self.lbm.initialize(solid_np=solid_np)
@@ -61,12 +65,78 @@ class FSISimulation:
 
     def step(self, body_force=None) -> dict[str, object]:
         """One coupled step and its diagnostics (simulation.py:84-89). ``body_force`` is the
-        extension of LBMMpmCoupler.step: this step's lattice driving force (3 components)."""
+        extension of LBMMpmCoupler.step: this step's lattice driving force (3 components).
+
+        With ``graph_steps`` (default), once the solvers' state repeats with period two (the
+        lattice's AA parity and force buffers, a settled gamma ramp, rho / u refreshed by the
+        last diagnostics), the step and its diagnostics run as the replay of one of two
+        captured CUDA graphs, the driving force read from a device buffer filled from pinned
+        host memory; the kernels and their arguments are those of the eager step."""
         self._validate_initialized()
+        if body_force is not None and np.asarray(body_force).shape != (3,):
+            raise ValueError("body_force must have 3 components.")
+        if self.graph_steps and self._graph_ready():
+            return self._graph_step(body_force)
         self.coupler.step(self.config.lbm_dt, body_force=body_force)
         self.step_index += 1
         self.time += self.config.lbm_dt
         return self.diagnostics()
+
+    # ------------------------------------------------------ graph stepping
+    def _graph_ready(self) -> bool:
+        lbm, c = self.lbm, self.coupler
+        return (lbm._macro_fresh and lbm._fcur == lbm._fprev and lbm._fcur >= 0
+                and c._gamma_settled() and self._dbuf is not None)
+
+    def _graph_key(self) -> tuple:
+        lbm, m = self.lbm, self.mpm
+        d = m.desc
+        c = self.coupler
+        return (lbm._steps_done % 2, lbm._fcur, m.particle_count(), d.launch_threads,
+                d.coupling_fold, lbm._pops.data_ptr(), m._grid.data_ptr(), c._accum.data_ptr(),
+                float(c._gamma_for_kernel()), c._ib_written)
+
+    def _graph_step(self, body_force) -> dict[str, object]:
+        import torch
+
+        lbm, c = self.lbm, self.coupler
+        if not hasattr(self, "_base_pin"):
+            self._base_pin = torch.zeros(3, dtype=torch.float32).pin_memory()
+            self._base_dev = torch.zeros(3, dtype=torch.float32, device=self._dbuf.device)
+        force = self.lbm.config.force if body_force is None else body_force
+        self._base_pin.numpy()[:] = np.asarray(force, dtype=np.float32)
+        key = self._graph_key()
+        entry = self._graphs.get(key)
+        if entry is None:
+            if len(self._graphs) >= 4:
+                self._graphs.clear()
+            g = torch.cuda.CUDAGraph()
+            c._device_base = self._base_dev
+            steps0, coupled0 = lbm._steps_done, c._coupled_step
+            try:
+                with torch.cuda.graph(g):
+                    # capture records the work without running it; the host-side counters
+                    # advance here, and the replay below performs it
+                    self._base_dev.copy_(self._base_pin, non_blocking=True)
+                    c.step(self.config.lbm_dt)
+                    self._diag_enqueue()
+            finally:
+                c._device_base = None
+            entry = (g, lbm._fcur, lbm._fprev)
+            self._graphs[key] = entry
+            lbm._steps_done, c._coupled_step = steps0, coupled0
+        g, fcur, fprev = entry
+        g.replay()
+        lbm._steps_done += 1
+        lbm._fcur, lbm._fprev = fcur, fprev
+        lbm._macro_fresh = True
+        lbm._mass_speed_cache = None
+        c._coupled_step += 1
+        if c.immersed_boundary_enabled:
+            c._ib_written = True
+        self.step_index += 1
+        self.time += self.config.lbm_dt
+        return self._diag_finish(None)
 
     def run(self, steps: int | None = None, write_output: bool = False,
             write_initial: bool = False) -> list[dict[str, object]]:
@@ -110,6 +180,11 @@ class FSISimulation:
         centre of mass is a float32 numpy sum, here the float64 quotient rounded to float32
         (MPMSolver3D.center_of_mass() keeps the float32 host arithmetic)."""
         self._validate_initialized()
+        return self._diag_finish(self._diag_enqueue())
+
+    def _diag_enqueue(self):
+        """Enqueue the device reductions and the copy of their record to pinned host memory;
+        returns the lattice's cached (mass, max |u|) of this state, or None."""
         import torch
 
         from . import _native as nat
@@ -124,6 +199,13 @@ class FSISimulation:
                  nat.ptr(c._accum), nat.ptr(self.lbm.flags), nat.ptr(c._counters),
                  nat.ptr(self._dbuf[8:]), nat.stream_ptr())
         self._dhost.copy_(self._dbuf, non_blocking=True)
+        return cached
+
+    def _diag_finish(self, cached) -> dict[str, object]:
+        """Wait for the enqueued record and build the reference's diagnostics dict."""
+        import torch
+
+        c = self.coupler
         torch.cuda.current_stream().synchronize()
         r = self._dhost.numpy().copy()
         if cached is None:
@@ -168,6 +250,7 @@ class FSISimulation:
     def load_state_dict(self, state: dict) -> None:
         if state.get("kind") != "FSISimulation":
             raise ValueError("not a simulation checkpoint")
+        self._graphs.clear()
         self.lbm.load_state_dict(state["lbm"])
         self.mpm.load_state_dict(state["mpm"])
         self.coupler.load_state_dict(state["coupler"])
