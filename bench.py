@@ -79,7 +79,8 @@ def touched_nodes(base: np.ndarray, dims) -> int:
 def launches_since(before, lbm_step_launches: int = 1, tiled_substep_launches: int = 4) -> int:
     """Kernel launches of the library entry points called since the snapshot `before`
     (fsi_lbm_step launches its face kernel too when the lattice has x faces; the tiled coupled
-    substep launches 3 kernels with the coupling inside P2G, 4 with its own kernel)."""
+    substep launches 3 kernels with the coupling inside P2G, 4 with its own kernel, 5 with
+    separate force and spread kernels)."""
     from fsi import _native as nat
     table = dict(LAUNCHES, fsi_lbm_step=lbm_step_launches,
                  fsi_coupled_substep_tiled=tiled_substep_launches)
@@ -319,8 +320,7 @@ def time_headline(args, world, stream) -> dict:
         sim.coupler.step(cfg.lbm_dt)
     b.record(stream)
     barrier(world)
-    fold = tuning["best"][1] == 1
-    launches = launches_since(before, faces, 3 if fold else 4)
+    launches = launches_since(before, faces, {1: 3, 2: 4, 3: 5}[tuning["best"][1]])
     step_ms = max_over_ranks(a.elapsed_time(b), world) / args.steps
     base = sim.mpm.base_cells_numpy()
     touched = touched_nodes(base, (cfg.lbm.nx, cfg.lbm.ny, cfg.lbm.nz))
@@ -348,7 +348,8 @@ def time_headline(args, world, stream) -> dict:
     out = {
         "step_ms": step_ms, "lattice_ms": lattice_ms, "e2e_s": e2e_s, "launches": launches,
         "tuning": {"threads_per_block": tuning["best"][0],
-                   "coupling": "in P2G" if tuning["best"][1] == 1 else "own kernel",
+                   "coupling": {1: "in P2G", 2: "own kernel",
+                                3: "force and spread kernels"}[tuning["best"][1]],
                    "candidates_ms_per_step": {k: round(v, 4) for k, v in tuning["ms"].items()}},
         "cells": sim.lbm.n_cells, "fluid_cells": int((solid == 0).sum()),
         "solid_cells": int((solid != 0).sum()), "particles": n_particles, "touched": touched,

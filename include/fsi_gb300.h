@@ -173,7 +173,8 @@ typedef struct fsi_mpm_desc {
   /* Launch tuning of the tiled scatter (no reference counterpart; fsi.autotune sets them):
    * threads per block of P2G and G2P, 128, 256 or 512 (0: 256), which sets the particles whose
    * stencils share one shared-memory tile; and where a coupled tiled substep forms the
-   * coupling force: 0 by particle count, 1 inside P2G, 2 in a kernel of its own first. */
+   * coupling force: 0 by particle count, 1 inside P2G, 2 in a kernel of its own first, 3 in
+   * a force kernel and a spread kernel of their own first. */
   int32_t launch_threads;
   int32_t coupling_fold;
 } fsi_mpm_desc;

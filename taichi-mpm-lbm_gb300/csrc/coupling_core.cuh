@@ -275,6 +275,71 @@ __device__ __forceinline__ void coupling_forces_body(const ForceArgs& a, int p) 
   warp_count(&a.cnt->clipped, clipped);
 }
 
+// The coupling force alone (the first half of coupling_forces_body): force, valid weight and
+// mask of particle p, counters; the spread is left to coupling_spread_body.
+__device__ __forceinline__ void coupling_gather_body(const ForceArgs& a, int p) {
+  const bool live = p < a.n;
+  const long long cap = a.cap;
+  bool partial = false, clipped = false, unsupported = false;
+  if (live) {
+    if (a.active[p] == 0) {
+      a.fp[p] = 0.f; a.fp[cap + p] = 0.f; a.fp[2 * cap + p] = 0.f;
+    } else {
+      int base[3];
+      float wv[3][3], valid, pf[3];
+      uint32_t usable;
+      coupling_particle<false>(a, p, base, wv, usable, valid, pf, partial, clipped, unsupported);
+    }
+  }
+  warp_count(&a.cnt->unsupported, unsupported);
+  warp_count(&a.cnt->partial, partial);
+  warp_count(&a.cnt->clipped, clipped);
+}
+
+// The fluid reaction and solid-fraction spread of a particle that coupling_gather_body coupled
+// (mask 1), from its position, stored force and valid weight: the same weights, usable nodes
+// and terms as the spread loop of coupling_forces_body.
+__device__ __forceinline__ void coupling_spread_body(const ForceArgs& a, int p) {
+  if (p >= a.n || a.active[p] == 0 || a.mask_out[p] == 0) return;
+  const long long cap = a.cap;
+  const float x[3] = {a.x[p], a.x[cap + p], a.x[2 * cap + p]};
+  int base[3];
+  float fx[3], wv[3][3];
+  stencil_base(a.c.inv_dx, x, base, fx);
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) wv[ax][i] = bspline_w(fx[ax], i);
+  uint32_t usable = 0;
+  const long long sx = (long long)a.g.ny * a.g.nz, sy = a.g.nz;
+  if (base[0] >= 0 && base[0] + 2 < a.g.nx && base[1] >= 0 && base[1] + 2 < a.g.ny &&
+      base[2] >= 0 && base[2] + 2 < a.g.nz) {
+    const uint32_t fl = a.flags[(base[0] + 1) * sx + (base[1] + 1) * sy + (base[2] + 1)];
+#pragma unroll
+    for (int s = 0; s < 27; ++s) usable |= ((~fl >> stencil_flag_bit(s)) & 1u) << s;
+  } else {
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int ni = base[0] + s / 9, nj = base[1] + (s / 3) % 3, nk = base[2] + s % 3;
+      if (ni < 0 || ni >= a.g.nx || nj < 0 || nj >= a.g.ny || nk < 0 || nk >= a.g.nz) continue;
+      if (!(a.flags[ni * sx + nj * sy + nk] & kFlagSolid)) usable |= 1u << s;
+    }
+  }
+  const float valid = a.valid_out[p];
+  const float pf[3] = {a.fp[p], a.fp[cap + p], a.fp[2 * cap + p]};
+  const float vp = a.vol[p];
+#pragma unroll
+  for (int s = 0; s < 27; ++s) {
+    if (!(usable & (1u << s))) continue;
+    const int i = s / 9, j = (s / 3) % 3, k = s % 3;
+    const long long c = (base[0] + i) * sx + (base[1] + j) * sy + (base[2] + k);
+    const float w = __fmul_rn(__fmul_rn(wv[0][i], wv[1][j]), wv[2][k]);
+    float4 t = coupling_spread_terms(a.c, w, valid, pf, vp);
+    if (!a.c.build_fraction) t.w = 0.f;
+    red_add_v4(a.accum + c, t.x, t.y, t.z, t.w);
+  }
+}
+
 struct AssembleArgs {
   fsi_coupling_desc c;
   Geo g;

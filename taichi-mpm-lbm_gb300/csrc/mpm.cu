@@ -46,6 +46,18 @@ __global__ void __launch_bounds__(kBlock) coupling_only_kernel(ForceArgs fa) {
   coupling_forces_body<false>(fa, blockIdx.x * kBlock + threadIdx.x);
 }
 
+// The coupling split in two lighter kernels: the force (gathers), then the spread (vector
+// reductions), each at its own register count (coupling_fold 3).
+#ifndef FSI_GATHER_MIN_BLOCKS
+#define FSI_GATHER_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kBlock, FSI_GATHER_MIN_BLOCKS) coupling_gather_kernel(ForceArgs fa) {
+  coupling_gather_body(fa, blockIdx.x * kBlock + threadIdx.x);
+}
+__global__ void __launch_bounds__(kBlock) coupling_spread_kernel(ForceArgs fa) {
+  coupling_spread_body(fa, blockIdx.x * kBlock + threadIdx.x);
+}
+
 // P2G with the penalty coupling folded in (one thread per particle).
 template <int kT>
 __global__ void __launch_bounds__(kT) coupled_p2g_kernel(Mpm m, PView P, float4* __restrict__ grid,
@@ -405,6 +417,12 @@ extern "C" int fsi_coupled_substep_tiled(const fsi_coupling_desc* c, const fsi_m
   const bool fold = m.fold == 1 || (m.fold == 0 && m.n < 2 * 152 * kBlock);
   if (fold) {
     if (int e = launch_tiled<CoupledP2G>(m, s, "coupled_p2g_kernel", m, P, g4, dirty, fa)) return e;
+  } else if (m.fold == 3) {
+    coupling_gather_kernel<<<grid_for(m.n, kBlock), kBlock, 0, s>>>(fa);
+    if (int e = check_launch("coupling_gather_kernel")) return e;
+    coupling_spread_kernel<<<grid_for(m.n, kBlock), kBlock, 0, s>>>(fa);
+    if (int e = check_launch("coupling_spread_kernel")) return e;
+    if (int e = launch_tiled<P2G>(m, s, "p2g_kernel", m, P, g4, dirty)) return e;
   } else {
     coupling_only_kernel<<<grid_for(m.n, kBlock), kBlock, 0, s>>>(fa);
     if (int e = check_launch("coupling_only_kernel")) return e;

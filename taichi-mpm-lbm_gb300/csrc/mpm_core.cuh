@@ -23,7 +23,8 @@ struct Mpm {
   int nbx, nby, nbz;  // 4^3 block grid
   int material;       // FSI_MATERIAL_*
   int threads;        // threads per block of the tiled P2G / G2P (128, 256 or 512)
-  int fold;           // coupled tiled substep: 0 by particle count, 1 in P2G, 2 separate
+  int fold;           // coupled tiled substep: 0 by particle count, 1 in P2G, 2 separate,
+                      // 3 separate force and spread kernels
 };
 
 struct PView {
@@ -586,7 +587,7 @@ int make_mpm(const fsi_mpm_desc* d, const fsi_particles* p, Mpm& m, PView& v) {
   FSI_REQUIRE(d->launch_threads == 0 || d->launch_threads == 128 || d->launch_threads == 256 ||
                   d->launch_threads == 512,
               "launch_threads %d is not 0, 128, 256 or 512", d->launch_threads);
-  FSI_REQUIRE(d->coupling_fold >= 0 && d->coupling_fold <= 2, "coupling_fold %d outside 0..2",
+  FSI_REQUIRE(d->coupling_fold >= 0 && d->coupling_fold <= 3, "coupling_fold %d outside 0..3",
               d->coupling_fold);
   m.threads = d->launch_threads ? d->launch_threads : kBlock;
   m.fold = d->coupling_fold;

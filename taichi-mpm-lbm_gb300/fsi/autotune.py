@@ -121,10 +121,11 @@ def coupled_signature(sim) -> str:
 def coupled_candidates(sim) -> list[tuple[int, int]]:
     """(threads per block of P2G / G2P, coupling placement) pairs of the tiled (atomic)
     scatter: 128, 256 or 512 particles share a shared-memory tile; the coupling force is formed
-    inside P2G (1) or by its own kernel first (2). The sorted scatter has no such choice."""
+    inside P2G (1), by its own kernel first (2), or by a force kernel and a spread kernel (3).
+    The sorted scatter has no such choice."""
     if sim.config.mpm.p2g_mode == "sorted":
         return []
-    return [(t, f) for t in (128, 256, 512) for f in (1, 2)]
+    return [(t, f) for t in (128, 256, 512) for f in (1, 2, 3)]
 
 
 def apply_coupled(sim, threads: int, fold: int) -> None:

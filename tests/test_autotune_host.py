@@ -94,7 +94,7 @@ def _sim(p2g_mode="atomic", particles=4096, shape=(48, 32, 32)):
 
 
 def test_coupled_candidates_and_signature(cache):
-    assert autotune.coupled_candidates(_sim()) == [(t, f) for t in (128, 256, 512) for f in (1, 2)]
+    assert autotune.coupled_candidates(_sim()) == [(t, f) for t in (128, 256, 512) for f in (1, 2, 3)]
     assert autotune.coupled_candidates(_sim(p2g_mode="sorted")) == []
     a = autotune.coupled_signature(_sim(particles=502304))
     # nearby particle counts share a record, other shapes and modes do not

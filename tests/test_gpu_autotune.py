@@ -13,7 +13,7 @@ from helpers import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = [(t, f) for t in (128, 256, 512) for f in (1, 2)]
+CANDIDATES = [(t, f) for t in (128, 256, 512) for f in (1, 2, 3)]
 
 
 def smoke():
