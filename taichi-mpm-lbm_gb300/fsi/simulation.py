@@ -89,12 +89,17 @@ class FSISimulation:
                 and c._gamma_settled() and self._dbuf is not None)
 
     def _graph_key(self) -> tuple:
+        """What a captured step bakes in: lattice parity and force buffer, particle count and
+        arrays (re-initialised particles may live elsewhere), launch tuning, gamma, state
+        buffers."""
         lbm, m = self.lbm, self.mpm
         d = m.desc
         c = self.coupler
+        parts = m.particles
+        arrays = tuple(int(getattr(parts, f) or 0) for f, _ in parts._fields_)
         return (lbm._steps_done % 2, lbm._fcur, m.particle_count(), d.launch_threads,
                 d.coupling_fold, lbm._pops.data_ptr(), m._grid.data_ptr(), c._accum.data_ptr(),
-                float(c._gamma_for_kernel()), c._ib_written)
+                float(c._gamma_for_kernel()), c._ib_written, arrays)
 
     def _graph_step(self, body_force) -> dict[str, object]:
         import torch
