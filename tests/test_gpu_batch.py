@@ -184,15 +184,18 @@ def test_batch_scene_generator_runs_in_fp16(tmp_path, monkeypatch):
         assert abs(float(rho.mean()) - 1.0) < 1e-2
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_persistent_run_matches_per_phase_steps(storage):
+@pytest.mark.parametrize("storage,ib", [("f32", False), ("f16", False), ("f32", True)])
+def test_persistent_run_matches_per_phase_steps(storage, ib):
     """SceneBatch.run_persistent (one cooperative launch per run, grid-wide barriers between
     the phases) against the same scenes stepped one launch per phase: the same per-item code
     in the same phase order, so the states agree to the float32 order noise of the atomic grid
     and coupling sums; counters and step bookkeeping are equal."""
     from fsi.batch import SceneBatch
     cfgs, masks, pos, _ = coupled_scenes()
-    cfgs = [dataclasses.replace(c, lbm=dataclasses.replace(c.lbm, population_storage=storage))
+    cfgs = [dataclasses.replace(c, lbm=dataclasses.replace(c.lbm, population_storage=storage),
+                                coupling=dataclasses.replace(c.coupling,
+                                                             immersed_boundary_enabled=ib,
+                                                             immersed_boundary_drag=0.05 * ib))
             for c in cfgs]
     steps = 9
     a, b = SceneBatch(cfgs), SceneBatch(cfgs)
@@ -203,6 +206,8 @@ def test_persistent_run_matches_per_phase_steps(storage):
     assert b.step_index == a.step_index == steps
     assert b.lattice.steps_done == a.lattice.steps_done
     np.testing.assert_array_equal(b.counters_numpy()[:, :3], a.counters_numpy()[:, :3])
+    if ib:  # immersed-boundary active / clipped cell counts
+        np.testing.assert_array_equal(b.counters_numpy()[:, 5:7], a.counters_numpy()[:, 5:7])
     for s in range(len(cfgs)):
         assert rel_l2(b.density_numpy(s), a.density_numpy(s)) < 1e-5
         assert rel_l2(b.velocity_numpy(s), a.velocity_numpy(s)) < 1e-3

@@ -94,3 +94,27 @@ def test_runner_graph_steps_are_the_eager_steps():
     eager.step(), eager.step()
     graph.step()
     np.testing.assert_array_equal(graph.mpm.positions_numpy(), eager.mpm.positions_numpy())
+
+
+def test_runner_graph_steps_with_immersed_boundary_and_contact():
+    """The captured runner step with the immersed-boundary drag (assembly in IB mode) and the
+    contact kernel (after every substep): the same diagnostics and state as eager steps; the
+    IB force total adds with float atomics, so its norm is held to float32 rounding."""
+    import dataclasses
+    cfg, solid, pos = coupled_smoke_config(steps=6)
+    coupling = dataclasses.replace(cfg.coupling, immersed_boundary_enabled=True,
+                                   immersed_boundary_drag=0.05, contact_enabled=True,
+                                   contact_velocity_damping=0.2)
+    cfg = dataclasses.replace(cfg, coupling=coupling,
+                              mpm=dataclasses.replace(cfg.mpm, p2g_mode="sorted"))
+    eager, graph = make(cfg, solid, pos), make(cfg, solid, pos, graph_steps=True)
+    for _ in range(6):
+        de, dg = eager.step(), graph.step()
+        for key in de:
+            if key == "coupling_ib_total_force_norm":
+                assert dg[key] == pytest.approx(de[key], rel=1e-5, abs=1e-12)
+            else:
+                np.testing.assert_array_equal(np.asarray(dg[key]), np.asarray(de[key]),
+                                              err_msg=key)
+    assert len(graph._graphs) == 2
+    assert rel_l2(graph.mpm.positions_numpy(), eager.mpm.positions_numpy()) < 1e-6
