@@ -93,3 +93,36 @@ def test_scene_context_layout_and_argument_checks():
     assert not handle.value
     with pytest.raises(ValueError, match="NULL context"):
         _native.call("fsi_coupled_step", None, 1.0, None, 10, 1, None)
+
+
+def _mpm_desc(**kw):
+    d = _native.MpmDesc()
+    d.nx = d.ny = d.nz = 16
+    d.num_particles = 0
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def _particles():
+    p = _native.Particles()
+    for f in ("x", "v", "C", "F", "mass", "volume", "active", "force"):
+        setattr(p, f, 256)  # never dereferenced: validation fails first or no particles
+    p.capacity = 0
+    return p
+
+
+@pytest.mark.parametrize("threads,fold,message", [(100, 0, "launch_threads"),
+                                                  (256, 5, "coupling_fold")])
+def test_launch_tuning_fields_are_validated_without_touching_the_gpu(threads, fold, message):
+    d = _mpm_desc(launch_threads=threads, coupling_fold=fold)
+    with pytest.raises(ValueError, match=message):
+        _native.call("fsi_mpm_substep", d, _particles(), 256, 256, None)
+
+
+def test_persistent_batch_call_rejects_a_missing_batch():
+    st = _native.BatchState()
+    with pytest.raises(ValueError, match="invalid batch handle"):
+        _native.call("fsi_batch_run_persistent", None, _particles(), st, 0, 1, 10, 0.1, 1, 2, 0,
+                     0, 0, None)
+    assert ctypes.sizeof(_native.BatchState) == 8 * 14
