@@ -125,20 +125,41 @@ struct RunnerDiagArgs {
   int pblocks;
 };
 
-__device__ __forceinline__ double block_sum(double v, double* sh) {
+
+// hi + lo += x with hi + lo kept as an unevaluated float32 pair (Knuth's TwoSum), so a thread
+// sums its particles to about 48 bits without float64 instructions.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+// Adds the block's per-thread float64 values v[0..NV) into out[dst[i]]: the threads' values go
+// to shared memory, warp 0 adds them column by column and in a shuffle tree, one atomic each.
+// Float64 instructions are this GPU's scarcest: 13 warp instructions per value and block.
+template <int NV>
+__device__ __forceinline__ void block_add(const double (&v)[NV], double* __restrict__ out,
+                                          const int (&dst)[NV]) {
+  __shared__ double sh[NV][kBlock];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  for (int i = 0; i < NV; ++i) sh[i][threadIdx.x] = v[i];
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kBlock / 32; ++w) t += sh[w];
-  return t;
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double t = 0.0;
+#pragma unroll
+      for (int r = 0; r < kBlock / 32; ++r) t += sh[i][threadIdx.x + 32 * r];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (threadIdx.x == 0) atomicAdd(out + dst[i], t);
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, double* __restrict__ out) {
-  __shared__ double sh[kBlock / 32];
   if (blockIdx.x == 0 && threadIdx.x < 12) {
     if (a.cnt) {
       if (threadIdx.x < 8) {
@@ -150,35 +171,42 @@ __global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, d
     }
   }
   if ((int)blockIdx.x < a.pblocks) {
-    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    // Sum m, sum m x (exact products split into a rounded part and its remainder), sum f_p:
+    // per-thread float32 pairs, one conversion to float64 per thread.
+    float hi[7] = {0, 0, 0, 0, 0, 0, 0}, lo[7] = {0, 0, 0, 0, 0, 0, 0};
     float vmax = 0.f;
     for (int p = blockIdx.x * kBlock + threadIdx.x; p < a.n; p += a.pblocks * kBlock) {
-      const double ms = a.mass[p];
-      acc[0] += ms;
+      const float ms = a.mass[p];
+      ff_add(hi[0], lo[0], ms);
 #pragma unroll
-      for (int ax = 0; ax < 3; ++ax) acc[1 + ax] += ms * (double)a.x[ax * a.cap + p];
+      for (int ax = 0; ax < 3; ++ax) {
+        const float xa = a.x[ax * a.cap + p];
+        const float pr = __fmul_rn(ms, xa);
+        ff_add(hi[1 + ax], lo[1 + ax], pr);
+        lo[1 + ax] = __fadd_rn(lo[1 + ax], fmaf(ms, xa, -pr));
+      }
       const float vx = a.v[p], vy = a.v[a.cap + p], vz = a.v[2 * a.cap + p];
       vmax = fmaxf(vmax, norm3(vx, vy, vz));
 #pragma unroll
-      for (int ax = 0; ax < 3; ++ax) acc[4 + ax] += (double)a.fp[ax * a.cap + p];
+      for (int ax = 0; ax < 3; ++ax) ff_add(hi[4 + ax], lo[4 + ax], a.fp[ax * a.cap + p]);
     }
-    for (int i = 0; i < 7; ++i) {
-      const double t = block_sum(acc[i], sh);
-      if (threadIdx.x == 0) atomicAdd(out + (i < 4 ? i : i + 1), t);
-    }
+    double acc[7];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) acc[i] = (double)hi[i] + (double)lo[i];
+    const int dst[7] = {0, 1, 2, 3, 5, 6, 7};
+    block_add<7>(acc, out, dst);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
     if ((threadIdx.x & 31) == 0)
       atomicMax(reinterpret_cast<unsigned long long*>(out + 4),
                 (unsigned long long)__double_as_longlong((double)vmax));
   } else if (a.accum) {
-    // Fluid-cell sums of the reaction field in warp tiles of 32 consecutive cells: float32
-    // butterfly warp sums, lane j keeping the warp's j-th tile of each run of 32 and adding it
-    // in float64 once per run (one float64 instruction per 32 tiles: FP64 is this GPU's scarce
-    // pipe), four tiles per pass with their loads issued together.
+    // Fluid-cell sums of the reaction field: each lane adds its cells in float32 for 64 cells
+    // and then into float64 (a few float64 instructions per 2,048 cells of a warp), four cells
+    // per lane and pass with their loads issued together; no per-cell shuffles.
     double s3[3] = {0, 0, 0};
-    float hold[3] = {0.f, 0.f, 0.f};
-    int slot = 0;
+    float f3[3] = {0.f, 0.f, 0.f};
+    int run = 0;
     const int lane = threadIdx.x & 31;
     const long long tiles = (a.g.n + 31) / 32;
     const long long warps = (long long)(gridDim.x - a.pblocks) * (kBlock / 32);
@@ -194,29 +222,22 @@ __global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, d
         v[u] = in ? a.accum[c] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        float w[3] = {0.f, 0.f, 0.f};
-        if (!(fl[u] & kFlagSolid)) { w[0] = v[u].x; w[1] = v[u].y; w[2] = v[u].z; }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-          for (int i = 0; i < 3; ++i) w[i] += __shfl_xor_sync(0xffffffffu, w[i], o);
-        if (lane == slot)
-#pragma unroll
-          for (int i = 0; i < 3; ++i) hold[i] = w[i];
-        if (++slot == 32) {
-#pragma unroll
-          for (int i = 0; i < 3; ++i) { s3[i] += (double)hold[i]; hold[i] = 0.f; }
-          slot = 0;
+      for (int u = 0; u < 4; ++u)
+        if (!(fl[u] & kFlagSolid)) {
+          f3[0] = __fadd_rn(f3[0], v[u].x);
+          f3[1] = __fadd_rn(f3[1], v[u].y);
+          f3[2] = __fadd_rn(f3[2], v[u].z);
         }
+      if (++run == 16) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) { s3[i] += (double)f3[i]; f3[i] = 0.f; }
+        run = 0;
       }
     }
 #pragma unroll
-    for (int i = 0; i < 3; ++i) s3[i] += (double)hold[i];
-    for (int i = 0; i < 3; ++i) {
-      const double t = block_sum(s3[i], sh);
-      if (threadIdx.x == 0) atomicAdd(out + 8 + i, t);
-    }
+    for (int i = 0; i < 3; ++i) s3[i] += (double)f3[i];
+    const int dst[3] = {8, 9, 10};
+    block_add<3>(s3, out, dst);
   }
 }
 
@@ -344,7 +365,7 @@ extern "C" int fsi_coupled_diagnostics(const fsi_mpm_desc* m, const fsi_particle
   int pb = (int)grid_for(a.n, kBlock);
   if (pb > 152 * 2) pb = 152 * 2;
   int cb = accum ? (int)grid_for(a.g.n, kBlock) : 0;
-  if (cb > 152 * 8) cb = 152 * 8;
+  if (cb > 152 * 4) cb = 152 * 4;
   a.pblocks = pb;
   runner_diag_kernel<<<pb + cb, kBlock, 0, s>>>(a, out);
   return check_launch("runner_diag_kernel");
