@@ -686,9 +686,9 @@ def run_gpu(args) -> dict:
         },
         "e2e": {
             "value": round(h["cells"] * args.steps / h["e2e_s"] / 1e6 * world, 3), "unit": "MLUPS",
-            "h2d_bytes_per_step": 12, "d2h_bytes_per_step": 240,
+            "h2d_bytes_per_step": 12, "d2h_bytes_per_step": 264,
             "api": "FSISimulation.step(body_force=g): the step's driving force from pinned host "
-                   "memory in, the 18 diagnostics (one 240-byte device record) out",
+                   "memory in, the 18 diagnostics (one 264-byte device record) out",
             "last_diagnostics": h["last_diagnostics"],
         },
         "lattice": {

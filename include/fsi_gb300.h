@@ -43,7 +43,7 @@ extern "C" {
 #define FSI_ERR_TIMEOUT 4
 #define FSI_ERR_UNSUPPORTED 5
 
-#define FSI_ABI_VERSION 3
+#define FSI_ABI_VERSION 4
 
 /* Library ABI version (FSI_ABI_VERSION). No reference counterpart. */
 int fsi_abi_version(void);
@@ -352,6 +352,16 @@ int fsi_coupling_assemble(const fsi_coupling_desc* desc, const fsi_lbm_desc* lbm
                           const uint32_t* flags, const float* base_force, int mode, float* accum,
                           const float* macro, float* force, float* ib_force, void* counters,
                           void* stream);
+
+/* fsi_coupling_assemble that also sets device double reaction[3] (zeroed here) to the sum
+ * of the fluid reaction accum.xyz over fluid cells, read in the same pass over the
+ * accumulator: the value fsi_coupling_reduce gives for the accumulator that the assembly
+ * read. Fuses total_fluid_coupling_force (coupling.py:229-232) into the assembly of
+ * coupling.py:408-461 for runners that report it every step (simulation.py:117-147). */
+int fsi_coupling_assemble_sum(const fsi_coupling_desc* desc, const fsi_lbm_desc* lbm,
+                              const uint32_t* flags, const float* base_force, int mode,
+                              float* accum, const float* macro, float* force, float* ib_force,
+                              void* counters, double* reaction, void* stream);
 
 /* Contact detection and damping after an MPM substep; resets and fills the
  * contact counters and the contact mask.

@@ -159,6 +159,29 @@ __device__ __forceinline__ void block_add(const double (&v)[NV], double* __restr
   }
 }
 
+// The force assembly with the sum of the fluid reaction over fluid cells read in the same pass
+// (the accumulator is read once for both). Warps walk 32-cell tiles grid-stride; each thread
+// keeps its running sum as a float32 pair, and each block adds its threads' sums in float64.
+constexpr int kAssembleSumPerSm = 6;
+__global__ void __launch_bounds__(kBlock, kAssembleSumPerSm)
+    assemble_sum_kernel(AssembleArgs a, double* __restrict__ reaction) {
+  float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+  const long long tiles = (a.g.n + 31) / 32;
+  const long long warps = (long long)gridDim.x * (kBlock / 32);
+  for (long long t = (long long)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); t < tiles;
+       t += warps) {
+    float r[3];
+    assemble_body(a, t * 32 + (threadIdx.x & 31), r);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) ff_add(hi[i], lo[i], r[i]);
+  }
+  double s3[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) s3[i] = (double)hi[i] + (double)lo[i];
+  const int dst[3] = {0, 1, 2};
+  block_add<3>(s3, reaction, dst);
+}
+
 __global__ void __launch_bounds__(kBlock) runner_diag_kernel(RunnerDiagArgs a, double* __restrict__ out) {
   if (blockIdx.x == 0 && threadIdx.x < 12) {
     if (a.cnt) {
@@ -280,10 +303,12 @@ extern "C" int fsi_coupling_forces(const fsi_coupling_desc* c, const fsi_mpm_des
   return check_launch("coupling_forces_kernel");
 }
 
-extern "C" int fsi_coupling_assemble(const fsi_coupling_desc* c, const fsi_lbm_desc* l,
-                                     const uint32_t* flags, const float* base_force, int mode,
-                                     float* accum, const float* macro, float* force,
-                                     float* ib_force, void* counters, void* stream) {
+namespace fsi {
+namespace {
+int assemble_launch(const fsi_coupling_desc* c, const fsi_lbm_desc* l, const uint32_t* flags,
+                    const float* base_force, int mode, float* accum, const float* macro,
+                    float* force, float* ib_force, void* counters, double* reaction,
+                    void* stream) {
   FSI_REQUIRE(c && l && base_force, "NULL descriptor");
   FSI_REQUIRE(flags && accum && counters, "NULL array");
   FSI_REQUIRE(!(mode & FSI_ASSEMBLE_IB) || (macro && ib_force), "IB needs macro and ib_force");
@@ -304,8 +329,39 @@ extern "C" int fsi_coupling_assemble(const fsi_coupling_desc* c, const fsi_lbm_d
   a.force = force;
   a.ib = ib_force;
   a.cnt = reinterpret_cast<Cnt*>(counters);
-  assemble_kernel<<<grid_for(a.g.n, kBlock), kBlock, 0, as_stream(stream)>>>(a);
-  return check_launch("assemble_kernel");
+  cudaStream_t s = as_stream(stream);
+  if (!reaction) {
+    assemble_kernel<<<grid_for(a.g.n, kBlock), kBlock, 0, s>>>(a);
+    return check_launch("assemble_kernel");
+  }
+  if (cudaMemsetAsync(reaction, 0, 3 * sizeof(double), s) != cudaSuccess)
+    return check_launch("memset");
+  // one wave of resident blocks (the kernel's launch bounds guarantee kAssembleSumPerSm per
+  // SM); the warps walk the tiles grid-stride
+  long long blocks = grid_for((a.g.n + 31) / 32, kBlock / 32);
+  if (blocks > 152ll * kAssembleSumPerSm) blocks = 152ll * kAssembleSumPerSm;
+  assemble_sum_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(a, reaction);
+  return check_launch("assemble_sum_kernel");
+}
+}  // namespace
+}  // namespace fsi
+
+extern "C" int fsi_coupling_assemble(const fsi_coupling_desc* c, const fsi_lbm_desc* l,
+                                     const uint32_t* flags, const float* base_force, int mode,
+                                     float* accum, const float* macro, float* force,
+                                     float* ib_force, void* counters, void* stream) {
+  return fsi::assemble_launch(c, l, flags, base_force, mode, accum, macro, force, ib_force,
+                              counters, nullptr, stream);
+}
+
+extern "C" int fsi_coupling_assemble_sum(const fsi_coupling_desc* c, const fsi_lbm_desc* l,
+                                         const uint32_t* flags, const float* base_force,
+                                         int mode, float* accum, const float* macro,
+                                         float* force, float* ib_force, void* counters,
+                                         double* reaction, void* stream) {
+  FSI_REQUIRE(reaction, "NULL reaction");
+  return fsi::assemble_launch(c, l, flags, base_force, mode, accum, macro, force, ib_force,
+                              counters, reaction, stream);
 }
 
 extern "C" int fsi_contact(const fsi_coupling_desc* c, const fsi_mpm_desc* m,

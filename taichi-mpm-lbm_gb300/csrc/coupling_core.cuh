@@ -356,13 +356,22 @@ struct AssembleArgs {
 
 // _clamp_solid_volume_fraction_kernel + reset_force + _apply_coupling_force_to_lbm_kernel +
 // _compute/_apply_immersed_boundary_force_kernel (coupling.py:408-461, lbm3d.py:504-510).
-// Cell c (this thread); every lane of the warp calls it.
-__device__ __forceinline__ void assemble_body(const AssembleArgs& a, long long c) {
+// Cell c (this thread); every lane of the warp calls it. With `reaction` non-NULL it also
+// returns the cell's fluid reaction (accum.xyz on a fluid cell, else 0), the term that
+// total_fluid_coupling_force (coupling.py:229-232) sums.
+__device__ __forceinline__ void assemble_body(const AssembleArgs& a, long long c,
+                                              float* reaction = nullptr) {
   bool ib_active = false, ib_clipped = false;
   float ibf[3] = {0.f, 0.f, 0.f};
+  if (reaction) reaction[0] = reaction[1] = reaction[2] = 0.f;
   if (c < a.g.n) {
     const bool fluid = !(a.flags[c] & kFlagSolid);
     float4 acc = a.accum[c];
+    if (reaction && fluid) {
+      reaction[0] = acc.x;
+      reaction[1] = acc.y;
+      reaction[2] = acc.z;
+    }
     if ((a.mode & FSI_ASSEMBLE_CLAMP_FRACTION) && !(acc.w <= 1.0f)) {
       // min(phi, 1): only cells above one (or NaN) change, so only they are written back
       acc.w = fminf(acc.w, 1.0f);

@@ -22,7 +22,7 @@ FSI_ERR_CUDA = 2
 FSI_ERR_GUARD = 3
 FSI_ERR_TIMEOUT = 4
 FSI_ERR_UNSUPPORTED = 5
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 STORAGE_F32, STORAGE_F16, STORAGE_BF16 = 0, 1, 2
 ARITH_EXACT, ARITH_FAST = 0, 1
@@ -199,6 +199,7 @@ _SIGNATURES = {
     "fsi_mpm_reduce": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP], ctypes.c_int),
     "fsi_coupling_forces": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_coupling_assemble": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(LbmDesc), _VP, ctypes.POINTER(ctypes.c_float), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "fsi_coupling_assemble_sum": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(LbmDesc), _VP, ctypes.POINTER(ctypes.c_float), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_contact": ([ctypes.POINTER(CouplingDesc), ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_coupling_reduce": ([ctypes.POINTER(LbmDesc), _VP, _VP, _VP, _VP], ctypes.c_int),
     "fsi_coupled_diagnostics": ([ctypes.POINTER(MpmDesc), ctypes.POINTER(Particles),

@@ -88,6 +88,11 @@ class LBMMpmCoupler:
         self._coupled_step = 0
         self._ib_written = False
         self._device_base = None  # device float32[3] driving force, when its owner sets it
+        # device float64[3]: when its owner sets it, every assembly also writes the sum of the
+        # fluid reaction over fluid cells there, read in the same pass over the accumulator;
+        # _reaction_fresh says that the sum belongs to the accumulator as it is now
+        self._reaction_out = None
+        self._reaction_fresh = False
         self._desc = nat.CouplingDesc()
         self._fill_desc()
 
@@ -115,6 +120,7 @@ class LBMMpmCoupler:
         self._desc.gamma_eff = self._gamma_for_kernel()
         self._desc.dt_ratio = float(np.float32(dt_ratio))
         self._desc.build_fraction = int(build_fraction)
+        self._reaction_fresh = False
         nat.call("fsi_coupling_forces", self._desc, self.mpm.desc, self.mpm.particles,
                  nat.ptr(self.lbm.macro), nat.ptr(self.lbm.flags), nat.ptr(self._accum),
                  nat.ptr(self._valid), nat.ptr(self._mask), nat.ptr(self._counters),
@@ -126,6 +132,7 @@ class LBMMpmCoupler:
         self._desc.gamma_eff = self._gamma_for_kernel()
         self._desc.dt_ratio = float(np.float32(dt_ratio))
         self._desc.build_fraction = int(build_fraction)
+        self._reaction_fresh = False
         mpm = self.mpm
         mpm.desc.dt = float(np.float32(mpm_dt))
         common = (self._desc, mpm.desc, mpm.particles, nat.ptr(self.lbm.macro),
@@ -160,9 +167,15 @@ class LBMMpmCoupler:
             self._counters[8:12].zero_()
             self._ib_written = True
         macro = self.lbm.macro if mode & nat.ASSEMBLE_IB else None
-        nat.call("fsi_coupling_assemble", self._desc, self.lbm._desc, nat.ptr(self.lbm.flags),
-                 base_p, mode, nat.ptr(self._accum), nat.ptr(macro), nat.ptr(force),
-                 nat.ptr(self._ib), nat.ptr(self._counters), nat.stream_ptr())
+        args = (self._desc, self.lbm._desc, nat.ptr(self.lbm.flags), base_p, mode,
+                nat.ptr(self._accum), nat.ptr(macro), nat.ptr(force), nat.ptr(self._ib),
+                nat.ptr(self._counters))
+        if self._reaction_out is None:
+            nat.call("fsi_coupling_assemble", *args, nat.stream_ptr())
+        else:
+            nat.call("fsi_coupling_assemble_sum", *args, nat.ptr(self._reaction_out),
+                     nat.stream_ptr())
+            self._reaction_fresh = True
 
     def step(self, lbm_dt: float, body_force=None) -> None:
         """One explicit coupled lattice step with the configured MPM substeps (coupling.py:135-173).
@@ -282,6 +295,7 @@ class LBMMpmCoupler:
 
     def clear_coupling_fields(self) -> None:
         self._accum.zero_()
+        self._reaction_fresh = False
         if self._ib_written:  # the IB force field stays zero while nothing writes it
             self._ib.zero_()
             self._ib_written = self.immersed_boundary_enabled
@@ -389,6 +403,7 @@ class LBMMpmCoupler:
         for name in ("accum", "ib", "valid", "mask", "contact_mask", "counters"):
             getattr(self, "_" + name).copy_(state[name])
         self._ib_written = True
+        self._reaction_fresh = False
         self._coupled_step = int(state["coupled_step"])
 
     def _validate_initialized(self) -> None:

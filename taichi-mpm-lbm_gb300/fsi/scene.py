@@ -89,6 +89,7 @@ class NativeScene:
         lbm._macro_fresh = bool(fresh.value)
         lbm._fcur, lbm._fprev = int(fnext.value), int(flast.value)
         c._coupled_step = int(coupled.value)
+        c._reaction_fresh = False  # the native step rewrote the accumulator
         if c.immersed_boundary_enabled:
             c._ib_written = True
 

@@ -25,6 +25,7 @@ class FSISimulation:
         self._lbm_initialized = False
         self._mpm_initialized = False
         self._dbuf = None
+        self._diag_fused = False
         self._dhost = None
         # step() replays a captured CUDA graph of (coupled step + diagnostics) once the state
         # repeats with period two (no reference counterpart; set False for eager steps)
@@ -127,10 +128,10 @@ class FSISimulation:
                     self._diag_enqueue()
             finally:
                 c._device_base = None
-            entry = (g, lbm._fcur, lbm._fprev)
+            entry = (g, lbm._fcur, lbm._fprev, self._diag_fused)
             self._graphs[key] = entry
             lbm._steps_done, c._coupled_step = steps0, coupled0
-        g, fcur, fprev = entry
+        g, fcur, fprev, self._diag_fused = entry
         g.replay()
         lbm._steps_done += 1
         lbm._fcur, lbm._fprev = fcur, fprev
@@ -139,6 +140,7 @@ class FSISimulation:
         c._coupled_step += 1
         if c.immersed_boundary_enabled:
             c._ib_written = True
+        c._reaction_fresh = True
         self.step_index += 1
         self.time += self.config.lbm_dt
         return self._diag_finish(None)
@@ -179,9 +181,10 @@ class FSISimulation:
         """Per-step diagnostics with the reference's keys (simulation.py:117-147).
 
         All reductions run on the device (float64 sums of the float32 fields): the lattice's
-        fused macro refresh + mass / max |u| pass and one launch for the particles, the fluid
-        reaction and the counters, followed by a single 240-byte copy to pinned host memory
-        and one synchronisation. The reference copies every field to the host instead; its
+        fused macro refresh + mass / max |u| pass and one launch for the particles and the
+        counters, followed by a single 264-byte copy to pinned host memory and one
+        synchronisation. The fluid reaction is summed by the step's force assembly in the same
+        pass over the accumulator (after the first step), else by the particle launch. The reference copies every field to the host instead; its
         centre of mass is a float32 numpy sum, here the float64 quotient rounded to float32
         (MPMSolver3D.center_of_mass() keeps the float32 host arithmetic)."""
         self._validate_initialized()
@@ -194,15 +197,21 @@ class FSISimulation:
 
         from . import _native as nat
 
+        c = self.coupler
         if self._dbuf is None:
             dev = self.lbm.macro.device
-            self._dbuf = torch.zeros(30, dtype=torch.float64, device=dev)
-            self._dhost = torch.zeros(30, dtype=torch.float64).pin_memory()
+            # [0:8] lattice, [8:30] particles / reaction / counters, [30:33] the fluid
+            # reaction that the coupler's assembly sums from here on
+            self._dbuf = torch.zeros(33, dtype=torch.float64, device=dev)
+            self._dhost = torch.zeros(33, dtype=torch.float64).pin_memory()
+            c._reaction_out = self._dbuf[30:33]
         cached = self.lbm._enqueue_mass_speed(self._dbuf[0:8])
-        c = self.coupler
+        # the fluid reaction comes from the last assembly when it read the accumulator as it
+        # is now; otherwise the diagnostics pass reads the accumulator again
+        self._diag_fused = c._reaction_out is not None and c._reaction_fresh
         nat.call("fsi_coupled_diagnostics", self.mpm.desc, self.mpm.particles, self.lbm._desc,
-                 nat.ptr(c._accum), nat.ptr(self.lbm.flags), nat.ptr(c._counters),
-                 nat.ptr(self._dbuf[8:]), nat.stream_ptr())
+                 nat.ptr(None if self._diag_fused else c._accum), nat.ptr(self.lbm.flags),
+                 nat.ptr(c._counters), nat.ptr(self._dbuf[8:30]), nat.stream_ptr())
         self._dhost.copy_(self._dbuf, non_blocking=True)
         return cached
 
@@ -218,7 +227,8 @@ class FSISimulation:
             self.lbm._remember_mass_speed(mass, speed)
         else:
             mass, speed = cached
-        d = r[8:]
+        d = r[8:30]
+        reaction = r[30:33] if self._diag_fused else d[8:11]
         n = self.mpm.particle_count()
         com = (d[1:4] / d[0]).astype(np.float32) if n and d[0] > 0.0 else np.zeros(3, np.float32)
         counts = d[11:19].astype(np.int64)
@@ -232,7 +242,7 @@ class FSISimulation:
             "mpm_center_of_mass": com,
             "mpm_max_velocity_norm": float(d[4]) if n else 0.0,
             "total_particle_coupling_force": d[5:8].astype(np.float32),
-            "total_fluid_coupling_force": d[8:11].astype(np.float32),
+            "total_fluid_coupling_force": reaction.astype(np.float32),
             "coupling_unsupported_particle_count": int(counts[0]),
             "coupling_partial_support_particle_count": int(counts[1]),
             "coupling_clipped_particle_count": int(counts[2]),

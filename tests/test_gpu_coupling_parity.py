@@ -332,6 +332,48 @@ def test_runner_diagnostics_are_device_resident():
         assert d["coupling_" + key] == cd[key], key
     assert d["coupling_ib_total_force_norm"] == pytest.approx(cd["ib_total_force_norm"], rel=1e-6)
     assert d["coupling_ib_active_cell_count"] > 0 and d["coupling_contact_candidate_count"] > 0
+    assert sim._diag_fused  # the fluid reaction came from the step's force assembly
+
+
+@pytest.mark.parametrize("ib", [False, True])
+def test_assembly_with_reaction_sum_is_the_plain_assembly(ib):
+    """fsi_coupling_assemble_sum writes the force field (and IB field and counters) of
+    fsi_coupling_assemble bit for bit, and its fluid-reaction sum is total_fluid_coupling_force
+    of the accumulator it read. The sorted scatter makes the two runs' states comparable bit
+    for bit."""
+    import torch
+
+    cfg, solid, pos = coupled_smoke_config(steps=5)
+    cfg = dataclasses.replace(cfg, mpm=dataclasses.replace(cfg.mpm, p2g_mode="sorted"))
+    if ib:
+        cfg = dataclasses.replace(cfg, coupling=dataclasses.replace(
+            cfg.coupling, immersed_boundary_enabled=True, immersed_boundary_drag=0.1,
+            immersed_boundary_fraction_threshold=0.05))
+    sims = []
+    for fused in (False, True):
+        sim = FSISimulation(cfg)
+        sim.initialize_lbm(solid)
+        sim.initialize_mpm_from_numpy(pos)
+        if fused:
+            sim.coupler._reaction_out = torch.zeros(3, dtype=torch.float64, device="cuda")
+        sims.append(sim)
+    plain, fused = sims
+    for _ in range(4):
+        for sim in sims:
+            sim.coupler.step(cfg.lbm_dt)
+        assert fused.coupler._reaction_fresh and not plain.coupler._reaction_fresh
+        np.testing.assert_allclose(fused.coupler._reaction_out.cpu().numpy(),
+                                   fused.coupler.total_fluid_coupling_force(),
+                                   rtol=1e-5, atol=1e-12)
+    np.testing.assert_array_equal(fused.lbm.distribution_numpy(), plain.lbm.distribution_numpy())
+    np.testing.assert_array_equal(fused.coupler.immersed_boundary_force_numpy(),
+                                  plain.coupler.immersed_boundary_force_numpy())
+    df, dp = fused.coupler.immersed_boundary_diagnostics(), plain.coupler.immersed_boundary_diagnostics()
+    assert df.keys() == dp.keys()
+    for key in df:  # the IB force totals are float atomic sums, the counts exact
+        assert df[key] == pytest.approx(dp[key], rel=1e-5, abs=1e-12), key
+    if ib:
+        assert df["ib_active_cell_count"] > 0
 
 
 def test_body_force_per_step_matches_config_force():

@@ -120,6 +120,14 @@ def test_launch_tuning_fields_are_validated_without_touching_the_gpu(threads, fo
         _native.call("fsi_mpm_substep", d, _particles(), 256, 256, None)
 
 
+def test_assembly_with_sum_requires_its_output():
+    c, l = _native.CouplingDesc(), _native.LbmDesc()
+    base = (ctypes.c_float * 3)()
+    with pytest.raises(ValueError, match="NULL reaction"):
+        _native.call("fsi_coupling_assemble_sum", c, l, None, base, 0, None, None, None, None,
+                     None, None, None)
+
+
 def test_persistent_batch_call_rejects_a_missing_batch():
     st = _native.BatchState()
     with pytest.raises(ValueError, match="invalid batch handle"):
