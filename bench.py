@@ -461,11 +461,13 @@ def time_closure(args, world, stream, snapshots: int = 40, every: int = 3,
     t0 = time.perf_counter()
     net = cl.ClosureMLP(seed=0)
     trainer = cl.ClosureTrainer(net)
-    for seed in train_seeds:
-        cfg, mask, _ = scenes.closure_channel(seed)
-        # snapshots over the 120-fine-step window the evaluation covers, from rest
-        trainer.add_run(cfg, mask, warmup=0, snapshots=snapshots, every=every,
-                        cell_fraction=cell_fraction, seed=seed)
+    train = [scenes.closure_channel(seed) for seed in train_seeds]
+    # the 200 fine runs advance as one autotuned LatticeBatch; snapshots over the
+    # 120-fine-step window the evaluation covers, from rest
+    batch_rec = trainer.add_batch([c for c, _, _ in train], [m for _, m, _ in train],
+                                  warmup=0, snapshots=snapshots, every=every,
+                                  cell_fraction=cell_fraction, seeds=list(train_seeds))
+    del train
     rows = trainer.build()
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -546,7 +548,14 @@ def time_closure(args, world, stream, snapshots: int = 40, every: int = 3,
                      "occupancy_feature": "solid fraction" if net.use_fraction else "0/1",
                      "ms_per_step": round(train_ms, 3),
                      "loss_first": round(hist[0], 5), "loss_last": round(hist[-1], 5),
-                     "wall_s_incl_data": round(data_s, 1)},
+                     "wall_s_incl_data": round(data_s, 1),
+                     "data": "ClosureTrainer.add_batch: the fine runs as one LatticeBatch "
+                             "whose step launch the batch autotuner picked on these scenes",
+                     "batch_tuning": {"best_step_tile_cells": (batch_rec["tuning"]["best"]
+                                                               or [None])[0],
+                                      "candidates_ms_per_step": {
+                                          k: round(v, 4) for k, v in
+                                          batch_rec["tuning"]["ms"].items()}}},
         "accuracy_heldout": {k: (round(v, 6) if isinstance(v, float) else v)
                              for k, v in acc.items()},
         "gpu_launches": steps * 3 + 2 * steps,

@@ -183,11 +183,16 @@ class LatticeBatch:
     def velocity_numpy(self, s: int) -> np.ndarray:
         return self._block(self.macro, s, 1)[:, :3].reshape(*self.shapes[s], 3).cpu().numpy()
 
-    def distribution_numpy(self, s: int) -> np.ndarray:
+    def distribution(self) -> torch.Tensor:
+        """Post-stream populations of every lattice in the reference layout, device float32
+        [cells][19]; lattice s is rows offsets[s]:offsets[s + 1]."""
         out = torch.empty((self.cells, _Q), dtype=torch.float32, device=self._device)
         nat.call("fsi_batch_lbm_distribution", self._handle, nat.ptr(self._pops),
                  nat.ptr(self._flags), self._steps_done, nat.ptr(out), nat.stream_ptr())
-        return self._block(out, s, 1).reshape(*self.shapes[s], _Q).cpu().numpy()
+        return out
+
+    def distribution_numpy(self, s: int) -> np.ndarray:
+        return self._block(self.distribution(), s, 1).reshape(*self.shapes[s], _Q).cpu().numpy()
 
     def mass_and_speed(self) -> np.ndarray:
         """Per lattice (sum of rho over fluid cells, max |u|) as float64[count, 2]."""

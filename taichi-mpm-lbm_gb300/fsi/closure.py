@@ -79,6 +79,33 @@ def restrict(fine: LBMSolver3D, coarse: LBMSolver3D) -> torch.Tensor:
     return out
 
 
+_W = (1.0 / 3.0,) + (1.0 / 18.0,) * 6 + (1.0 / 36.0,) * 12
+
+
+def restrict_rows(dist: torch.Tensor, shape, solid: torch.Tensor, rho0: float) -> torch.Tensor:
+    """``restrict`` of fine lattices given as their post-stream populations in the reference
+    layout: ``dist`` device float32 [k*nx*ny*nz][19] holds k lattices of one shape one after
+    another (e.g. consecutive lattices of ``LatticeBatch.distribution``), ``solid`` their
+    solid masks (device bool [k, nx, ny, nz], or [nx, ny, nz] for k = 1). The fluid children of
+    each coarse cell are summed in the kernel's order (child (di, dj, dk) = 4 di + 2 dj + dk)
+    and divided by their count, w_q rho0 where all eight are solid: bit for bit the kernel's
+    result. Returns [k*Nc][19]."""
+    nx, ny, nz = shape
+    k = dist.shape[0] // (nx * ny * nz)
+    f = dist.view(k, nx // 2, 2, ny // 2, 2, nz // 2, 2, OUT)
+    fluid = (~solid).reshape(k, nx // 2, 2, ny // 2, 2, nz // 2, 2, 1)
+    acc = torch.zeros((k, nx // 2, ny // 2, nz // 2, OUT), dtype=torch.float32,
+                      device=dist.device)
+    nf = torch.zeros((k, nx // 2, ny // 2, nz // 2, 1), dtype=torch.float32, device=dist.device)
+    for ch in range(8):
+        di, dj, dk = ch >> 2, (ch >> 1) & 1, ch & 1
+        keep = fluid[:, :, di, :, dj, :, dk, :]
+        acc = acc + torch.where(keep, f[:, :, di, :, dj, :, dk, :], 0.0)
+        nf = nf + keep.to(torch.float32)
+    rest = torch.tensor(_W, dtype=torch.float32, device=dist.device) * np.float32(rho0)
+    return torch.where(nf > 0, acc / nf.clamp(min=1.0), rest).reshape(-1, OUT)
+
+
 def prolongate(coarse_f: torch.Tensor, shape) -> torch.Tensor:
     """Each fine cell takes its parent's populations, [Nf, 19]."""
     nx, ny, nz = shape
@@ -323,6 +350,59 @@ def training_pairs(fine_cfg: LBMConfig, fine_mask: np.ndarray, warmup: int, snap
             fine.step()
 
 
+def batched_training_pairs(batch, fine_masks: list[np.ndarray], warmup: int, snapshots: int,
+                           every: int = 2):
+    """``training_pairs`` of every lattice of ``batch`` (an initialised ``LatticeBatch`` of
+    the fine scenes, periodic faces, masks ``fine_masks``), the fine runs advancing together
+    as one batched launch per step. Yields (lattice index, coarse solver after its step,
+    fluid cells, target [m][19]) for each snapshot and lattice; with exact float32
+    arithmetic these are the pairs ``training_pairs`` gives scene by scene."""
+    dev = batch._device
+    coarse, fluid = [], []
+    for s, cfg in enumerate(batch.configs):
+        c = LBMSolver3D(coarse_config(cfg))
+        cmask = coarse_mask(fine_masks[s])
+        c.initialize(cmask)
+        coarse.append(c)
+        fluid.append(torch.nonzero(torch.from_numpy(cmask.reshape(-1) == 0)).reshape(-1).to(
+            torch.int32).to(dev))
+    # runs of consecutive lattices of one shape and rho0 are restricted in one call
+    groups, s = [], 0
+    while s < batch.count:
+        e = s + 1
+        while (e < batch.count and batch.shapes[e] == batch.shapes[s]
+               and batch.configs[e].rho0 == batch.configs[s].rho0):
+            e += 1
+        solid = torch.from_numpy(np.stack([np.asarray(m) > 0 for m in fine_masks[s:e]])).to(dev)
+        groups.append((s, e, solid))
+        s = e
+
+    def restricted(d):
+        out = []
+        for a, e, solid in groups:
+            rows = d[int(batch.offsets[a]):int(batch.offsets[e])]
+            r = restrict_rows(rows, batch.shapes[a], solid, batch.configs[a].rho0)
+            out.extend(r.view(e - a, -1, OUT).unbind(0))
+        return out
+
+    for _ in range(warmup):
+        batch.step()
+    for _ in range(snapshots):
+        r0s = restricted(batch.distribution())
+        batch.step()
+        batch.step()
+        r1s = restricted(batch.distribution())
+        for s in range(batch.count):
+            r0, r1 = r0s[s], r1s[s]
+            c = coarse[s]
+            c.load_populations(r0)
+            c.step()
+            cstate = torch.from_numpy(c.distribution_numpy().reshape(-1, OUT)).to(dev)
+            yield s, c, fluid[s], (r1 - cstate)[fluid[s].long()]
+        for _ in range(every - 2):
+            batch.step()
+
+
 def rollout_pairs(fine_cfg: LBMConfig, fine_mask: np.ndarray, net: "ClosureMLP",
                   coarse_steps: int, every: int = 2):
     """Training pairs along the closure's own trajectory (solver in the loop): the coarse run
@@ -361,6 +441,7 @@ class ClosureTrainer:
         self.rows_x: list[torch.Tensor] = []
         self.rows_t: list[torch.Tensor] = []
         self._pending = []  # (coarse state copy, cells, raw target) before scales are known
+        self.batch_records: list[dict] = []  # add_batch: scene count, steps, autotuner record
 
     def add_run(self, fine_cfg: LBMConfig, fine_mask: np.ndarray, warmup: int = 40,
                 snapshots: int = 10, every: int = 4, cell_fraction: float = 1.0,
@@ -375,6 +456,44 @@ class ClosureTrainer:
                 keep = keep.to(cells.device)
                 cells, target = cells[keep], target[keep]
             self._pending.append((coarse.state_dict(), coarse.config, cells, target.clone(), frac))
+
+    def add_batch(self, fine_cfgs: list[LBMConfig], fine_masks: list[np.ndarray],
+                  warmup: int = 40, snapshots: int = 10, every: int = 4,
+                  cell_fraction: float = 1.0, seeds: list[int] | None = None,
+                  tune: bool = True) -> dict:
+        """``add_run`` for many scenes at once: their fine runs advance as one
+        ``LatticeBatch``, whose launch the batch autotuner first picks on these scenes
+        (``fsi.autotune.tune_lattice_batch``; the state is restored after tuning). Rows are
+        kept per scene in the order ``add_run`` would give them, scene ``s`` subsampled with
+        ``seeds[s]``. Returns the tuning record, also kept in ``batch_records``."""
+        from .batch import LatticeBatch
+
+        n = len(fine_cfgs)
+        seeds = list(range(n)) if seeds is None else list(seeds)
+        if len(fine_masks) != n or len(seeds) != n:
+            raise ValueError("one mask and one seed per scene.")
+        batch = LatticeBatch(fine_cfgs)
+        batch.initialize(fine_masks)
+        record = batch.autotune() if tune else {"best": None, "ms": {}}
+        fracs = [solid_fraction(m, self.net.device) if self.net.use_fraction else None
+                 for m in fine_masks]
+        gens = [torch.Generator(device="cpu").manual_seed(sd) for sd in seeds]
+        per_scene = [[] for _ in range(n)]
+        for s, coarse, cells, target in batched_training_pairs(batch, fine_masks, warmup,
+                                                                snapshots, every):
+            if cell_fraction < 1.0:
+                keep = (torch.rand(cells.numel(), generator=gens[s]) < cell_fraction)
+                keep = keep.to(cells.device)
+                cells, target = cells[keep], target[keep]
+            per_scene[s].append((coarse.state_dict(), coarse.config, cells, target.clone(),
+                                 fracs[s]))
+        for pending in per_scene:
+            self._pending.extend(pending)
+        del batch
+        rec = {"scenes": n, "fine_steps": warmup + snapshots * max(every, 2),
+               "tuning": record}
+        self.batch_records.append(rec)
+        return rec
 
     def add_rollout_run(self, fine_cfg: LBMConfig, fine_mask: np.ndarray, coarse_steps: int,
                         every: int = 2, cell_fraction: float = 1.0, seed: int = 0) -> None:

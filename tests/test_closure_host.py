@@ -58,3 +58,30 @@ def test_prolongation_copies_each_parent_to_its_eight_children():
         for j in range(ny):
             for k in range(nz):
                 assert torch.equal(fine[i, j, k], c[i // 2, j // 2, k // 2])
+
+
+def test_restrict_rows_sums_fluid_children_in_kernel_order():
+    """restrict_rows: fluid children added one by one in child order 4 di + 2 dj + dk (float32),
+    divided by their count; w_q rho0 where all eight children are solid."""
+    import torch
+    from fsi import closure as cl
+    rng = np.random.default_rng(0)
+    nx, ny, nz = 8, 6, 4
+    dist = rng.random((nx * ny * nz, 19)).astype(np.float32)
+    solid = rng.random((nx, ny, nz)) < 0.4
+    solid[0:2, 0:2, 0:2] = True
+    rows = cl.restrict_rows(torch.from_numpy(dist), (nx, ny, nz), torch.from_numpy(solid),
+                            1.25).numpy()
+    f = dist.reshape(nx, ny, nz, 19)
+    ref = np.zeros((nx // 2, ny // 2, nz // 2, 19), np.float32)
+    for I in range(nx // 2):
+        for J in range(ny // 2):
+            for K in range(nz // 2):
+                acc, n = np.zeros(19, np.float32), 0
+                for ch in range(8):
+                    i, j, k = 2 * I + (ch >> 2), 2 * J + ((ch >> 1) & 1), 2 * K + (ch & 1)
+                    if not solid[i, j, k]:
+                        acc, n = (acc + f[i, j, k]).astype(np.float32), n + 1
+                ref[I, J, K] = acc / np.float32(n) if n else \
+                    np.array(cl._W, np.float32) * np.float32(1.25)
+    np.testing.assert_array_equal(rows, ref.reshape(-1, 19))

@@ -375,3 +375,43 @@ def test_evaluation_reports_drag_and_fallback():
         assert np.isfinite(r[k]), k
     assert r["drag_fine"] > 0.0
     assert r["fallback"] is None or isinstance(r["fallback"], str)
+
+
+def test_restrict_rows_is_the_restriction_kernel():
+    from fsi import scenes
+    cfg, mask, _ = scenes.closure_channel(7, nx=16, ny=12, nz=12, balls=2, rmin=2.0, rmax=3.0)
+    fine = LBMSolver3D(cfg)
+    fine.initialize(mask)
+    for _ in range(5):
+        fine.step()
+    coarse = LBMSolver3D(cl.coarse_config(cfg))
+    coarse.initialize(cl.coarse_mask(mask))
+    dist = torch.from_numpy(fine.distribution_numpy().reshape(-1, 19)).cuda()
+    rows = cl.restrict_rows(dist, (cfg.nx, cfg.ny, cfg.nz),
+                            torch.from_numpy(mask > 0).cuda(), cfg.rho0)
+    assert torch.equal(rows, cl.restrict(fine, coarse))
+
+
+def test_batched_training_rows_are_the_per_scene_rows(tmp_path, monkeypatch):
+    """ClosureTrainer.add_batch (the scenes' fine runs as one autotuned LatticeBatch) gives
+    the rows of add_run scene by scene, bit for bit, and keeps the autotuner's record."""
+    from fsi import scenes
+    monkeypatch.setenv("FSI_AUTOTUNE_CACHE", str(tmp_path / "autotune.json"))
+    seeds = [100, 101, 102]
+    scenes_ = [scenes.closure_channel(sd, nx=24, ny=12, nz=12, balls=2, rmin=2.0, rmax=3.0)
+               for sd in seeds]
+    kw = dict(warmup=2, snapshots=3, every=3, cell_fraction=0.5)
+    one = cl.ClosureTrainer(cl.ClosureMLP(seed=0))
+    for sd, (cfg, mask, _) in zip(seeds, scenes_):
+        one.add_run(cfg, mask, seed=sd, **kw)
+    many = cl.ClosureTrainer(cl.ClosureMLP(seed=0))
+    rec = many.add_batch([c for c, _, _ in scenes_], [m for _, m, _ in scenes_], seeds=seeds,
+                         **kw)
+    assert rec["scenes"] == 3 and rec["fine_steps"] == 2 + 3 * 3
+    assert rec["tuning"]["best"] is not None and rec["tuning"]["ms"]
+    assert many.batch_records == [rec]
+    assert one.build() == many.build() > 0
+    assert torch.equal(one.x, many.x)
+    assert torch.equal(one.t, many.t)
+    assert (one.net.pop_scale, one.net.force_scale, one.net.out_scale) == \
+        (many.net.pop_scale, many.net.force_scale, many.net.out_scale)
