@@ -11,7 +11,13 @@ Both advance in lockstep; at the listed steps the script records the relative L2
 the fluid density and velocity, of the body drag (sum of the particles' coupling forces) and
 of the particle displacement from the start.
 
-    python oracle/error_table_bodies.py --steps 2000 --out table.json
+The horizon is 200 steps. From about step 250 this channel grows a disturbance at the inlet
+face next to a wall corner, cell (0, 42, 42), with or without the bodies and in both
+precisions: max |u| 0.060 at step 250, 0.098 at step 450, 0.99 at step 500, NaN by step 550
+(the lattice alone, float64). The face conditions are the reference's literally
+(fsi/lbm3d.py:363-407), so the growth belongs to its scheme on this channel.
+
+    python oracle/error_table_bodies.py --steps 200 --out table.json
 """
 from __future__ import annotations
 
@@ -39,8 +45,8 @@ def rel_l2(a, b) -> float:
 
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--at", default="100,250,500,1000,1500,2000",
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--at", default="25,50,100,150,200",
                     help="steps at which the errors are recorded")
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--out", default=None, help="JSON file for the table")
