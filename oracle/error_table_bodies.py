@@ -15,7 +15,8 @@ The horizon is 200 steps. From about step 250 this channel grows a disturbance a
 face next to a wall corner, cell (0, 42, 42), with or without the bodies and in both
 precisions: max |u| 0.060 at step 250, 0.098 at step 450, 0.99 at step 500, NaN by step 550
 (the lattice alone, float64). The face conditions are the reference's literally
-(fsi/lbm3d.py:363-407), so the growth belongs to its scheme on this channel.
+(fsi/lbm3d.py:363-407): its velocity inlet, updated in place in q order, is what grows. The
+same channel with a velocity condition that reads the pre-update populations stays finite.
 
     python oracle/error_table_bodies.py --steps 200 --out table.json
 """
