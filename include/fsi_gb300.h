@@ -43,7 +43,7 @@ extern "C" {
 #define FSI_ERR_TIMEOUT 4
 #define FSI_ERR_UNSUPPORTED 5
 
-#define FSI_ABI_VERSION 4
+#define FSI_ABI_VERSION 5
 
 /* Library ABI version (FSI_ABI_VERSION). No reference counterpart. */
 int fsi_abi_version(void);
@@ -59,7 +59,9 @@ size_t fsi_last_error(char* buf, size_t len);
  * (fsi/lbm3d.py:110-191): relaxation rates, rho0 and the x-face conditions. */
 typedef struct fsi_lbm_desc {
   int32_t nx, ny, nz;
-  int32_t bc_mode_left;   /* x = 0 face: 0 periodic, 1 pressure, 2 velocity (lbm3d.py:16-27) */
+  int32_t bc_mode_left;   /* x = 0 face: 0 periodic, 1 pressure, 2 velocity (lbm3d.py:16-27);
+                             3 velocity with every population read from before the update
+                             (no reference counterpart; the reference updates in place) */
   int32_t bc_mode_right;  /* x = nx-1 face, same codes */
   float s[19];            /* MRT relaxation rates S_k (lbm3d.py:141-168) */
   float rho0;

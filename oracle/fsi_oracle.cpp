@@ -154,7 +154,9 @@ void stream(const Lattice<T>& L, const T* f, T* F, const int32_t* solid, int nth
       }
 }
 
-// apply_boundary, fsi/lbm3d.py:363-407. mode 1 = pressure, 2 = velocity.
+// apply_boundary, fsi/lbm3d.py:363-407. mode 1 = pressure, 2 = velocity (in place, in q
+// order, as the reference), 3 = velocity with every population read from before the update
+// (an extension with no reference counterpart).
 template <class T>
 void apply_boundary_face(const Lattice<T>& L, T* F, const T* v, const int32_t* solid, int xi,
                          int xin, int mode, T bc_rho, const T bc_vel[3], T rho0) {
@@ -168,10 +170,19 @@ void apply_boundary_face(const Lattice<T>& L, T* F, const T* v, const int32_t* s
         const T* uu = solid[ci] > 0 ? v + 3 * ci : v + 3 * c;
         T u[3] = {uu[0], uu[1], uu[2]};
         for (int q = 0; q < Q; ++q) F[c * Q + q] = feq(L, q, bc_rho, u);
-      } else {
+      } else if (mode == 2) {
         for (int q = 0; q < Q; ++q) {
           int o = LR[q];
           T val = feq(L, o, rho0, bc_vel) - F[c * Q + o];
+          val = val + feq(L, q, rho0, bc_vel);
+          F[c * Q + q] = val;
+        }
+      } else {
+        T old[Q];
+        for (int q = 0; q < Q; ++q) old[q] = F[c * Q + q];
+        for (int q = 0; q < Q; ++q) {
+          int o = LR[q];
+          T val = feq(L, o, rho0, bc_vel) - old[o];
           val = val + feq(L, q, rho0, bc_vel);
           F[c * Q + q] = val;
         }

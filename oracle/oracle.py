@@ -109,7 +109,8 @@ def boundary_mode(boundary) -> int:
     if t == "pressure":
         return 1
     if t == "velocity":
-        return 2
+        # 3: the extension that reads every population from before the update
+        return 3 if getattr(boundary, "velocity_update", "sequential") == "simultaneous" else 2
     if t == "wall":
         raise NotImplementedError("wall face boundaries are reserved; use solid masks.")
     raise ValueError(f"Unsupported boundary type: {t}.")

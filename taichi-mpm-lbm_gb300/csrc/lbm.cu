@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kBlock) lbm_face_kernel(FaceArgs a) {
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) F[q] = feq_ref(q, a.bc_rho[side], ux, uy, uz);
-  } else {
+  } else if (mode == 2) {
     // Velocity: F_q = feq_opp - F_opp + feq_q, sequentially in q with the
     // already-updated F_opp (the reference updates the field in place).
     const float* v = a.bc_vel[side];
@@ -94,6 +94,18 @@ __global__ void __launch_bounds__(kBlock) lbm_face_kernel(FaceArgs a) {
       float val = __fsub_rn(feq_ref(o, a.rho0, v[0], v[1], v[2]), F[o]);
       F[q] = __fadd_rn(val, feq_ref(q, a.rho0, v[0], v[1], v[2]));
     }
+  } else {
+    // Velocity, every F_opp read from before the update (mode 3, an extension).
+    const float* v = a.bc_vel[side];
+    float G[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      const int o = opp(q);
+      float val = __fsub_rn(feq_ref(o, a.rho0, v[0], v[1], v[2]), F[o]);
+      G[q] = __fadd_rn(val, feq_ref(q, a.rho0, v[0], v[1], v[2]));
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) F[q] = G[q];
   }
 #pragma unroll
   for (int q = 0; q < 19; ++q) St::st(pops, slot[q], F[q], a.shift[q]);
@@ -321,7 +333,7 @@ int check_desc(const fsi_lbm_desc* d) {
               "conserved moments (0, 3, 5, 7) must have zero relaxation rate");
   for (int side = 0; side < 2; ++side) {
     int m = side == 0 ? d->bc_mode_left : d->bc_mode_right;
-    FSI_REQUIRE(m >= 0 && m <= 2, "unknown x boundary mode %d", m);
+    FSI_REQUIRE(m >= 0 && m <= 3, "unknown x boundary mode %d", m);
   }
   FSI_REQUIRE(d->storage >= FSI_STORAGE_F32 && d->storage <= FSI_STORAGE_BF16,
               "unknown population storage %d", d->storage);

@@ -22,7 +22,7 @@ FSI_ERR_CUDA = 2
 FSI_ERR_GUARD = 3
 FSI_ERR_TIMEOUT = 4
 FSI_ERR_UNSUPPORTED = 5
-ABI_VERSION = 4
+ABI_VERSION = 5
 
 STORAGE_F32, STORAGE_F16, STORAGE_BF16 = 0, 1, 2
 ARITH_EXACT, ARITH_FAST = 0, 1

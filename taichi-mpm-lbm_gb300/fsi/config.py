@@ -44,12 +44,20 @@ class BoundaryConfig:
     rho: float = 1.0
     velocity: tuple[float, float, float] = (0.0, 0.0, 0.0)
 
+    # Extension (velocity faces): "sequential" is the reference's update, in place in q order
+    # (lbm3d.py:375-383), so one member of each opposite pair reads its partner's new value;
+    # "simultaneous" reads every population from before the update. On an inflow/outflow
+    # channel at tau 0.55 the sequential form grows without bound after a few hundred steps.
+    velocity_update: str = "sequential"
+
     def validate(self) -> None:
         if self.boundary_type not in _BOUNDARY_TYPES:
             raise ValueError(f"Unsupported boundary type: {self.boundary_type}.")
         if self.rho <= 0.0:
             raise ValueError(f"Boundary rho must be positive, got {self.rho}.")
         _check_vec3(self.velocity, "Boundary velocity must have 3 components.")
+        if self.velocity_update not in ("sequential", "simultaneous"):
+            raise ValueError(f"Unsupported velocity_update: {self.velocity_update}.")
 
 
 @dataclass(frozen=True)

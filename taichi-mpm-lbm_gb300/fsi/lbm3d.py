@@ -39,6 +39,8 @@ def _boundary_mode(boundary: BoundaryConfig) -> int:
     codes = {"periodic": 0, "pressure": 1, "velocity": 2}
     if kind not in codes:
         raise ValueError(f"Unsupported boundary type: {kind}.")
+    if kind == "velocity" and getattr(boundary, "velocity_update", "sequential") == "simultaneous":
+        return 3
     return codes[kind]
 
 

@@ -44,6 +44,7 @@ def test_defaults_validate_and_mpm_dt():
     CouplingConfig(contact_velocity_damping=1.1), CouplingConfig(contact_fraction_threshold=-0.1),
     CouplingConfig(contact_fraction_threshold=1.1), OutputConfig(output_interval=0),
     OutputConfig(output_format="bad"), BoundaryConfig(velocity=(0.0, 1.0)),
+    BoundaryConfig("velocity", velocity_update="in_order"),
     MPMConfig(constitutive_model="plastic"),
     LBMConfig(population_storage="f8"), LBMConfig(collision_arithmetic="approx"),
     LBMConfig(population_storage="f16", collision_arithmetic="exact"),

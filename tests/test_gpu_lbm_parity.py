@@ -68,6 +68,8 @@ def test_channel_with_obstacle_100_steps():
     (BoundaryConfig("velocity", velocity=(0.02, 0.0, 0.0)), BoundaryConfig("pressure", rho=1.0)),
     (BoundaryConfig("pressure", rho=1.01), BoundaryConfig("pressure", rho=1.0)),
     (BoundaryConfig("periodic"), BoundaryConfig("velocity", velocity=(-0.01, 0.005, 0.0))),
+    (BoundaryConfig("velocity", velocity=(0.02, 0.003, 0.0), velocity_update="simultaneous"),
+     BoundaryConfig("pressure", rho=1.0)),
 ])
 def test_x_face_conditions(left, right):
     faces = dict(PERIODIC, x_left=left, x_right=right)

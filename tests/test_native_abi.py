@@ -49,6 +49,14 @@ def test_invalid_descriptor_is_rejected_without_touching_the_gpu():
         _native.call("fsi_lbm_step", d, None, None, None, None, None, 0, None)
 
 
+def test_unknown_face_mode_is_rejected_without_touching_the_gpu():
+    d = _native.LbmDesc()
+    d.nx = d.ny = d.nz = 8
+    d.bc_mode_left = 4
+    with pytest.raises(ValueError, match="unknown x boundary mode 4"):
+        _native.call("fsi_lbm_step", d, None, None, None, None, None, 0, None)
+
+
 def test_struct_sizes_match_header_layout():
     assert ctypes.sizeof(_native.LbmDesc) == 4 * (5 + 19 + 3 + 6 + 2)
     assert ctypes.sizeof(_native.BatchLattice) == 4 * 4 + 8 + 4 * (19 + 1 + 3) + 4  # + tail pad

@@ -66,6 +66,12 @@ def reference_step(f, F, rho, v, force, solid, M, invM, S, w, left, right, rho0)
                 for q in range(19):  # in place, in q order
                     o = LR[q]
                     Fn[x, j, k, q] = feq(w, o, rho0, ub) - Fn[x, j, k, o] + feq(w, q, rho0, ub)
+            elif bc[0] == "velocity-simultaneous":  # the extension: all partners read before
+                ub = np.asarray(bc[1], np.float32).astype(np.float64)
+                old = Fn[x, j, k].copy()
+                for q in range(19):
+                    o = LR[q]
+                    Fn[x, j, k, q] = feq(w, o, rho0, ub) - old[o] + feq(w, q, rho0, ub)
     for i, j, k in np.ndindex(nx, ny, nz):
         if solid[i, j, k]:
             rho[i, j, k], v[i, j, k] = rho0, 0.0
@@ -79,12 +85,15 @@ def reference_step(f, F, rho, v, force, solid, M, invM, S, w, left, right, rho0)
 def bc(kind, value):
     if kind == "pressure":
         return BoundaryConfig("pressure", rho=value)
+    if kind == "velocity-simultaneous":
+        return BoundaryConfig("velocity", velocity=value, velocity_update="simultaneous")
     return BoundaryConfig("velocity", velocity=value)
 
 
 @pytest.mark.parametrize("left,right", [
     (("velocity", (0.05, 0.01, -0.02)), ("pressure", 1.02)),
     (("pressure", 0.98), ("velocity", (-0.03, 0.0, 0.01))),
+    (("velocity-simultaneous", (0.05, 0.01, -0.02)), ("pressure", 1.02)),
 ])
 def test_face_conditions_match_a_second_restatement(left, right):
     nx, ny, nz = 6, 5, 5
@@ -110,10 +119,13 @@ def test_face_conditions_match_a_second_restatement(left, right):
                           float(lat.rho0))
     for name, got, exp in zip(("f", "F", "rho", "v"), (lat.f, lat.F, lat.rho, lat.v), want):
         np.testing.assert_allclose(got, exp, rtol=1e-12, atol=1e-14, err_msg=name)
-    # the in-place order matters at O(1): a simultaneous update differs on the velocity face
-    x = 0 if left[0] == "velocity" else nx - 1
-    ub = np.asarray((left if x == 0 else right)[1], np.float32).astype(np.float64)
-    j, k = 2, 1
-    simultaneous = [feq(lat.w, LR[q], float(lat.rho0), ub) - want[1][x, j, k, LR[q]]
-                    + feq(lat.w, q, float(lat.rho0), ub) for q in range(19)]
-    assert np.abs(np.array(simultaneous) - lat.F[x, j, k]).max() > 1e-3
+    # the two velocity updates differ at O(1) on the velocity face: the other one's result is
+    # far from what the oracle computed
+    swap = {"velocity": "velocity-simultaneous", "velocity-simultaneous": "velocity"}
+    other_l = (swap.get(left[0], left[0]), left[1])
+    other_r = (swap.get(right[0], right[0]), right[1])
+    other = reference_step(*start, solid, lat.M, lat.invM, lat.S, lat.w, other_l, other_r,
+                           float(lat.rho0))
+    x = 0 if left[0].startswith("velocity") else nx - 1
+    assert np.abs(other[1][x] - lat.F[x]).max() > 1e-3
+    np.testing.assert_allclose(other[1][2:4], lat.F[2:4], rtol=1e-12)  # interior cells agree
